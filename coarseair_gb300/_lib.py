@@ -1,0 +1,98 @@
+"""ctypes bindings of the C ABI in include/cair_gpu.h (the library libcair_gpu.so built in-tree).
+
+The product path always goes through this library; if it is missing or no GPU is present the
+calls raise.  There is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcair_gpu.so")
+CAIR_MAX_PES = 8
+CAIR_ABI_VERSION = 1
+
+STATUS = {0: "CAIR_OK", 1: "CAIR_EINVAL", 2: "CAIR_ECUDA", 3: "CAIR_ETIMEOUT", 4: "CAIR_ENONFINITE",
+          5: "CAIR_EUNSUPPORTED"}
+
+
+class PesDesc(C.Structure):
+    _fields_ = [("model", C.c_int32), ("ncoef", C.c_int32), ("coef", C.POINTER(C.c_double)),
+                ("a", C.c_double), ("ab", C.c_double), ("ra", C.c_double), ("rb", C.c_double),
+                ("eref", C.c_double), ("totdiss", C.c_double)]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("abi_version", C.c_int32), ("natoms", C.c_int32), ("npes", C.c_int32),
+                ("diat_model", C.c_int32), ("mass", C.c_double * 4), ("tpq", C.POINTER(C.c_double)),
+                ("pes", PesDesc * CAIR_MAX_PES),
+                ("dt0", C.c_double), ("eps", C.c_double), ("relax", C.c_double), ("rmax", C.c_double),
+                ("tmax", C.c_double), ("ham_abs_tol", C.c_double),
+                ("nsteps", C.c_int32), ("inc_step", C.c_int32), ("ncall", C.c_int32), ("nquad", C.c_int32),
+                ("rsmal", C.c_double), ("rcent", C.c_double), ("rfact", C.c_double), ("tthresau", C.c_double)]
+
+
+class MolState(C.Structure):
+    _fields_ = [("ipair", C.c_int32), ("itype", C.c_int32), ("eint", C.c_double), ("angmom", C.c_double),
+                ("viba", C.c_double)]
+
+
+class TrajPoint(C.Structure):
+    _fields_ = [("mol", MolState * 2), ("b", C.c_double), ("xkin", C.c_double), ("vrel", C.c_double * 3),
+                ("nmol", C.c_int32), ("pad", C.c_int32)]
+
+
+TRAJ_POINT_DTYPE = np.dtype([("ipair0", "i4"), ("itype0", "i4"), ("eint0", "f8"), ("angmom0", "f8"),
+                             ("viba0", "f8"), ("ipair1", "i4"), ("itype1", "i4"), ("eint1", "f8"),
+                             ("angmom1", "f8"), ("viba1", "f8"), ("b", "f8"), ("xkin", "f8"),
+                             ("vrel", "f8", (3,)), ("nmol", "i4"), ("pad", "i4")])
+
+# (name, restype, argtypes) of every entry point declared in include/cair_gpu.h
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int32)
+_L = C.POINTER(C.c_int64)
+SIGNATURES = [
+    ("cair_create", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(SystemDesc)]),
+    ("cair_destroy", None, [_P]),
+    ("cair_last_error", C.c_char_p, [_P]),
+    ("cair_dims", C.c_int, [_P, _I, _I, _I]),
+    ("cair_get_tpq", C.c_int, [_P, _D]),
+    ("cair_pes_eval", C.c_int, [_P, C.c_int64, _I, _D, _D, _D, _D, _D]),
+    ("cair_rhs", C.c_int, [_P, C.c_int64, _I, _D, _D]),
+    ("cair_hamiltonian", C.c_int, [_P, C.c_int64, _I, _D, _D, _D]),
+    ("cair_bs_steps", C.c_int, [_P, C.c_int64, _I, _D, _D, _D, _D, C.c_int32]),
+    ("cair_integrate", C.c_int, [_P, C.c_int64, _I, _D, _D, _D, _D, _D, _D, _D, _I, _I, _I, C.c_int64]),
+    ("cair_integrate_dev", C.c_int, [_P, C.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int64, _P]),
+    ("cair_find_state", C.c_int, [_P, C.c_int64, _D, C.POINTER(TrajPoint)]),
+    ("cair_apply_transformation", C.c_int, [_P, C.c_int64, _D, _D]),
+    ("cair_flop_model", C.c_int, [_P, C.c_int32, _D, _D, _D, _D]),
+    ("cair_last_counters", C.c_int, [_P, _L]),
+]
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libcair_gpu.so and declare its entry points.  Raises if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libcair_gpu.so is not built (run __graft_entry__.build()): %s" % path)
+    lib = C.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def dptr(a):
+    return a.ctypes.data_as(_D) if a is not None else None
+
+
+def iptr(a):
+    return a.ctypes.data_as(_I) if a is not None else None

@@ -1,0 +1,240 @@
+"""Host-side interface mirroring the reference's operators for the trajectory path.
+
+    PES(system).Compute(R, Q)          -> V, dVdR, dVdQ      PES_Type%Compute   (PES_Class.F90:43-72)
+    PES(system).Potential(R)           -> V                  PES_Type%Potential
+    Collision(system).Hamiltonian(PaQ) -> H, Rpi             Collision_Type%Hamiltonian_1d
+    Collision(system).EvaluateRHS(y)   -> dy/dt              HamiltonODESystem (RHS_Evaluation)
+    Collision(system).ApplyTransformation(PaQ) -> PaQ with velocities
+    ODE(system).Integrate(traj, n)     -> n BS attempts      ODE_Solver_Type%Integrate
+    Integrator(system).Integrate(traj) -> to end of collision Integrator_Type%Integrate (propagation)
+    MolecularState.FindState(PaQ)      -> final states       TrajectoryPoint%Analyze + FindState
+
+All arrays are FP64 numpy arrays laid out as the Fortran arrays (PaQ per trajectory
+contiguous).  Every call runs on the GPU through libcair_gpu.so; no CPU path exists.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import dptr, iptr
+
+
+class CairError(RuntimeError):
+    pass
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Handle:
+    """Owns one cair_handle (device copies of the surfaces, stream, scratch)."""
+
+    def __init__(self, cfg, tpq=None):
+        lib = _lib.load()
+        self.lib = lib
+        self.cfg = cfg
+        d = _lib.SystemDesc()
+        d.abi_version = _lib.CAIR_ABI_VERSION
+        d.natoms = cfg.natoms
+        d.npes = len(cfg.surfaces)
+        d.diat_model = cfg.diat_model
+        for i, m in enumerate(cfg.masses):
+            d.mass[i] = m
+        self._keep = []
+        for i, s in enumerate(cfg.surfaces):
+            c = np.ascontiguousarray(s.coef, dtype=np.float64)
+            self._keep.append(c)
+            p = d.pes[i]
+            p.model, p.ncoef, p.coef = s.model, c.size, dptr(c)
+            p.a, p.ab, p.ra, p.rb, p.eref, p.totdiss = s.a, s.ab, s.ra, s.rb, s.eref, s.totdiss
+        if tpq is not None:
+            t = np.asfortranarray(tpq, dtype=np.float64).ravel(order="F")
+            self._keep.append(t)
+            d.tpq = dptr(t)
+        d.dt0, d.eps, d.relax, d.rmax, d.tmax, d.ham_abs_tol = (cfg.dt0, cfg.eps, cfg.relax, cfg.rmax,
+                                                                cfg.tmax, cfg.ham_abs_tol)
+        d.nsteps, d.inc_step, d.ncall, d.nquad = cfg.nsteps, cfg.inc_step, cfg.ncall, cfg.nquad
+        d.rsmal, d.rcent, d.rfact, d.tthresau = cfg.rsmal, cfg.rcent, cfg.rfact, cfg.tthresau
+        h = C.c_void_p()
+        rc = lib.cair_create(C.byref(h), C.byref(d))
+        self.h = h
+        if rc != 0:
+            msg = lib.cair_last_error(h).decode() if h else ""
+            if h:
+                lib.cair_destroy(h)
+            self.h = None
+            raise CairError("cair_create: %s (%s)" % (_lib.STATUS.get(rc, rc), msg))
+        nv, ne, np_ = C.c_int32(), C.c_int32(), C.c_int32()
+        lib.cair_dims(h, C.byref(nv), C.byref(ne), C.byref(np_))
+        self.nv, self.ne, self.npairs = nv.value, ne.value, np_.value
+
+    def check(self, rc, what):
+        if rc != 0:
+            raise CairError("%s: %s (%s)" % (what, _lib.STATUS.get(rc, rc), self.lib.cair_last_error(self.h).decode()))
+
+    def close(self):
+        if self.h:
+            self.lib.cair_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tpq(self):
+        t = np.zeros(self.nv * self.nv)
+        self.check(self.lib.cair_get_tpq(self.h, dptr(t)), "cair_get_tpq")
+        return t.reshape(self.nv, self.nv, order="F")
+
+    def flop_model(self, ipes=0):
+        a, b, c, d = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        self.check(self.lib.cair_flop_model(self.h, ipes, C.byref(a), C.byref(b), C.byref(c), C.byref(d)),
+                   "cair_flop_model")
+        return dict(grad=a.value, energy=b.value, attempt=c.value, exp=d.value)
+
+    def counters(self):
+        c = np.zeros(5, dtype=np.int64)
+        self.check(self.lib.cair_last_counters(self.h, c.ctypes.data_as(C.POINTER(C.c_int64))), "counters")
+        return dict(attempts=int(c[0]), accepted=int(c[1]), rejected=int(c[2]), grad_evals=int(c[3]),
+                    energy_evals=int(c[4]))
+
+
+class PES:
+    """Batched PES_Type%Compute / %Potential."""
+
+    def __init__(self, handle):
+        self.H = handle
+
+    def Compute(self, R, Qall, ipes=None):
+        H = self.H
+        R = _f64(R, (-1, H.npairs))
+        n = R.shape[0]
+        Qall = _f64(Qall, (n, 3 * H.cfg.natoms))
+        V = np.zeros(n)
+        dVdR = np.zeros((n, H.npairs))
+        dVdQ = np.zeros((n, H.nv))
+        H.check(H.lib.cair_pes_eval(H.h, n, iptr(_i32(ipes)), dptr(R), dptr(Qall), dptr(V), dptr(dVdR), dptr(dVdQ)),
+                "cair_pes_eval")
+        return V, dVdR, dVdQ
+
+    def Potential(self, R, Qall=None, ipes=None):
+        H = self.H
+        R = _f64(R, (-1, H.npairs))
+        n = R.shape[0]
+        if Qall is None:
+            Qall = np.zeros((n, 3 * H.cfg.natoms))
+        Qall = _f64(Qall, (n, 3 * H.cfg.natoms))
+        V = np.zeros(n)
+        H.check(H.lib.cair_pes_eval(H.h, n, iptr(_i32(ipes)), dptr(R), dptr(Qall), dptr(V), None, None),
+                "cair_pes_eval")
+        return V
+
+
+class Collision:
+    def __init__(self, handle):
+        self.H = handle
+
+    def EvaluateRHS(self, y, ipes=None):
+        H = self.H
+        y = _f64(y, (-1, H.ne))
+        yp = np.zeros_like(y)
+        H.check(H.lib.cair_rhs(H.h, y.shape[0], iptr(_i32(ipes)), dptr(y), dptr(yp)), "cair_rhs")
+        return yp
+
+    def Hamiltonian(self, paq, ipes=None):
+        H = self.H
+        paq = _f64(paq, (-1, H.ne))
+        n = paq.shape[0]
+        h = np.zeros(n)
+        rpi = np.zeros((n, H.npairs))
+        H.check(H.lib.cair_hamiltonian(H.h, n, iptr(_i32(ipes)), dptr(paq), dptr(h), dptr(rpi)), "cair_hamiltonian")
+        return h, rpi
+
+    def ApplyTransformation(self, paq):
+        H = self.H
+        paq = _f64(paq, (-1, H.ne))
+        out = np.zeros_like(paq)
+        H.check(H.lib.cair_apply_transformation(H.h, paq.shape[0], dptr(paq), dptr(out)), "cair_apply_transformation")
+        return out
+
+
+@dataclass
+class Trajectories:
+    """Trajectories_Type state (Trajectories_Class.F90:34-68), one row per trajectory."""
+    paq: np.ndarray
+    t: np.ndarray
+    dt: np.ndarray
+    erra: np.ndarray
+    ipes: np.ndarray
+    H: np.ndarray = None
+    smax: np.ndarray = None
+    smin: np.ndarray = None
+    irej: np.ndarray = None
+    iste: np.ndarray = None
+    status: np.ndarray = None
+
+    @classmethod
+    def start(cls, paq, erra, dt0, ipes=None):
+        """Initial state as SetIniCondForward sets it (Collision_Class.F90:1100-1108)."""
+        paq = _f64(paq)
+        n = paq.shape[0]
+        return cls(paq=paq.copy(), t=np.zeros(n), dt=np.full(n, float(dt0)), erra=_f64(erra).copy(),
+                   ipes=np.zeros(n, np.int32) if ipes is None else _i32(ipes).copy(),
+                   H=np.zeros(n), smax=np.full(n, -np.finfo(np.float64).max),
+                   smin=np.full(n, np.finfo(np.float64).max), irej=np.zeros(n, np.int32),
+                   iste=np.zeros(n, np.int32), status=np.zeros(n, np.int32))
+
+
+class ODE:
+    def __init__(self, handle):
+        self.H = handle
+
+    def Integrate(self, traj, nattempts):
+        """Exactly `nattempts` Bulirsch-Stoer attempts per trajectory (no end checks)."""
+        H = self.H
+        n = traj.paq.shape[0]
+        H.check(H.lib.cair_bs_steps(H.h, n, iptr(traj.ipes), dptr(traj.paq), dptr(traj.t), dptr(traj.dt),
+                                    dptr(traj.erra), int(nattempts)), "cair_bs_steps")
+        return traj
+
+
+class Integrator:
+    def __init__(self, handle):
+        self.H = handle
+
+    def Integrate(self, traj, max_attempts=None):
+        """Propagate to the end of the collision; fills H (last end check) and status."""
+        H = self.H
+        n = traj.paq.shape[0]
+        ma = int(max_attempts if max_attempts is not None else H.cfg.max_attempts)
+        H.check(H.lib.cair_integrate(H.h, n, iptr(traj.ipes), dptr(traj.paq), dptr(traj.t), dptr(traj.dt),
+                                     dptr(traj.erra), dptr(traj.H), dptr(traj.smax), dptr(traj.smin),
+                                     iptr(traj.irej), iptr(traj.iste), iptr(traj.status), ma), "cair_integrate")
+        return traj
+
+
+class MolecularState:
+    def __init__(self, handle):
+        self.H = handle
+
+    def FindState(self, paq_vel):
+        """Analyse trajectory points given velocities+coordinates; returns a structured array."""
+        H = self.H
+        paq_vel = _f64(paq_vel, (-1, H.ne))
+        n = paq_vel.shape[0]
+        out = np.zeros(n, dtype=_lib.TRAJ_POINT_DTYPE)
+        H.check(H.lib.cair_find_state(H.h, n, dptr(paq_vel), out.ctypes.data_as(C.POINTER(_lib.TrajPoint))),
+                "cair_find_state")
+        return out

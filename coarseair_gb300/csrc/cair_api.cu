@@ -1,0 +1,585 @@
+// C-ABI implementation (include/cair_gpu.h): handle management, host<->device staging and
+// kernel dispatch.  No CPU fallback: every numerical entry point runs on the GPU and
+// returns CAIR_ECUDA when no device is usable.
+#include <cuda_runtime.h>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "cair_kernels.cuh"
+
+using namespace cair;
+
+struct cair_handle {
+  int device = 0;
+  int nsm = 0;
+  DevSys sys;
+  FsArgs fs;
+  double* d_coef[CAIR_MAX_PES] = {nullptr};
+  double* d_gauss = nullptr;
+  double tqp[81], tpq[81];
+  double mass[4];
+  std::string err;
+  cudaStream_t stream = nullptr;
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  unsigned long long* d_ctl = nullptr;   // [0] queue, [1..5] counters
+  long long last_counters[5] = {0, 0, 0, 0, 0};
+  double watchdog_s = 0.0;
+};
+
+namespace {
+
+int fail(cair_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CUDA_TRY(h, call)                                                                        \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      return fail(h, CAIR_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+  } while (0)
+
+// libgfortran's pow_r8_i4 (binary powering), as the reference evaluates beta**k
+double powi_gf(double a, int b) {
+  double p = 1.0, x = a;
+  unsigned u;
+  if (b == 0) return 1.0;
+  if (b < 0) { u = (unsigned)(-b); x = 1.0 / x; } else u = (unsigned)b;
+  for (;;) {
+    if (u & 1u) p *= x;
+    u >>= 1;
+    if (u) x *= x; else break;
+  }
+  return p;
+}
+
+// Gauss-Jordan inverse with partial pivoting (the reference uses LAPACK DGETRF/DGETRI;
+// callers that need its exact matrix pass it through cair_system_desc::tpq)
+int invert(int n, const double* A, double* Ainv) {
+  double M[9][18];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < 2 * n; ++j) M[i][j] = (j < n) ? A[i + 9 * j] : (j - n == i ? 1.0 : 0.0);
+  for (int c = 0; c < n; ++c) {
+    int p = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(M[r][c]) > std::fabs(M[p][c])) p = r;
+    if (M[p][c] == 0.0) return -1;
+    if (p != c)
+      for (int j = 0; j < 2 * n; ++j) std::swap(M[p][j], M[c][j]);
+    double piv = M[c][c];
+    for (int j = 0; j < 2 * n; ++j) M[c][j] /= piv;
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      double f = M[r][c];
+      if (f == 0.0) continue;
+      for (int j = 0; j < 2 * n; ++j) M[r][j] -= f * M[c][j];
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) Ainv[i + 9 * j] = M[i][n + j];
+  return 0;
+}
+
+int grid_for(const cair_handle* h, int64_t n, int block = 128) {
+  int64_t g = (n + block - 1) / block;
+  int64_t cap = (int64_t)h->nsm * 16;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+// Device scratch arena: one allocation reused across calls, grown on demand.
+int ensure_scratch(cair_handle* h, size_t bytes) {
+  if (bytes <= h->scratch_bytes) return 0;
+  if (h->d_scratch) cudaFree(h->d_scratch);
+  h->d_scratch = nullptr;
+  h->scratch_bytes = 0;
+  size_t b = bytes + bytes / 4 + (1 << 20);
+  CUDA_TRY(h, cudaMalloc(&h->d_scratch, b));
+  h->scratch_bytes = b;
+  return 0;
+}
+
+struct Carver {
+  char* base;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+int wait_stream(cair_handle* h) {
+  if (h->watchdog_s <= 0.0) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return 0;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(h->stream);
+    if (e == cudaSuccess) return 0;
+    if (e != cudaErrorNotReady) return fail(h, CAIR_ECUDA, std::string("stream: ") + cudaGetErrorString(e));
+    double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (dt > h->watchdog_s) return fail(h, CAIR_ETIMEOUT, "watchdog: GPU work did not finish in time");
+    std::this_thread::sleep_for(std::chrono::microseconds(200));
+  }
+}
+
+int check_launch(cair_handle* h) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(h, CAIR_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+bool three_atoms(const cair_handle* h) { return h->sys.natoms == 3; }
+
+int model_of(const cair_handle* h) { return h->sys.pes[0].model; }
+
+int check_ipes(cair_handle* h, int64_t n, const int32_t* ipes) {
+  if (!ipes) return 0;
+  for (int64_t k = 0; k < n; ++k)
+    if (ipes[k] < 0 || ipes[k] >= h->sys.npes) return fail(h, CAIR_EINVAL, "ipes out of range");
+  return 0;
+}
+
+}  // namespace
+
+// 1-thread helper used at create time for Vinf
+__global__ void cair_k_diat_v(DevSys S, const double* r, double* v, int64_t n) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) v[k] = diat_v(S, r[k]);
+}
+
+extern "C" {
+
+int cair_create(cair_handle** out, const cair_system_desc* d) {
+  if (!out || !d) return CAIR_EINVAL;
+  *out = nullptr;
+  cair_handle* h = new cair_handle();
+  auto bad = [&](int code, const std::string& msg) {
+    h->err = msg;
+    *out = h;  // caller reads the message, then destroys
+    return code;
+  };
+  if (d->abi_version != CAIR_ABI_VERSION) return bad(CAIR_EINVAL, "abi_version mismatch");
+  if (d->natoms != 3 && d->natoms != 4) return bad(CAIR_EINVAL, "natoms must be 3 or 4");
+  if (d->npes < 1 || d->npes > CAIR_MAX_PES) return bad(CAIR_EINVAL, "npes out of range");
+  if (d->nsteps < 2 || d->nsteps > 4) return bad(CAIR_EUNSUPPORTED, "Nb of extrapolation steps must be 2..4");
+  if (d->ncall < 1) return bad(CAIR_EINVAL, "ncall must be >= 1");
+  if (d->nquad < 1 || d->nquad > 256) return bad(CAIR_EINVAL, "nquad must be 1..256");
+  for (int i = 0; i < d->natoms; ++i)
+    if (!(d->mass[i] > 0.0)) return bad(CAIR_EINVAL, "atom masses must be positive");
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev == 0) return bad(CAIR_ECUDA, "no CUDA device available");
+  cudaGetDevice(&h->device);
+  cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
+  if (const char* w = std::getenv("CAIR_WATCHDOG_S")) h->watchdog_s = std::atof(w);
+
+  DevSys& S = h->sys;
+  std::memset(&S, 0, sizeof(S));
+  S.natoms = d->natoms;
+  S.nv = 3 * (d->natoms - 1);
+  S.ne = 2 * S.nv;
+  S.npairs = d->natoms * (d->natoms - 1) / 2;
+  S.npes = d->npes;
+  S.nsteps = d->nsteps;
+  S.ncall = d->ncall;
+  S.incstp = d->inc_step;
+  S.diat = d->diat_model;
+  S.relax = d->relax;
+  S.rmax = d->rmax;
+  S.tmax = d->tmax;
+  S.rpimax = 1.0 / d->rmax;
+  for (int i = 0; i < 4; ++i) h->mass[i] = d->mass[i];
+  for (int i = 0; i < d->natoms - 1; ++i) S.mMiMn[i] = -d->mass[i] / d->mass[d->natoms - 1];
+  // Tqp (Transformation_Class.F90:53-128)
+  std::memset(h->tqp, 0, sizeof(h->tqp));
+  double xmi = 1.0 / d->mass[d->natoms - 1];
+  int ic = 0;
+  for (int i = 0; i < d->natoms - 1; ++i) {
+    double temp1 = d->mass[i] * xmi;
+    double temp = (d->mass[d->natoms - 1] + d->mass[i]) * temp1;
+    for (int j = 0; j < 3; ++j) {
+      h->tqp[ic + 9 * ic] = temp;
+      for (int ip = i + 1; ip < d->natoms - 1; ++ip) {
+        double temp2 = temp1 * d->mass[ip];
+        h->tqp[ic + 9 * (ip * 3 + j)] = temp2;
+        h->tqp[(ip * 3 + j) + 9 * ic] = temp2;
+      }
+      ++ic;
+    }
+  }
+  if (d->tpq) {
+    std::memset(h->tpq, 0, sizeof(h->tpq));
+    for (int j = 0; j < S.nv; ++j)
+      for (int i = 0; i < S.nv; ++i) h->tpq[i + 9 * j] = d->tpq[i + S.nv * j];
+  } else if (invert(S.nv, h->tqp, h->tpq) != 0) {
+    return bad(CAIR_EINVAL, "mass matrix is singular");
+  }
+  std::memcpy(S.Tpq, h->tpq, sizeof(S.Tpq));
+  // O2 UMN exponent factors (O2_UMN_DiatomicPotential_Class.F90 Ev2gm2/_Grad)
+  {
+    const double a[8] = {-1.488979427684798e3, 1.881435846488955e4, -1.053475425838226e5,
+                         2.755135591229064e5,  -4.277588997761775e5, 4.404104009614092e5,
+                         -2.946204062950765e5, 1.176861219078620e5};
+    const double alpha = 9.439784362354936e-1, beta = 1.262242998506810;
+    for (int k = 0; k < 8; ++k) {
+      double bk = powi_gf(beta, k);
+      S.o2_ab[k] = alpha * bk;
+      S.o2_cd[k] = 2.0 * a[k] * alpha * bk;
+    }
+  }
+  for (int p = 0; p < d->npes; ++p) {
+    const cair_pes_desc& src = d->pes[p];
+    int expect = src.model == CAIR_PES_O3_UMN ? 56 : src.model == CAIR_PES_N3_UMN ? 276
+                 : src.model == CAIR_PES_O4_UMN ? 430 : -1;
+    if (expect < 0) return bad(CAIR_EINVAL, "unknown surface model");
+    if (src.ncoef != expect || !src.coef) return bad(CAIR_EINVAL, "wrong coefficient count for surface");
+    if (src.model != d->pes[0].model) return bad(CAIR_EUNSUPPORTED, "all surfaces of a handle must share a model");
+    if ((src.model == CAIR_PES_O4_UMN) != (d->natoms == 4)) return bad(CAIR_EINVAL, "surface/atom count mismatch");
+    if (src.model == CAIR_PES_O4_UMN) return bad(CAIR_EUNSUPPORTED, "O4 UMN kernels are not built in this library");
+    DevPes& P = S.pes[p];
+    P.model = src.model;
+    P.ncoef = src.ncoef;
+    P.a = src.a; P.ab = src.ab; P.ra = src.ra; P.rb = src.rb;
+    P.inv_a = (src.a != 0.0) ? 1.0 / src.a : 0.0;
+    if (cudaMalloc(&h->d_coef[p], sizeof(double) * src.ncoef) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
+    if (cudaMemcpy(h->d_coef[p], src.coef, sizeof(double) * src.ncoef, cudaMemcpyHostToDevice) != cudaSuccess)
+      return bad(CAIR_ECUDA, "cudaMemcpy coefficients");
+    P.coef = h->d_coef[p];
+  }
+  // final-state analysis parameters and Chebyshev-2 nodes (GAUSSQ kind 3)
+  FsArgs& F = h->fs;
+  F.nquad = d->nquad;
+  F.rsmal = d->rsmal;
+  F.rcent = d->rcent;
+  F.rfact = d->rfact;
+  F.tthresau = d->tthresau;
+  for (int i = 0; i < 4; ++i) F.mass[i] = d->mass[i];
+  {
+    // Vinf = DiatomicPotential(1.0E+03) of the target (MolecularStateParam_Class.F90:94)
+    std::vector<double> gx(d->nquad), gw(d->nquad);
+    const double pi = std::acos(-1.0);
+    for (int i = 0; i < d->nquad; ++i) {
+      int k = d->nquad - i;
+      double th = (double)k * pi / (double)(d->nquad + 1);
+      double s = std::sin(th);
+      gx[i] = std::cos(th);
+      gw[i] = pi / (double)(d->nquad + 1) * (s * s);
+      gw[i] = gw[i] / std::sqrt(1.0 - gx[i] * gx[i]);
+    }
+    if (cudaMalloc(&h->d_gauss, sizeof(double) * 2 * d->nquad) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
+    cudaMemcpy(h->d_gauss, gx.data(), sizeof(double) * d->nquad, cudaMemcpyHostToDevice);
+    cudaMemcpy(h->d_gauss + d->nquad, gw.data(), sizeof(double) * d->nquad, cudaMemcpyHostToDevice);
+    F.gx = h->d_gauss;
+    F.gw = h->d_gauss + d->nquad;
+    F.vinf = 0.0;  // filled below on the device
+  }
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bad(CAIR_ECUDA, "stream");
+  if (cudaMalloc(&h->d_ctl, sizeof(unsigned long long) * 8) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
+  // Vinf on the device with the same diatomic code as the kernels
+  {
+    double* dv = nullptr;
+    if (cudaMalloc(&dv, sizeof(double)) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
+    double r = 1.0E+03, *dr = nullptr;
+    cudaMalloc(&dr, sizeof(double));
+    cudaMemcpy(dr, &r, sizeof(double), cudaMemcpyHostToDevice);
+    cair_k_diat_v<<<1, 32, 0, h->stream>>>(S, dr, dv, 1);
+    cudaStreamSynchronize(h->stream);
+    cudaError_t e = cudaMemcpy(&F.vinf, dv, sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(dv);
+    cudaFree(dr);
+    if (e != cudaSuccess) return bad(CAIR_ECUDA, std::string("Vinf: ") + cudaGetErrorString(e));
+  }
+  *out = h;
+  return CAIR_OK;
+}
+
+void cair_destroy(cair_handle* h) {
+  if (!h) return;
+  for (int p = 0; p < CAIR_MAX_PES; ++p)
+    if (h->d_coef[p]) cudaFree(h->d_coef[p]);
+  if (h->d_gauss) cudaFree(h->d_gauss);
+  if (h->d_scratch) cudaFree(h->d_scratch);
+  if (h->d_ctl) cudaFree(h->d_ctl);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+const char* cair_last_error(const cair_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int cair_dims(const cair_handle* h, int32_t* nv, int32_t* ne, int32_t* np) {
+  if (!h) return CAIR_EINVAL;
+  if (nv) *nv = h->sys.nv;
+  if (ne) *ne = h->sys.ne;
+  if (np) *np = h->sys.npairs;
+  return 0;
+}
+
+int cair_get_tpq(const cair_handle* h, double* tpq) {
+  if (!h || !tpq) return CAIR_EINVAL;
+  int nv = h->sys.nv;
+  for (int j = 0; j < nv; ++j)
+    for (int i = 0; i < nv; ++i) tpq[i + nv * j] = h->tpq[i + 9 * j];
+  return 0;
+}
+
+int cair_pes_eval(cair_handle* h, int64_t n, const int32_t* ipes, const double* R, const double* Qall, double* V,
+                  double* dVdR, double* dVdQ) {
+  if (!h || n < 0 || !R || !Qall || !V) return fail(h, CAIR_EINVAL, "cair_pes_eval: bad argument");
+  if (n == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_pes_eval: 4-atom surfaces not built");
+  if (int e = check_ipes(h, n, ipes)) return e;
+  bool grad = dVdR != nullptr;
+  if (grad && !dVdQ) return fail(h, CAIR_EINVAL, "cair_pes_eval: dVdQ required with dVdR");
+  const int np = 3, na3 = 9, nv = 6;
+  size_t bytes = n * (sizeof(int32_t) + sizeof(double) * (np + na3 + 1 + np + nv)) + 8 * 256;
+  if (int e = ensure_scratch(h, bytes)) return e;
+  Carver c{(char*)h->d_scratch};
+  int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
+  double *d_R = c.take<double>(n * np), *d_Q = c.take<double>(n * na3), *d_V = c.take<double>(n);
+  double *d_g = c.take<double>(n * np), *d_m = c.take<double>(n * nv);
+  if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_R, R, n * np * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_Q, Qall, n * na3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int g = grid_for(h, n);
+  int m = model_of(h);
+  if (m == CAIR_PES_O3_UMN) {
+    if (grad) k_pes_eval3<CAIR_PES_O3_UMN, true><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
+    else k_pes_eval3<CAIR_PES_O3_UMN, false><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
+  } else {
+    if (grad) k_pes_eval3<CAIR_PES_N3_UMN, true><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
+    else k_pes_eval3<CAIR_PES_N3_UMN, false><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
+  }
+  if (int e = check_launch(h)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(V, d_V, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (grad) {
+    CUDA_TRY(h, cudaMemcpyAsync(dVdR, d_g, n * np * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(dVdQ, d_m, n * nv * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  }
+  return wait_stream(h);
+}
+
+int cair_rhs(cair_handle* h, int64_t n, const int32_t* ipes, const double* y, double* yp) {
+  if (!h || n < 0 || !y || !yp) return fail(h, CAIR_EINVAL, "cair_rhs: bad argument");
+  if (n == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_rhs: 4-atom systems not built");
+  if (int e = check_ipes(h, n, ipes)) return e;
+  if (int e = ensure_scratch(h, n * (4 + 24 * 8) + 1024)) return e;
+  Carver c{(char*)h->d_scratch};
+  int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
+  double *d_y = c.take<double>(n * 12), *d_yp = c.take<double>(n * 12);
+  if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_y, y, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int g = grid_for(h, n);
+  if (model_of(h) == CAIR_PES_O3_UMN) k_rhs3<CAIR_PES_O3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_yp);
+  else k_rhs3<CAIR_PES_N3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_yp);
+  if (int e = check_launch(h)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(yp, d_yp, n * 12 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return wait_stream(h);
+}
+
+int cair_hamiltonian(cair_handle* h, int64_t n, const int32_t* ipes, const double* paq, double* H, double* Rpi) {
+  if (!h || n < 0 || !paq || !H) return fail(h, CAIR_EINVAL, "cair_hamiltonian: bad argument");
+  if (n == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_hamiltonian: 4-atom systems not built");
+  if (int e = check_ipes(h, n, ipes)) return e;
+  if (int e = ensure_scratch(h, n * (4 + 16 * 8) + 1024)) return e;
+  Carver c{(char*)h->d_scratch};
+  int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
+  double *d_y = c.take<double>(n * 12), *d_H = c.take<double>(n), *d_r = c.take<double>(n * 3);
+  if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_y, paq, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int g = grid_for(h, n);
+  if (model_of(h) == CAIR_PES_O3_UMN)
+    k_hamiltonian3<CAIR_PES_O3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_H, d_r);
+  else k_hamiltonian3<CAIR_PES_N3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_H, d_r);
+  if (int e = check_launch(h)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(H, d_H, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (Rpi) CUDA_TRY(h, cudaMemcpyAsync(Rpi, d_r, n * 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return wait_stream(h);
+}
+
+int cair_bs_steps(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                  const double* erra, int32_t nattempts) {
+  if (!h || n < 0 || !paq || !t || !dt || !erra || nattempts < 0)
+    return fail(h, CAIR_EINVAL, "cair_bs_steps: bad argument");
+  if (n == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_bs_steps: 4-atom systems not built");
+  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_bs_steps: only NSteps = 3 is built");
+  if (int e = check_ipes(h, n, ipes)) return e;
+  if (int e = ensure_scratch(h, n * (4 + 26 * 8) + 2048)) return e;
+  Carver c{(char*)h->d_scratch};
+  int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
+  double *d_y = c.take<double>(n * 12), *d_t = c.take<double>(n), *d_dt = c.take<double>(n),
+         *d_e = c.take<double>(n * 12);
+  if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_y, paq, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_t, t, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_dt, dt, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_e, erra, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int g = grid_for(h, n);
+  if (model_of(h) == CAIR_PES_O3_UMN)
+    k_bs_steps3<CAIR_PES_O3_UMN, 3><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_t, d_dt, d_e, nattempts);
+  else k_bs_steps3<CAIR_PES_N3_UMN, 3><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_t, d_dt, d_e, nattempts);
+  if (int e = check_launch(h)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(paq, d_y, n * 12 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(t, d_t, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(dt, d_dt, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return wait_stream(h);
+}
+
+static int launch_integrate(cair_handle* h, const IntegrateArgs& A, cudaStream_t st) {
+  int m = model_of(h);
+  int block = 128, per_sm = 0;
+  if (m == CAIR_PES_O3_UMN)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate3<CAIR_PES_O3_UMN, 3>, block, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate3<CAIR_PES_N3_UMN, 3>, block, 0);
+  if (per_sm < 1) per_sm = 1;
+  int64_t g = (int64_t)h->nsm * per_sm;
+  int64_t need = (A.n + block - 1) / block;
+  if (g > need) g = need;
+  if (g < 1) g = 1;
+  if (m == CAIR_PES_O3_UMN) k_integrate3<CAIR_PES_O3_UMN, 3><<<(int)g, block, 0, st>>>(h->sys, A);
+  else k_integrate3<CAIR_PES_N3_UMN, 3><<<(int)g, block, 0, st>>>(h->sys, A);
+  return check_launch(h);
+}
+
+int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                       const double* erra, double* H, double* smax, double* smin, int32_t* irej, int32_t* iste,
+                       int32_t* status, int64_t max_attempts, void* stream) {
+  if (!h || n < 0 || !paq || !t || !dt || !erra || !H || !smax || !smin || !irej || !iste || !status ||
+      max_attempts < 1)
+    return fail(h, CAIR_EINVAL, "cair_integrate_dev: bad argument");
+  if (n == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: 4-atom systems not built");
+  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: only NSteps = 3 is built");
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
+  IntegrateArgs A{n, ipes, paq, t, dt, erra, H, smax, smin, irej, iste, status, max_attempts, h->d_ctl,
+                  h->d_ctl + 1};
+  return launch_integrate(h, A, st);
+}
+
+int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                   const double* erra, double* H, double* smax, double* smin, int32_t* irej, int32_t* iste,
+                   int32_t* status, int64_t max_attempts) {
+  if (!h || n < 0 || !paq || !t || !dt || !erra || !H || !smax || !smin || !irej || !iste || !status ||
+      max_attempts < 1)
+    return fail(h, CAIR_EINVAL, "cair_integrate: bad argument");
+  if (n == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: 4-atom systems not built");
+  if (int e = check_ipes(h, n, ipes)) return e;
+  const int ne = h->sys.ne;
+  size_t bytes = n * (3 * sizeof(int32_t) + sizeof(int32_t) + sizeof(double) * (2 * ne + 5)) + 16 * 256;
+  if (int e = ensure_scratch(h, bytes)) return e;
+  Carver c{(char*)h->d_scratch};
+  int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
+  double *d_y = c.take<double>(n * ne), *d_e = c.take<double>(n * ne), *d_t = c.take<double>(n),
+         *d_dt = c.take<double>(n), *d_H = c.take<double>(n), *d_smax = c.take<double>(n),
+         *d_smin = c.take<double>(n);
+  int32_t *d_irej = c.take<int32_t>(n), *d_iste = c.take<int32_t>(n), *d_st = c.take<int32_t>(n);
+  cudaStream_t st = h->stream;
+  if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_y, paq, n * ne * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_e, erra, n * ne * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_t, t, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_dt, dt, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_smax, smax, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_smin, smin, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_irej, irej, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_iste, iste, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
+  IntegrateArgs A{n, d_ip, d_y, d_t, d_dt, d_e, d_H, d_smax, d_smin, d_irej, d_iste, d_st, max_attempts,
+                  h->d_ctl, h->d_ctl + 1};
+  if (int e = launch_integrate(h, A, st)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(paq, d_y, n * ne * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(t, d_t, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(dt, d_dt, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(H, d_H, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(smax, d_smax, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(smin, d_smin, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(irej, d_irej, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(iste, d_iste, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(status, d_st, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  unsigned long long ctr[5];
+  CUDA_TRY(h, cudaMemcpyAsync(ctr, h->d_ctl + 1, sizeof(ctr), cudaMemcpyDeviceToHost, st));
+  if (int e = wait_stream(h)) return e;
+  for (int i = 0; i < 5; ++i) h->last_counters[i] = (long long)ctr[i];
+  return 0;
+}
+
+int cair_last_counters(cair_handle* h, int64_t* c5) {
+  if (!h || !c5) return CAIR_EINVAL;
+  unsigned long long ctr[5];
+  CUDA_TRY(h, cudaMemcpy(ctr, h->d_ctl + 1, sizeof(ctr), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 5; ++i) c5[i] = (int64_t)ctr[i];
+  return 0;
+}
+
+int cair_apply_transformation(cair_handle* h, int64_t n, const double* paq, double* out) {
+  if (!h || n < 0 || !paq || !out) return fail(h, CAIR_EINVAL, "cair_apply_transformation: bad argument");
+  if (n == 0) return 0;
+  const int ne = h->sys.ne;
+  if (int e = ensure_scratch(h, n * 2 * ne * 8 + 1024)) return e;
+  Carver c{(char*)h->d_scratch};
+  double *d_a = c.take<double>(n * ne), *d_b = c.take<double>(n * ne);
+  CUDA_TRY(h, cudaMemcpyAsync(d_a, paq, n * ne * 8, cudaMemcpyHostToDevice, h->stream));
+  k_apply_transformation<<<grid_for(h, n), 128, 0, h->stream>>>(h->sys, n, d_a, d_b);
+  if (int e = check_launch(h)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(out, d_b, n * ne * 8, cudaMemcpyDeviceToHost, h->stream));
+  return wait_stream(h);
+}
+
+int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_point* out) {
+  if (!h || n < 0 || !paq_vel || !out) return fail(h, CAIR_EINVAL, "cair_find_state: bad argument");
+  if (n == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_find_state: 4-atom analysis not built");
+  if (int e = ensure_scratch(h, n * (12 * 8 + sizeof(cair_traj_point)) + 1024)) return e;
+  Carver c{(char*)h->d_scratch};
+  double* d_p = c.take<double>(n * 12);
+  cair_traj_point* d_o = c.take<cair_traj_point>(n);
+  CUDA_TRY(h, cudaMemcpyAsync(d_p, paq_vel, n * 12 * 8, cudaMemcpyHostToDevice, h->stream));
+  k_find_state3<<<grid_for(h, n), 128, 0, h->stream>>>(h->sys, h->fs, n, d_p, d_o);
+  if (int e = check_launch(h)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(out, d_o, n * sizeof(cair_traj_point), cudaMemcpyDeviceToHost, h->stream));
+  return wait_stream(h);
+}
+
+int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, double* fa, double* ex) {
+  if (!h || ipes < 0 || ipes >= h->sys.npes) return CAIR_EINVAL;
+  // Counted from the executed formulation: PIP part from the generator's operation
+  // counts, plus MEG variables, diatomics, pair distances, TransToCart and the RHS.
+  const int m = h->sys.pes[ipes].model;
+  const bool o2 = h->sys.diat == CAIR_DIAT_O2_UMN;
+  // per pair: diatomic energy+gradient and MEG with its derivative
+  double diat_g = o2 ? 8 * 4 + 30 : 40, diat_e = o2 ? 8 * 2 + 20 : 24;
+  double meg_g = 9, meg_e = 6;
+  double pip_g = m == CAIR_PES_O3_UMN ? PIP_O3_EVAL_FLOPS : PIP_N3_EVAL_FLOPS;
+  double pip_e = m == CAIR_PES_O3_UMN ? PIP_O3_VALUE_FLOPS : PIP_N3_VALUE_FLOPS;
+  double geom = 3 * 8 + 6;          // pair distances + last atom
+  double t2c = 3 + 6 * 6 + 4;       // TransToCart_3Atoms
+  double rhs = 12 + 6;              // dq/dt and sign flip
+  if (fg) *fg = pip_g + 3 * (diat_g + meg_g) + geom + t2c + rhs + 8;
+  if (fe) *fe = pip_e + 3 * (diat_e + meg_e) + geom + 6 * 4 + 3;
+  // per attempt outside the surface: mmidv updates, extrapolation, error norms
+  if (fa) *fa = 12 * (2 * 13 + 3 * 3) + 12 * 3 * 8 + 12 * 2 * 3 + 20;
+  if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1);
+  return 0;
+}
+
+}  // extern "C"
+

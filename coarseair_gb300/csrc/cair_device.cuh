@@ -1,0 +1,458 @@
+// Device-side building blocks of the GB300 trajectory path: diatomic potentials, MEG
+// variables, the UMN surfaces with analytic gradients, pair distances, Hamilton's
+// equations and the Bulirsch-Stoer attempt.  FP64 throughout; one thread owns one
+// trajectory and keeps its phase-space state in registers.
+#pragma once
+#include <cstdint>
+#include "../../include/cair_gpu.h"
+
+#define CAIR_B_TO_ANG 0.52917721092
+#define CAIR_KCM_TO_HARTREE 0.159360144e-2
+#define CAIR_KCMANG_TO_HARTB 0.843297564e-3
+
+namespace cair {
+
+struct DevPes {
+  int32_t model;
+  int32_t ncoef;
+  const double* coef;   // device copy of C(1:ncoef)
+  double a, ab, ra, rb; // MEG parameters
+  double inv_a;         // One/This%a, evaluated once on the host
+};
+
+struct DevSys {
+  int32_t natoms, nv, ne, npairs, npes, nsteps, ncall, incstp, diat;
+  double mMiMn[3];
+  double Tpq[81];       // column-major (i,j) -> [i + 9 j]
+  double relax, rmax, tmax, rpimax;
+  double o2_ab[8];      // alpha * beta**k          (O2_UMN Ev2gm2 exponent factors)
+  double o2_cd[8];      // 2 * a(k) * alpha * beta**k (O2_UMN Ev2gm2_Grad factors)
+  DevPes pes[CAIR_MAX_PES];
+};
+
+// ------------------------------------------------------------------------------------------
+// Diatomic potentials
+// ------------------------------------------------------------------------------------------
+__device__ __constant__ static const double kO2A[8] = {
+    -1.488979427684798e3, 1.881435846488955e4, -1.053475425838226e5, 2.755135591229064e5,
+    -4.277588997761775e5, 4.404104009614092e5, -2.946204062950765e5, 1.176861219078620e5};
+
+// O2 UMN dispersion (O2_UMN_DiatomicPotential_Class.F90 edisp / edisp_Grad)
+template <bool GRAD>
+__device__ __forceinline__ void o2_disp(double rb, double& vd, double& dvd) {
+  const double r2r4 = 2.59361680, rs6 = 0.5299, rs8 = 2.20, c6 = 12.8;
+  const double c8step = 3.0 * c6 * (r2r4 * r2r4);
+  double tmp = sqrt(c8step / c6);
+  double ss = rs6 * tmp + rs8;
+  double s2 = ss * ss, s3 = s2 * ss, s6 = s3 * s3, s4 = s2 * s2, s8 = s4 * s4;
+  double r2 = rb * rb, r3 = r2 * rb, r4 = r2 * r2, r6 = r3 * r3, r8 = r4 * r4;
+  double d6 = r6 + s6, d8 = r8 + s8;
+  double e6 = c6 / d6, e8 = c8step / d8;
+  vd = -e6 - 2.0 * e8;
+  if (GRAD) {
+    double r5 = r4 * rb, r7 = r4 * r3;
+    double e6dr = c6 * (-6.0 * r5) / (d6 * d6);
+    double e8dr = c8step * (-8.0 * r7) / (d8 * d8);
+    dvd = (-e6dr - 2.0 * e8dr) / CAIR_B_TO_ANG;
+  }
+}
+
+// O2 UMN (Ev2gm2 / Ev2gm2_Grad): V [Eh] and dV/dR [Eh/bohr] for R in bohr
+template <bool GRAD>
+__device__ __forceinline__ void o2_umn(const DevSys& S, double r, double& v, double& dv) {
+  double rang = r * CAIR_B_TO_ANG;
+  double r2 = rang * rang;
+  double vv = 0.0, dd = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    double e = exp(-(S.o2_ab[k] * r2));
+    vv = vv + kO2A[k] * e;
+    if (GRAD) dd = dd - S.o2_cd[k] * rang * e;
+  }
+  vv = vv * 1.e-3;
+  double vd, dvd = 0.0;
+  o2_disp<GRAD>(rang / CAIR_B_TO_ANG, vd, dvd);
+  v = vv + vd;
+  if (GRAD) dv = (dd * 1.e-3 + dvd) * CAIR_B_TO_ANG;
+}
+
+// N2 UMN_ForN4 (Ev2gm2 / Ev2gm2_Grad): V [Eh], dV/dR [Eh/bohr]
+template <bool GRAD>
+__device__ __forceinline__ void n2_umn(double r, double& v, double& dv) {
+  const double cs0 = 2.70963254293, cs1 = 1.32620177271e-1, cs2 = 2.96757048793e-1,
+               cs3 = 1.97112432229e-1, cs4 = -5.02002309588e-1, cs5 = 3.80734244606e-1,
+               cs6 = 1.21001628750;
+  const double de = 228.7, red = 1.098, red4 = 1.4534810048;
+  double rang = r * CAIR_B_TO_ANG;
+  double r3 = (rang * rang) * rang;
+  double r4 = r3 * rang;
+  double ts = r4 + red4;
+  double y = (r4 - red4) / ts;
+  double y2 = y * y, y3 = y2 * y, y4 = y2 * y2, y5 = y3 * y2, y6 = y3 * y3;
+  double fy = cs0 + cs1 * y + cs2 * y2 + cs3 * y3 + cs4 * y4 + cs5 * y5 + cs6 * y6;
+  double u = exp(-(fy * (rang - red)));
+  double minu = 1.0 - u;
+  v = (de * (minu * minu) - de) * CAIR_KCM_TO_HARTREE + 0.0;
+  if (GRAD) {
+    double dfdy = cs1 + 2.0 * cs2 * y + 3.0 * cs3 * y2 + 4.0 * cs4 * y3 + 5.0 * cs5 * y4 + 6.0 * cs6 * y5;
+    double dydr = 8.0 * r3 * red4 / (ts * ts);
+    double dfdr = dfdy * dydr;
+    double dvk = 2.0 * de * minu * u * (dfdr * (rang - red) + fy);
+    dv = dvk * CAIR_KCM_TO_HARTREE * CAIR_B_TO_ANG;
+  }
+}
+
+template <bool GRAD>
+__device__ __forceinline__ void diat(const DevSys& S, double r, double& v, double& dv) {
+  if (S.diat == CAIR_DIAT_O2_UMN) o2_umn<GRAD>(S, r, v, dv);
+  else n2_umn<GRAD>(r, v, dv);
+}
+
+}  // namespace cair
+
+#include "generated/pip_n3.cuh"
+#include "generated/pip_o3.cuh"
+
+namespace cair {
+
+// ------------------------------------------------------------------------------------------
+// TransToCart (PES_Class.F90:252-360, implementation 2)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void trans_to_cart_3(const DevSys& S, const double* R, const double* Q,
+                                                const double* dVdR, double* m) {
+  double d0 = dVdR[0] / R[0], d1 = dVdR[1] / R[1], d2 = dVdR[2] / R[2];
+  double m1 = S.mMiMn[0], m2 = S.mMiMn[1];
+  double a1 = (1.0 - m1) * d1, b1 = m1 * d2, a2 = m2 * d1, b2 = (1.0 - m2) * d2;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double X0 = Q[c] - Q[3 + c], X1 = Q[c] - Q[6 + c], X2 = Q[3 + c] - Q[6 + c];
+    m[c] = d0 * X0 + a1 * X1 - b1 * X2;
+    m[3 + c] = -(d0 * X0) - a2 * X1 + b2 * X2;
+  }
+}
+
+__device__ __forceinline__ void trans_to_cart_4(const DevSys& S, const double* R, const double* Q,
+                                                const double* dVdR, double* m) {
+  double d[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) d[i] = dVdR[i] / R[i];
+  double m1 = S.mMiMn[0], m2 = S.mMiMn[1], m3 = S.mMiMn[2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double X0 = Q[c] - Q[3 + c], X1 = Q[c] - Q[6 + c], X2 = Q[c] - Q[9 + c];
+    double X3 = Q[3 + c] - Q[6 + c], X4 = Q[3 + c] - Q[9 + c], X5 = Q[6 + c] - Q[9 + c];
+    m[c] = d[0] * X0 + d[1] * X1 + (1.0 - m1) * d[2] * X2 - m1 * d[4] * X4 - m1 * d[5] * X5;
+    m[3 + c] = -(d[0] * X0) - m2 * d[2] * X2 + d[3] * X3 + (1.0 - m2) * d[4] * X4 - m2 * d[5] * X5;
+    m[6 + c] = -(d[1] * X1) - m3 * d[2] * X2 - d[3] * X3 - m3 * d[4] * X4 + (1.0 - m3) * d[5] * X5;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Surfaces.  GRAD = false gives PES%Potential (energy only).
+// ------------------------------------------------------------------------------------------
+// O3 UMN (Compute_O3_UMN_PES_1d, O3_UMN_PES_Class.F90:259-326)
+template <bool GRAD>
+__device__ __forceinline__ void pes_o3(const DevSys& S, const DevPes& P, const double* R, const double* Q,
+                                       double& V, double* dVdR, double* dVdQ) {
+  double x[3], dx[3], vd[3], dvd[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double rang = R[i] * CAIR_B_TO_ANG;
+    double d1 = rang - P.ra, d2 = rang - P.rb;
+    double e = exp(-(d1 / P.a) - (d2 * d2) / P.ab);
+    x[i] = e;
+    if (GRAD) dx[i] = (-(2.0 * d2 / P.ab) - P.inv_a) * e;
+    diat<GRAD>(S, R[i], vd[i], dvd[i]);
+  }
+  double vdiat = (vd[0] + vd[1]) + vd[2];
+  double vp;
+  const double* __restrict__ C = P.coef;
+  if (GRAD) {
+    double g[3];
+    pip_o3_eval(x, dx, C, 0.0, vp, g);
+    V = (vp * CAIR_KCM_TO_HARTREE) + vdiat;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dVdR[i] = g[i] * CAIR_KCMANG_TO_HARTB + dvd[i];
+    trans_to_cart_3(S, R, Q, dVdR, dVdQ);
+  } else {
+    pip_o3_value(x, C, 0.0, vp);
+    V = (vp * CAIR_KCM_TO_HARTREE) + vdiat;
+  }
+}
+
+// N3 UMN (Compute_N3_UMN_PES_1d, N3_UMN_PES_Class.F90:332-382, on the N4 PIP with the
+// three pinned 10^3-bohr pairs contributing exact zeros)
+template <bool GRAD>
+__device__ __forceinline__ void pes_n3(const DevSys& S, const DevPes& P, const double* R, const double* Q,
+                                       double& V, double* dVdR, double* dVdQ) {
+  double x[6], dx[6], vd[3], dvd[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    double d = R[i] * CAIR_B_TO_ANG - 1.098;
+    double e = exp(-d - (d * d) / 1.5);
+    int j = i == 2 ? 3 : i;  // RTemp(1), RTemp(2), RTemp(4)
+    x[j] = e;
+    if (GRAD) dx[j] = (-(2.0 * d / 1.5) - 1.0) * e;
+    diat<GRAD>(S, R[i], vd[i], dvd[i]);
+  }
+  x[2] = x[4] = x[5] = 0.0;
+  dx[2] = dx[4] = dx[5] = 0.0;
+  double vdiat = ((0.0 + vd[0]) + vd[1]) + vd[2];
+  double vp;
+  const double* __restrict__ C = P.coef;
+  if (GRAD) {
+    double g[3];
+    pip_n3_eval(x, dx, C, 457.4, vp, g);
+    V = vdiat + (vp + 0.0) * CAIR_KCM_TO_HARTREE;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dVdR[i] = dvd[i] + g[i] * CAIR_KCM_TO_HARTREE * CAIR_B_TO_ANG;
+    trans_to_cart_3(S, R, Q, dVdR, dVdQ);
+  } else {
+    pip_n3_value(x, C, 457.4, vp);
+    V = vdiat + (vp + 0.0) * CAIR_KCM_TO_HARTREE;
+  }
+}
+
+template <int MODEL, bool GRAD>
+__device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const double* R, const double* Q,
+                                    double& V, double* dVdR, double* dVdQ) {
+  if (MODEL == CAIR_PES_O3_UMN) pes_o3<GRAD>(S, P, R, Q, V, dVdR, dVdQ);
+  else pes_n3<GRAD>(S, P, R, Q, V, dVdR, dVdQ);
+}
+
+// ------------------------------------------------------------------------------------------
+// Pair distances (Compute_Rp_CartCoord_3Atoms, Collision_Class.F90:2244-2275); Q has room
+// for the last atom, which is written to Q[NV..NV+2].
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void rp3(const DevSys& S, double* Q, double* Rp) {
+  const double m1 = S.mMiMn[0], m2 = S.mMiMn[1];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) Q[6 + c] = m1 * Q[c] + m2 * Q[3 + c];
+  double a, b, c;
+  a = Q[0] - Q[3]; b = Q[1] - Q[4]; c = Q[2] - Q[5];
+  Rp[0] = sqrt(a * a + b * b + c * c);
+  a = Q[0] - Q[6]; b = Q[1] - Q[7]; c = Q[2] - Q[8];
+  Rp[1] = sqrt(a * a + b * b + c * c);
+  a = Q[3] - Q[6]; b = Q[4] - Q[7]; c = Q[5] - Q[8];
+  Rp[2] = sqrt(a * a + b * b + c * c);
+}
+
+// ------------------------------------------------------------------------------------------
+// Hamilton's equations (ODE_System.F90:45-96) for 3 atoms: y = [p(6), q(6)]
+// ------------------------------------------------------------------------------------------
+template <int MODEL>
+struct Rhs3 {
+  const DevSys& S;
+  const DevPes& P;
+  __device__ Rhs3(const DevSys& s, const DevPes& p) : S(s), P(p) {}
+  __device__ __forceinline__ void operator()(const double (&y)[12], double (&yp)[12]) const {
+    // dq_j/dt = sum_{i = j mod 3, ascending} Tpq(j,i) p_i
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      int i0 = j % 3;
+      double acc = 0.0 + S.Tpq[j + 9 * i0] * y[i0];
+      acc = acc + S.Tpq[j + 9 * (i0 + 3)] * y[i0 + 3];
+      yp[6 + j] = acc;
+    }
+    double Q[9], R[3], V, dVdR[3], dVdQ[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) Q[i] = y[6 + i];
+    rp3(S, Q, R);
+    pes<MODEL, true>(S, P, R, Q, V, dVdR, dVdQ);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) yp[i] = -dVdQ[i];
+  }
+};
+
+// Hamiltonian_1d (Collision_Class.F90:2046-2111) for 3 atoms; returns H, fills Rpi
+template <int MODEL>
+__device__ __forceinline__ double hamiltonian3(const DevSys& S, const DevPes& P, const double (&y)[12],
+                                               double (&Rpi)[3]) {
+  double h = 0.0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    int j0 = i % 3;
+    double eki = 0.0 + S.Tpq[j0 + 9 * i] * y[j0];
+    eki = eki + S.Tpq[j0 + 3 + 9 * i] * y[j0 + 3];
+    h = h + y[i] * eki;
+  }
+  double Q[9], R[3], V;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) Q[i] = y[6 + i];
+  rp3(S, Q, R);
+  pes<MODEL, false>(S, P, R, Q, V, nullptr, nullptr);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) Rpi[k] = 1.0 / R[k];
+  return h * 0.5 + V;
+}
+
+// ------------------------------------------------------------------------------------------
+// Bulirsch-Stoer attempt (Integrate_ODE_1d, ODE_Solver.F90:225-358; mmidv 363-462;
+// RatPolExtrap 467-541), one trajectory, NS extrapolation steps.
+// ------------------------------------------------------------------------------------------
+__host__ __device__ constexpr int nseq_of(int i) {
+  return i == 0 ? 2 : i == 1 ? 4 : i == 2 ? 6 : i == 3 ? 8 : i == 4 ? 12 : i == 5 ? 16 : i == 6 ? 24 : 32;
+}
+
+// |a - b| / s < 1 exactly as IEEE division then comparison would decide, without the
+// division in the common case: fl(|d|/s) < 1  <=>  |d| < s and fl(|d|/s) != 1.
+__device__ __forceinline__ bool err_below_one(double d, double s) {
+  double ad = fabs(d), as = fabs(s);
+  if (ad < as * 0.99999999999999) return true;
+  if (!(ad < as)) return false;
+  return fabs(d / s) < 1.0;
+}
+
+// Extrapolation step `S1` (1-based) of RatPolExtrap for one system of NE equations.
+// d holds the columns 1..NS-1 of the reference's d table (column NS is only ever read
+// as zero); yt receives ytry(:, S1) for S1 < NS, ylast receives ytry(:, NS).
+template <int S1, int NE, int NS>
+__device__ __forceinline__ void extrap_stage(const double (&yest)[NE], const double (&xs)[NS],
+                                             double (&d)[NS - 1][NE], double (&yt)[NS - 1][NE],
+                                             double (&ylast)[NE]) {
+  const double xest = xs[S1 - 1];
+  if (S1 == 1) {
+#pragma unroll
+    for (int j = 0; j < NE; ++j) {
+      if (NS > 1) { yt[0][j] = yest[j]; d[0][j] = yest[j]; }
+      else ylast[j] = yest[j];
+    }
+    return;
+  }
+  constexpr int m1 = S1 < NS ? S1 : NS;
+  double fx[NS + 1];
+#pragma unroll
+  for (int k = 1; k <= m1 - 1; ++k) fx[k + 1] = xs[S1 - k - 1] / xest;
+#pragma unroll
+  for (int j = 0; j < NE; ++j) {
+    double yy = yest[j], v = d[0][j], c = yy;
+    d[0][j] = yy;
+#pragma unroll
+    for (int k = 2; k <= m1; ++k) {
+      double b1 = fx[k] * v;
+      double b = (c - v) / ((b1 - c) + 1.0E-40);
+      double ddy = c * b;
+      c = b1 * b;
+      // column k was written at an earlier stage unless k == S1 (then it is still zero)
+      v = (k < S1 && k - 1 < NS - 1) ? d[k - 1][j] : 0.0;
+      if (k - 1 < NS - 1) d[k - 1][j] = ddy;
+      yy = yy + ddy;
+    }
+    if (S1 < NS) yt[S1 - 1][j] = yy;
+    else ylast[j] = yy;
+  }
+}
+
+template <int NE, int NS>
+__device__ __forceinline__ void extrap_dispatch(int stage, const double (&yest)[NE], const double (&xs)[NS],
+                                                double (&d)[NS - 1][NE], double (&yt)[NS - 1][NE],
+                                                double (&ylast)[NE]) {
+  switch (stage) {
+    case 1: extrap_stage<1, NE, NS>(yest, xs, d, yt, ylast); break;
+    case 2: if (NS >= 2) extrap_stage<(NS >= 2 ? 2 : 1), NE, NS>(yest, xs, d, yt, ylast); break;
+    case 3: if (NS >= 3) extrap_stage<(NS >= 3 ? 3 : 1), NE, NS>(yest, xs, d, yt, ylast); break;
+    case 4: if (NS >= 4) extrap_stage<(NS >= 4 ? 4 : 1), NE, NS>(yest, xs, d, yt, ylast); break;
+    default: break;
+  }
+}
+
+__host__ __device__ constexpr int nseq_total(int ns) { return ns == 0 ? 1 : nseq_of(ns - 1) + nseq_total(ns - 1); }
+
+__device__ __forceinline__ double htemp_of(int stage) {
+  // One / dfloat(nseq(iSteps)), folded at compile time (same value as the division)
+  return stage == 1 ? 1.0 / 2.0 : stage == 2 ? 1.0 / 4.0 : stage == 3 ? 1.0 / 6.0 : 1.0 / 8.0;
+}
+
+// One Bulirsch-Stoer attempt.  The 1 + sum(nseq) right-hand-side evaluations of the
+// attempt run through a single call site of f, so the surface is inlined once and every
+// thread of a warp evaluates its right-hand side in lockstep.
+template <int NE, int NS, class F>
+__device__ __forceinline__ int bs_attempt(const F& f, double (&y)[NE], double& x, double& h,
+                                          const double* __restrict__ yscal, double relax, bool incstp,
+                                          double& smax, double& smin, int& irej, int& iste) {
+  static_assert(NS >= 2 && NS <= 4, "NSteps 2..4 are built");
+  constexpr int NTOT = nseq_total(NS);
+  double dydx[NE], ym[NE], yn[NE], fo[NE], ylast[NE];
+  double d[NS - 1][NE], yt[NS - 1][NE], xs[NS];
+#pragma unroll
+  for (int i = 0; i < NE; ++i) yn[i] = y[i];
+  int stage = 0, sub = 0, nst = 1;
+  double hs = 0.0, h2 = 0.0;
+#pragma unroll 1
+  for (int e = 0; e < NTOT; ++e) {
+    f(yn, fo);
+    if (stage == 0 || sub == nst) {
+      if (stage == 0) {
+#pragma unroll
+        for (int i = 0; i < NE; ++i) dydx[i] = fo[i];
+      } else {
+        // end of mmidv: yout = Half*(ym + yn + h*yout), then the extrapolation
+#pragma unroll
+        for (int i = 0; i < NE; ++i) fo[i] = 0.5 * (ym[i] + yn[i] + hs * fo[i]);
+        const double hh = h * htemp_of(stage);
+        xs[stage - 1] = hh * hh;
+        extrap_dispatch<NE, NS>(stage, fo, xs, d, yt, ylast);
+      }
+      ++stage;
+      if (stage <= NS) {
+        nst = nseq_of(stage - 1);
+        hs = h * htemp_of(stage);
+        h2 = 2.0 * hs;
+        sub = 1;
+#pragma unroll
+        for (int i = 0; i < NE; ++i) { ym[i] = y[i]; yn[i] = y[i] + hs * dydx[i]; }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < NE; ++i) {
+        double ys = ym[i] + h2 * fo[i];
+        ym[i] = yn[i];
+        yn[i] = ys;
+      }
+      ++sub;
+    }
+  }
+  // errmax(k) < 1 for k = 1..NS-1
+  bool below[NS - 1];
+  int nan = 0;
+#pragma unroll
+  for (int k = 0; k < NS - 1; ++k) {
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+      double dd = yt[k][i] - ylast[i];
+      if (dd != dd) nan = 1;
+      ok = err_below_one(dd, __ldg(yscal + i)) && ok;
+    }
+    below[k] = ok;
+  }
+  int iconv = 0;
+#pragma unroll
+  for (int is = 2; is <= NS; ++is) {
+    int j = NS + 1 - is;
+    if (!below[j - 1]) break;
+    iconv = j;
+  }
+  if (below[NS - 2]) {
+    x = x + h;
+#pragma unroll
+    for (int i = 0; i < NE; ++i) y[i] = ylast[i];
+    smin = (smin < h) ? smin : h;
+    smax = (smax > h) ? smax : h;
+    iste += 1;
+    if (iconv < NS - 1 && incstp) {
+      double ratio = 0.0;
+#pragma unroll
+      for (int k = 1; k < NS - 1; ++k)
+        if (iconv == k) ratio = (double)nseq_of(NS - 1) / (double)nseq_of(k);
+      h = h * (ratio + relax) / (1.0 + relax);
+    }
+  } else {
+    constexpr int kk = (NS / 2) < 1 ? 1 : NS / 2;
+    h = h / (double)nseq_of(kk - 1);
+    irej += 1;
+  }
+  return nan;
+}
+
+}  // namespace cair

@@ -1,0 +1,448 @@
+// GB300 kernels of the trajectory path: batched surface evaluation, right-hand side,
+// Hamiltonian, fixed-count Bulirsch-Stoer attempts, the persistent end-to-end integrator
+// and the final-state analysis.  One thread owns one trajectory.
+#pragma once
+#include "cair_device.cuh"
+
+namespace cair {
+
+// ------------------------------------------------------------------------------------------
+// Batched PES%Compute / PES%Potential (3 atoms)
+// ------------------------------------------------------------------------------------------
+template <int MODEL, bool GRAD>
+__global__ void __launch_bounds__(128) k_pes_eval3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                                   const double* __restrict__ Rin, const double* __restrict__ Qin,
+                                                   double* __restrict__ V, double* __restrict__ dVdR,
+                                                   double* __restrict__ dVdQ) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const DevPes& P = S.pes[ipes ? ipes[k] : 0];
+    double R[3], Q[9], v, g[3], m[6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) R[i] = Rin[3 * k + i];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Q[i] = Qin[9 * k + i];
+    pes<MODEL, GRAD>(S, P, R, Q, v, g, m);
+    V[k] = v;
+    if (GRAD) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) dVdR[3 * k + i] = g[i];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) dVdQ[6 * k + i] = m[i];
+    }
+  }
+}
+
+template <int MODEL>
+__global__ void __launch_bounds__(128) k_rhs3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                              const double* __restrict__ y, double* __restrict__ yp) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    Rhs3<MODEL> f(S, S.pes[ipes ? ipes[k] : 0]);
+    double a[12], b[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) a[i] = y[12 * k + i];
+    f(a, b);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) yp[12 * k + i] = b[i];
+  }
+}
+
+template <int MODEL>
+__global__ void __launch_bounds__(128) k_hamiltonian3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                                      const double* __restrict__ paq, double* __restrict__ H,
+                                                      double* __restrict__ Rpi) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    double y[12], r[3];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) y[i] = paq[12 * k + i];
+    H[k] = hamiltonian3<MODEL>(S, S.pes[ipes ? ipes[k] : 0], y, r);
+    if (Rpi) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Rpi[3 * k + i] = r[i];
+    }
+  }
+}
+
+template <int MODEL, int NS>
+__global__ void __launch_bounds__(128) k_bs_steps3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                                   double* __restrict__ paq, double* __restrict__ t,
+                                                   double* __restrict__ dt, const double* __restrict__ erra,
+                                                   int32_t nattempts) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    Rhs3<MODEL> f(S, S.pes[ipes ? ipes[k] : 0]);
+    double y[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) y[i] = paq[12 * k + i];
+    double x = t[k], h = dt[k], smax = 0.0, smin = 0.0;
+    int irej = 0, iste = 0;
+#pragma unroll 1
+    for (int a = 0; a < nattempts; ++a)
+      bs_attempt<12, NS>(f, y, x, h, erra + 12 * k, S.relax, S.incstp != 0, smax, smin, irej, iste);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) paq[12 * k + i] = y[i];
+    t[k] = x;
+    dt[k] = h;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Persistent integrator: every thread takes a trajectory from the device work queue,
+// integrates it to the end of the collision (ncall attempts, then the end check of
+// Integrator_Class.F90:457-465) and takes the next one.  Finished threads refill
+// immediately, so the attempt loop of a warp stays converged while trajectory lengths
+// differ by orders of magnitude.
+// ------------------------------------------------------------------------------------------
+struct IntegrateArgs {
+  int64_t n;
+  const int32_t* ipes;
+  double* paq;
+  double* t;
+  double* dt;
+  const double* erra;
+  double* H;
+  double* smax;
+  double* smin;
+  int32_t* irej;
+  int32_t* iste;
+  int32_t* status;
+  int64_t max_attempts;
+  unsigned long long* queue;    // next trajectory index
+  unsigned long long* counters; // attempts, accepted, rejected, grad evals, energy evals
+};
+
+template <int MODEL, int NS>
+__global__ void __launch_bounds__(128) k_integrate3(DevSys S, IntegrateArgs A) {
+  unsigned long long c_att = 0, c_acc = 0, c_rej = 0;
+  const bool incstp = S.incstp != 0;
+  const int ncall = S.ncall;
+  for (;;) {
+    const unsigned long long k = atomicAdd(A.queue, 1ull);
+    if (k >= (unsigned long long)A.n) break;
+    const int ip = A.ipes ? A.ipes[k] : 0;
+    const DevPes& P = S.pes[ip];
+    Rhs3<MODEL> f(S, P);
+    double y[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) y[i] = A.paq[12 * k + i];
+    double x = A.t[k], h = A.dt[k], smax = A.smax[k], smin = A.smin[k], H = 0.0;
+    int irej = A.irej[k], iste = A.iste[k];
+    const int irej0 = irej, iste0 = iste;
+    int64_t att = 0;
+    int st = CAIR_TRAJ_ATTEMPT_CAP;
+    const double* yscal = A.erra + 12 * k;
+#pragma unroll 1
+    for (;;) {
+      int bad = 0;
+#pragma unroll 1
+      for (int c = 0; c < ncall; ++c) bad |= bs_attempt<12, NS>(f, y, x, h, yscal, S.relax, incstp, smax, smin, irej, iste);
+      att += ncall;
+      double rpi[3];
+      H = hamiltonian3<MODEL>(S, P, y, rpi);
+      if (bad) { st = CAIR_TRAJ_NONFINITE; break; }
+      bool conv = x > S.tmax;
+#pragma unroll
+      for (int p = 0; p < 3; ++p) conv = conv || (rpi[p] < S.rpimax);
+      if (conv) { st = CAIR_TRAJ_DONE; break; }
+      if (att >= A.max_attempts) break;
+    }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) A.paq[12 * k + i] = y[i];
+    A.t[k] = x;
+    A.dt[k] = h;
+    A.H[k] = H;
+    A.smax[k] = smax;
+    A.smin[k] = smin;
+    A.irej[k] = irej;
+    A.iste[k] = iste;
+    A.status[k] = st;
+    c_att += att;
+    c_acc += iste - iste0;
+    c_rej += irej - irej0;
+  }
+  if (c_att) {
+    atomicAdd(A.counters + 0, c_att);
+    atomicAdd(A.counters + 1, c_acc);
+    atomicAdd(A.counters + 2, c_rej);
+    atomicAdd(A.counters + 3, c_att * (unsigned long long)nseq_total(NS));
+    atomicAdd(A.counters + 4, c_att / (unsigned long long)(ncall > 0 ? ncall : 1));
+  }
+}
+
+// ApplyTransformation (Collision_Class.F90:2406-2432), any NEqtVar
+__global__ void k_apply_transformation(DevSys S, int64_t n, const double* __restrict__ paq,
+                                       double* __restrict__ out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int nv = S.nv, ne = S.ne;
+    for (int i = 0; i < ne; ++i) out[ne * k + i] = paq[ne * k + i];
+    for (int i = 0; i < nv; ++i) {
+      double a = 0.0;
+      for (int j = 0; j < nv; ++j) a = a + S.Tpq[i + 9 * j] * paq[ne * k + j];
+      out[ne * k + i] = a;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Final-state analysis (TrajectoryPoint_Class.F90:128-495, MolecularState_Class.F90:61-429,
+// DiatomicPotential_Class.F90:626-1009)
+// ------------------------------------------------------------------------------------------
+struct FsArgs {
+  int32_t nquad;
+  double rsmal, rcent, rfact, tthresau, vinf;
+  const double* gx;   // Chebyshev-2 nodes (ascending)
+  const double* gw;   // weights already divided by sqrt(1 - x^2)
+  double mass[4];
+};
+
+__device__ __forceinline__ double diat_v(const DevSys& S, double r) {
+  double v, dv;
+  diat<false>(S, r, v, dv);
+  return v;
+}
+__device__ __forceinline__ double eff_pot(const DevSys& S, double r, double vc_r2) {
+  return diat_v(S, r) + vc_r2 / (r * r);
+}
+
+__device__ int turning_point(const DevSys& S, double ra, double rc, double vc_r2, double eint, int nbis, int nnew,
+                             double& rt_out) {
+  double rt = 0.0;
+  if (nbis > 0) {
+    double va = eff_pot(S, ra, vc_r2) - eint;
+    double vc = eff_pot(S, rc, vc_r2) - eint;
+    double v2 = vc * va;
+    if (v2 > 0.0 && v2 > 1.0E-10) { rt_out = 0.0; return 1; }
+    for (int it = 0; it < nbis; ++it) {
+      rt = 0.5 * (ra + rc);
+      double vb = eff_pot(S, rt, vc_r2) - eint;
+      v2 = vb * va;
+      if (v2 > 0.0) { ra = rt; va = vb; } else { rc = rt; vc = vb; }
+    }
+  }
+  for (int it = 0; it < nnew; ++it) {
+    double vcen = vc_r2 / (rt * rt), vb, dvb;
+    diat<true>(S, rt, vb, dvb);
+    double v = vb + vcen;
+    double dv = dvb - 2.0 * vcen / rt;
+    rt = rt + (eint - v) / dv;
+  }
+  rt_out = rt;
+  return 0;
+}
+
+__device__ double action_integral(const DevSys& S, const FsArgs& F, double ri, double ro, double vc_r2,
+                                  double eint, double twomu) {
+  const int n = F.nquad;
+  double rm = (ro - ri) * 0.5;
+  double rp = (ro + ri) * 0.5 + rm * F.gx[0];
+  double act = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double e = eint - eff_pot(S, rp, vc_r2);
+    if (!(e > 0.0)) e = -e;
+    act = act + sqrt(e) * F.gw[i];
+    if (i != n - 1) rp = rp + rm * (F.gx[i + 1] - F.gx[i]);
+  }
+  return 2.0 * sqrt(twomu) * act * rm;
+}
+
+__device__ int find_extremum(const DevSys& S, double sig, double re, double rlim, double vc_r2, double tol,
+                             double& rout, double& vout) {
+  const double factor = 0.3819660115, step = 0.005;
+  double vlast = eff_pot(S, re, vc_r2) * sig;
+  double ri = re, vtry = 0.0;
+  for (;;) {
+    ri = ri + step;
+    if (ri >= rlim) { rout = ri - step; vout = vlast * sig; return 1; }
+    vtry = eff_pot(S, ri, vc_r2) * sig;
+    if (vtry > vlast) break;
+    vlast = vtry;
+  }
+  double rb = ri - step, vb = vlast, rc = ri, ra = rb - step;
+  for (int it = 0; it < 100000; ++it) {
+    double rt1, vt1;
+    if (rb - ra > rc - rb) {
+      rt1 = (ra - rb) * factor + rb;
+      vt1 = eff_pot(S, rt1, vc_r2) * sig;
+      if (vb < vt1) ra = rt1; else { rc = rb; rb = rt1; vb = vt1; }
+    } else {
+      rt1 = (rc - rb) * factor + rb;
+      vt1 = eff_pot(S, rt1, vc_r2) * sig;
+      if (vb < vt1) rc = rt1; else { ra = rb; rb = rt1; vb = vt1; }
+    }
+    if (fabs(rc - ra) <= tol) break;
+  }
+  rout = rb;
+  vout = vb * sig;
+  return 0;
+}
+
+__device__ double gamma_fct(double y) {
+  double sum = -1.963510026021423 * y;
+  if (y == 0.0) return sum;
+  for (int it = 0; it <= 1000000; ++it) {
+    double t1 = y / (0.5 + it);
+    double term = t1 - atan(t1);
+    sum = sum + term;
+    if (fabs(term / sum) < 1.0E-06) return sum;
+  }
+  return sum;
+}
+
+__device__ void find_state(const DevSys& S, const FsArgs& F, int ipair, int ia, int ib, const double* X,
+                           const double* XD, cair_mol_state& m) {
+  const double PI = 3.141592653589793;
+  double xma = F.mass[ia], xmb = F.mass[ib];
+  double fa = xma / (xma + xmb), fb = xmb / (xma + xmb);
+  double x[3][2], xd[3][2];
+  double eint = 0.0, rbond = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    double xc = fa * X[2 * i] + fb * X[2 * i + 1];
+    double xdc = fa * XD[2 * i] + fb * XD[2 * i + 1];
+    x[i][0] = X[2 * i] - xc; x[i][1] = X[2 * i + 1] - xc;
+    xd[i][0] = XD[2 * i] - xdc; xd[i][1] = XD[2 * i + 1] - xdc;
+    double dd = x[i][0] - x[i][1];
+    rbond = rbond + dd * dd;
+    eint = eint + 0.5 * (xma * (xd[i][0] * xd[i][0]) + xmb * (xd[i][1] * xd[i][1]));
+  }
+  rbond = sqrt(rbond);
+  double tx = 0.0, ty = 0.0, tz = 0.0;
+  for (int a = 0; a < 2; ++a) {
+    double mass = a == 0 ? xma : xmb;
+    tx = tx + (x[1][a] * xd[2][a] - x[2][a] * xd[1][a]) * mass;
+    ty = ty + (x[2][a] * xd[0][a] - x[0][a] * xd[2][a]) * mass;
+    tz = tz + (x[0][a] * xd[1][a] - x[1][a] * xd[0][a]) * mass;
+  }
+  double tis = tx * tx + ty * ty + tz * tz;
+  double angmom = sqrt(tis);
+  double rms = xma * xmb / (xma + xmb);
+  double twomu = rms * 2.0;
+  double vc_r2 = 0.5 * tis / rms;
+  const double eps = 1.0E-5;
+  double rmin, vmin, rmax = 0.0, vmax = 0.0, viba = 0.5;
+  int itype = 1;
+  int ierr = find_extremum(S, 1.0, F.rsmal, F.rcent, vc_r2, eps, rmin, vmin);
+  int imin = 1;
+  if (ierr != 0) { rmin = (F.rsmal + F.rcent) * 0.5; imin = 0; }
+  if (imin == 1) {
+    ierr = find_extremum(S, -1.0, rmin, F.rcent, vc_r2, eps, rmax, vmax);
+    if (ierr != 0) rmax = F.rcent;
+  }
+  if (imin == 0 || rbond > rmax) {
+    itype = 3;
+    viba = 0.5;
+  } else {
+    eint = eint + diat_v(S, rbond);
+    itype = (eint < F.vinf) ? 1 : 2;
+    double r1 = rmin;
+    if (eint > vmax) {
+      viba = 0.5;
+      itype = 3;
+    } else {
+      double r00 = F.rsmal, ri = 0.0, ro = 0.0;
+      for (int itry = 1; itry <= 10; ++itry) {
+        turning_point(S, r00, r1, vc_r2, eint, 4, 4, ri);
+        if (ri != 0.0) break;
+        r00 = r00 * 0.5;
+      }
+      turning_point(S, r1, rmax, vc_r2, eint, 10, 4, ro);
+      viba = action_integral(S, F, ri, ro, vc_r2, eint, twomu);
+      if (eint > F.vinf) {
+        double rga = rmax, rgb = rmax * 2.0, r3 = 0.0;
+        for (int ip = 1; ip <= 10; ++ip) {
+          if (turning_point(S, rga, rgb, vc_r2, eint, 10, 4, r3) == 0) break;
+          rga = rgb;
+          rgb = rgb * 2.0;
+        }
+        double eint_p = eint + 1.0E-5;
+        if (eint_p > vmax) eint_p = eint + 0.5 * (vmax - eint);
+        double deint = eint_p - eint, rip, rop, rim, rom;
+        turning_point(S, r00, r1, vc_r2, eint_p, 4, 4, rip);
+        turning_point(S, r1, rmax, vc_r2, eint_p, 10, 4, rop);
+        double act_p = action_integral(S, F, rip, rop, vc_r2, eint_p, twomu);
+        double eint_m = eint - deint;
+        turning_point(S, r00, r1, vc_r2, eint_m, 4, 4, rim);
+        turning_point(S, r1, rmax, vc_r2, eint_m, 10, 4, rom);
+        double act_m = action_integral(S, F, rim, rom, vc_r2, eint_m, twomu);
+        double dade = 0.5 * (act_p - act_m) / deint;
+        double act = action_integral(S, F, ro, r3, vc_r2, eint, twomu);
+        double gam = exp(-act) / dade;
+        if (1.0 / gam < F.tthresau) itype = 4;
+        act = act * 0.5 / PI;
+        double rho2 = gamma_fct(act) - act * (log(fabs(act)) - 1.0);
+        viba = viba + rho2 * F.rfact;
+      }
+      viba = viba * 0.5 / PI;
+    }
+  }
+  itype = itype - 1;
+  if (itype == 2) angmom = 0.5;
+  m.ipair = ipair;
+  m.itype = itype;
+  m.eint = eint;
+  m.angmom = angmom;
+  m.viba = viba;
+}
+
+// Analyze for 3 atoms (the atom-diatom systems)
+__global__ void __launch_bounds__(128) k_find_state3(DevSys S, FsArgs F, int64_t n, const double* __restrict__ paq,
+                                                     cair_traj_point* __restrict__ out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double* p = paq + 12 * k;
+    double xx[3][3], xd[3][3];
+    for (int a = 0; a < 2; ++a)
+      for (int d = 0; d < 3; ++d) { xd[d][a] = p[d + 3 * a]; xx[d][a] = p[d + 3 * a + 6]; }
+    for (int d = 0; d < 3; ++d) {
+      xd[d][2] = (0.0 + S.mMiMn[0] * p[d]) + S.mMiMn[1] * p[d + 3];
+      xx[d][2] = (0.0 + S.mMiMn[0] * p[d + 6]) + S.mMiMn[1] * p[d + 9];
+    }
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+    double rbs[3];
+    for (int q = 0; q < 3; ++q) {
+      double a = xx[0][pa[q]] - xx[0][pb[q]], b = xx[1][pa[q]] - xx[1][pb[q]], c = xx[2][pa[q]] - xx[2][pb[q]];
+      rbs[q] = a * a + b * b + c * c;
+    }
+    int ip = 1;
+    if (rbs[1] < rbs[ip - 1]) ip = 2;
+    if (rbs[2] < rbs[ip - 1]) ip = 3;
+    int m1a = pa[ip - 1], m1b = pb[ip - 1];
+    double cm[3][2], cmd[3][2];
+    for (int d = 0; d < 3; ++d) {
+      cm[d][0] = cm[d][1] = cmd[d][0] = cmd[d][1] = 0.0;
+      for (int j = 0; j < 3; ++j) {
+        int w = (j == m1a || j == m1b) ? 0 : 1;
+        cm[d][w] = cm[d][w] + F.mass[j] * xx[d][j];
+        cmd[d][w] = cmd[d][w] + F.mass[j] * xd[d][j];
+      }
+    }
+    double xp = 0.0, xt = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      if (j == m1a || j == m1b) xp = xp + F.mass[j];
+      else xt = xt + F.mass[j];
+    }
+    double xpi = 1.0 / xp, xti = 1.0 / xt, xrel[3], vrel[3];
+    for (int d = 0; d < 3; ++d) {
+      cm[d][0] *= xpi; cm[d][1] *= xti; cmd[d][0] *= xpi; cmd[d][1] *= xti;
+      xrel[d] = cm[d][0] - cm[d][1];
+      vrel[d] = cmd[d][0] - cmd[d][1];
+    }
+    double xnum = xrel[0] * vrel[0] + xrel[1] * vrel[1] + xrel[2] * vrel[2];
+    double v = vrel[0] * vrel[0] + vrel[1] * vrel[1] + vrel[2] * vrel[2];
+    double tt = -xnum / v;
+    double e0 = xrel[0] + tt * vrel[0], e1 = xrel[1] + tt * vrel[1], e2 = xrel[2] + tt * vrel[2];
+    cair_traj_point o;
+    o.b = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+    o.xkin = 0.0;
+    for (int d = 0; d < 3; ++d) o.xkin = o.xkin + 0.5 * xp * (cmd[d][0] * cmd[d][0]) + 0.5 * xt * (cmd[d][1] * cmd[d][1]);
+    for (int d = 0; d < 3; ++d) o.vrel[d] = vrel[d];
+    o.nmol = 1;
+    o.pad = 0;
+    double X[6], XD[6];
+    for (int d = 0; d < 3; ++d) {
+      X[2 * d] = xx[d][m1a]; X[2 * d + 1] = xx[d][m1b];
+      XD[2 * d] = xd[d][m1a]; XD[2 * d + 1] = xd[d][m1b];
+    }
+    find_state(S, F, ip, m1a, m1b, X, XD, o.mol[0]);
+    o.mol[1].ipair = 0; o.mol[1].itype = 0; o.mol[1].eint = 0.0; o.mol[1].angmom = 0.0; o.mol[1].viba = 0.0;
+    out[k] = o;
+  }
+}
+
+}  // namespace cair

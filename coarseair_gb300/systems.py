@@ -1,0 +1,161 @@
+"""System descriptions for the trajectory path: surfaces, masses, integrator and final-state
+parameters, level lists.
+
+This module reads the same data the reference reads at start-up:
+
+* O3 UMN surfaces: ``dtb/Systems/O3/PESs/<Model>.inp`` (O3_UMN_PES_Class.F90:114-131): a title
+  line, then ``a ab ra rb`` and ``C(1:56)`` in list-directed format;
+* O4 UMN surfaces: ``dtb/Systems/O4/PESs/UMN/<Model>.dat`` (O4_UMN_PES_Class.F90:179-203):
+  ``a, ab, ra, rb, Eref, totdiss``, 143 lines of three coefficients, then ``C(430)``;
+* N3 UMN: the 276 coefficients the reference keeps inline (N3_UMN_PES_Class.F90:108-201),
+  stored here as ``data/N3_UMN.dat``;
+* level lists ``vqn jqn eint egam rmin rmax vmin vmax tau ri ro`` (LevelsContainer_Class.F90).
+
+and fills the input-file keys of the hot path with the values of the reference's own input
+templates (input/O3/UMN/input/CoarseAIR.inp, input/N3/UMN/input/CoarseAIR.inp).
+"""
+import gzip
+import os
+import re
+from dataclasses import dataclass, field
+
+import numpy as np
+
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+AMU_TO_AU = 1822.888486209          # [amu] -> electron masses (kgm_To_au / 1000)
+PES_O3_UMN, PES_N3_UMN, PES_O4_UMN = 1, 2, 3
+DIAT_O2_UMN, DIAT_N2_UMN_FORN4 = 1, 2
+
+_FNUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[dDeE][-+]?\d+)?")
+
+
+def _fortran_floats(text):
+    return [float(x.replace("d", "e").replace("D", "e")) for x in _FNUM.findall(text)]
+
+
+@dataclass
+class Surface:
+    model: int
+    coef: np.ndarray
+    a: float = 0.0
+    ab: float = 0.0
+    ra: float = 0.0
+    rb: float = 0.0
+    eref: float = 0.0
+    totdiss: float = 0.0
+    name: str = ""
+
+
+def load_o3_umn(model="UMN_11A1"):
+    """O3_UMN_PES_Class.F90:114-131."""
+    with open(os.path.join(DATA, "O3_UMN", model + ".inp")) as f:
+        lines = f.read().split("\n")
+    vals = _fortran_floats("\n".join(lines[1:]))
+    a, ab, ra, rb = vals[:4]
+    coef = np.array(vals[4:60], dtype=np.float64)
+    assert coef.size == 56
+    return Surface(PES_O3_UMN, coef, a, ab, ra, rb, name="O3 " + model)
+
+
+def load_o4_umn(model="UMN_Singlet"):
+    """O4_UMN_PES_Class.F90:179-203."""
+    with open(os.path.join(DATA, "O4_UMN", model + ".dat")) as f:
+        vals = _fortran_floats(f.read())
+    a, ab, ra, rb, eref, totdiss = vals[:6]
+    coef = np.array(vals[6:436], dtype=np.float64)
+    assert coef.size == 430
+    return Surface(PES_O4_UMN, coef, a, ab, ra, rb, eref, totdiss, name="O4 " + model)
+
+
+def load_n3_umn():
+    """N3_UMN_PES_Class.F90:96-201 (a = 1 Ang, ab = 1.5 Ang^2, re = 1.098 Ang, totdiss = 457.4)."""
+    with open(os.path.join(DATA, "N3_UMN.dat")) as f:
+        vals = [float(l) for l in f if l.strip() and not l.startswith("#")]
+    coef = np.array(vals, dtype=np.float64)
+    assert coef.size == 276
+    return Surface(PES_N3_UMN, coef, 1.0, 1.5, 1.098, 1.098, 0.0, 457.4, name="N3 UMN")
+
+
+LEVEL_COLS = ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax", "tau", "ri", "ro")
+
+
+def load_levels(name):
+    """Level list as a structured array (columns LEVEL_COLS)."""
+    fn = {"N2": "N2_UMN_ForN4_FromRoss.inp.gz", "O2": "O2_UMN_FromUMN_Sorted.inp.gz"}[name]
+    rows = []
+    with gzip.open(os.path.join(DATA, "levels", fn), "rt") as f:
+        for line in f:
+            s = line.strip()
+            if not s or s.startswith("#"):
+                continue
+            rows.append([float(x.replace("D", "E")) for x in s.split()])
+    arr = np.array(rows, dtype=np.float64)
+    out = np.zeros(arr.shape[0], dtype=[(c, "f8") for c in LEVEL_COLS] + [("rlim", "f8")])
+    for i, c in enumerate(LEVEL_COLS):
+        out[c] = arr[:, i]
+    return out
+
+
+@dataclass
+class SystemConfig:
+    """The hot-path subset of the reference's input file, plus the surfaces."""
+    name: str
+    natoms: int
+    masses: tuple
+    surfaces: list
+    diat_model: int
+    dt0: float = 5.0                # "Initial time step"
+    eps: float = 1.0e-8             # "Error control parameter"
+    relax: float = 0.5              # "Stepsize increase damping factor"
+    nsteps: int = 3                 # "Nb of extrapolation steps"
+    inc_step: int = 1               # "Try to increase stepsize?"
+    ncall: int = 10                 # "Nb of integration between end checking"
+    rmax: float = 16.0              # "Max distance between atom pair [bohr]"
+    tmax: float = 4.0e5             # "Max trajectory time [a.u.]"
+    ham_abs_tol: float = 1.0e-5     # "Tolerance on Hamiltonian" (Input_Class.F90:227 default)
+    nquad: int = 50                 # "Nb of Quadrature Pts for Action Integral"
+    rsmal: float = 1.0              # "Lower Bound for Position of Centrifugal Barrier Max"
+    rcent: float = 30.0             # "Upper Bound for Position of Centrifugal Barrier Max"
+    rfact: float = 0.0              # "Factor for q.b. Levels"
+    tthresau: float = 1.0e-100      # "Time threshold for q.b. Levels [Eh]"
+    max_attempts: int = 1000000     # IterMax (1e5) x ncall (Integrator_Class.F90:269)
+    ttra: float = 10000.0           # "Translational Temperature [K] 1"
+    bmax: float = 6.0               # impact-parameter ring bound (Circles, one ring)
+    dinit: float = 15.0             # "Initial Distance between Target and Projectile"
+    seed: int = 1                   # "Initial Random Nb Seed"
+    degeneracy: tuple = (1.0,)
+
+    @property
+    def neqtvar(self):
+        return 3 * (self.natoms - 1)
+
+    @property
+    def neqttot(self):
+        return 2 * self.neqtvar
+
+    @property
+    def npairs(self):
+        return self.natoms * (self.natoms - 1) // 2
+
+
+def o3_config(model="UMN_11A1", mass_amu=15.9994, **kw):
+    """O2 + O on one O3 UMN surface (the ground state UMN_11A1 by default)."""
+    m = mass_amu * AMU_TO_AU
+    return SystemConfig("O2+O " + model, 3, (m, m, m), [load_o3_umn(model)], DIAT_O2_UMN, **kw)
+
+
+def n3_config(mass_amu=14.0067, **kw):
+    """N2 + N on the N3 UMN surface (N4 PIP) with the UMN_ForN4 N2 diatomic."""
+    m = mass_amu * AMU_TO_AU
+    kw.setdefault("bmax", 7.0)
+    return SystemConfig("N2+N UMN", 3, (m, m, m), [load_n3_umn()], DIAT_N2_UMN_FORN4, **kw)
+
+
+def o4_config(mass_amu=15.9994, **kw):
+    """O2 + O2 on the three O4 UMN surfaces (degeneracies 1/3/5, CoarseAIR_StS.inp)."""
+    m = mass_amu * AMU_TO_AU
+    kw.setdefault("bmax", 8.0)
+    kw.setdefault("dinit", 18.0)
+    surfs = [load_o4_umn(x) for x in ("UMN_Singlet", "UMN_Triplet", "UMN_Quintet")]
+    return SystemConfig("O2+O2 UMN", 4, (m, m, m, m), surfs, DIAT_O2_UMN, degeneracy=(1.0, 3.0, 5.0), **kw)

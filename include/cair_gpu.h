@@ -1,0 +1,206 @@
+/*
+ * cair_gpu.h -- C ABI of the GB300 (sm_103a) trajectory library for CoarseAIR's
+ * quasi-classical trajectory hot path.
+ *
+ * The library replaces, for one process on one GPU, the path
+ *   app/RunTrajectories/RunTrajectories.F90:277  call Integrator%Integrate(Input, Collision)
+ *   -> src/Collision/Integrator_Class.F90:231-579  (batch loop, end checks, compaction)
+ *   -> src/Collision/ODE/ODE_Solver.F90:225-541    (Bulirsch-Stoer step, mmidv, RatPolExtrap)
+ *   -> src/Collision/ODE/ODE_System.F90:45-96      (Hamilton's equations)
+ *   -> src/Collision/Collision_Class.F90:2148-2316 (Compute_PES_1d, pair distances)
+ *   -> src/PESs/PES_Class.F90:43-72,252-360        (PES_Type%Compute / Potential, TransToCart)
+ * and the final-state analysis of
+ *   src/Collision/Trajectories/TrajectoryPoint_Class.F90:128-495 and
+ *   src/Collision/MolecularState/MolecularState_Class.F90:61-429.
+ *
+ * Conventions (those of the Fortran arrays, so a Fortran ISO_C_BINDING shim passes its
+ * arrays unchanged):
+ *   - FP64 everywhere; atomic units (bohr, hartree, a.u. of time, electron masses).
+ *   - PaQ is stored per trajectory contiguously: paq[k*NEqtTot + i], i.e. the Fortran
+ *     column-major PaQ(NEqtTot, NTraj).  PaQ = [p(1:NEqtVar), q(1:NEqtVar)], where q are
+ *     the Cartesian coordinates of atoms 1..NAtoms-1 (the last atom is eliminated through
+ *     the centre of mass) and p the conjugate momenta.
+ *   - Pair order: 3 atoms (1-2, 1-3, 2-3); 4 atoms (1-2, 1-3, 1-4, 2-3, 2-4, 3-4).
+ *   - PES indices `ipes` are 0-based here (the Fortran Traj%iPES is 1-based).
+ *   - Pointers named *_host are host memory; the *_dev entry points take device pointers
+ *     and a cudaStream_t passed as void*.
+ *
+ * Errors: every entry point returns 0 on success or a cair_status code; the message is
+ * available from cair_last_error() until the next call on the same handle.  The library
+ * never calls exit() or abort().  Per-trajectory numerical outcomes are reported in the
+ * status[] arrays (cair_traj_status).
+ *
+ * Threading: a handle is used by one host thread at a time; distinct handles may be used
+ * concurrently from distinct threads.  Calls are synchronous unless named *_dev (those
+ * are asynchronous on the given stream).
+ */
+#ifndef CAIR_GPU_H
+#define CAIR_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CAIR_MAX_PES 8
+#define CAIR_ABI_VERSION 1
+
+/* Surface models (PES_Factory_Class.F90:46-329, System x PES_Model strings). */
+enum cair_pes_model {
+  CAIR_PES_O3_UMN = 1, /* O3_UMN_PES_Class.F90  (System O3, Model UMN_*)            */
+  CAIR_PES_N3_UMN = 2, /* N3_UMN_PES_Class.F90  (System N3, Model UMN)              */
+  CAIR_PES_O4_UMN = 3  /* O4_UMN_PES_Class.F90  (System O4, Model UMN_Singlet/...)  */
+};
+
+/* Diatomic potentials of the pairs (DiatomicPotential_Factory_Class.F90:115-229). */
+enum cair_diat_model {
+  CAIR_DIAT_O2_UMN = 1,      /* O2_UMN_DiatomicPotential_Class.F90       */
+  CAIR_DIAT_N2_UMN_FORN4 = 2 /* N2_UMN_ForN4_DiatomicPotential_Class.F90 */
+};
+
+enum cair_status {
+  CAIR_OK = 0,
+  CAIR_EINVAL = 1,      /* bad argument (null pointer, size, model)            */
+  CAIR_ECUDA = 2,       /* CUDA runtime error (no device, launch failure, ...) */
+  CAIR_ETIMEOUT = 3,    /* host watchdog expired while waiting for the GPU     */
+  CAIR_ENONFINITE = 4,  /* non-finite input                                    */
+  CAIR_EUNSUPPORTED = 5 /* combination not built (e.g. 4-atom final states)    */
+};
+
+/* Per-trajectory outcome of cair_integrate. */
+enum cair_traj_status {
+  CAIR_TRAJ_DONE = 0,        /* t > tmax or a pair beyond rmax at an end check      */
+  CAIR_TRAJ_ATTEMPT_CAP = 1, /* max_attempts reached (reference: IterMax*ncall)      */
+  CAIR_TRAJ_NONFINITE = 2    /* NaN in the error estimate (reference: stop in ODE)   */
+};
+
+/* One surface: linear coefficients and MEG parameters.  Replaces the data a
+ * PES%Initialize reads (O3_UMN_PES_Class.F90:67-135, O4_UMN_PES_Class.F90:118-210;
+ * the N3 coefficients are inline in N3_UMN_PES_Class.F90:108-201). */
+typedef struct cair_pes_desc {
+  int32_t model;       /* cair_pes_model                                      */
+  int32_t ncoef;       /* 56 (O3), 276 (N3), 430 (O4)                         */
+  const double* coef;  /* C(1:ncoef) [kcal/mol], copied at cair_create        */
+  double a, ab, ra, rb;/* MEG parameters [Ang, Ang^2, Ang, Ang] (O3, O4)      */
+  double eref;         /* O4 file value (unused by the energy, as in the reference) */
+  double totdiss;      /* O4 file value (unused by the energy, as in the reference) */
+} cair_pes_desc;
+
+/* Everything Collision%Initialize and Integrator%Initialize derive from the input file
+ * for this path (Input_Class.F90:1192-1241 ODE keys; 1079 nquad; masses; surfaces). */
+typedef struct cair_system_desc {
+  int32_t abi_version;   /* CAIR_ABI_VERSION                                      */
+  int32_t natoms;        /* 3 or 4                                                */
+  int32_t npes;          /* 1..CAIR_MAX_PES                                       */
+  int32_t diat_model;    /* cair_diat_model of every pair                         */
+  double mass[4];        /* atom masses [a.u.]                                    */
+  const double* tpq;     /* optional Tpq(NEqtVar,NEqtVar) column-major, e.g. the
+                            matrix the caller's LAPACK produced; NULL: computed   */
+  cair_pes_desc pes[CAIR_MAX_PES];
+  /* "Initial time step", "Error control parameter", "Stepsize increase damping factor",
+     "Nb of extrapolation steps", "Try to increase stepsize?",
+     "Nb of integration between end checking", "Max distance between atom pair [bohr]",
+     "Max trajectory time [a.u.]", "Tolerance on Hamiltonian" */
+  double dt0, eps, relax, rmax, tmax, ham_abs_tol;
+  int32_t nsteps, inc_step, ncall;
+  /* final-state analysis: "Nb of Quadrature Pts for Action Integral", "Lower/Upper Bound
+     for Position of Centrifugal Barrier Max", "Factor for q.b. Levels",
+     "Time threshold for q.b. Levels [Eh]" */
+  int32_t nquad;
+  double rsmal, rcent, rfact, tthresau;
+} cair_system_desc;
+
+/* Final state of one molecule (MolecularState_Type after FindState). */
+typedef struct cair_mol_state {
+  int32_t ipair;   /* 1-based pair index of the molecule                          */
+  int32_t itype;   /* 0 bound, 1 quasi-bound, 2 dissociated/unbound, 3 short-lived */
+  double eint;     /* internal energy [Eh]                                        */
+  double angmom;   /* |L| (= J + 1/2 semiclassically), 1/2 when itype == 2         */
+  double viba;     /* action / 2 pi (= v + 1/2)                                     */
+} cair_mol_state;
+
+/* Analysed trajectory point (TrajectoryPoint_Type after Analyze). */
+typedef struct cair_traj_point {
+  cair_mol_state mol[2];
+  double b;        /* impact parameter of the relative motion [bohr]              */
+  double xkin;     /* relative kinetic energy [Eh]                                */
+  double vrel[3];  /* relative velocity                                           */
+  int32_t nmol;
+  int32_t pad;
+} cair_traj_point;
+
+typedef struct cair_handle cair_handle;
+
+/* Create a handle on the current CUDA device: copies the surfaces to device memory and
+ * computes Tqp/Tpq (Transformation_Class.F90:53-128) unless sys->tpq is given.
+ * Replaces PES_Factory%Construct_PES + Transformation%Initialize + ODE%Initialize. */
+int cair_create(cair_handle** h, const cair_system_desc* sys);
+void cair_destroy(cair_handle* h);
+const char* cair_last_error(const cair_handle* h);
+/* NEqtVar, NEqtTot, NPairs of the handle's system */
+int cair_dims(const cair_handle* h, int32_t* neqtvar, int32_t* neqttot, int32_t* npairs);
+/* Tpq(NEqtVar,NEqtVar) column-major as used by the kernels */
+int cair_get_tpq(const cair_handle* h, double* tpq_host);
+
+/* Batched PES%Compute (PES_Class.F90:43-72; e.g. Compute_N3_UMN_PES_1d,
+ * N3_UMN_PES_Class.F90:332-382) for n geometries:
+ *   R[n][NPairs] pair distances [bohr], Qall[n][3*NAtoms] Cartesian coordinates of all
+ *   atoms (the last atom included, as Compute_PES_1d builds QAll) ->
+ *   V[n] [Eh], dVdR[n][NPairs] [Eh/bohr], dVdQ[n][NEqtVar] (+dV/dq, before the sign flip
+ *   of Compute_PES_1d).  dVdR == NULL and dVdQ == NULL gives the energy-only
+ *   PES%Potential (O3_UMN_PES_Class.F90:153-191). */
+int cair_pes_eval(cair_handle* h, int64_t n, const int32_t* ipes, const double* R, const double* Qall,
+                  double* V, double* dVdR, double* dVdQ);
+
+/* Batched HamiltonODESystem (ODE_System.F90:45-96) -- the RHS_Evaluation interface of
+ * ODE_Solver.F90:53-60: y[n][NEqtTot] -> yp[n][NEqtTot]. */
+int cair_rhs(cair_handle* h, int64_t n, const int32_t* ipes, const double* y, double* yp);
+
+/* Batched Hamiltonian_1d (Collision_Class.F90:2046-2111): H[n], Rpi[n][NPairs]. */
+int cair_hamiltonian(cair_handle* h, int64_t n, const int32_t* ipes, const double* paq, double* H,
+                     double* Rpi);
+
+/* Exactly `nattempts` Bulirsch-Stoer attempts (Integrate_ODE_1d, ODE_Solver.F90:225-358)
+ * per trajectory, without end checks.  paq, t, dt are updated in place. */
+int cair_bs_steps(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                  const double* erra, int32_t nattempts);
+
+/* Propagate each trajectory to the end of the collision (Integrator_Class.F90:422-466 and
+ * AssessConvergence, Trajectories_Class.F90:240-280): repeat {ncall attempts; Hamiltonian;
+ * stop if t > tmax or any 1/Rp < 1/rmax} up to max_attempts attempts.  In/out: paq, t, dt,
+ * smax, smin, irej, iste (initialise as SetIniCondForward does: t = 0, dt = dt0,
+ * smin = +huge, smax = -huge, irej = iste = 0).  Out: H (last end check), status.
+ * One GPU thread owns one trajectory; a persistent kernel refills finished threads from a
+ * device work queue, so a batch of any length runs in one launch. */
+int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                   const double* erra, double* H, double* smax, double* smin, int32_t* irej, int32_t* iste,
+                   int32_t* status, int64_t max_attempts);
+
+/* Same as cair_integrate on device pointers, asynchronous on `stream` (cudaStream_t). */
+int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                       const double* erra, double* H, double* smax, double* smin, int32_t* irej, int32_t* iste,
+                       int32_t* status, int64_t max_attempts, void* stream);
+
+/* Final-state analysis of n trajectory points (TrajectoryPoint%Analyze + FindState).
+ * paq_vel[n][NEqtTot] holds VELOCITIES and coordinates, i.e. PaQ after
+ * Collision%ApplyTransformation (Collision_Class.F90:2406-2432) or PaQ0. */
+int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_point* out);
+
+/* ApplyTransformation on device: momenta -> velocities, in place on a copy. */
+int cair_apply_transformation(cair_handle* h, int64_t n, const double* paq, double* paq_vel);
+
+/* Algorithmic FP64 operation counts the library's kernels execute per PES energy+gradient
+ * evaluation, per energy-only evaluation and per BS attempt (excluding the PES), for
+ * roofline accounting.  `exp_per_eval` counts exponentials separately. */
+int cair_flop_model(const cair_handle* h, int32_t ipes, double* flops_grad, double* flops_energy,
+                    double* flops_attempt_overhead, double* exp_per_eval);
+
+/* Device counters of the last cair_integrate*: total BS attempts, accepted, rejected,
+ * PES gradient evaluations, PES energy evaluations. */
+int cair_last_counters(cair_handle* h, int64_t* counters5);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CAIR_GPU_H */

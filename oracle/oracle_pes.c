@@ -1,0 +1,355 @@
+/*
+ * Oracle (test infrastructure): diatomic potentials, PIP evaluation and the three UMN
+ * surfaces of the hot path, restated from the CoarseAIR Fortran.  Build with
+ * -ffp-contract=off so that no multiply-add is fused (the reference's x86 gfortran
+ * build has no FMA).
+ */
+#include <math.h>
+#include <string.h>
+#include "oracle.h"
+#include "pip_tables.h"
+
+/* src/Parameters/Parameters_Module.F90:82-87 */
+#define B_TO_ANG        0.52917721092
+#define KCM_TO_HARTREE  0.159360144e-2
+#define KCMANG_TO_HARTB 0.843297564e-3
+
+/* libgfortran pow_r8_i4 (binary powering), used where the reference raises to a
+ * variable integer power (O2_UMN_DiatomicPotential_Class.F90 beta**k). */
+static double powi_gf(double a, int b) {
+  double p = 1.0, x = a;
+  unsigned u;
+  if (b == 0) return 1.0;
+  if (b < 0) { u = (unsigned)(-b); x = 1.0 / x; } else u = (unsigned)b;
+  for (;;) {
+    if (u & 1u) p *= x;
+    u >>= 1;
+    if (u) x *= x; else break;
+  }
+  return p;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* O2 UMN diatomic: src/DiatomicPotentials/O2_UMN_DiatomicPotential_Class.F90                 */
+/* ------------------------------------------------------------------------------------------ */
+static const double O2_A[8] = {-1.488979427684798e3, 1.881435846488955e4, -1.053475425838226e5,
+                               2.755135591229064e5, -4.277588997761775e5, 4.404104009614092e5,
+                               -2.946204062950765e5, 1.176861219078620e5};
+static const double O2_ALPHA = 9.439784362354936e-1;
+static const double O2_BETA = 1.262242998506810;
+
+/* edisp / edisp_Grad (lines 323-381) */
+static void o2_edisp(double rb, double* e6, double* e8, double* e6dr, double* e8dr) {
+  const double r2r4 = 2.59361680, rs6 = 0.5299, rs8 = 2.20, c6 = 12.8;
+  double c8step = 3.0 * c6 * (r2r4 * r2r4);
+  double tmp = sqrt(c8step / c6);
+  double s = rs6 * tmp + rs8;
+  double s2 = s * s, s3 = s2 * s, s6 = s3 * s3, s4 = s2 * s2, s8 = s4 * s4;
+  double r2 = rb * rb, r3 = r2 * rb, r4 = r2 * r2, r5 = r4 * rb, r6 = r3 * r3, r7 = r4 * r3, r8 = r4 * r4;
+  double d6 = r6 + s6, d8 = r8 + s8;
+  *e6 = c6 / d6;
+  *e8 = c8step / d8;
+  if (e6dr) {
+    *e6dr = c6 * (-6.0 * r5) / (d6 * d6);
+    *e8dr = c8step * (-8.0 * r7) / (d8 * d8);
+  }
+}
+
+/* Ev2gm2 (lines 214-247) + d3disp (283-300): energy in hartree from R in Angstrom */
+static double o2_ev2gm2(double rang) {
+  double v = 0.0;
+  for (int k = 0; k <= 7; ++k) v = v + O2_A[k] * exp(-(O2_ALPHA * powi_gf(O2_BETA, k) * (rang * rang)));
+  v = v * 1.e-3;
+  double rb = rang / B_TO_ANG, e6, e8;
+  o2_edisp(rb, &e6, &e8, 0, 0);
+  return v + (-e6 - 2.0 * e8);
+}
+
+/* Ev2gm2_Grad (lines 250-280) + d3disp_Grad (303-320): V [Eh], dV [Eh/Ang] */
+static void o2_ev2gm2_grad(double rang, double* v, double* dv) {
+  double vv = 0.0, dd = 0.0;
+  for (int k = 0; k <= 7; ++k) vv = vv + O2_A[k] * exp(-(O2_ALPHA * powi_gf(O2_BETA, k) * (rang * rang)));
+  vv = vv * 1.e-3;
+  for (int k = 0; k <= 7; ++k)
+    dd = dd - 2.0 * O2_A[k] * O2_ALPHA * powi_gf(O2_BETA, k) * rang *
+                  exp(-(O2_ALPHA * powi_gf(O2_BETA, k) * (rang * rang)));
+  dd = dd * 1.e-3;
+  double rb = rang / B_TO_ANG, e6, e8, e6dr, e8dr;
+  o2_edisp(rb, &e6, &e8, &e6dr, &e8dr);
+  *v = vv + (-e6 - 2.0 * e8);
+  *dv = dd + (-e6dr - 2.0 * e8dr) / B_TO_ANG;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* N2 UMN_ForN4 diatomic: src/DiatomicPotentials/N2_UMN_ForN4_DiatomicPotential_Class.F90     */
+/* ------------------------------------------------------------------------------------------ */
+static const double N2_CS[7] = {2.70963254293, 1.32620177271e-1, 2.96757048793e-1, 1.97112432229e-1,
+                                -5.02002309588e-1, 3.80734244606e-1, 1.21001628750};
+static const double N2_DE = 228.7, N2_RED = 1.098, N2_RED4 = 1.4534810048;
+
+/* Ev2gm2 / Ev2gm2_Grad (lines 139-207): kcal/mol, kcal/mol/Ang */
+static void n2_ev2gm2(double rang, double* v, double* dv) {
+  double r3 = (rang * rang) * rang;
+  double r4 = r3 * rang;
+  double ts = r4 + N2_RED4;
+  double y = (r4 - N2_RED4) / ts;
+  double y2 = y * y, y3 = y2 * y, y4 = y2 * y2, y5 = y3 * y2, y6 = y3 * y3;
+  double fy = N2_CS[0] + N2_CS[1] * y + N2_CS[2] * y2 + N2_CS[3] * y3 + N2_CS[4] * y4 + N2_CS[5] * y5 +
+              N2_CS[6] * y6;
+  double u = exp(-(fy * (rang - N2_RED)));
+  double minu = 1.0 - u;
+  *v = N2_DE * (minu * minu) - N2_DE;
+  if (dv) {
+    double dfdy = N2_CS[1] + 2.0 * N2_CS[2] * y + 3.0 * N2_CS[3] * y2 + 4.0 * N2_CS[4] * y3 +
+                  5.0 * N2_CS[5] * y4 + 6.0 * N2_CS[6] * y5;
+    double dydr = 8.0 * r3 * N2_RED4 / (ts * ts);
+    double dfdr = dfdy * dydr;
+    *dv = 2.0 * N2_DE * minu * u * (dfdr * (rang - N2_RED) + fy);
+  }
+}
+
+double orc_diat_V(int model, double r) {
+  double rang = r * B_TO_ANG;
+  if (model == ORC_DIAT_O2_UMN) return o2_ev2gm2(rang);          /* DiatomicPotential_O2_UMN 95-106 */
+  double v;
+  n2_ev2gm2(rang, &v, 0);
+  return v * KCM_TO_HARTREE + 0.0;                                /* DiatomicPotential_N2 99-110 */
+}
+
+void orc_diat_VdV(int model, double r, double* v, double* dv) {
+  double rang = r * B_TO_ANG, vd, dvd;
+  if (model == ORC_DIAT_O2_UMN) {                                 /* Compute_Vd_dVd_O2_UMN 109-124 */
+    o2_ev2gm2_grad(rang, &vd, &dvd);
+    *v = vd;
+    *dv = dvd * B_TO_ANG;
+  } else {                                                        /* Compute_Vd_dVd_N2 114-130 */
+    n2_ev2gm2(rang, &vd, &dvd);
+    *v = vd * KCM_TO_HARTREE + 0.0;
+    *dv = dvd * KCM_TO_HARTREE * B_TO_ANG;
+  }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Generic PIP evaluator over the generated tables.  Follows EvMono/EvPoly/evbas and the      */
+/* forward-mode EvdMdR/EvdPdr/evdbdr of N3_UMN_PES_Class.F90:677-2053 (same structure in      */
+/* O4_UMN_PES_Class.F90:571-1962 and O3 Unified/UnifiedBis, O3_UMN_PES_Class.F90:336-638).   */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct pip_tab {
+  int nvar, nmono, npoly, nbasis;
+  const short *mo, *ma, *mb, *po, *pa, *pb, *poff, *plen, *plist, *basis;
+} pip_tab;
+
+static pip_tab pip_table(int t) {
+  pip_tab T;
+  if (t == 0) {
+    T.nvar = 3; T.nmono = PIP_O3_NMONO; T.npoly = PIP_O3_NPOLY; T.nbasis = PIP_O3_NBASIS;
+    T.mo = pip_o3_mono_op; T.ma = pip_o3_mono_a; T.mb = pip_o3_mono_b; T.po = pip_o3_poly_op;
+    T.pa = pip_o3_poly_a; T.pb = pip_o3_poly_b; T.poff = pip_o3_poly_off; T.plen = pip_o3_poly_len;
+    T.plist = pip_o3_poly_list; T.basis = pip_o3_basis;
+  } else if (t == 1) {
+    T.nvar = 6; T.nmono = PIP_N4_NMONO; T.npoly = PIP_N4_NPOLY; T.nbasis = PIP_N4_NBASIS;
+    T.mo = pip_n4_mono_op; T.ma = pip_n4_mono_a; T.mb = pip_n4_mono_b; T.po = pip_n4_poly_op;
+    T.pa = pip_n4_poly_a; T.pb = pip_n4_poly_b; T.poff = pip_n4_poly_off; T.plen = pip_n4_poly_len;
+    T.plist = pip_n4_poly_list; T.basis = pip_n4_basis;
+  } else {
+    T.nvar = 6; T.nmono = PIP_O4_NMONO; T.npoly = PIP_O4_NPOLY; T.nbasis = PIP_O4_NBASIS;
+    T.mo = pip_o4_mono_op; T.ma = pip_o4_mono_a; T.mb = pip_o4_mono_b; T.po = pip_o4_poly_op;
+    T.pa = pip_o4_poly_a; T.pb = pip_o4_poly_b; T.poff = pip_o4_poly_off; T.plen = pip_o4_poly_len;
+    T.plist = pip_o4_poly_list; T.basis = pip_o4_basis;
+  }
+  return T;
+}
+
+/* table: 0 = O3 (3 variables), 1 = N4 PIP used by N3, 2 = O4.  V = V0 + sum_i C_i B_i and
+ * dV[i] = sum_j C_j dB_j/dvar_i with dvar_i/dR_i = dmsdr_diag[i]. */
+void orc_pip_eval(int table, const double* rms, const double* dmsdr_diag, int want_grad, const double* C,
+                  double V0, double* V, double* dV) {
+  pip_tab T = pip_table(table);
+  double rm[128], p[480], dm[6][128], dp[6][480];
+  for (int k = 0; k < T.nmono; ++k) {
+    if (T.mo[k] == 0) rm[k] = 1.0;
+    else if (T.mo[k] == 1) rm[k] = rms[T.ma[k]];
+    else rm[k] = rm[T.ma[k]] * rm[T.mb[k]];
+  }
+  for (int k = 0; k < T.npoly; ++k) {
+    const short* L = T.plist + T.poff[k];
+    int n = T.plen[k];
+    if (T.po[k] == 0) {
+      double s = rm[L[0]];
+      for (int i = 1; i < n; ++i) s = s + rm[L[i]];
+      p[k] = s;
+    } else {
+      double s = p[T.pa[k]] * p[T.pb[k]];
+      for (int i = 0; i < n; ++i) s = s - p[L[i]];
+      p[k] = s;
+    }
+  }
+  double v = V0;
+  for (int i = 0; i < T.nbasis; ++i) v = v + C[i] * p[T.basis[i]];
+  *V = v;
+  if (!want_grad) return;
+  for (int d = 0; d < T.nvar; ++d) {
+    for (int k = 0; k < T.nmono; ++k) {
+      if (T.mo[k] == 0) dm[d][k] = 0.0;
+      else if (T.mo[k] == 1) dm[d][k] = (T.ma[k] == d) ? dmsdr_diag[d] : 0.0;
+      else dm[d][k] = dm[d][T.ma[k]] * rm[T.mb[k]] + rm[T.ma[k]] * dm[d][T.mb[k]];
+    }
+    for (int k = 0; k < T.npoly; ++k) {
+      const short* L = T.plist + T.poff[k];
+      int n = T.plen[k];
+      if (T.po[k] == 0) {
+        double s = dm[d][L[0]];
+        for (int i = 1; i < n; ++i) s = s + dm[d][L[i]];
+        dp[d][k] = s;
+      } else {
+        double s = dp[d][T.pa[k]] * p[T.pb[k]] + p[T.pa[k]] * dp[d][T.pb[k]];
+        for (int i = 0; i < n; ++i) s = s - dp[d][L[i]];
+        dp[d][k] = s;
+      }
+    }
+    double g = 0.0;
+    for (int j = 0; j < T.nbasis; ++j) g = g + C[j] * dp[d][T.basis[j]];
+    dV[d] = g;
+  }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* TransToCart (src/PESs/PES_Class.F90:252-360, implementation 2)                              */
+/* ------------------------------------------------------------------------------------------ */
+static void trans_to_cart_3(const double* mMiMn, const double* R, const double* Q, const double* dVdR,
+                            double* m) {
+  double Rx[3] = {Q[0] - Q[3], Q[0] - Q[6], Q[3] - Q[6]};
+  double Ry[3] = {Q[1] - Q[4], Q[1] - Q[7], Q[4] - Q[7]};
+  double Rz[3] = {Q[2] - Q[5], Q[2] - Q[8], Q[5] - Q[8]};
+  double d[3];
+  for (int i = 0; i < 3; ++i) d[i] = dVdR[i] / R[i];
+  double m1 = mMiMn[0], m2 = mMiMn[1];
+  m[0] = d[0] * Rx[0] + (1.0 - m1) * d[1] * Rx[1] - m1 * d[2] * Rx[2];
+  m[1] = d[0] * Ry[0] + (1.0 - m1) * d[1] * Ry[1] - m1 * d[2] * Ry[2];
+  m[2] = d[0] * Rz[0] + (1.0 - m1) * d[1] * Rz[1] - m1 * d[2] * Rz[2];
+  m[3] = -(d[0] * Rx[0]) - m2 * d[1] * Rx[1] + (1.0 - m2) * d[2] * Rx[2];
+  m[4] = -(d[0] * Ry[0]) - m2 * d[1] * Ry[1] + (1.0 - m2) * d[2] * Ry[2];
+  m[5] = -(d[0] * Rz[0]) - m2 * d[1] * Rz[1] + (1.0 - m2) * d[2] * Rz[2];
+}
+
+static void trans_to_cart_4(const double* mMiMn, const double* R, const double* Q, const double* dVdR,
+                            double* m) {
+  double Rx[6] = {Q[0] - Q[3], Q[0] - Q[6], Q[0] - Q[9], Q[3] - Q[6], Q[3] - Q[9], Q[6] - Q[9]};
+  double Ry[6] = {Q[1] - Q[4], Q[1] - Q[7], Q[1] - Q[10], Q[4] - Q[7], Q[4] - Q[10], Q[7] - Q[10]};
+  double Rz[6] = {Q[2] - Q[5], Q[2] - Q[8], Q[2] - Q[11], Q[5] - Q[8], Q[5] - Q[11], Q[8] - Q[11]};
+  double d[6];
+  for (int i = 0; i < 6; ++i) d[i] = dVdR[i] / R[i];
+  double m1 = mMiMn[0], m2 = mMiMn[1], m3 = mMiMn[2];
+  const double* RR[3] = {Rx, Ry, Rz};
+  for (int c = 0; c < 3; ++c) {
+    const double* X = RR[c];
+    m[0 + c] = d[0] * X[0] + d[1] * X[1] + (1.0 - m1) * d[2] * X[2] - m1 * d[4] * X[4] - m1 * d[5] * X[5];
+    m[3 + c] = -(d[0] * X[0]) - m2 * d[2] * X[2] + d[3] * X[3] + (1.0 - m2) * d[4] * X[4] - m2 * d[5] * X[5];
+    m[6 + c] = -(d[1] * X[1]) - m3 * d[2] * X[2] - d[3] * X[3] - m3 * d[4] * X[4] + (1.0 - m3) * d[5] * X[5];
+  }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Surfaces                                                                                   */
+/* ------------------------------------------------------------------------------------------ */
+/* O3 UMN: Compute_O3_UMN_PES_1d (O3_UMN_PES_Class.F90:259-326), O3_UMN_Potential_From_R (153-191) */
+static void o3_compute(const orc_sys* s, const orc_pes* P, const double* R, const double* Qall, double* V,
+                       double* dVdR, double* dVdQ) {
+  double rang[3], rms[3], dms[3], vp, dvp[3];
+  for (int i = 0; i < 3; ++i) {
+    rang[i] = R[i] * B_TO_ANG;
+    double d1 = rang[i] - P->ra, d2 = rang[i] - P->rb;
+    double e = exp(-(d1 / P->a) - (d2 * d2) / P->ab);
+    rms[i] = e;
+    dms[i] = (-(2.0 * d2 / P->ab) - 1.0 / P->a) * e;
+  }
+  double vd[3], dvd[3];
+  if (dVdR) {
+    for (int i = 0; i < 3; ++i) orc_diat_VdV(s->diat, R[i], &vd[i], &dvd[i]);
+  } else {
+    for (int i = 0; i < 3; ++i) vd[i] = orc_diat_V(s->diat, R[i]);
+  }
+  double vdiat = (vd[0] + vd[1]) + vd[2];
+  orc_pip_eval(0, rms, dms, dVdR != 0, P->coef, 0.0, &vp, dvp);
+  *V = (vp * KCM_TO_HARTREE) + vdiat;
+  if (!dVdR) return;
+  for (int i = 0; i < 3; ++i) dVdR[i] = dvp[i] * KCMANG_TO_HARTB + dvd[i];
+  trans_to_cart_3(s->mMiMn, R, Qall, dVdR, dVdQ);
+}
+
+/* N3 UMN: Compute_N3_UMN_PES_1d (N3_UMN_PES_Class.F90:332-382) -> n4pes (442-489) */
+static void n3_compute(const orc_sys* s, const orc_pes* P, const double* R, const double* Qall, double* V,
+                       double* dVdR, double* dVdQ) {
+  const double a = 1.0, ab = 1.5, re = 1.098, totdiss = 457.4, eref = 0.0;
+  double rt[6], rms[6], dms[6], vp, dvp[6];
+  for (int i = 0; i < 6; ++i) rt[i] = 1.e3;             /* RTemp = 1.e3 (default-real literal) */
+  rt[0] = R[0]; rt[1] = R[1]; rt[3] = R[2];
+  for (int i = 0; i < 6; ++i) {
+    double r = rt[i] * B_TO_ANG, d = r - re;
+    double e = exp(-(d / a) - (d * d) / ab);          /* EvMorse 624-641 */
+    rms[i] = e;
+    dms[i] = (-(2.0 * d / ab) - 1.0 / a) * e;          /* EvdMsdR 646-672 */
+  }
+  double vdiat = 0.0, dd[3];
+  for (int i = 0; i < 3; ++i) {
+    double v;
+    if (dVdR) orc_diat_VdV(s->diat, R[i], &v, &dd[i]);
+    else v = orc_diat_V(s->diat, R[i]);
+    vdiat = vdiat + v;
+  }
+  orc_pip_eval(1, rms, dms, dVdR != 0, P->coef, totdiss, &vp, dvp);
+  double vt = (vp + eref) * KCM_TO_HARTREE;
+  *V = vdiat + vt;
+  if (!dVdR) return;
+  for (int i = 0; i < 6; ++i) dvp[i] = dvp[i] * KCM_TO_HARTREE * B_TO_ANG;
+  dVdR[0] = dd[0] + dvp[0];
+  dVdR[1] = dd[1] + dvp[1];
+  dVdR[2] = dd[2] + dvp[3];
+  trans_to_cart_3(s->mMiMn, R, Qall, dVdR, dVdQ);
+}
+
+/* O4 UMN: Compute_O4_UMN_PES_1d (O4_UMN_PES_Class.F90:269-298) -> O4pes (310-370) */
+static void o4_compute(const orc_sys* s, const orc_pes* P, const double* R, const double* Qall, double* V,
+                       double* dVdR, double* dVdQ) {
+  double rms[6], dms[6], vp, dvp[6];
+  double vdiat = 0.0, dd[6];
+  for (int i = 0; i < 6; ++i) {
+    double v;
+    if (dVdR) orc_diat_VdV(s->diat, R[i], &v, &dd[i]);
+    else v = orc_diat_V(s->diat, R[i]);
+    vdiat = vdiat + v;
+  }
+  for (int i = 0; i < 6; ++i) {
+    double r = R[i] * B_TO_ANG, d1 = r - P->ra, d2 = r - P->rb;
+    double e = exp(-(d1 / P->a) - (d2 * d2) / P->ab);  /* EvMorse 510-531 */
+    rms[i] = e;
+    dms[i] = (-(2.0 * d2 / P->ab) - 1.0 / P->a) * e;   /* EvdMsdR 536-566 */
+  }
+  orc_pip_eval(2, rms, dms, dVdR != 0, P->coef, 0.0, &vp, dvp);
+  double vt = vp * KCM_TO_HARTREE;
+  *V = vt + vdiat;
+  if (!dVdR) return;
+  for (int i = 0; i < 6; ++i) dVdR[i] = dvp[i] * KCM_TO_HARTREE * B_TO_ANG + dd[i];
+  trans_to_cart_4(s->mMiMn, R, Qall, dVdR, dVdQ);
+}
+
+void orc_pes_compute(const orc_sys* s, int ipes, const double* R, const double* Qall, double* V, double* dVdR,
+                     double* dVdQ) {
+  const orc_pes* P = &s->pes[ipes];
+  if (P->model == ORC_PES_O3_UMN) o3_compute(s, P, R, Qall, V, dVdR, dVdQ);
+  else if (P->model == ORC_PES_N3_UMN) n3_compute(s, P, R, Qall, V, dVdR, dVdQ);
+  else o4_compute(s, P, R, Qall, V, dVdR, dVdQ);
+}
+
+double orc_pes_potential(const orc_sys* s, int ipes, const double* R) {
+  double v;
+  orc_pes_compute(s, ipes, R, 0, &v, 0, 0);
+  return v;
+}
+
+double orc_const(const char* name) {
+  if (!strcmp(name, "B_To_Ang")) return B_TO_ANG;
+  if (!strcmp(name, "Kcm_To_Hartree")) return KCM_TO_HARTREE;
+  if (!strcmp(name, "KcmAng_To_HartB")) return KCMANG_TO_HARTB;
+  return 0.0;
+}

@@ -1,0 +1,172 @@
+"""GPU parity tests: the CUDA library (through its C ABI) against the CPU oracle on the same inputs.
+
+Tolerances (the benchmark spec): surface energies and gradients 1e-12 relative; phase-space points after
+1000 fixed Bulirsch-Stoer attempts 1e-9 relative on non-chaotic trajectories; final (v, J,
+arrangement) identical on at least 99.5 % of trajectories; exact integers and 1e-9 for the
+final-state analysis of identical points.
+"""
+import numpy as np
+import pytest
+
+from coarseair_gb300 import api, systems
+
+pytestmark = pytest.mark.gpu
+
+CFGS = {"O3": lambda: systems.o3_config(), "N3": lambda: systems.n3_config()}
+LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 10)}
+
+
+def _setup(name, **kw):
+    from oracle import Oracle
+    cfg = CFGS[name]()
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    o = Oracle(cfg)
+    H = api.Handle(cfg, tpq=o.tpq)
+    return cfg, o, H
+
+
+def _ics(o, name, n, v=None, j=None, seed=None):
+    mol, v0, j0 = LEVELS[name]
+    lv = systems.load_levels(mol)
+    sel = lv[(lv["vqn"] == (v0 if v is None else v)) & (lv["jqn"] == (j0 if j is None else j))]
+    return o.sample_ics(n, sel, seed=seed)
+
+
+def _geometries(o, n, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    while sum(len(x) for x in out) < n:
+        Q = rng.uniform(-3.0, 3.0, size=(4 * n, 6))
+        R, Qall = o.rp(Q)
+        keep = np.all((R > 1.5) & (R < 9.0), axis=1)
+        out.append(Qall[keep])
+    Qall = np.concatenate(out)[:n]
+    R, Qall = o.rp(Qall[:, :6])
+    return R, Qall
+
+
+@pytest.mark.parametrize("name", ["O3", "N3"])
+def test_surface_energy_and_gradient_parity(gpu_lib, oracle_lib, name):
+    cfg, o, H = _setup(name)
+    R, Qall = _geometries(o, 512, 3)
+    ic = _ics(o, name, 64)
+    R2, Q2 = o.rp(ic["paq"][:, 6:])
+    R, Qall = np.concatenate([R, R2]), np.concatenate([Qall, Q2])
+    V_o, g_o, m_o = o.compute(R, Qall)
+    V_g, g_g, m_g = api.PES(H).Compute(R, Qall)
+    assert np.all(np.abs(V_g - V_o) <= 1e-12 * np.abs(V_o))
+    gs = np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2)
+    assert np.all(np.abs(g_g - g_o) <= 1e-12 * gs)
+    ms = np.maximum(np.abs(m_o).max(axis=1, keepdims=True), 1e-2)
+    assert np.all(np.abs(m_g - m_o) <= 1e-12 * ms)
+    # energy-only path (PES%Potential)
+    Ve = api.PES(H).Potential(R, Qall)
+    assert np.all(np.abs(Ve - V_o) <= 1e-12 * np.abs(V_o))
+
+
+@pytest.mark.parametrize("name", ["O3", "N3"])
+def test_rhs_and_hamiltonian_parity(gpu_lib, oracle_lib, name):
+    cfg, o, H = _setup(name)
+    ic = _ics(o, name, 128)
+    y = ic["paq"]
+    yp_o = o.rhs(y)
+    yp_g = api.Collision(H).EvaluateRHS(y)
+    sc = np.abs(yp_o).max(axis=1, keepdims=True)
+    assert np.all(np.abs(yp_g - yp_o) <= 1e-12 * sc)
+    h_o, r_o = o.hamiltonian(y)
+    h_g, r_g = api.Collision(H).Hamiltonian(y)
+    assert np.all(np.abs(h_g - h_o) <= 1e-12 * np.maximum(np.abs(h_o), 1e-3))
+    assert np.allclose(r_g, r_o, rtol=1e-15, atol=0)
+    assert np.allclose(api.Collision(H).ApplyTransformation(y), o.apply_transformation(y), rtol=1e-14, atol=1e-300)
+    assert np.allclose(H.tpq(), o.tpq, rtol=0, atol=0)
+
+
+def _non_chaotic(o, ic, nattempts, thresh=1e-11):
+    """Trajectories whose 1000-attempt state moves by < thresh under a 1e-14 relative perturbation
+    of the initial conditions (the oracle's own sensitivity)."""
+    n = ic["paq"].shape[0]
+    t0, dt0 = np.zeros(n), np.full(n, o.cfg.dt0)
+    a, _, _ = o.bs_attempts(ic["paq"], t0, dt0, ic["erra"], nattempts)
+    b, _, _ = o.bs_attempts(ic["paq"] * (1 + 1e-14), t0, dt0, ic["erra"], nattempts)
+    dev = np.abs(a - b).max(axis=1) / np.abs(a).max(axis=1)
+    return dev < thresh, a
+
+
+@pytest.mark.parametrize("name", ["O3", "N3"])
+def test_phase_space_after_1000_attempts(gpu_lib, oracle_lib, name):
+    cfg, o, H = _setup(name)
+    ic = _ics(o, name, 24)
+    nattempts = 1000
+    ok, a_o = _non_chaotic(o, ic, nattempts)
+    assert ok.sum() >= 4, "too few non-chaotic trajectories in the sample"
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.ODE(H).Integrate(tr, nattempts)
+    rel = np.abs(tr.paq - a_o).max(axis=1) / np.abs(a_o).max(axis=1)
+    assert np.all(rel[ok] < 1e-9), rel[ok]
+
+
+def _final_qn(fs):
+    """Histogram assignment (Statistics_Class.F90:626-656): nint(Q - 1/2) for J, v, arrangement."""
+    J = np.rint(np.asarray([f["angmom"] for f in fs]) - 0.5).astype(int)
+    v = np.rint(np.asarray([f["viba"] for f in fs]) - 0.5).astype(int)
+    arr = np.asarray([16 * f["ipair"] + f["itype"] for f in fs])
+    return J, v, arr
+
+
+def _gpu_final_qn(fs):
+    J = np.rint(fs["angmom0"] - 0.5).astype(int)
+    v = np.rint(fs["viba0"] - 0.5).astype(int)
+    arr = 16 * fs["ipair0"] + fs["itype0"]
+    return J, v, arr
+
+
+@pytest.mark.parametrize("name", ["O3", "N3"])
+def test_final_state_analysis_parity_on_identical_points(gpu_lib, oracle_lib, name):
+    cfg, o, H = _setup(name)
+    ic = _ics(o, name, 96)
+    res = o.integrate(ic["paq"], ic["erra"])
+    pts = np.concatenate([ic["paq0"], o.apply_transformation(res["paq"])])
+    fs_o = o.analyze(pts)
+    fs_g = api.MolecularState(H).FindState(pts)
+    Jo, vo, ao = _final_qn(fs_o)
+    Jg, vg, ag = _gpu_final_qn(fs_g)
+    assert np.array_equal(Jo, Jg) and np.array_equal(vo, vg) and np.array_equal(ao, ag)
+    assert np.allclose(fs_g["viba0"], [f["viba"] for f in fs_o], rtol=1e-9, atol=1e-12)
+    assert np.allclose(fs_g["angmom0"], [f["angmom"] for f in fs_o], rtol=1e-12, atol=1e-12)
+    assert np.allclose(fs_g["b"], [f["b"] for f in fs_o], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["O3", "N3"])
+def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
+    cfg, o, H = _setup(name)
+    n = 200
+    ic = _ics(o, name, n)
+    ref = o.integrate(ic["paq"], ic["erra"])
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.Integrator(H).Integrate(tr)
+    assert np.all(tr.status == 0) and np.all(ref["status"] == 0)
+    assert np.max(np.abs(tr.H - ic["H0"])) < cfg.ham_abs_tol
+    fo = o.analyze(o.apply_transformation(ref["paq"]))
+    fg = api.MolecularState(H).FindState(api.Collision(H).ApplyTransformation(tr.paq))
+    Jo, vo, ao = _final_qn(fo)
+    Jg, vg, ag = _gpu_final_qn(fg)
+    same = (Jo == Jg) & (vo == vg) & (ao == ag)
+    assert same.mean() >= 0.995, same.mean()
+    c = H.counters()
+    assert c["attempts"] == int(np.sum(tr.iste + tr.irej))
+
+
+def test_attempt_cap_and_errors(gpu_lib, oracle_lib):
+    cfg, o, H = _setup("N3")
+    ic = _ics(o, "N3", 8)
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.Integrator(H).Integrate(tr, max_attempts=20)
+    assert np.all(tr.status == 1)
+    assert np.all(tr.iste + tr.irej == 20)
+    tr2 = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0, ipes=np.full(8, 3))
+    with pytest.raises(api.CairError, match="CAIR_EINVAL"):
+        api.Integrator(H).Integrate(tr2)
+    # empty batch is a no-op
+    empty = api.Trajectories.start(np.zeros((0, 12)), np.zeros((0, 12)), cfg.dt0)
+    api.Integrator(H).Integrate(empty)

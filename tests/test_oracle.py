@@ -1,0 +1,231 @@
+"""CPU tests of the oracle (the CPU restatement of the reference path) -- its pins.
+
+The reference ships no golden values for these surfaces or the integrator, so the oracle is
+pinned by: finite-difference gradients, permutation symmetry and dissociation limits of each
+surface; an independent big-integer restatement of the random-number generator; the inverse
+of the Boltzmann energy CDF; energy conservation of the integrator; and the shipped level lists
+read as known-answer tests of the final-state chain (turning points and action -> v + 1/2).
+"""
+import numpy as np
+import pytest
+
+from coarseair_gb300 import systems
+
+
+def _cfgs():
+    return [systems.o3_config(), systems.n3_config(), systems.o4_config()]
+
+
+def _random_geometry(rng, natoms, n):
+    """Random Cartesian coordinates of the NAtoms-1 free atoms with pair distances 1.6..5 bohr."""
+    out = []
+    while len(out) < n:
+        q = rng.uniform(-2.5, 2.5, size=3 * (natoms - 1))
+        out.append(q)
+    return np.array(out)
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_surface_gradient_matches_finite_differences(oracle_lib, idx):
+    from oracle import Oracle
+    cfg = _cfgs()[idx]
+    o = Oracle(cfg)
+    rng = np.random.default_rng(7 + idx)
+    Q = _random_geometry(rng, cfg.natoms, 40)
+    R, Qall = o.rp(Q)
+    keep = np.all((R > 1.6) & (R < 6.0), axis=1)
+    R, Qall = R[keep][:8], Qall[keep][:8]
+    assert R.shape[0] >= 4
+    V, g, _ = o.compute(R, Qall)
+    # the 430-term O4 fit carries ~1e-12 Eh of cancellation noise; h = 2e-3 keeps the
+    # fourth-order difference's round-off and truncation both near 1e-9
+    h = 2e-3
+    for i in range(cfg.npairs):
+        def f(dx):
+            Rs = R.copy()
+            Rs[:, i] += dx
+            return o.potential(Rs)
+        # fourth-order central difference
+        fd = (8 * (f(h) - f(-h)) - (f(2 * h) - f(-2 * h))) / (12 * h)
+        scale = np.maximum(np.abs(g).max(axis=1), 1e-3)
+        assert np.all(np.abs(fd - g[:, i]) / scale < 1e-8), (i, fd, g[:, i])
+
+
+@pytest.mark.parametrize("idx", [0, 1])
+def test_cartesian_forces_match_finite_differences(oracle_lib, idx):
+    from oracle import Oracle
+    cfg = _cfgs()[idx]
+    o = Oracle(cfg)
+    Q = np.array([[0.3, 0.2, -0.1, 2.5, 0.1, 0.05], [-1.0, 0.4, 0.3, 1.2, -0.2, 0.7]])
+    R, Qall = o.rp(Q)
+    _, _, m = o.compute(R, Qall)
+    h = 1e-4
+    for i in range(6):
+        def f(dx):
+            Qs = Q.copy()
+            Qs[:, i] += dx
+            return o.potential(o.rp(Qs)[0])
+        fd = (8 * (f(h) - f(-h)) - (f(2 * h) - f(-2 * h))) / (12 * h)
+        assert np.all(np.abs(fd - m[:, i]) < 1e-8 * np.abs(m).max(axis=1) + 1e-11), (i, fd, m[:, i])
+
+
+@pytest.mark.parametrize("idx", [0, 1])
+def test_three_atom_surfaces_are_permutation_invariant(oracle_lib, idx):
+    """Identical atoms: swapping atoms 1 and 2 maps the pairs (12, 13, 23) to (12, 23, 13)."""
+    from oracle import Oracle
+    o = Oracle(_cfgs()[idx])
+    R = np.array([[2.1, 2.9, 3.7], [2.3, 2.4, 4.0], [3.0, 3.1, 3.2]])
+    v = o.potential(R)
+    for perm in ([0, 2, 1], [2, 1, 0], [1, 0, 2], [1, 2, 0], [2, 0, 1]):
+        assert np.allclose(o.potential(R[:, perm]), v, rtol=1e-12, atol=1e-13)
+
+
+def test_four_atom_surface_is_permutation_invariant(oracle_lib):
+    """O4: swapping atoms 1 <-> 2 maps pairs (12,13,14,23,24,34) -> (12,23,24,13,14,34)."""
+    from oracle import Oracle
+    o = Oracle(_cfgs()[2])
+    R = np.array([[2.3, 3.1, 4.2, 3.6, 3.9, 2.4], [2.2, 5.0, 5.5, 4.7, 5.2, 2.3]])
+    v = o.potential(R)
+    assert np.allclose(o.potential(R[:, [0, 3, 4, 1, 2, 5]]), v, rtol=1e-11, atol=1e-12)
+    # atoms 3 <-> 4: (12,13,14,23,24,34) -> (12,14,13,24,23,34)
+    assert np.allclose(o.potential(R[:, [0, 2, 1, 4, 3, 5]]), v, rtol=1e-11, atol=1e-12)
+    # molecules swapped (1,2) <-> (3,4): (12,13,14,23,24,34) -> (34,13,23,14,24,12)
+    assert np.allclose(o.potential(R[:, [5, 1, 3, 2, 4, 0]]), v, rtol=1e-11, atol=1e-12)
+
+
+def test_n3_dissociation_limit(oracle_lib):
+    """With atom 3 far away the N3 surface is the N2 diatomic plus the constant totdiss term."""
+    from oracle import Oracle
+    L = oracle_lib.lib()
+    o = Oracle(systems.n3_config())
+    for r in (1.8, 2.07, 2.6):
+        v = o.potential(np.array([[r, 60.0, 60.0 + r]]))[0]
+        vd = L.orc_diat_V(2, r) + 2 * L.orc_diat_V(2, 60.0)
+        assert abs(v - (vd + 457.4 * 0.159360144e-2)) < 1e-10
+
+
+def test_o3_dissociation_limit(oracle_lib):
+    from oracle import Oracle
+    L = oracle_lib.lib()
+    o = Oracle(systems.o3_config())
+    for r in (2.0, 2.28, 3.0):
+        v = o.potential(np.array([[r, 60.0, 60.0 + r]]))[0]
+        vd = L.orc_diat_V(1, r) + L.orc_diat_V(1, 60.0) + L.orc_diat_V(1, 60.0 + r)
+        assert abs(v - vd) < 1e-10
+
+
+def _rand12_bigint(digits):
+    """Independent restatement of rand12 (RandomVector_Module.F90:166-229) on base-256 digits."""
+    ia = [45, 127, 149, 76, 45, 244, 81, 88]
+    idd = [0] * 16
+    for j in range(8):
+        for i in range(8 - j):
+            k = j + i
+            ip = ia[j] * digits[i]
+            while True:
+                ip = ip + idd[k]
+                idd[k] = ip % 256
+                ip = ip // 256
+                if ip == 0 or k == 7:
+                    break
+                k += 1
+    digits[:] = idd[:8]
+    r = float(digits[0])
+    for i in range(1, 8):
+        r = float(digits[i]) + r * 3.90625e-3
+    return r * 3.90625e-3
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 12345])
+def test_rng_matches_independent_base256_restatement(oracle_lib, seed):
+    import ctypes
+    L = oracle_lib.lib()
+    st = oracle_lib.OrcRng()
+    L.orc_rng_seed(ctypes.byref(st), seed)
+    s = seed - 1 if seed % 2 == 0 else seed
+    digits = [(s >> (8 * i)) & 0xFF for i in range(8)]
+    table = [_rand12_bigint(digits) for _ in range(100)]
+    for _ in range(300):
+        i = int(99.0 * table[99]) + 1
+        expect = table[99]
+        table[99] = table[i - 1]
+        table[i - 1] = _rand12_bigint(digits)
+        assert L.orc_rng_draw(ctypes.byref(st)) == expect
+
+
+def test_boltzmann_energy_inverts_flux_weighted_cdf(oracle_lib):
+    L = oracle_lib.lib()
+    kelvin_to_hartree = 1.0 / 3.1577513e5
+    for u in (0.05, 0.3, 0.5, 0.77, 0.95):
+        er = L.orc_boltzmann_er(10000.0, u)
+        x = er / (10000.0 * kelvin_to_hartree)
+        assert abs((1 - (1 + x) * np.exp(-x)) - u) < 1e-4
+
+
+# reference masses of the shipped level lists (input/O3/UMN/input/CoarseAIR.inp, input/N3/...)
+REF_MASS = {"O2": 29148.94559, "N2": 25526.04298}
+DIAT = {"O2": 1, "N2": 2}
+
+
+# (max |V_eff(ri) - V_eff(ro)|, max |v + 1/2 - action/2pi|, median of the latter, offset spread)
+KAT_TOL = {"O2": (2e-4, 0.05, 0.005, 3e-4), "N2": (1e-3, 0.25, 0.01, 6e-4)}
+
+
+@pytest.mark.parametrize("mol", ["N2", "O2"])
+def test_level_list_known_answers(oracle_lib, mol):
+    """Shipped level lists as known answers for the final-state chain.
+
+    The lists give (v, J) with turning points ri, ro.  On the surface's diatomic potential the
+    effective potential must agree at ri and ro, each list's energy zero differs from the
+    potential's by one constant, and the semiclassical action over [ri, ro] divided by 2 pi is
+    v + 1/2 (MolecularState_Class.F90:297).  The lists were generated with earlier versions of
+    the diatomic potentials (the O2 list puts the zero at the well bottom, the N2 list comes
+    from another fit), so these hold to the tolerances of KAT_TOL, not to rounding.
+    """
+    L = oracle_lib.lib()
+    lv = systems.load_levels(mol)
+    mu = REF_MASS[mol] / 2.0
+    rows = lv[np.random.default_rng(11).choice(len(lv), 300, replace=False)]
+    rows = rows[rows["egam"] == 0.0]
+    dv, off, dvib = [], [], []
+    for r in rows:
+        vc_r2 = 0.5 / mu * (r["jqn"] + 0.5) ** 2
+        vri = L.orc_diat_V(DIAT[mol], r["ri"]) + vc_r2 / r["ri"] ** 2
+        vro = L.orc_diat_V(DIAT[mol], r["ro"]) + vc_r2 / r["ro"] ** 2
+        e = 0.5 * (vri + vro)
+        dv.append(abs(vri - vro))
+        off.append(r["eint"] - e)
+        act = L.orc_action_integral(DIAT[mol], r["ri"], r["ro"], vc_r2, e, 50, 2 * mu)
+        dvib.append(abs(act * 0.5 / np.pi - (r["vqn"] + 0.5)))
+    tol = KAT_TOL[mol]
+    assert max(dv) < tol[0]
+    assert max(dvib) < tol[1] and np.median(dvib) < tol[2]
+    assert max(off) - min(off) < tol[3]
+
+
+def test_initial_conditions_recover_sampled_level(oracle_lib):
+    """IC sampler (BondLength, orientation) + FindState on PaQ0 returns the sampled (v, J)."""
+    from oracle import Oracle
+    cfg = systems.n3_config(mass_amu=REF_MASS["N2"] / systems.AMU_TO_AU)
+    o = Oracle(cfg)
+    lv = systems.load_levels("N2")
+    for v, j in ((0, 0), (3, 20), (10, 45)):
+        sel = lv[(lv["vqn"] == v) & (lv["jqn"] == j)]
+        ic = o.sample_ics(6, sel)
+        fs = o.analyze(ic["paq0"])
+        for f in fs:
+            assert f["ipair"] == 1
+            assert abs(f["viba"] - (v + 0.5)) < 2e-2  # list ro vs this potential (see KAT_TOL)
+            assert abs(f["angmom"] - (j + 0.5)) < 1e-6
+
+
+def test_integration_conserves_energy(oracle_lib):
+    from oracle import Oracle
+    cfg = systems.o3_config()
+    o = Oracle(cfg)
+    lv = systems.load_levels("O2")
+    sel = lv[(lv["vqn"] == 0) & (lv["jqn"] == 1)]
+    ic = o.sample_ics(6, sel)
+    res = o.integrate(ic["paq"], ic["erra"])
+    assert np.all(res["status"] == 0)
+    assert np.max(np.abs(res["H"] - ic["H0"])) < cfg.ham_abs_tol
