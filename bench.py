@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Throughput of the trajectory hot path on one GB300: trajectories/s for N2 + N on the N3 UMN surface.
+
+Workload (one "step"): a batch of trajectories over 64 initial (v, J) levels drawn uniformly (seed 2)
+from the N2 UMN_ForN4 level list x translational temperatures {5000, 10000, 20000} K (192 work items,
+each one state-specific RunTrajectories run with its own random-number stream), b = 7 bohr sqrt(U),
+separation 15 bohr, masses 14.0067 amu, plain FP64.  A step samples the initial conditions on the
+device, integrates every trajectory to the end of the collision with the persistent queue-refilled
+kernel, and analyses the initial and final points into trajectories.out rows.  The full 1M-trajectory
+configuration is `--ntraj 1000000`; the default step is 65536 trajectories so that a run ends in
+about a minute.
+
+value: device-resident inputs, CUDA events on the launch stream around K steps.
+e2e:   the public host entry point cair_run_queue from pinned host buffers (level table and work
+       items in, result rows out) with the copies inside the timed region.
+cpu_baseline / --impl reference: the CPU oracle (C restatement of the reference path; the reference's
+Fortran cannot be built here) on the host cores, one process per core, on a bounded sample of the
+same work items.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+TEMPS = (5000.0, 10000.0, 20000.0)
+
+
+def workload(ntraj, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=15.0):
+    """Level table and work items of the N2 + N configuration."""
+    from coarseair_gb300 import api, systems
+    lv = systems.load_levels("N2")
+    rng = np.random.default_rng(seed_levels)
+    pick = np.sort(rng.choice(len(lv), nlevels, replace=False))
+    table = api.level_table(lv[pick])
+    nitems = nlevels * len(TEMPS)
+    base, extra = divmod(ntraj, nitems)
+    entries = []
+    for il in range(nlevels):
+        for it, T in enumerate(TEMPS):
+            k = il * len(TEMPS) + it
+            n = base + (1 if k < extra else 0)
+            entries.append((il, 0, n, api.process_seed(iseed, k + 1), T, bmax, dinit))
+    return table, api.work_items(entries)
+
+
+def config():
+    from coarseair_gb300 import systems
+    return systems.n3_config(dinit=15.0, bmax=7.0, rmax=30.0, tmax=4.0e5)
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU side: the oracle on host cores (one process per core, spawned before any GPU work)
+# ------------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    items, table, wall = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    o = Oracle(config())
+    done, t0 = 0, time.perf_counter()
+    for (il, ntraj, seed, ttra, bmax, dinit) in items:
+        lv = table[il:il + 1]
+        lvs = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax",
+                                                       "tau", "ri", "ro", "rlim")])
+        for c in lvs.dtype.names:
+            lvs[c] = lv[c] if c in lv.dtype.names else 0.0
+        ic = o.sample_ics(ntraj, lvs, seed=seed, ttra=ttra, bmax=bmax, dinit=dinit)
+        for k in range(ntraj):
+            res = o.integrate(ic["paq"][k:k + 1], ic["erra"][k:k + 1])
+            o.analyze(ic["paq0"][k:k + 1])
+            o.analyze(o.apply_transformation(res["paq"]))
+            done += 1
+            if time.perf_counter() - t0 > wall:
+                return done, time.perf_counter() - t0
+    return done, time.perf_counter() - t0
+
+
+def cpu_baseline(table, items, cores, wall):
+    """Trajectories/s of the oracle on `cores` processes, each running trajectories of its own
+    work items for about `wall` seconds (a bounded sample of the same workload)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    per = [[] for _ in range(cores)]
+    for k, it in enumerate(items):
+        per[k % cores].append((int(it["ilevel"]), int(it["ntraj"]), int(it["seed"]), float(it["ttra"]),
+                               float(it["bmax"]), float(it["dinit"])))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        out = pool.map(_cpu_worker, [(p, table, wall) for p in per])
+    n = sum(o[0] for o in out)
+    t = max(o[1] for o in out)
+    return n / t, n, t
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, path):
+        self.path = path
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.p or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or not f[0].isdigit():
+                continue
+            try:
+                sm.append(float(f[1].split()[0]))
+                mx = float(f[2].split()[0])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ntraj", type=int, default=65536, help="trajectories per step")
+    ap.add_argument("--max-attempts", type=int, default=1000000)
+    ap.add_argument("--cpu-wall", type=float, default=20.0, help="seconds of CPU work per core for the baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    table, items = workload(args.ntraj)
+    cores = host_cores()
+    metric = "trajectories/s"
+    cfg_json = {"workload": "N2+N on N3 UMN (N4 PIP), plain FP64: 64 levels (seed 2) x {5000,10000,20000} K, "
+                            "b = 7 sqrt(U) bohr, Dinit 15 bohr, rmax 30 bohr, m = 14.0067 amu",
+                "trajectories_per_step": int(args.ntraj), "work_items": int(len(items)),
+                "full_config_trajectories": 1000000, "parallelism": "replicas" if world > 1 else "single",
+                "l2": "inputs stay resident; each step re-samples initial conditions and rewrites all state "
+                      "(state per step %.0f MB, above the 129 MB L2 from 1M trajectories)" % (args.ntraj * 0.4e-3)}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        K, W = args.steps, args.warmup
+        times, total = [], 0
+        for s in range(W + K):
+            rate, n, t = cpu_baseline(table, items, cores, max(2.0, args.cpu_wall / 4))
+            if s >= W:
+                times.append(t)
+                total += n
+        value = total / sum(times)
+        line = {"impl": "reference", "metric": metric, "value": value, "unit": "trajectories/s", "n_gpus": 0,
+                "steps": K, "warmup": W, "ms_per_step": 1e3 * sum(times) / K, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": cfg_json,
+                "cpu_baseline": {"value": value, "unit": "trajectories/s", "cores": cores, "kind": "port",
+                                 "sample": "each step: %d processes x ~%.0f s of the same work items "
+                                           "(C restatement of the reference CPU path)" % (cores, max(2.0, args.cpu_wall / 4))},
+                "e2e": {"value": value, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    # CPU baseline first (spawned processes before any GPU call)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, n, t = cpu_baseline(table, items, cores, args.cpu_wall)
+        cpu = {"value": rate, "unit": "trajectories/s", "cores": cores, "kind": "port",
+               "sample": "%d trajectories of the same work items in %.1f s on %d processes "
+                         "(C restatement of the reference CPU path, -O2 no FMA)" % (n, t, cores)}
+
+    import torch
+    from coarseair_gb300 import api, _lib
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cfg = config()
+    H = api.Handle(cfg)
+    lib = H.lib
+    n = int(items["ntraj"].sum())
+    d_lv = torch.from_numpy(table.view(np.uint8).copy()).to(dev)
+    d_it = torch.from_numpy(items.view(np.uint8).copy()).to(dev)
+    d_res = torch.empty(n * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        H.check(lib.cair_run_queue_dev(H.h, len(table), d_lv.data_ptr(), len(items), d_it.data_ptr(), n,
+                                       args.max_attempts, d_res.data_ptr(), stream.cuda_stream), "cair_run_queue_dev")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                    else "/tmp/bench_clocks.csv")
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    counters = H.counters()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * args.steps * world / (ms / 1e3)
+
+    # integrator kernel time alone, on the same stream (roofline of the dominant kernel)
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=_lib.RESULT_DTYPE)
+    fm = H.flop_model()
+    flops_step = (counters["grad_evals"] * fm["grad"] + counters["energy_evals"] * fm["energy"] +
+                  counters["attempts"] * fm["attempt"])
+
+    # e2e through the host entry point with pinned buffers
+    e2e = None
+    if not args.no_e2e:
+        pin_res = torch.empty(n * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+        pin_lv = torch.from_numpy(table.view(np.uint8).copy()).pin_memory()
+        pin_it = torch.from_numpy(items.view(np.uint8).copy()).pin_memory()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps)):
+            H.check(lib.cair_run_queue(H.h, len(table), pin_lv.data_ptr(), len(items), pin_it.data_ptr(), n,
+                                       args.max_attempts, pin_res.data_ptr()), "cair_run_queue")
+        t1 = time.perf_counter()
+        e2e = {"value": n * max(1, args.steps) / (t1 - t0), "unit": "trajectories/s",
+               "h2d_bytes_per_step": int(table.nbytes + items.nbytes),
+               "d2h_bytes_per_step": int(n * _lib.RESULT_DTYPE.itemsize)}
+
+    # dominant kernel: the persistent integrator; its share of the step is measured in profiles/
+    peak_fp64 = fp64_peak_probe(lib, H)
+    ms_step = ms / args.steps
+    achieved = flops_step / (ms_step / 1e3) / 1e12
+    line = {"metric": metric, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg_json,
+            "gpu_launches": 5 * args.steps,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_fp64["tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / peak_fp64["tflops"], "traffic": None,
+                         "peak_source": peak_fp64["source"],
+                         "work": "executed FP64 operations of the pruned formulation per step "
+                                 "(exp, division and sqrt counted as one operation each)"},
+            "pes_evals_per_s": counters["grad_evals"] / (ms_step / 1e3),
+            "attempts_per_trajectory": counters["attempts"] / n,
+            "converged_fraction": float(np.mean(res["status"] == 0)),
+            "energy_not_conserved_fraction": float(np.mean(np.abs(res["dH"]) > cfg.ham_abs_tol))}
+    if e2e:
+        line["e2e"] = e2e
+    if cpu:
+        line["cpu_baseline"] = cpu
+    cs = clocks.summary()
+    if cs:
+        line["clocks"] = cs
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def fp64_peak_probe(lib, H):
+    """FP64 FMA throughput of this GPU, measured live (MEASURED_PEAKS.json carries bf16 and HBM only)."""
+    import ctypes
+    g = ctypes.c_double()
+    rc = lib.cair_fp64_peak_probe(H.h, ctypes.byref(g))
+    if rc == 0 and g.value > 0:
+        return {"tflops": g.value / 1e3, "source": "live DFMA probe (cair_fp64_peak_probe)"}
+    return {"tflops": 1.2, "source": "fallback"}
+
+
+if __name__ == "__main__":
+    main()

@@ -238,3 +238,71 @@ class MolecularState:
         H.check(H.lib.cair_find_state(H.h, n, dptr(paq_vel), out.ctypes.data_as(C.POINTER(_lib.TrajPoint))),
                 "cair_find_state")
         return out
+
+
+def level_table(levels):
+    """Level rows (systems.load_levels) as the C struct array cair_level[]."""
+    out = np.zeros(len(levels), dtype=_lib.LEVEL_DTYPE)
+    for c in _lib.LEVEL_DTYPE.names:
+        out[c] = levels[c]
+    return out
+
+
+def work_items(entries):
+    """entries: iterable of (ilevel, ipes, ntraj, seed, ttra, bmax, dinit) -> cair_work_item[] tiling
+    the batch in order."""
+    entries = list(entries)
+    out = np.zeros(len(entries), dtype=_lib.ITEM_DTYPE)
+    first = 0
+    for i, (il, ip, nt, seed, ttra, bmax, dinit) in enumerate(entries):
+        out[i] = (il, ip, first, nt, seed, ttra, bmax, dinit)
+        first += nt
+    return out
+
+
+def process_seed(iseed, iproc, npes=1, inode=1, rndnb=0):
+    """Stream seed of process iProc (Collision_Class.F90:295-296)."""
+    return int(iseed * (1 + (iproc - 1) * (npes + 1) + (inode - 1) * 200.0 * (npes + 1)) +
+               rndnb * 200.0 * 100.0 * (npes + 2))
+
+
+class InitialConditions:
+    """SetIniCondForward for diatom + atom work items, on the GPU."""
+
+    def __init__(self, handle):
+        self.H = handle
+
+    def sample(self, levels, items):
+        H = self.H
+        lv = np.ascontiguousarray(levels, dtype=_lib.LEVEL_DTYPE)
+        it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+        n = int(it["ntraj"].sum())
+        paq, paq0, erra = np.zeros((n, H.ne)), np.zeros((n, H.ne)), np.zeros((n, H.ne))
+        H0, b, ipes = np.zeros(n), np.zeros(n), np.zeros(n, np.int32)
+        H.check(H.lib.cair_sample_ics(H.h, len(lv), lv.ctypes.data, len(it), it.ctypes.data, n, dptr(paq),
+                                      dptr(paq0), dptr(erra), dptr(H0), dptr(b), iptr(ipes)), "cair_sample_ics")
+        return dict(paq=paq, paq0=paq0, erra=erra, H0=H0, b=b, ipes=ipes)
+
+
+class RunTrajectories:
+    """RunTrajectories for work items, end to end on the GPU; returns trajectories.out rows."""
+
+    def __init__(self, handle):
+        self.H = handle
+
+    def run(self, levels, items, max_attempts=None):
+        H = self.H
+        lv = np.ascontiguousarray(levels, dtype=_lib.LEVEL_DTYPE)
+        it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+        n = int(it["ntraj"].sum())
+        out = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+        ma = int(max_attempts if max_attempts is not None else H.cfg.max_attempts)
+        H.check(H.lib.cair_run_queue(H.h, len(lv), lv.ctypes.data, len(it), it.ctypes.data, n, ma, out.ctypes.data),
+                "cair_run_queue")
+        return out
+
+
+def histogram_assign(j, v, arr):
+    """Final (J, v, arrangement) integers of the histogram method (Statistics_Class.F90:626-656)."""
+    return (np.rint(np.asarray(j) - 0.5).astype(np.int64), np.rint(np.asarray(v) - 0.5).astype(np.int64),
+            np.rint(np.asarray(arr) - 0.5).astype(np.int64))

@@ -11,7 +11,7 @@
 #include <thread>
 #include <vector>
 
-#include "cair_kernels.cuh"
+#include "cair_ic.cuh"
 
 using namespace cair;
 
@@ -26,8 +26,10 @@ struct cair_handle {
   double mass[4];
   std::string err;
   cudaStream_t stream = nullptr;
-  void* d_scratch = nullptr;
+  void* d_scratch = nullptr;     // staging of host-pointer calls
   size_t scratch_bytes = 0;
+  void* d_work = nullptr;        // batch state of the *_dev / queue paths
+  size_t work_bytes = 0;
   unsigned long long* d_ctl = nullptr;   // [0] queue, [1..5] counters
   long long last_counters[5] = {0, 0, 0, 0, 0};
   double watchdog_s = 0.0;
@@ -108,6 +110,17 @@ int ensure_scratch(cair_handle* h, size_t bytes) {
   return 0;
 }
 
+int ensure_work(cair_handle* h, size_t bytes) {
+  if (bytes <= h->work_bytes) return 0;
+  if (h->d_work) cudaFree(h->d_work);
+  h->d_work = nullptr;
+  h->work_bytes = 0;
+  size_t b = bytes + bytes / 8 + (1 << 20);
+  CUDA_TRY(h, cudaMalloc(&h->d_work, b));
+  h->work_bytes = b;
+  return 0;
+}
+
 struct Carver {
   char* base;
   size_t off = 0;
@@ -155,6 +168,35 @@ int check_ipes(cair_handle* h, int64_t n, const int32_t* ipes) {
 
 }  // namespace
 
+// SetIniCondForward's per-trajectory integrator state (Collision_Class.F90:1102-1108)
+__global__ void cair_k_init_state(int64_t n, double dt0, double* t, double* dt, double* smax, double* smin,
+                                  int32_t* irej, int32_t* iste) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    t[k] = 0.0;
+    dt[k] = dt0;
+    smax[k] = -1.7976931348623157e308;
+    smin[k] = 1.7976931348623157e308;
+    irej[k] = 0;
+    iste[k] = 0;
+  }
+}
+
+// Register-resident DFMA chains: the FP64 pipe's throughput
+__global__ void cair_k_dfma_probe(double* out, int iters, double a, double b) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = 1.0 + 1e-3 * (tid & 7) + 1e-4 * i;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = fma(x[i], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += x[i];
+  out[tid] = s;
+}
+
 // 1-thread helper used at create time for Vinf
 __global__ void cair_k_diat_v(DevSys S, const double* r, double* v, int64_t n) {
   int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -199,6 +241,9 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
   S.incstp = d->inc_step;
   S.diat = d->diat_model;
   S.relax = d->relax;
+  S.eps = d->eps;
+  S.dt0 = d->dt0;
+  for (int i = 0; i < 4; ++i) S.mass[i] = d->mass[i];
   S.rmax = d->rmax;
   S.tmax = d->tmax;
   S.rpimax = 1.0 / d->rmax;
@@ -229,6 +274,7 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
     return bad(CAIR_EINVAL, "mass matrix is singular");
   }
   std::memcpy(S.Tpq, h->tpq, sizeof(S.Tpq));
+  std::memcpy(S.Tqp, h->tqp, sizeof(S.Tqp));
   // O2 UMN exponent factors (O2_UMN_DiatomicPotential_Class.F90 Ev2gm2/_Grad)
   {
     const double a[8] = {-1.488979427684798e3, 1.881435846488955e4, -1.053475425838226e5,
@@ -313,6 +359,7 @@ void cair_destroy(cair_handle* h) {
     if (h->d_coef[p]) cudaFree(h->d_coef[p]);
   if (h->d_gauss) cudaFree(h->d_gauss);
   if (h->d_scratch) cudaFree(h->d_scratch);
+  if (h->d_work) cudaFree(h->d_work);
   if (h->d_ctl) cudaFree(h->d_ctl);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -559,25 +606,198 @@ int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_
   return wait_stream(h);
 }
 
+namespace {
+struct BatchBufs {
+  double *paq, *paq0, *erra, *t, *dt, *H, *H0, *smax, *smin, *b, *draws;
+  int32_t *irej, *iste, *status, *ipes, *item_of;
+};
+
+int carve_batch(cair_handle* h, int64_t n, bool with_state, BatchBufs& B) {
+  size_t per = sizeof(double) * (12 * 3 + 8 + kDraws) + sizeof(int32_t) * 5;
+  if (int e = ensure_work(h, n * per + 32 * 256)) return e;
+  Carver c{(char*)h->d_work};
+  B.paq = c.take<double>(n * 12); B.paq0 = c.take<double>(n * 12); B.erra = c.take<double>(n * 12);
+  B.t = c.take<double>(n); B.dt = c.take<double>(n); B.H = c.take<double>(n); B.H0 = c.take<double>(n);
+  B.smax = c.take<double>(n); B.smin = c.take<double>(n); B.b = c.take<double>(n);
+  B.draws = c.take<double>(n * kDraws);
+  B.irej = c.take<int32_t>(n); B.iste = c.take<int32_t>(n); B.status = c.take<int32_t>(n);
+  B.ipes = c.take<int32_t>(n); B.item_of = c.take<int32_t>(n);
+  (void)with_state;
+  return 0;
+}
+
+int sample_ics_into(cair_handle* h, int32_t nitems, const cair_work_item* d_items, const cair_level* d_levels,
+                    int64_t ntot, double* paq, double* paq0, double* erra, double* H0, double* b, int32_t* ipes,
+                    int32_t* item_of, double* draws, cudaStream_t st) {
+  k_ic_draws<<<(nitems + 63) / 64, 64, 0, st>>>(nitems, d_items, d_levels, draws, item_of);
+  if (int e = check_launch(h)) return e;
+  int g = grid_for(h, ntot);
+  if (model_of(h) == CAIR_PES_O3_UMN)
+    k_sample_ic3<CAIR_PES_O3_UMN><<<g, 128, 0, st>>>(h->sys, ntot, d_items, d_levels, draws, item_of, paq, paq0,
+                                                     erra, H0, b, ipes);
+  else
+    k_sample_ic3<CAIR_PES_N3_UMN><<<g, 128, 0, st>>>(h->sys, ntot, d_items, d_levels, draws, item_of, paq, paq0,
+                                                     erra, H0, b, ipes);
+  return check_launch(h);
+}
+
+int validate_items(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                   const cair_work_item* items, int64_t ntot) {
+  int64_t sum = 0;
+  for (int i = 0; i < nitems; ++i) {
+    const cair_work_item& w = items[i];
+    if (w.ilevel < 0 || w.ilevel >= nlevels) return fail(h, CAIR_EINVAL, "work item level out of range");
+    if (w.ipes < 0 || w.ipes >= h->sys.npes) return fail(h, CAIR_EINVAL, "work item surface out of range");
+    if (w.ntraj < 0 || w.first != sum) return fail(h, CAIR_EINVAL, "work items must tile [0, ntot) in order");
+    if (!(w.dinit > 0.0) || std::fabs(w.bmax) > w.dinit) return fail(h, CAIR_EINVAL, "impact parameter exceeds Dinit");
+    if (!(w.ttra > 0.0)) return fail(h, CAIR_EINVAL, "translational temperature must be positive");
+    sum += w.ntraj;
+  }
+  if (sum != ntot) return fail(h, CAIR_EINVAL, "ntot differs from the sum of the items' ntraj");
+  for (int i = 0; i < nlevels; ++i)
+    if (!(levels[i].tau > 0.0) || !(levels[i].ro > 0.0)) return fail(h, CAIR_EINVAL, "level with tau or ro <= 0");
+  return 0;
+}
+}  // namespace
+
+int cair_sample_ics_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                        const cair_work_item* items, int64_t ntot, double* paq, double* paq0, double* erra,
+                        double* H0, double* b, int32_t* ipes, int32_t* item_of, void* stream) {
+  if (!h || nlevels < 1 || nitems < 0 || ntot < 0 || !levels || !items || !paq || !paq0 || !erra || !H0 || !b ||
+      !ipes || !item_of)
+    return fail(h, CAIR_EINVAL, "cair_sample_ics_dev: bad argument");
+  if (ntot == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "initial conditions: diatom + atom only");
+  if (int e = ensure_scratch(h, ntot * kDraws * sizeof(double) + 1024)) return e;
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  return sample_ics_into(h, nitems, items, levels, ntot, paq, paq0, erra, H0, b, ipes, item_of,
+                         (double*)h->d_scratch, st);
+}
+
+int cair_sample_ics(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                    const cair_work_item* items, int64_t ntot, double* paq, double* paq0, double* erra,
+                    double* H0, double* b, int32_t* ipes) {
+  if (!h || nlevels < 1 || nitems < 0 || ntot < 0 || !levels || !items || !paq || !paq0 || !erra || !H0 || !b ||
+      !ipes)
+    return fail(h, CAIR_EINVAL, "cair_sample_ics: bad argument");
+  if (ntot == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "initial conditions: diatom + atom only");
+  if (int e = validate_items(h, nlevels, levels, nitems, items, ntot)) return e;
+  BatchBufs B;
+  if (int e = carve_batch(h, ntot, false, B)) return e;
+  if (int e = ensure_scratch(h, nlevels * sizeof(cair_level) + nitems * sizeof(cair_work_item) + 1024)) return e;
+  Carver c{(char*)h->d_scratch};
+  cair_level* d_lv = c.take<cair_level>(nlevels);
+  cair_work_item* d_it = c.take<cair_work_item>(nitems > 0 ? nitems : 1);
+  cudaStream_t st = h->stream;
+  CUDA_TRY(h, cudaMemcpyAsync(d_lv, levels, nlevels * sizeof(cair_level), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_it, items, nitems * sizeof(cair_work_item), cudaMemcpyHostToDevice, st));
+  if (int e = sample_ics_into(h, nitems, d_it, d_lv, ntot, B.paq, B.paq0, B.erra, B.H0, B.b, B.ipes, B.item_of,
+                              B.draws, st))
+    return e;
+  CUDA_TRY(h, cudaMemcpyAsync(paq, B.paq, ntot * 12 * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(paq0, B.paq0, ntot * 12 * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(erra, B.erra, ntot * 12 * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(H0, B.H0, ntot * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(b, B.b, ntot * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(ipes, B.ipes, ntot * 4, cudaMemcpyDeviceToHost, st));
+  return wait_stream(h);
+}
+
+int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                       const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results,
+                       void* stream) {
+  if (!h || nlevels < 1 || nitems < 0 || ntot < 0 || !levels || !items || !results || max_attempts < 1)
+    return fail(h, CAIR_EINVAL, "cair_run_queue_dev: bad argument");
+  if (ntot == 0) return 0;
+  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_run_queue: diatom + atom only");
+  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_run_queue: only NSteps = 3 is built");
+  BatchBufs B;
+  if (int e = carve_batch(h, ntot, true, B)) return e;
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  if (int e = sample_ics_into(h, nitems, items, levels, ntot, B.paq, B.paq0, B.erra, B.H0, B.b, B.ipes, B.item_of,
+                              B.draws, st))
+    return e;
+  cair_k_init_state<<<grid_for(h, ntot), 128, 0, st>>>(ntot, h->sys.dt0, B.t, B.dt, B.smax, B.smin, B.irej, B.iste);
+  if (int e = check_launch(h)) return e;
+  CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
+  IntegrateArgs A{ntot, B.ipes, B.paq, B.t, B.dt, B.erra, B.H, B.smax, B.smin, B.irej, B.iste, B.status,
+                  max_attempts, h->d_ctl, h->d_ctl + 1};
+  if (int e = launch_integrate(h, A, st)) return e;
+  k_results3<<<grid_for(h, ntot), 128, 0, st>>>(h->sys, h->fs, ntot, B.paq0, B.paq, B.H0, B.H, B.t, B.status,
+                                                  B.item_of, items, results);
+  return check_launch(h);
+}
+
+int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                   const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results) {
+  if (!h || nlevels < 1 || nitems < 0 || ntot < 0 || !levels || !items || !results || max_attempts < 1)
+    return fail(h, CAIR_EINVAL, "cair_run_queue: bad argument");
+  if (ntot == 0) return 0;
+  if (int e = validate_items(h, nlevels, levels, nitems, items, ntot)) return e;
+  if (int e = ensure_scratch(h, nlevels * sizeof(cair_level) + nitems * sizeof(cair_work_item) +
+                                     ntot * sizeof(cair_traj_result) + 4096))
+    return e;
+  Carver c{(char*)h->d_scratch};
+  cair_level* d_lv = c.take<cair_level>(nlevels);
+  cair_work_item* d_it = c.take<cair_work_item>(nitems > 0 ? nitems : 1);
+  cair_traj_result* d_res = c.take<cair_traj_result>(ntot);
+  cudaStream_t st = h->stream;
+  CUDA_TRY(h, cudaMemcpyAsync(d_lv, levels, nlevels * sizeof(cair_level), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_it, items, nitems * sizeof(cair_work_item), cudaMemcpyHostToDevice, st));
+  if (int e = cair_run_queue_dev(h, nlevels, d_lv, nitems, d_it, ntot, max_attempts, d_res, st)) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(results, d_res, ntot * sizeof(cair_traj_result), cudaMemcpyDeviceToHost, st));
+  unsigned long long ctr[5];
+  CUDA_TRY(h, cudaMemcpyAsync(ctr, h->d_ctl + 1, sizeof(ctr), cudaMemcpyDeviceToHost, st));
+  if (int e = wait_stream(h)) return e;
+  for (int i = 0; i < 5; ++i) h->last_counters[i] = (long long)ctr[i];
+  return 0;
+}
+
 int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, double* fa, double* ex) {
   if (!h || ipes < 0 || ipes >= h->sys.npes) return CAIR_EINVAL;
-  // Counted from the executed formulation: PIP part from the generator's operation
-  // counts, plus MEG variables, diatomics, pair distances, TransToCart and the RHS.
+  // FP64 operations of the executed formulation, counted from the device code (an FMA counts
+  // two, exp / division / sqrt one each): PIP part from the generator's counts; per pair the
+  // diatomic (O2 UMN 107 with gradient, 64 energy only; N2 UMN_ForN4 64 / 40) and the MEG
+  // variable (11 / 7); pair distances 36, TransToCart 46, Hamilton's equations 18, assembly 15.
   const int m = h->sys.pes[ipes].model;
   const bool o2 = h->sys.diat == CAIR_DIAT_O2_UMN;
-  // per pair: diatomic energy+gradient and MEG with its derivative
-  double diat_g = o2 ? 8 * 4 + 30 : 40, diat_e = o2 ? 8 * 2 + 20 : 24;
-  double meg_g = 9, meg_e = 6;
-  double pip_g = m == CAIR_PES_O3_UMN ? PIP_O3_EVAL_FLOPS : PIP_N3_EVAL_FLOPS;
-  double pip_e = m == CAIR_PES_O3_UMN ? PIP_O3_VALUE_FLOPS : PIP_N3_VALUE_FLOPS;
-  double geom = 3 * 8 + 6;          // pair distances + last atom
-  double t2c = 3 + 6 * 6 + 4;       // TransToCart_3Atoms
-  double rhs = 12 + 6;              // dq/dt and sign flip
-  if (fg) *fg = pip_g + 3 * (diat_g + meg_g) + geom + t2c + rhs + 8;
-  if (fe) *fe = pip_e + 3 * (diat_e + meg_e) + geom + 6 * 4 + 3;
-  // per attempt outside the surface: mmidv updates, extrapolation, error norms
-  if (fa) *fa = 12 * (2 * 13 + 3 * 3) + 12 * 3 * 8 + 12 * 2 * 3 + 20;
+  const double diat_g = o2 ? 107 : 64, diat_e = o2 ? 64 : 40, meg_g = 11, meg_e = 7;
+  const double pip_g = m == CAIR_PES_O3_UMN ? PIP_O3_EVAL_FLOPS : PIP_N3_EVAL_FLOPS;
+  const double pip_e = m == CAIR_PES_O3_UMN ? PIP_O3_VALUE_FLOPS : PIP_N3_VALUE_FLOPS;
+  if (fg) *fg = pip_g + 3 * (diat_g + meg_g) + 36 + 46 + 18 + 15;
+  if (fe) *fe = pip_e + 3 * (diat_e + meg_e) + 36 + 30 + 8;
+  // per attempt outside the right-hand side: modified-midpoint updates (432), rational
+  // extrapolation (297), error norms and step control (82)
+  if (fa) *fa = 811;
   if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1);
+  return 0;
+}
+
+int cair_fp64_peak_probe(cair_handle* h, double* gflops) {
+  if (!h || !gflops) return CAIR_EINVAL;
+  const int block = 256, grid = h->nsm * 8, iters = 4096;
+  double* d = nullptr;
+  CUDA_TRY(h, cudaMalloc(&d, sizeof(double) * grid * block));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0, h->stream);
+    cair_k_dfma_probe<<<grid, block, 0, h->stream>>>(d, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1, h->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    double gf = 2.0 * 8.0 * iters * (double)grid * block / (ms * 1e-3) / 1e9;
+    if (rep > 0 && gf > best) best = gf;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (int e = check_launch(h)) return e;
+  *gflops = best;
   return 0;
 }
 

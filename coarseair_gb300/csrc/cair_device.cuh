@@ -22,8 +22,12 @@ struct DevPes {
 
 struct DevSys {
   int32_t natoms, nv, ne, npairs, npes, nsteps, ncall, incstp, diat;
+  double mass[4];
   double mMiMn[3];
   double Tpq[81];       // column-major (i,j) -> [i + 9 j]
+  double Tqp[81];
+  double eps;           // "Error control parameter" (SetErrorFactor)
+  double dt0;
   double relax, rmax, tmax, rpimax;
   double o2_ab[8];      // alpha * beta**k          (O2_UMN Ev2gm2 exponent factors)
   double o2_cd[8];      // 2 * a(k) * alpha * beta**k (O2_UMN Ev2gm2_Grad factors)
@@ -422,7 +426,7 @@ __device__ __forceinline__ int bs_attempt(const F& f, double (&y)[NE], double& x
     for (int i = 0; i < NE; ++i) {
       double dd = yt[k][i] - ylast[i];
       if (dd != dd) nan = 1;
-      ok = err_below_one(dd, __ldg(yscal + i)) && ok;
+      ok = err_below_one(dd, yscal[i]) && ok;
     }
     below[k] = ok;
   }

@@ -381,66 +381,69 @@ __device__ void find_state(const DevSys& S, const FsArgs& F, int ipair, int ia, 
   m.viba = viba;
 }
 
-// Analyze for 3 atoms (the atom-diatom systems)
+// Analyze for 3 atoms (the atom-diatom systems); p = velocities + coordinates
+__device__ void analyze3(const DevSys& S, const FsArgs& F, const double* __restrict__ p, cair_traj_point& o) {
+  double xx[3][3], xd[3][3];
+  for (int a = 0; a < 2; ++a)
+    for (int d = 0; d < 3; ++d) { xd[d][a] = p[d + 3 * a]; xx[d][a] = p[d + 3 * a + 6]; }
+  for (int d = 0; d < 3; ++d) {
+    xd[d][2] = (0.0 + S.mMiMn[0] * p[d]) + S.mMiMn[1] * p[d + 3];
+    xx[d][2] = (0.0 + S.mMiMn[0] * p[d + 6]) + S.mMiMn[1] * p[d + 9];
+  }
+  const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+  double rbs[3];
+  for (int q = 0; q < 3; ++q) {
+    double a = xx[0][pa[q]] - xx[0][pb[q]], b = xx[1][pa[q]] - xx[1][pb[q]], c = xx[2][pa[q]] - xx[2][pb[q]];
+    rbs[q] = a * a + b * b + c * c;
+  }
+  int ip = 1;
+  if (rbs[1] < rbs[ip - 1]) ip = 2;
+  if (rbs[2] < rbs[ip - 1]) ip = 3;
+  int m1a = pa[ip - 1], m1b = pb[ip - 1];
+  double cm[3][2], cmd[3][2];
+  for (int d = 0; d < 3; ++d) {
+    cm[d][0] = cm[d][1] = cmd[d][0] = cmd[d][1] = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      int w = (j == m1a || j == m1b) ? 0 : 1;
+      cm[d][w] = cm[d][w] + F.mass[j] * xx[d][j];
+      cmd[d][w] = cmd[d][w] + F.mass[j] * xd[d][j];
+    }
+  }
+  double xp = 0.0, xt = 0.0;
+  for (int j = 0; j < 3; ++j) {
+    if (j == m1a || j == m1b) xp = xp + F.mass[j];
+    else xt = xt + F.mass[j];
+  }
+  double xpi = 1.0 / xp, xti = 1.0 / xt, xrel[3], vrel[3];
+  for (int d = 0; d < 3; ++d) {
+    cm[d][0] *= xpi; cm[d][1] *= xti; cmd[d][0] *= xpi; cmd[d][1] *= xti;
+    xrel[d] = cm[d][0] - cm[d][1];
+    vrel[d] = cmd[d][0] - cmd[d][1];
+  }
+  double xnum = xrel[0] * vrel[0] + xrel[1] * vrel[1] + xrel[2] * vrel[2];
+  double v = vrel[0] * vrel[0] + vrel[1] * vrel[1] + vrel[2] * vrel[2];
+  double tt = -xnum / v;
+  double e0 = xrel[0] + tt * vrel[0], e1 = xrel[1] + tt * vrel[1], e2 = xrel[2] + tt * vrel[2];
+  o.b = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+  o.xkin = 0.0;
+  for (int d = 0; d < 3; ++d) o.xkin = o.xkin + 0.5 * xp * (cmd[d][0] * cmd[d][0]) + 0.5 * xt * (cmd[d][1] * cmd[d][1]);
+  for (int d = 0; d < 3; ++d) o.vrel[d] = vrel[d];
+  o.nmol = 1;
+  o.pad = 0;
+  double X[6], XD[6];
+  for (int d = 0; d < 3; ++d) {
+    X[2 * d] = xx[d][m1a]; X[2 * d + 1] = xx[d][m1b];
+    XD[2 * d] = xd[d][m1a]; XD[2 * d + 1] = xd[d][m1b];
+  }
+  find_state(S, F, ip, m1a, m1b, X, XD, o.mol[0]);
+  o.mol[1].ipair = 0; o.mol[1].itype = 0; o.mol[1].eint = 0.0; o.mol[1].angmom = 0.0; o.mol[1].viba = 0.0;
+}
+
 __global__ void __launch_bounds__(128) k_find_state3(DevSys S, FsArgs F, int64_t n, const double* __restrict__ paq,
                                                      cair_traj_point* __restrict__ out) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    const double* p = paq + 12 * k;
-    double xx[3][3], xd[3][3];
-    for (int a = 0; a < 2; ++a)
-      for (int d = 0; d < 3; ++d) { xd[d][a] = p[d + 3 * a]; xx[d][a] = p[d + 3 * a + 6]; }
-    for (int d = 0; d < 3; ++d) {
-      xd[d][2] = (0.0 + S.mMiMn[0] * p[d]) + S.mMiMn[1] * p[d + 3];
-      xx[d][2] = (0.0 + S.mMiMn[0] * p[d + 6]) + S.mMiMn[1] * p[d + 9];
-    }
-    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
-    double rbs[3];
-    for (int q = 0; q < 3; ++q) {
-      double a = xx[0][pa[q]] - xx[0][pb[q]], b = xx[1][pa[q]] - xx[1][pb[q]], c = xx[2][pa[q]] - xx[2][pb[q]];
-      rbs[q] = a * a + b * b + c * c;
-    }
-    int ip = 1;
-    if (rbs[1] < rbs[ip - 1]) ip = 2;
-    if (rbs[2] < rbs[ip - 1]) ip = 3;
-    int m1a = pa[ip - 1], m1b = pb[ip - 1];
-    double cm[3][2], cmd[3][2];
-    for (int d = 0; d < 3; ++d) {
-      cm[d][0] = cm[d][1] = cmd[d][0] = cmd[d][1] = 0.0;
-      for (int j = 0; j < 3; ++j) {
-        int w = (j == m1a || j == m1b) ? 0 : 1;
-        cm[d][w] = cm[d][w] + F.mass[j] * xx[d][j];
-        cmd[d][w] = cmd[d][w] + F.mass[j] * xd[d][j];
-      }
-    }
-    double xp = 0.0, xt = 0.0;
-    for (int j = 0; j < 3; ++j) {
-      if (j == m1a || j == m1b) xp = xp + F.mass[j];
-      else xt = xt + F.mass[j];
-    }
-    double xpi = 1.0 / xp, xti = 1.0 / xt, xrel[3], vrel[3];
-    for (int d = 0; d < 3; ++d) {
-      cm[d][0] *= xpi; cm[d][1] *= xti; cmd[d][0] *= xpi; cmd[d][1] *= xti;
-      xrel[d] = cm[d][0] - cm[d][1];
-      vrel[d] = cmd[d][0] - cmd[d][1];
-    }
-    double xnum = xrel[0] * vrel[0] + xrel[1] * vrel[1] + xrel[2] * vrel[2];
-    double v = vrel[0] * vrel[0] + vrel[1] * vrel[1] + vrel[2] * vrel[2];
-    double tt = -xnum / v;
-    double e0 = xrel[0] + tt * vrel[0], e1 = xrel[1] + tt * vrel[1], e2 = xrel[2] + tt * vrel[2];
     cair_traj_point o;
-    o.b = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
-    o.xkin = 0.0;
-    for (int d = 0; d < 3; ++d) o.xkin = o.xkin + 0.5 * xp * (cmd[d][0] * cmd[d][0]) + 0.5 * xt * (cmd[d][1] * cmd[d][1]);
-    for (int d = 0; d < 3; ++d) o.vrel[d] = vrel[d];
-    o.nmol = 1;
-    o.pad = 0;
-    double X[6], XD[6];
-    for (int d = 0; d < 3; ++d) {
-      X[2 * d] = xx[d][m1a]; X[2 * d + 1] = xx[d][m1b];
-      XD[2 * d] = xd[d][m1a]; XD[2 * d + 1] = xd[d][m1b];
-    }
-    find_state(S, F, ip, m1a, m1b, X, XD, o.mol[0]);
-    o.mol[1].ipair = 0; o.mol[1].itype = 0; o.mol[1].eint = 0.0; o.mol[1].angmom = 0.0; o.mol[1].viba = 0.0;
+    analyze3(S, F, paq + 12 * k, o);
     out[k] = o;
   }
 }

@@ -130,6 +130,41 @@ typedef struct cair_traj_point {
   int32_t pad;
 } cair_traj_point;
 
+/* One row of a level list (LevelsContainer_Class.F90:86-262; columns of FromUMN_Sorted.inp). */
+typedef struct cair_level {
+  int32_t vqn, jqn;
+  double eint, egam, rmin, rmax, vmin, vmax, tau, ri, ro;
+} cair_level;
+
+/* One state-specific run of RunTrajectories: ntraj trajectories from one initial level at one
+ * translational temperature, drawn from their own random-number stream (the per-process
+ * stream of Collision_Class.F90:286-313).  Its trajectories occupy rows
+ * [first, first + ntraj) of the batch arrays. */
+typedef struct cair_work_item {
+  int32_t ilevel;   /* row of the level table                                  */
+  int32_t ipes;     /* 0-based surface                                          */
+  int64_t first;    /* first row of this item in the batch arrays               */
+  int64_t ntraj;    /* number of trajectories                                   */
+  int64_t seed;     /* stream seed ("Initial Random Nb Seed" mapped per process) */
+  double ttra;      /* translational temperature [K] (Boltzmann model)         */
+  double bmax;      /* impact-parameter bound [bohr] (Circles, one ring)       */
+  double dinit;     /* initial separation [bohr]                               */
+} cair_work_item;
+
+/* One row of trajectories.out (Integrator_Class.F90:884-933) plus diagnostics. */
+typedef struct cair_traj_result {
+  int64_t idx;      /* trajectory index within its item, 1-based (Traj%Idx)          */
+  int32_t item;     /* work item                                                   */
+  int32_t ipes;     /* 0-based surface                                              */
+  int32_t status;   /* cair_traj_status                                             */
+  int32_t pad;
+  double bmax, b;   /* ring bound and impact parameter of the analysed initial point */
+  double j_i, v_i, arr_i;  /* AngMom, viba, 16*iPair + itype + 1/2 of the initial point */
+  double j_f, v_f, arr_f;  /* the same for the final point                             */
+  double t;         /* final time [a.u.]                                            */
+  double dH;        /* H_final - H0 [Eh]; |dH| > HamAbsTol goes to the HNotCons file */
+} cair_traj_result;
+
 typedef struct cair_handle cair_handle;
 
 /* Create a handle on the current CUDA device: copies the surfaces to device memory and
@@ -190,11 +225,37 @@ int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_
 /* ApplyTransformation on device: momenta -> velocities, in place on a copy. */
 int cair_apply_transformation(cair_handle* h, int64_t n, const double* paq, double* paq_vel);
 
+/* Initial conditions of diatom + atom trajectories on the device (SetIniCondForward,
+ * Collision_Class.F90:1065-1211: level, BondLength vibrational phase, orientation, Boltzmann
+ * translational energy, impact parameter, momenta, H0, error scales).  One device thread
+ * per work item runs the item's random-number stream in the reference's draw order; one
+ * thread per trajectory does the rest.  Host arrays; ntot = sum of items[].ntraj. */
+int cair_sample_ics(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                    const cair_work_item* items, int64_t ntot, double* paq, double* paq0, double* erra,
+                    double* H0, double* b, int32_t* ipes);
+int cair_sample_ics_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                        const cair_work_item* items, int64_t ntot, double* paq, double* paq0, double* erra,
+                        double* H0, double* b, int32_t* ipes, int32_t* item_of, void* stream);
+
+/* RunTrajectories for a set of work items, end to end on the GPU: initial conditions,
+ * propagation (persistent kernel), ApplyTransformation, analysis of the initial and final
+ * points and the trajectories.out rows.  Host arrays: results[ntot]. */
+int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                   const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results);
+/* The same on device pointers (levels, items, results on the device), asynchronous. */
+int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                       const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results,
+                       void* stream);
+
 /* Algorithmic FP64 operation counts the library's kernels execute per PES energy+gradient
  * evaluation, per energy-only evaluation and per BS attempt (excluding the PES), for
  * roofline accounting.  `exp_per_eval` counts exponentials separately. */
 int cair_flop_model(const cair_handle* h, int32_t ipes, double* flops_grad, double* flops_energy,
                     double* flops_attempt_overhead, double* exp_per_eval);
+
+/* FP64 fused-multiply-add throughput of the handle's GPU in GFLOP/s (2 flops per DFMA),
+ * measured with a register-resident DFMA kernel; the denominator of the FP64 roofline. */
+int cair_fp64_peak_probe(cair_handle* h, double* gflops);
 
 /* Device counters of the last cair_integrate*: total BS attempts, accepted, rejected,
  * PES gradient evaluations, PES energy evaluations. */

@@ -51,6 +51,11 @@ int main(void) {
   P(cair_system_desc, nsteps); P(cair_system_desc, nquad); P(cair_system_desc, rsmal); P(cair_system_desc, tthresau);
   P(cair_pes_desc, coef); P(cair_pes_desc, totdiss);
   P(cair_traj_point, b); P(cair_traj_point, vrel); P(cair_traj_point, nmol);
+  printf("sizeof.cair_level %zu\n", sizeof(cair_level));
+  printf("sizeof.cair_work_item %zu\n", sizeof(cair_work_item));
+  printf("sizeof.cair_traj_result %zu\n", sizeof(cair_traj_result));
+  P(cair_level, eint); P(cair_level, ro); P(cair_work_item, first); P(cair_work_item, dinit);
+  P(cair_traj_result, status); P(cair_traj_result, bmax); P(cair_traj_result, dH);
   return 0;
 }
 """
@@ -68,10 +73,17 @@ def test_struct_layout_matches_c(tmp_path):
     assert int(out["sizeof.cair_system_desc"]) == ctypes.sizeof(_lib.SystemDesc)
     assert int(out["sizeof.cair_pes_desc"]) == ctypes.sizeof(_lib.PesDesc)
     assert int(out["sizeof.cair_traj_point"]) == ctypes.sizeof(_lib.TrajPoint) == _lib.TRAJ_POINT_DTYPE.itemsize
+    assert int(out["sizeof.cair_level"]) == _lib.LEVEL_DTYPE.itemsize
+    assert int(out["sizeof.cair_work_item"]) == _lib.ITEM_DTYPE.itemsize
+    assert int(out["sizeof.cair_traj_result"]) == _lib.RESULT_DTYPE.itemsize
+    dt = {"cair_level": _lib.LEVEL_DTYPE, "cair_work_item": _lib.ITEM_DTYPE, "cair_traj_result": _lib.RESULT_DTYPE}
     for key, val in out.items():
         if key.startswith("sizeof"):
             continue
         T, F = key.split(".")
+        if T in dt:
+            assert dt[T].fields[F][1] == int(val), key
+            continue
         cls = {"cair_system_desc": _lib.SystemDesc, "cair_pes_desc": _lib.PesDesc, "cair_traj_point": _lib.TrajPoint}[T]
         assert getattr(cls, F).offset == int(val), key
 

@@ -55,14 +55,17 @@ def test_surface_energy_and_gradient_parity(gpu_lib, oracle_lib, name):
     R, Qall = np.concatenate([R, R2]), np.concatenate([Qall, Q2])
     V_o, g_o, m_o = o.compute(R, Qall)
     V_g, g_g, m_g = api.PES(H).Compute(R, Qall)
-    assert np.all(np.abs(V_g - V_o) <= 1e-12 * np.abs(V_o))
+    # relative to the energy scale of the surface (0.1 Eh, about half a well depth): V crosses
+    # zero, where a pointwise relative error is undefined
+    vs = np.maximum(np.abs(V_o), 0.1)
+    assert np.all(np.abs(V_g - V_o) <= 1e-12 * vs)
     gs = np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2)
     assert np.all(np.abs(g_g - g_o) <= 1e-12 * gs)
     ms = np.maximum(np.abs(m_o).max(axis=1, keepdims=True), 1e-2)
     assert np.all(np.abs(m_g - m_o) <= 1e-12 * ms)
     # energy-only path (PES%Potential)
     Ve = api.PES(H).Potential(R, Qall)
-    assert np.all(np.abs(Ve - V_o) <= 1e-12 * np.abs(V_o))
+    assert np.all(np.abs(Ve - V_o) <= 1e-12 * vs)
 
 
 @pytest.mark.parametrize("name", ["O3", "N3"])
@@ -76,7 +79,7 @@ def test_rhs_and_hamiltonian_parity(gpu_lib, oracle_lib, name):
     assert np.all(np.abs(yp_g - yp_o) <= 1e-12 * sc)
     h_o, r_o = o.hamiltonian(y)
     h_g, r_g = api.Collision(H).Hamiltonian(y)
-    assert np.all(np.abs(h_g - h_o) <= 1e-12 * np.maximum(np.abs(h_o), 1e-3))
+    assert np.all(np.abs(h_g - h_o) <= 1e-12 * np.maximum(np.abs(h_o), 0.1))
     assert np.allclose(r_g, r_o, rtol=1e-15, atol=0)
     assert np.allclose(api.Collision(H).ApplyTransformation(y), o.apply_transformation(y), rtol=1e-14, atol=1e-300)
     assert np.allclose(H.tpq(), o.tpq, rtol=0, atol=0)
