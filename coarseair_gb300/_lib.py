@@ -52,7 +52,8 @@ LEVEL_DTYPE = np.dtype([("vqn", "i4"), ("jqn", "i4"), ("eint", "f8"), ("egam", "
                         ("rmax", "f8"), ("vmin", "f8"), ("vmax", "f8"), ("tau", "f8"), ("ri", "f8"), ("ro", "f8")])
 ITEM_DTYPE = np.dtype([("ilevel", "i4"), ("ipes", "i4"), ("first", "i8"), ("ntraj", "i8"), ("seed", "i8"),
                        ("ttra", "f8"), ("bmax", "f8"), ("dinit", "f8")])
-RESULT_DTYPE = np.dtype([("idx", "i8"), ("item", "i4"), ("ipes", "i4"), ("status", "i4"), ("pad", "i4"),
+RESULT_DTYPE = np.dtype([("idx", "i8"), ("item", "i4"), ("ipes", "i4"), ("status", "i4"), ("iste", "i4"),
+                         ("irej", "i4"), ("pad", "i4"),
                          ("bmax", "f8"), ("b", "f8"), ("j_i", "f8"), ("v_i", "f8"), ("arr_i", "f8"),
                          ("j_f", "f8"), ("v_f", "f8"), ("arr_f", "f8"), ("t", "f8"), ("dH", "f8")])
 
@@ -78,7 +79,8 @@ SIGNATURES = [
     ("cair_sample_ics", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, _D, _D, _D, _D, _D, _I]),
     ("cair_sample_ics_dev", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("cair_run_queue", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P]),
-    ("cair_run_queue_dev", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, _P]),
+    ("cair_run_queue_dev", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, _P, _P]),
+    ("cair_queue_workspace_bytes", C.c_int64, [C.c_int64]),
     ("cair_flop_model", C.c_int, [_P, C.c_int32, _D, _D, _D, _D]),
     ("cair_last_counters", C.c_int, [_P, _L]),
     ("cair_fp64_peak_probe", C.c_int, [_P, _D]),

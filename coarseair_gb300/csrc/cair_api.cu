@@ -181,6 +181,35 @@ __global__ void cair_k_init_state(int64_t n, double dt0, double* t, double* dt, 
   }
 }
 
+// Queue ordering: 256 buckets of log2(initial relative speed), slowest (longest) first.
+__device__ __forceinline__ int speed_bucket(double v) {
+  double l = log2(v > 1e-300 ? v : 1e-300);
+  int b = (int)floor((l + 20.0) * 8.0);
+  return b < 0 ? 0 : (b > 255 ? 255 : b);
+}
+__global__ void cair_k_bucket_count(int64_t n, const double* __restrict__ key, unsigned long long* counts) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(counts + speed_bucket(key[k]), 1ull);
+}
+__global__ void cair_k_bucket_scan(const unsigned long long* counts, unsigned long long* offsets) {
+  __shared__ unsigned long long c[256];
+  c[threadIdx.x] = counts[threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long acc = 0;
+    for (int i = 0; i < 256; ++i) { unsigned long long v = c[i]; c[i] = acc; acc += v; }
+  }
+  __syncthreads();
+  offsets[threadIdx.x] = c[threadIdx.x];
+}
+__global__ void cair_k_bucket_scatter(int64_t n, const double* __restrict__ key, unsigned long long* offsets,
+                                      int32_t* __restrict__ order) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long pos = atomicAdd(offsets + speed_bucket(key[k]), 1ull);
+    order[pos] = (int32_t)k;
+  }
+}
+
 // Register-resident DFMA chains: the FP64 pipe's throughput
 __global__ void cair_k_dfma_probe(double* out, int iters, double a, double b) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -490,7 +519,9 @@ int cair_bs_steps(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, d
 
 static int launch_integrate(cair_handle* h, const IntegrateArgs& A, cudaStream_t st) {
   int m = model_of(h);
-  int block = 128, per_sm = 0;
+  // 64-thread blocks: a block holding one long trajectory frees the rest of its SM for the
+  // next batch on another stream
+  int block = 64, per_sm = 0;
   if (m == CAIR_PES_O3_UMN)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate3<CAIR_PES_O3_UMN, 3>, block, 0);
   else
@@ -514,10 +545,10 @@ int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* p
   if (n == 0) return 0;
   if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: 4-atom systems not built");
   if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: only NSteps = 3 is built");
-  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
   IntegrateArgs A{n, ipes, paq, t, dt, erra, H, smax, smin, irej, iste, status, max_attempts, h->d_ctl,
-                  h->d_ctl + 1};
+                  h->d_ctl + 1, nullptr};
   return launch_integrate(h, A, st);
 }
 
@@ -551,7 +582,7 @@ int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, 
   CUDA_TRY(h, cudaMemcpyAsync(d_iste, iste, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
   IntegrateArgs A{n, d_ip, d_y, d_t, d_dt, d_e, d_H, d_smax, d_smin, d_irej, d_iste, d_st, max_attempts,
-                  h->d_ctl, h->d_ctl + 1};
+                  h->d_ctl, h->d_ctl + 1, nullptr};
   if (int e = launch_integrate(h, A, st)) return e;
   CUDA_TRY(h, cudaMemcpyAsync(paq, d_y, n * ne * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(t, d_t, n * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -608,36 +639,46 @@ int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_
 
 namespace {
 struct BatchBufs {
-  double *paq, *paq0, *erra, *t, *dt, *H, *H0, *smax, *smin, *b, *draws;
-  int32_t *irej, *iste, *status, *ipes, *item_of;
+  unsigned long long* ctl;  // [0] queue head, [1..5] counters, [8..8+255] bucket counts/offsets
+  double *paq, *paq0, *erra, *t, *dt, *H, *H0, *smax, *smin, *b, *draws, *key;
+  int32_t *irej, *iste, *status, *ipes, *item_of, *order;
 };
 
-int carve_batch(cair_handle* h, int64_t n, bool with_state, BatchBufs& B) {
-  size_t per = sizeof(double) * (12 * 3 + 8 + kDraws) + sizeof(int32_t) * 5;
-  if (int e = ensure_work(h, n * per + 32 * 256)) return e;
-  Carver c{(char*)h->d_work};
+size_t batch_bytes(int64_t n) {
+  size_t per = sizeof(double) * (12 * 3 + 9 + kDraws) + sizeof(int32_t) * 6;
+  return (size_t)n * per + 40 * 256 + sizeof(unsigned long long) * (8 + 2 * 256);
+}
+
+void carve_into(char* base, int64_t n, BatchBufs& B) {
+  Carver c{base};
+  B.ctl = c.take<unsigned long long>(8 + 2 * 256);
   B.paq = c.take<double>(n * 12); B.paq0 = c.take<double>(n * 12); B.erra = c.take<double>(n * 12);
   B.t = c.take<double>(n); B.dt = c.take<double>(n); B.H = c.take<double>(n); B.H0 = c.take<double>(n);
   B.smax = c.take<double>(n); B.smin = c.take<double>(n); B.b = c.take<double>(n);
-  B.draws = c.take<double>(n * kDraws);
+  B.draws = c.take<double>(n * kDraws); B.key = c.take<double>(n);
   B.irej = c.take<int32_t>(n); B.iste = c.take<int32_t>(n); B.status = c.take<int32_t>(n);
-  B.ipes = c.take<int32_t>(n); B.item_of = c.take<int32_t>(n);
+  B.ipes = c.take<int32_t>(n); B.item_of = c.take<int32_t>(n); B.order = c.take<int32_t>(n);
+}
+
+int carve_batch(cair_handle* h, int64_t n, bool with_state, BatchBufs& B) {
   (void)with_state;
+  if (int e = ensure_work(h, batch_bytes(n))) return e;
+  carve_into((char*)h->d_work, n, B);
   return 0;
 }
 
 int sample_ics_into(cair_handle* h, int32_t nitems, const cair_work_item* d_items, const cair_level* d_levels,
                     int64_t ntot, double* paq, double* paq0, double* erra, double* H0, double* b, int32_t* ipes,
-                    int32_t* item_of, double* draws, cudaStream_t st) {
+                    int32_t* item_of, double* draws, cudaStream_t st, double* key = nullptr) {
   k_ic_draws<<<(nitems + 63) / 64, 64, 0, st>>>(nitems, d_items, d_levels, draws, item_of);
   if (int e = check_launch(h)) return e;
   int g = grid_for(h, ntot);
   if (model_of(h) == CAIR_PES_O3_UMN)
     k_sample_ic3<CAIR_PES_O3_UMN><<<g, 128, 0, st>>>(h->sys, ntot, d_items, d_levels, draws, item_of, paq, paq0,
-                                                     erra, H0, b, ipes);
+                                                     erra, H0, b, ipes, key);
   else
     k_sample_ic3<CAIR_PES_N3_UMN><<<g, 128, 0, st>>>(h->sys, ntot, d_items, d_levels, draws, item_of, paq, paq0,
-                                                     erra, H0, b, ipes);
+                                                     erra, H0, b, ipes, key);
   return check_launch(h);
 }
 
@@ -669,7 +710,7 @@ int cair_sample_ics_dev(cair_handle* h, int32_t nlevels, const cair_level* level
   if (ntot == 0) return 0;
   if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "initial conditions: diatom + atom only");
   if (int e = ensure_scratch(h, ntot * kDraws * sizeof(double) + 1024)) return e;
-  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  cudaStream_t st = (cudaStream_t)stream;
   return sample_ics_into(h, nitems, items, levels, ntot, paq, paq0, erra, H0, b, ipes, item_of,
                          (double*)h->d_scratch, st);
 }
@@ -704,29 +745,41 @@ int cair_sample_ics(cair_handle* h, int32_t nlevels, const cair_level* levels, i
   return wait_stream(h);
 }
 
+int64_t cair_queue_workspace_bytes(int64_t ntot) { return ntot < 0 ? 0 : (int64_t)batch_bytes(ntot); }
+
 int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
                        const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results,
-                       void* stream) {
+                       void* workspace, void* stream) {
   if (!h || nlevels < 1 || nitems < 0 || ntot < 0 || !levels || !items || !results || max_attempts < 1)
     return fail(h, CAIR_EINVAL, "cair_run_queue_dev: bad argument");
   if (ntot == 0) return 0;
   if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_run_queue: diatom + atom only");
   if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_run_queue: only NSteps = 3 is built");
+  if (workspace && ((uintptr_t)workspace & 255)) return fail(h, CAIR_EINVAL, "workspace must be 256-byte aligned");
   BatchBufs B;
-  if (int e = carve_batch(h, ntot, true, B)) return e;
-  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  if (workspace) carve_into((char*)workspace, ntot, B);
+  else if (int e = carve_batch(h, ntot, true, B)) return e;
+  cudaStream_t st = (cudaStream_t)stream;
   if (int e = sample_ics_into(h, nitems, items, levels, ntot, B.paq, B.paq0, B.erra, B.H0, B.b, B.ipes, B.item_of,
-                              B.draws, st))
+                              B.draws, st, B.key))
     return e;
-  cair_k_init_state<<<grid_for(h, ntot), 128, 0, st>>>(ntot, h->sys.dt0, B.t, B.dt, B.smax, B.smin, B.irej, B.iste);
+  // queue order: longest predicted duration first (bucketed by initial relative speed)
+  CUDA_TRY(h, cudaMemsetAsync(B.ctl, 0, sizeof(unsigned long long) * (8 + 2 * 256), st));
+  const int g = grid_for(h, ntot);
+  cair_k_bucket_count<<<g, 256, 0, st>>>(ntot, B.key, B.ctl + 8);
+  cair_k_bucket_scan<<<1, 256, 0, st>>>(B.ctl + 8, B.ctl + 8 + 256);
+  cair_k_bucket_scatter<<<g, 256, 0, st>>>(ntot, B.key, B.ctl + 8 + 256, B.order);
+  cair_k_init_state<<<g, 128, 0, st>>>(ntot, h->sys.dt0, B.t, B.dt, B.smax, B.smin, B.irej, B.iste);
   if (int e = check_launch(h)) return e;
-  CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
   IntegrateArgs A{ntot, B.ipes, B.paq, B.t, B.dt, B.erra, B.H, B.smax, B.smin, B.irej, B.iste, B.status,
-                  max_attempts, h->d_ctl, h->d_ctl + 1};
+                  max_attempts, B.ctl, B.ctl + 1, B.order};
   if (int e = launch_integrate(h, A, st)) return e;
-  k_results3<<<grid_for(h, ntot), 128, 0, st>>>(h->sys, h->fs, ntot, B.paq0, B.paq, B.H0, B.H, B.t, B.status,
-                                                  B.item_of, items, results);
-  return check_launch(h);
+  k_results3<<<g, 128, 0, st>>>(h->sys, h->fs, ntot, B.paq0, B.paq, B.H0, B.H, B.t, B.status, B.iste, B.irej,
+                                  B.item_of, items, results);
+  if (int e = check_launch(h)) return e;
+  if (!workspace)
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_ctl + 1, B.ctl + 1, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToDevice, st));
+  return 0;
 }
 
 int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
@@ -745,7 +798,7 @@ int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, in
   cudaStream_t st = h->stream;
   CUDA_TRY(h, cudaMemcpyAsync(d_lv, levels, nlevels * sizeof(cair_level), cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemcpyAsync(d_it, items, nitems * sizeof(cair_work_item), cudaMemcpyHostToDevice, st));
-  if (int e = cair_run_queue_dev(h, nlevels, d_lv, nitems, d_it, ntot, max_attempts, d_res, st)) return e;
+  if (int e = cair_run_queue_dev(h, nlevels, d_lv, nitems, d_it, ntot, max_attempts, d_res, nullptr, st)) return e;
   CUDA_TRY(h, cudaMemcpyAsync(results, d_res, ntot * sizeof(cair_traj_result), cudaMemcpyDeviceToHost, st));
   unsigned long long ctr[5];
   CUDA_TRY(h, cudaMemcpyAsync(ctr, h->d_ctl + 1, sizeof(ctr), cudaMemcpyDeviceToHost, st));

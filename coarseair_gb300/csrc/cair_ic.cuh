@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(128) k_sample_ic3(DevSys S, int64_t ntot, cons
                                                     const int32_t* __restrict__ item_of, double* __restrict__ paq,
                                                     double* __restrict__ paq0, double* __restrict__ erra,
                                                     double* __restrict__ H0, double* __restrict__ bout,
-                                                    int32_t* __restrict__ ipes_out) {
+                                                    int32_t* __restrict__ ipes_out, double* __restrict__ key) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ntot; g += (int64_t)gridDim.x * blockDim.x) {
     const cair_work_item W = items[item_of[g]];
     const cair_level L = levels[W.ilevel];
@@ -197,6 +197,7 @@ __global__ void __launch_bounds__(128) k_sample_ic3(DevSys S, int64_t ntot, cons
     }
     H0[g] = h0;
     bout[g] = b;
+    if (key) key[g] = ver;  // initial relative speed: slow collisions run longest
     ipes_out[g] = W.ipes;
   }
 }
@@ -206,6 +207,8 @@ __global__ void __launch_bounds__(128) k_results3(DevSys S, FsArgs F, int64_t n,
                                                   const double* __restrict__ paq, const double* __restrict__ H0,
                                                   const double* __restrict__ H, const double* __restrict__ t,
                                                   const int32_t* __restrict__ status,
+                                                  const int32_t* __restrict__ iste,
+                                                  const int32_t* __restrict__ irej,
                                                   const int32_t* __restrict__ item_of,
                                                   const cair_work_item* __restrict__ items,
                                                   cair_traj_result* __restrict__ out) {
@@ -227,6 +230,9 @@ __global__ void __launch_bounds__(128) k_results3(DevSys S, FsArgs F, int64_t n,
     r.idx = item_of ? (k - items[it].first + 1) : (k + 1);
     r.ipes = item_of ? items[it].ipes : 0;
     r.status = status[k];
+    r.iste = iste[k];
+    r.irej = irej[k];
+    r.pad = 0;
     r.bmax = item_of ? fabs(items[it].bmax) : 0.0;
     r.b = pi.b;
     r.j_i = pi.mol[0].angmom;

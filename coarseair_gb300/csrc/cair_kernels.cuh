@@ -105,18 +105,20 @@ struct IntegrateArgs {
   int32_t* iste;
   int32_t* status;
   int64_t max_attempts;
-  unsigned long long* queue;    // next trajectory index
+  unsigned long long* queue;    // next queue position
   unsigned long long* counters; // attempts, accepted, rejected, grad evals, energy evals
+  const int32_t* order;         // queue position -> trajectory (NULL: identity)
 };
 
 template <int MODEL, int NS>
-__global__ void __launch_bounds__(128) k_integrate3(DevSys S, IntegrateArgs A) {
+__global__ void __launch_bounds__(64) k_integrate3(DevSys S, IntegrateArgs A) {
   unsigned long long c_att = 0, c_acc = 0, c_rej = 0;
   const bool incstp = S.incstp != 0;
   const int ncall = S.ncall;
   for (;;) {
-    const unsigned long long k = atomicAdd(A.queue, 1ull);
-    if (k >= (unsigned long long)A.n) break;
+    const unsigned long long q = atomicAdd(A.queue, 1ull);
+    if (q >= (unsigned long long)A.n) break;
+    const unsigned long long k = A.order ? (unsigned long long)A.order[q] : q;
     const int ip = A.ipes ? A.ipes[k] : 0;
     const DevPes& P = S.pes[ip];
     Rhs3<MODEL> f(S, P);

@@ -157,6 +157,8 @@ typedef struct cair_traj_result {
   int32_t item;     /* work item                                                   */
   int32_t ipes;     /* 0-based surface                                              */
   int32_t status;   /* cair_traj_status                                             */
+  int32_t iste;     /* accepted Bulirsch-Stoer steps                                 */
+  int32_t irej;     /* rejected attempts                                             */
   int32_t pad;
   double bmax, b;   /* ring bound and impact parameter of the analysed initial point */
   double j_i, v_i, arr_i;  /* AngMom, viba, 16*iPair + itype + 1/2 of the initial point */
@@ -242,10 +244,16 @@ int cair_sample_ics_dev(cair_handle* h, int32_t nlevels, const cair_level* level
  * points and the trajectories.out rows.  Host arrays: results[ntot]. */
 int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
                    const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results);
-/* The same on device pointers (levels, items, results on the device), asynchronous. */
+/* The same on device pointers (levels, items, results on the device), asynchronous on
+ * `stream` (a cudaStream_t; NULL is the default stream).  The batch state lives in
+ * `workspace` (device memory of cair_queue_workspace_bytes(ntot) bytes, 256-byte aligned),
+ * so calls with distinct workspaces may run concurrently on distinct streams; a NULL
+ * workspace uses the handle's own arena (one call at a time).  The queue is ordered
+ * longest-first by the predicted duration (initial relative speed) of each trajectory. */
 int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
                        const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results,
-                       void* stream);
+                       void* workspace, void* stream);
+int64_t cair_queue_workspace_bytes(int64_t ntot);
 
 /* Algorithmic FP64 operation counts the library's kernels execute per PES energy+gradient
  * evaluation, per energy-only evaluation and per BS attempt (excluding the PES), for

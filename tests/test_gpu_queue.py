@@ -44,10 +44,12 @@ def test_device_initial_conditions_match_oracle(gpu_lib, oracle_lib, name):
 
 
 def test_quasibound_level_consumes_rejection_draws(gpu_lib, oracle_lib):
+    """The shipped lists hold no quasi-bound rows; a synthetic one (egam > 0) exercises the
+    rejection sampling of ComputeKineticEnergy, whose draws shift the rest of the stream."""
     cfg, o, H, lv = _setup("N3")
-    qb = np.where(lv["egam"] > 0)[0]
-    assert qb.size > 0
-    rows = lv[[int(qb[0])]]
+    rows = lv[[40]].copy()
+    rows["egam"] = 2.0e-3
+    rows["vmax"] = rows["eint"] + 1.0e-3
     items = api.work_items([(0, 0, 16, 5, 10000.0, 7.0, 15.0)])
     ic = api.InitialConditions(H).sample(api.level_table(rows), items)
     ref = o.sample_ics(16, _oracle_levels(rows), seed=5, ttra=10000.0, bmax=7.0, dinit=15.0)
