@@ -330,6 +330,7 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
     P.ncoef = src.ncoef;
     P.a = src.a; P.ab = src.ab; P.ra = src.ra; P.rb = src.rb;
     P.inv_a = (src.a != 0.0) ? 1.0 / src.a : 0.0;
+    P.inv_ab = (src.ab != 0.0) ? 1.0 / src.ab : 0.0;
     if (cudaMalloc(&h->d_coef[p], sizeof(double) * src.ncoef) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
     if (cudaMemcpy(h->d_coef[p], src.coef, sizeof(double) * src.ncoef, cudaMemcpyHostToDevice) != cudaSuccess)
       return bad(CAIR_ECUDA, "cudaMemcpy coefficients");

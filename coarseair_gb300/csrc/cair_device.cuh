@@ -18,6 +18,7 @@ struct DevPes {
   const double* coef;   // device copy of C(1:ncoef)
   double a, ab, ra, rb; // MEG parameters
   double inv_a;         // One/This%a, evaluated once on the host
+  double inv_ab;
 };
 
 struct DevSys {
@@ -33,6 +34,45 @@ struct DevSys {
   double o2_cd[8];      // 2 * a(k) * alpha * beta**k (O2_UMN Ev2gm2_Grad factors)
   DevPes pes[CAIR_MAX_PES];
 };
+
+// ------------------------------------------------------------------------------------------
+// Exponential on the FP64 pipe with 11 operations: Tang's table-driven method (ACM TOMS
+// 15(2), 144-157, 1989) with 64 subintervals.  x = (64 k + j) ln2/64 + r, |r| <= ln2/128;
+// exp(x) = 2^k 2^(j/64) (1 + p(r)), p the degree-6 Taylor polynomial of exp(r) - 1
+// (truncation < 1e-19).  The result is within about one ulp; |x| > 707 (not met on this
+// path's surfaces) goes to the CUDA library.
+// ------------------------------------------------------------------------------------------
+}  // namespace cair
+#include "generated/exp_table.h"
+namespace cair {
+__device__ static const double kExpTab[64] = {
+#define X(i) kCairExp2Table[i]
+    X(0),  X(1),  X(2),  X(3),  X(4),  X(5),  X(6),  X(7),  X(8),  X(9),  X(10), X(11), X(12),
+    X(13), X(14), X(15), X(16), X(17), X(18), X(19), X(20), X(21), X(22), X(23), X(24), X(25),
+    X(26), X(27), X(28), X(29), X(30), X(31), X(32), X(33), X(34), X(35), X(36), X(37), X(38),
+    X(39), X(40), X(41), X(42), X(43), X(44), X(45), X(46), X(47), X(48), X(49), X(50), X(51),
+    X(52), X(53), X(54), X(55), X(56), X(57), X(58), X(59), X(60), X(61), X(62), X(63)
+#undef X
+};
+
+__device__ __forceinline__ double fexp(double x) {
+  if (!(fabs(x) <= 707.0)) return exp(x);
+  const double shifter = 6755399441055744.0;  // 1.5 * 2^52: the sum rounds to an integer
+  const double t = fma(x, CAIR_EXP_INV_L, shifter);
+  const double N = t - shifter;
+  const int n = __double2loint(t);
+  double r = fma(-N, CAIR_EXP_L1, x);
+  r = fma(-N, CAIR_EXP_L2, r);
+  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
+  p = fma(p, r, 1.0 / 24.0);
+  p = fma(p, r, 1.0 / 6.0);
+  p = fma(p, r, 0.5);
+  p = fma(p, r, 1.0);
+  p = p * r;
+  const double T = __ldg(kExpTab + (n & 63));
+  const double y = fma(T, p, T);
+  return __hiloint2double(__double2hiint(y) + ((n >> 6) << 20), __double2loint(y));
+}
 
 // ------------------------------------------------------------------------------------------
 // Diatomic potentials
@@ -51,13 +91,16 @@ __device__ __forceinline__ void o2_disp(double rb, double& vd, double& dvd) {
   double s2 = ss * ss, s3 = s2 * ss, s6 = s3 * s3, s4 = s2 * s2, s8 = s4 * s4;
   double r2 = rb * rb, r3 = r2 * rb, r4 = r2 * r2, r6 = r3 * r3, r8 = r4 * r4;
   double d6 = r6 + s6, d8 = r8 + s8;
-  double e6 = c6 / d6, e8 = c8step / d8;
+  // one division for both denominators: 1/d6 = d8/(d6 d8), 1/d8 = d6/(d6 d8)
+  double q = 1.0 / (d6 * d8);
+  double i6 = d8 * q, i8 = d6 * q;
+  double e6 = c6 * i6, e8 = c8step * i8;
   vd = -e6 - 2.0 * e8;
   if (GRAD) {
     double r5 = r4 * rb, r7 = r4 * r3;
-    double e6dr = c6 * (-6.0 * r5) / (d6 * d6);
-    double e8dr = c8step * (-8.0 * r7) / (d8 * d8);
-    dvd = (-e6dr - 2.0 * e8dr) / CAIR_B_TO_ANG;
+    double e6dr = c6 * (-6.0 * r5) * (i6 * i6);
+    double e8dr = c8step * (-8.0 * r7) * (i8 * i8);
+    dvd = (-e6dr - 2.0 * e8dr) * (1.0 / CAIR_B_TO_ANG);
   }
 }
 
@@ -69,13 +112,13 @@ __device__ __forceinline__ void o2_umn(const DevSys& S, double r, double& v, dou
   double vv = 0.0, dd = 0.0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    double e = exp(-(S.o2_ab[k] * r2));
+    double e = fexp(-(S.o2_ab[k] * r2));
     vv = vv + kO2A[k] * e;
     if (GRAD) dd = dd - S.o2_cd[k] * rang * e;
   }
   vv = vv * 1.e-3;
   double vd, dvd = 0.0;
-  o2_disp<GRAD>(rang / CAIR_B_TO_ANG, vd, dvd);
+  o2_disp<GRAD>(r, vd, dvd);
   v = vv + vd;
   if (GRAD) dv = (dd * 1.e-3 + dvd) * CAIR_B_TO_ANG;
 }
@@ -91,15 +134,16 @@ __device__ __forceinline__ void n2_umn(double r, double& v, double& dv) {
   double r3 = (rang * rang) * rang;
   double r4 = r3 * rang;
   double ts = r4 + red4;
-  double y = (r4 - red4) / ts;
+  double its = 1.0 / ts;
+  double y = (r4 - red4) * its;
   double y2 = y * y, y3 = y2 * y, y4 = y2 * y2, y5 = y3 * y2, y6 = y3 * y3;
   double fy = cs0 + cs1 * y + cs2 * y2 + cs3 * y3 + cs4 * y4 + cs5 * y5 + cs6 * y6;
-  double u = exp(-(fy * (rang - red)));
+  double u = fexp(-(fy * (rang - red)));
   double minu = 1.0 - u;
   v = (de * (minu * minu) - de) * CAIR_KCM_TO_HARTREE + 0.0;
   if (GRAD) {
     double dfdy = cs1 + 2.0 * cs2 * y + 3.0 * cs3 * y2 + 4.0 * cs4 * y3 + 5.0 * cs5 * y4 + 6.0 * cs6 * y5;
-    double dydr = 8.0 * r3 * red4 / (ts * ts);
+    double dydr = 8.0 * r3 * red4 * (its * its);
     double dfdr = dfdy * dydr;
     double dvk = 2.0 * de * minu * u * (dfdr * (rang - red) + fy);
     dv = dvk * CAIR_KCM_TO_HARTREE * CAIR_B_TO_ANG;
@@ -116,15 +160,24 @@ __device__ __forceinline__ void diat(const DevSys& S, double r, double& v, doubl
 
 #include "generated/pip_n3.cuh"
 #include "generated/pip_o3.cuh"
+// gradient of the PIP part: reverse mode (adjoint sweep) unless CAIR_PIP_FORWARD selects the
+// forward mode, whose operation order is the reference's
+#ifdef CAIR_PIP_FORWARD
+#define CAIR_PIP_O3 pip_o3_eval
+#define CAIR_PIP_N3 pip_n3_eval
+#else
+#define CAIR_PIP_O3 pip_o3_eval_rev
+#define CAIR_PIP_N3 pip_n3_eval_rev
+#endif
 
 namespace cair {
 
 // ------------------------------------------------------------------------------------------
 // TransToCart (PES_Class.F90:252-360, implementation 2)
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ void trans_to_cart_3(const DevSys& S, const double* R, const double* Q,
+__device__ __forceinline__ void trans_to_cart_3(const DevSys& S, const double* Ri, const double* Q,
                                                 const double* dVdR, double* m) {
-  double d0 = dVdR[0] / R[0], d1 = dVdR[1] / R[1], d2 = dVdR[2] / R[2];
+  double d0 = dVdR[0] * Ri[0], d1 = dVdR[1] * Ri[1], d2 = dVdR[2] * Ri[2];
   double m1 = S.mMiMn[0], m2 = S.mMiMn[1];
   double a1 = (1.0 - m1) * d1, b1 = m1 * d2, a2 = m2 * d1, b2 = (1.0 - m2) * d2;
 #pragma unroll
@@ -156,16 +209,16 @@ __device__ __forceinline__ void trans_to_cart_4(const DevSys& S, const double* R
 // ------------------------------------------------------------------------------------------
 // O3 UMN (Compute_O3_UMN_PES_1d, O3_UMN_PES_Class.F90:259-326)
 template <bool GRAD>
-__device__ __forceinline__ void pes_o3(const DevSys& S, const DevPes& P, const double* R, const double* Q,
-                                       double& V, double* dVdR, double* dVdQ) {
+__device__ __forceinline__ void pes_o3(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
+                                       const double* Q, double& V, double* dVdR, double* dVdQ) {
   double x[3], dx[3], vd[3], dvd[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     double rang = R[i] * CAIR_B_TO_ANG;
     double d1 = rang - P.ra, d2 = rang - P.rb;
-    double e = exp(-(d1 / P.a) - (d2 * d2) / P.ab);
+    double e = fexp(-(d1 * P.inv_a) - (d2 * d2) * P.inv_ab);
     x[i] = e;
-    if (GRAD) dx[i] = (-(2.0 * d2 / P.ab) - P.inv_a) * e;
+    if (GRAD) dx[i] = (-((2.0 * d2) * P.inv_ab) - P.inv_a) * e;
     diat<GRAD>(S, R[i], vd[i], dvd[i]);
   }
   double vdiat = (vd[0] + vd[1]) + vd[2];
@@ -173,11 +226,11 @@ __device__ __forceinline__ void pes_o3(const DevSys& S, const DevPes& P, const d
   const double* __restrict__ C = P.coef;
   if (GRAD) {
     double g[3];
-    pip_o3_eval(x, dx, C, 0.0, vp, g);
+    CAIR_PIP_O3(x, dx, C, 0.0, vp, g);
     V = (vp * CAIR_KCM_TO_HARTREE) + vdiat;
 #pragma unroll
     for (int i = 0; i < 3; ++i) dVdR[i] = g[i] * CAIR_KCMANG_TO_HARTB + dvd[i];
-    trans_to_cart_3(S, R, Q, dVdR, dVdQ);
+    trans_to_cart_3(S, Ri, Q, dVdR, dVdQ);
   } else {
     pip_o3_value(x, C, 0.0, vp);
     V = (vp * CAIR_KCM_TO_HARTREE) + vdiat;
@@ -187,16 +240,17 @@ __device__ __forceinline__ void pes_o3(const DevSys& S, const DevPes& P, const d
 // N3 UMN (Compute_N3_UMN_PES_1d, N3_UMN_PES_Class.F90:332-382, on the N4 PIP with the
 // three pinned 10^3-bohr pairs contributing exact zeros)
 template <bool GRAD>
-__device__ __forceinline__ void pes_n3(const DevSys& S, const DevPes& P, const double* R, const double* Q,
-                                       double& V, double* dVdR, double* dVdQ) {
+__device__ __forceinline__ void pes_n3(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
+                                       const double* Q, double& V, double* dVdR, double* dVdQ) {
   double x[6], dx[6], vd[3], dvd[3];
+  const double inv_ab = 1.0 / 1.5;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     double d = R[i] * CAIR_B_TO_ANG - 1.098;
-    double e = exp(-d - (d * d) / 1.5);
+    double e = fexp(-d - (d * d) * inv_ab);
     int j = i == 2 ? 3 : i;  // RTemp(1), RTemp(2), RTemp(4)
     x[j] = e;
-    if (GRAD) dx[j] = (-(2.0 * d / 1.5) - 1.0) * e;
+    if (GRAD) dx[j] = (-((2.0 * d) * inv_ab) - 1.0) * e;
     diat<GRAD>(S, R[i], vd[i], dvd[i]);
   }
   x[2] = x[4] = x[5] = 0.0;
@@ -206,11 +260,11 @@ __device__ __forceinline__ void pes_n3(const DevSys& S, const DevPes& P, const d
   const double* __restrict__ C = P.coef;
   if (GRAD) {
     double g[3];
-    pip_n3_eval(x, dx, C, 457.4, vp, g);
+    CAIR_PIP_N3(x, dx, C, 457.4, vp, g);
     V = vdiat + (vp + 0.0) * CAIR_KCM_TO_HARTREE;
 #pragma unroll
     for (int i = 0; i < 3; ++i) dVdR[i] = dvd[i] + g[i] * CAIR_KCM_TO_HARTREE * CAIR_B_TO_ANG;
-    trans_to_cart_3(S, R, Q, dVdR, dVdQ);
+    trans_to_cart_3(S, Ri, Q, dVdR, dVdQ);
   } else {
     pip_n3_value(x, C, 457.4, vp);
     V = vdiat + (vp + 0.0) * CAIR_KCM_TO_HARTREE;
@@ -218,27 +272,28 @@ __device__ __forceinline__ void pes_n3(const DevSys& S, const DevPes& P, const d
 }
 
 template <int MODEL, bool GRAD>
-__device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const double* R, const double* Q,
-                                    double& V, double* dVdR, double* dVdQ) {
-  if (MODEL == CAIR_PES_O3_UMN) pes_o3<GRAD>(S, P, R, Q, V, dVdR, dVdQ);
-  else pes_n3<GRAD>(S, P, R, Q, V, dVdR, dVdQ);
+__device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
+                                    const double* Q, double& V, double* dVdR, double* dVdQ) {
+  if (MODEL == CAIR_PES_O3_UMN) pes_o3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
+  else pes_n3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
 }
 
 // ------------------------------------------------------------------------------------------
 // Pair distances (Compute_Rp_CartCoord_3Atoms, Collision_Class.F90:2244-2275); Q has room
 // for the last atom, which is written to Q[NV..NV+2].
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ void rp3(const DevSys& S, double* Q, double* Rp) {
+// Distances from one reciprocal square root each: 1/R = rsqrt(R^2), R = R^2 (1/R).
+__device__ __forceinline__ void rp3(const DevSys& S, double* Q, double* Rp, double* Ri) {
   const double m1 = S.mMiMn[0], m2 = S.mMiMn[1];
 #pragma unroll
   for (int c = 0; c < 3; ++c) Q[6 + c] = m1 * Q[c] + m2 * Q[3 + c];
-  double a, b, c;
+  double a, b, c, s2;
   a = Q[0] - Q[3]; b = Q[1] - Q[4]; c = Q[2] - Q[5];
-  Rp[0] = sqrt(a * a + b * b + c * c);
+  s2 = a * a + b * b + c * c; Ri[0] = rsqrt(s2); Rp[0] = s2 * Ri[0];
   a = Q[0] - Q[6]; b = Q[1] - Q[7]; c = Q[2] - Q[8];
-  Rp[1] = sqrt(a * a + b * b + c * c);
+  s2 = a * a + b * b + c * c; Ri[1] = rsqrt(s2); Rp[1] = s2 * Ri[1];
   a = Q[3] - Q[6]; b = Q[4] - Q[7]; c = Q[5] - Q[8];
-  Rp[2] = sqrt(a * a + b * b + c * c);
+  s2 = a * a + b * b + c * c; Ri[2] = rsqrt(s2); Rp[2] = s2 * Ri[2];
 }
 
 // ------------------------------------------------------------------------------------------
@@ -258,11 +313,11 @@ struct Rhs3 {
       acc = acc + S.Tpq[j + 9 * (i0 + 3)] * y[i0 + 3];
       yp[6 + j] = acc;
     }
-    double Q[9], R[3], V, dVdR[3], dVdQ[6];
+    double Q[9], R[3], Ri[3], V, dVdR[3], dVdQ[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) Q[i] = y[6 + i];
-    rp3(S, Q, R);
-    pes<MODEL, true>(S, P, R, Q, V, dVdR, dVdQ);
+    rp3(S, Q, R, Ri);
+    pes<MODEL, true>(S, P, R, Ri, Q, V, dVdR, dVdQ);
 #pragma unroll
     for (int i = 0; i < 6; ++i) yp[i] = -dVdQ[i];
   }
@@ -283,10 +338,8 @@ __device__ __forceinline__ double hamiltonian3(const DevSys& S, const DevPes& P,
   double Q[9], R[3], V;
 #pragma unroll
   for (int i = 0; i < 6; ++i) Q[i] = y[6 + i];
-  rp3(S, Q, R);
-  pes<MODEL, false>(S, P, R, Q, V, nullptr, nullptr);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) Rpi[k] = 1.0 / R[k];
+  rp3(S, Q, R, Rpi);
+  pes<MODEL, false>(S, P, R, Rpi, Q, V, nullptr, nullptr);
   return h * 0.5 + V;
 }
 

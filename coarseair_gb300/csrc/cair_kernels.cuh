@@ -16,12 +16,12 @@ __global__ void __launch_bounds__(128) k_pes_eval3(DevSys S, int64_t n, const in
                                                    double* __restrict__ dVdQ) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     const DevPes& P = S.pes[ipes ? ipes[k] : 0];
-    double R[3], Q[9], v, g[3], m[6];
+    double R[3], Ri[3], Q[9], v, g[3], m[6];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) R[i] = Rin[3 * k + i];
+    for (int i = 0; i < 3; ++i) { R[i] = Rin[3 * k + i]; Ri[i] = 1.0 / R[i]; }
 #pragma unroll
     for (int i = 0; i < 9; ++i) Q[i] = Qin[9 * k + i];
-    pes<MODEL, GRAD>(S, P, R, Q, v, g, m);
+    pes<MODEL, GRAD>(S, P, R, Ri, Q, v, g, m);
     V[k] = v;
     if (GRAD) {
 #pragma unroll

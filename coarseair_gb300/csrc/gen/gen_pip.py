@@ -429,6 +429,151 @@ def emit_device(S, key, name, zero_vars, dirs, path, coeff_symbol, value_only=Fa
     return live_v, E.nt, nflop
 
 
+def emit_device_reverse(S, key, name, zero_vars, dirs, path, coeff_symbol):
+    """Energy and gradient with a reverse-mode (adjoint) sweep over the PIP graph.
+
+    Forward: the pruned monomial and polynomial values (as the value-only function).
+    Reverse: adjoints seeded with the linear coefficients C_i on the basis polynomials and
+    propagated through p_k = p_a p_b - sum p_c (adj_a += adj_k p_b, adj_b += adj_k p_a,
+    adj_c -= adj_k) and the monomial products down to the MEG variables; dV/dvar_d is the
+    MEG variable's adjoint times dx_d.  Nodes that are exactly zero (pinned pairs) and terms
+    whose factor is exactly zero are skipped.  Same signature as emit_device's function.
+    """
+    s = S[key]
+    mono, poly, basis = s["mono"], s["poly"], s["basis"]
+    L = []
+    nt = [0]
+
+    def tmp(expr):
+        nm = "t%d" % nt[0]
+        nt[0] += 1
+        L.append("  const double %s = %s;" % (nm, expr))
+        return nm
+
+    flops = [0]
+    # forward values
+    mv = []
+    for t in mono:
+        if t[0] == "one":
+            mv.append("1.0")
+        elif t[0] == "var":
+            mv.append(None if t[1] in zero_vars else "x[%d]" % t[1])
+        else:
+            a, b = mv[t[1]], mv[t[2]]
+            if a is None or b is None:
+                mv.append(None)
+            else:
+                mv.append(tmp("%s * %s" % (a, b)))
+                flops[0] += 1
+    pv = []
+    for t in poly:
+        if t[0] == "sum":
+            terms = [mv[x] for x in t[1] if mv[x] is not None]
+            if not terms:
+                pv.append(None)
+            elif len(terms) == 1:
+                pv.append(terms[0])
+            else:
+                e = terms[0]
+                for x in terms[1:]:
+                    e = "(%s + %s)" % (e, x)
+                flops[0] += len(terms) - 1
+                pv.append(tmp(e))
+        else:
+            a, b, subs = pv[t[1]], pv[t[2]], t[3]
+            lead = None if (a is None or b is None) else "%s * %s" % (a, b)
+            chain = [("+", lead)] + [("-", pv[c]) for c in subs]
+            e = Emitter.chain(chain)
+            nterm = sum(1 for _, x in chain if x is not None)
+            flops[0] += (1 if lead else 0) + max(0, nterm - 1)
+            pv.append(None if e is None else tmp(e))
+    # energy
+    L.append("  double v = V0;")
+    live = 0
+    for i, j in enumerate(basis):
+        if pv[j] is not None:
+            L.append("  v = v + %s[%d] * %s;" % (coeff_symbol, i, pv[j]))
+            live += 1
+            flops[0] += 2
+    L.append("  V = v;")
+    # adjoint seeds: basis polynomials carry their coefficients
+    adj_p = {}
+    adj_m = {}
+    decl = []
+
+    def add_adj(table, k, expr, sign="+"):
+        """adj[k] (+|-)= expr, declaring the variable at the first contribution."""
+        nm = table.get(k)
+        if nm is None:
+            nm = ("ap%d" if table is adj_p else "am%d") % k
+            table[k] = nm
+            L.append("  double %s = %s%s;" % (nm, "" if sign == "+" else "-", expr))
+        else:
+            L.append("  %s = %s %s %s;" % (nm, nm, sign, expr))
+            flops[0] += 1
+
+    for i, j in enumerate(basis):
+        if pv[j] is not None:
+            add_adj(adj_p, j, "%s[%d]" % (coeff_symbol, i))
+    for k in range(len(poly) - 1, -1, -1):
+        if pv[k] is None or k not in adj_p:
+            continue
+        t = poly[k]
+        ak = adj_p[k]
+        if t[0] == "sum":
+            for x in t[1]:
+                if mv[x] is not None and mono[x][0] != "one":
+                    add_adj(adj_m, x, ak)
+        else:
+            a, b, subs = t[1], t[2], t[3]
+            if pv[a] is not None and pv[b] is not None:
+                if a == b:
+                    add_adj(adj_p, a, "(2.0 * %s) * %s" % (ak, pv[b]))
+                    flops[0] += 2
+                else:
+                    add_adj(adj_p, a, "%s * %s" % (ak, pv[b]))
+                    add_adj(adj_p, b, "%s * %s" % (ak, pv[a]))
+                    flops[0] += 2
+            for c in subs:
+                if pv[c] is not None:
+                    add_adj(adj_p, c, ak, sign="-")
+    gsum = {d: None for d in dirs}
+    for k in range(len(mono) - 1, -1, -1):
+        if mv[k] is None or k not in adj_m:
+            continue
+        t = mono[k]
+        ak = adj_m[k]
+        if t[0] == "mul":
+            a, b = t[1], t[2]
+            if a == b:
+                add_adj(adj_m, a, "(2.0 * %s) * %s" % (ak, mv[b]))
+                flops[0] += 2
+            else:
+                add_adj(adj_m, a, "%s * %s" % (ak, mv[b]))
+                add_adj(adj_m, b, "%s * %s" % (ak, mv[a]))
+                flops[0] += 2
+        elif t[0] == "var" and t[1] in dirs:
+            d = t[1]
+            if gsum[d] is None:
+                gsum[d] = ak
+            else:
+                gsum[d] = "(%s + %s)" % (gsum[d], ak)
+                flops[0] += 1
+    for n, d in enumerate(dirs):
+        L.append("  dV[%d] = %s * dx[%d];" % (n, gsum[d] if gsum[d] else "0.0", d))
+        flops[0] += 1
+    out = ["/* %s: reverse-mode gradient, %d live basis terms of %d, %d FP64 operations. Generated, do not edit. */"
+           % (name, live, len(basis), flops[0]),
+           "#define %s_FLOPS %d" % (name.upper(), flops[0]),
+           "__device__ __forceinline__ void %s(const double* __restrict__ x, const double* __restrict__ dx," % name,
+           "    const double* __restrict__ %s, double V0, double& V, double* __restrict__ dV) {" % coeff_symbol]
+    out += L
+    out.append("}")
+    with open(path, "a") as f:
+        f.write("\n".join(out) + "\n")
+    return live, nt[0], flops[0]
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("COARSEAIR_REF", "")
     if not ref or not os.path.isdir(ref):
@@ -444,12 +589,18 @@ def main():
     info = emit_device(S, "N4", "pip_n3_value", zero_vars={2, 4, 5}, dirs=[0, 1, 3],
                        path=os.path.join(gen, "pip_n3.cuh"), coeff_symbol="C", value_only=True)
     print("N3 pruned value:", info)
+    info = emit_device_reverse(S, "N4", "pip_n3_eval_rev", zero_vars={2, 4, 5}, dirs=[0, 1, 3],
+                               path=os.path.join(gen, "pip_n3.cuh"), coeff_symbol="C")
+    print("N3 pruned reverse:", info)
     info = emit_device(S, "O3", "pip_o3_eval", zero_vars=set(), dirs=[0, 1, 2],
                        path=os.path.join(gen, "pip_o3.cuh"), coeff_symbol="C")
     print("O3:", info)
     info = emit_device(S, "O3", "pip_o3_value", zero_vars=set(), dirs=[0, 1, 2],
                        path=os.path.join(gen, "pip_o3.cuh"), coeff_symbol="C", value_only=True)
     print("O3 value:", info)
+    info = emit_device_reverse(S, "O3", "pip_o3_eval_rev", zero_vars=set(), dirs=[0, 1, 2],
+                               path=os.path.join(gen, "pip_o3.cuh"), coeff_symbol="C")
+    print("O3 reverse:", info)
     with open(os.path.join(REPO, "coarseair_gb300", "data", "N3_UMN.dat"), "w") as f:
         f.write("# N3 UMN surface (N4 PIP, MEG variables): 276 linear coefficients [kcal/mol]\n")
         f.write("# a = 1.0 Ang, ab = 1.5 Ang^2, re = 1.098 Ang, totdiss = 457.4 kcal/mol\n")

@@ -70,6 +70,9 @@ double orc_pes_potential(const orc_sys* s, int ipes, const double* R);
 void   orc_pip_eval(int table, const double* rms, const double* dmsdr_diag, int want_grad,
                     const double* C, double V0, double* V, double* dV);
 
+void   orc_pip_scale(int table, const double* rms, const double* dmsdr_diag, const double* C, double* scale);
+void   orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale);
+
 /* ---- dynamics ---- */
 void   orc_rp(const orc_sys* s, const double* Q, double* Rxyz, double* Rp);
 void   orc_rhs(const orc_sys* s, int ipes, const double* y, double* yp);

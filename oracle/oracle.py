@@ -81,6 +81,7 @@ def lib():
         L.orc_pes_potential.restype = C.c_double
         L.orc_pes_potential.argtypes = [C.POINTER(OrcSys), C.c_int, _D]
         L.orc_pip_eval.argtypes = [C.c_int, _D, _D, C.c_int, _D, C.c_double, _D, _D]
+        L.orc_pes_scale.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D]
         L.orc_rp.argtypes = [C.POINTER(OrcSys), _D, _D, _D]
         L.orc_rhs.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D]
         L.orc_hamiltonian.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D, _D]
@@ -162,6 +163,15 @@ class Oracle:
             self.L.orc_pes_compute(C.byref(self.s), 0 if ipes is None else int(ipes[k]), dp(R[k]), dp(Q[k]),
                                    dp(V[k:k + 1]), dp(g[k]), dp(m[k]))
         return V, g, m
+
+    def condition_scale(self, R, ipes=None):
+        """Magnitudes of the terms summed into V (column 0) and dV/dR_i (columns 1..3): the scale at
+        which a different evaluation order of the same surface changes the result."""
+        R = np.ascontiguousarray(R, np.float64).reshape(-1, self.npairs)
+        out = np.zeros((R.shape[0], 4))
+        for k in range(R.shape[0]):
+            self.L.orc_pes_scale(C.byref(self.s), 0 if ipes is None else int(ipes[k]), dp(R[k]), dp(out[k]))
+        return out
 
     def potential(self, R, ipes=None):
         R = np.ascontiguousarray(R, np.float64).reshape(-1, self.npairs)

@@ -213,6 +213,80 @@ void orc_pip_eval(int table, const double* rms, const double* dmsdr_diag, int wa
   }
 }
 
+/* Condition scale of the PIP sum: scale[0] = sum_i |C_i B_i| and scale[1 + d] =
+ * sum_j |C_j dB_j/dvar_d| -- the magnitude of the terms that cancel in V and dV, used to
+ * state rounding-level agreement of other evaluation orders. */
+void orc_pip_scale(int table, const double* rms, const double* dmsdr_diag, const double* C, double* scale) {
+  pip_tab T = pip_table(table);
+  double rm[128], p[480], dm[128], dp[480];
+  for (int k = 0; k < T.nmono; ++k) {
+    if (T.mo[k] == 0) rm[k] = 1.0;
+    else if (T.mo[k] == 1) rm[k] = rms[T.ma[k]];
+    else rm[k] = rm[T.ma[k]] * rm[T.mb[k]];
+  }
+  for (int k = 0; k < T.npoly; ++k) {
+    const short* L = T.plist + T.poff[k];
+    double s = 0.0;
+    if (T.po[k] == 0) { for (int i = 0; i < T.plen[k]; ++i) s += rm[L[i]]; }
+    else { s = p[T.pa[k]] * p[T.pb[k]]; for (int i = 0; i < T.plen[k]; ++i) s -= p[L[i]]; }
+    p[k] = s;
+  }
+  double v = 0.0;
+  for (int i = 0; i < T.nbasis; ++i) v += fabs(C[i] * p[T.basis[i]]);
+  scale[0] = v;
+  for (int d = 0; d < T.nvar; ++d) {
+    for (int k = 0; k < T.nmono; ++k) {
+      if (T.mo[k] == 0) dm[k] = 0.0;
+      else if (T.mo[k] == 1) dm[k] = (T.ma[k] == d) ? dmsdr_diag[d] : 0.0;
+      else dm[k] = dm[T.ma[k]] * rm[T.mb[k]] + rm[T.ma[k]] * dm[T.mb[k]];
+    }
+    for (int k = 0; k < T.npoly; ++k) {
+      const short* L = T.plist + T.poff[k];
+      double s = 0.0;
+      if (T.po[k] == 0) { for (int i = 0; i < T.plen[k]; ++i) s += dm[L[i]]; }
+      else { s = dp[T.pa[k]] * p[T.pb[k]] + p[T.pa[k]] * dp[T.pb[k]]; for (int i = 0; i < T.plen[k]; ++i) s -= dp[L[i]]; }
+      dp[k] = s;
+    }
+    double g = 0.0;
+    for (int j = 0; j < T.nbasis; ++j) g += fabs(C[j] * dp[T.basis[j]]);
+    scale[1 + d] = g;
+  }
+}
+
+/* Condition scale of a 3-atom surface evaluation at distances R [bohr]: scale[0] for V [Eh],
+ * scale[1..3] for dV/dR [Eh/bohr] (PIP terms plus the diatomic terms' magnitudes). */
+void orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale) {
+  const orc_pes* P = &s->pes[ipes];
+  double rms[6] = {0}, dms[6] = {0}, sc[7];
+  if (P->model == ORC_PES_O3_UMN) {
+    for (int i = 0; i < 3; ++i) {
+      double r = R[i] * B_TO_ANG, d1 = r - P->ra, d2 = r - P->rb;
+      double e = exp(-(d1 / P->a) - (d2 * d2) / P->ab);
+      rms[i] = e; dms[i] = (-(2.0 * d2 / P->ab) - 1.0 / P->a) * e;
+    }
+    orc_pip_scale(0, rms, dms, P->coef, sc);
+    scale[0] = sc[0] * KCM_TO_HARTREE;
+    for (int i = 0; i < 3; ++i) scale[1 + i] = sc[1 + i] * KCMANG_TO_HARTB;
+  } else {
+    double rt[6] = {R[0], R[1], 1.e3, R[2], 1.e3, 1.e3};
+    for (int i = 0; i < 6; ++i) {
+      double d = rt[i] * B_TO_ANG - 1.098, e = exp(-d - (d * d) / 1.5);
+      rms[i] = e; dms[i] = (-(2.0 * d / 1.5) - 1.0) * e;
+    }
+    orc_pip_scale(1, rms, dms, P->coef, sc);
+    scale[0] = (sc[0] + 457.4) * KCM_TO_HARTREE;
+    scale[1] = sc[1] * KCM_TO_HARTREE * B_TO_ANG;
+    scale[2] = sc[2] * KCM_TO_HARTREE * B_TO_ANG;
+    scale[3] = sc[4] * KCM_TO_HARTREE * B_TO_ANG;
+  }
+  for (int i = 0; i < 3; ++i) {
+    double v, dv;
+    orc_diat_VdV(s->diat, R[i], &v, &dv);
+    scale[0] += fabs(v);
+    scale[1 + i] += fabs(dv);
+  }
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* TransToCart (src/PESs/PES_Class.F90:252-360, implementation 2)                              */
 /* ------------------------------------------------------------------------------------------ */

@@ -55,17 +55,25 @@ def test_surface_energy_and_gradient_parity(gpu_lib, oracle_lib, name):
     R, Qall = np.concatenate([R, R2]), np.concatenate([Qall, Q2])
     V_o, g_o, m_o = o.compute(R, Qall)
     V_g, g_g, m_g = api.PES(H).Compute(R, Qall)
-    # relative to the energy scale of the surface (0.1 Eh, about half a well depth): V crosses
-    # zero, where a pointwise relative error is undefined
-    vs = np.maximum(np.abs(V_o), 0.1)
-    assert np.all(np.abs(V_g - V_o) <= 1e-12 * vs)
-    gs = np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2)
-    assert np.all(np.abs(g_g - g_o) <= 1e-12 * gs)
+    # 1e-12 relative to max(|V|, 0.1 Eh) (V crosses zero), or 100 rounding units of the condition
+    # scale (sum of the magnitudes of the terms the fit adds, which reaches 10^4..10^6 |V| for O3 at
+    # short range, where any other evaluation order of the same sum moves V by that much)
+    cs = o.condition_scale(R)
+    vs = np.maximum(1e-12 * np.maximum(np.abs(V_o), 0.1), 100 * 2.2e-16 * cs[:, 0])
+    err = np.abs(V_g - V_o)
+    assert np.all(err <= vs), (err / vs).max()
+    gs = np.maximum(1e-12 * np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2), 100 * 2.2e-16 * cs[:, 1:])
+    assert np.all(np.abs(g_g - g_o) <= gs), (np.abs(g_g - g_o) / gs).max()
     ms = np.maximum(np.abs(m_o).max(axis=1, keepdims=True), 1e-2)
-    assert np.all(np.abs(m_g - m_o) <= 1e-12 * ms)
+    mt = np.maximum(1e-12 * ms, 100 * 2.2e-16 * cs[:, 1:].max(axis=1, keepdims=True))
+    assert np.all(np.abs(m_g - m_o) <= mt), (np.abs(m_g - m_o) / mt).max()
     # energy-only path (PES%Potential)
     Ve = api.PES(H).Potential(R, Qall)
-    assert np.all(np.abs(Ve - V_o) <= 1e-12 * vs)
+    assert np.all(np.abs(Ve - V_o) <= vs)
+    # the plain relative agreement, for the record
+    print("%s: max |dV|/max(|V|,0.1) = %.2e, max |dg|/|g|max = %.2e" %
+          (name, (err / np.maximum(np.abs(V_o), 0.1)).max(),
+           (np.abs(g_g - g_o) / np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2)).max()))
 
 
 @pytest.mark.parametrize("name", ["O3", "N3"])
@@ -75,12 +83,16 @@ def test_rhs_and_hamiltonian_parity(gpu_lib, oracle_lib, name):
     y = ic["paq"]
     yp_o = o.rhs(y)
     yp_g = api.Collision(H).EvaluateRHS(y)
-    sc = np.abs(yp_o).max(axis=1, keepdims=True)
-    assert np.all(np.abs(yp_g - yp_o) <= 1e-12 * sc)
+    R, _ = o.rp(y[:, 6:])
+    cs = o.condition_scale(R)
+    sc = np.maximum(1e-12 * np.abs(yp_o).max(axis=1, keepdims=True),
+                    100 * 2.2e-16 * cs[:, 1:].max(axis=1, keepdims=True))
+    assert np.all(np.abs(yp_g - yp_o) <= sc), (np.abs(yp_g - yp_o) / sc).max()
     h_o, r_o = o.hamiltonian(y)
     h_g, r_g = api.Collision(H).Hamiltonian(y)
-    assert np.all(np.abs(h_g - h_o) <= 1e-12 * np.maximum(np.abs(h_o), 0.1))
-    assert np.allclose(r_g, r_o, rtol=1e-15, atol=0)
+    hs = np.maximum(1e-12 * np.maximum(np.abs(h_o), 0.1), 100 * 2.2e-16 * cs[:, 0])
+    assert np.all(np.abs(h_g - h_o) <= hs)
+    assert np.allclose(r_g, r_o, rtol=4e-16, atol=0)
     assert np.allclose(api.Collision(H).ApplyTransformation(y), o.apply_transformation(y), rtol=1e-14, atol=1e-300)
     assert np.allclose(H.tpq(), o.tpq, rtol=0, atol=0)
 
@@ -142,20 +154,30 @@ def test_final_state_analysis_parity_on_identical_points(gpu_lib, oracle_lib, na
 
 @pytest.mark.parametrize("name", ["O3", "N3"])
 def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
+    """Final (v, J, arrangement) from the GPU path against the oracle on the same initial
+    conditions.  Rounding differs (FMA, exp), so chaotic trajectories can end differently; the
+    oracle itself, rerun with its initial conditions perturbed by 1e-14, shows how many.  The
+    GPU must agree on >= 99.5 % of the trajectories whose oracle outcome is stable under that
+    perturbation, and overall no worse than the oracle's own reproducibility minus 1 %."""
     cfg, o, H = _setup(name)
-    n = 200
+    n = 400
     ic = _ics(o, name, n)
     ref = o.integrate(ic["paq"], ic["erra"])
+    pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"])
     tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
     api.Integrator(H).Integrate(tr)
     assert np.all(tr.status == 0) and np.all(ref["status"] == 0)
     assert np.max(np.abs(tr.H - ic["H0"])) < cfg.ham_abs_tol
-    fo = o.analyze(o.apply_transformation(ref["paq"]))
+    Jo, vo, ao = _final_qn(o.analyze(o.apply_transformation(ref["paq"])))
+    Jp, vp, ap = _final_qn(o.analyze(o.apply_transformation(pert["paq"])))
     fg = api.MolecularState(H).FindState(api.Collision(H).ApplyTransformation(tr.paq))
-    Jo, vo, ao = _final_qn(fo)
     Jg, vg, ag = _gpu_final_qn(fg)
     same = (Jo == Jg) & (vo == vg) & (ao == ag)
-    assert same.mean() >= 0.995, same.mean()
+    stable = (Jo == Jp) & (vo == vp) & (ao == ap)
+    print("%s: GPU vs oracle %.4f overall, %.4f on oracle-stable (%.4f of trajectories stable)" %
+          (name, same.mean(), same[stable].mean(), stable.mean()))
+    assert same[stable].mean() >= 0.995
+    assert same.mean() >= stable.mean() - 0.01
     c = H.counters()
     assert c["attempts"] == int(np.sum(tr.iste + tr.irej))
 
