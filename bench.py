@@ -6,9 +6,11 @@ from the N2 UMN_ForN4 level list x translational temperatures {5000, 10000, 2000
 each one state-specific RunTrajectories run with its own random-number stream), b = 7 bohr sqrt(U),
 separation 15 bohr, masses 14.0067 amu, plain FP64.  A step samples the initial conditions on the
 device, integrates every trajectory to the end of the collision with the persistent queue-refilled
-kernel, and analyses the initial and final points into trajectories.out rows.  The full 1M-trajectory
-configuration is `--ntraj 1000000`; the default step is 65536 trajectories so that a run ends in
-about a minute.
+kernel, and analyses the initial and final points into trajectories.out rows.  The default step is
+the full 1M-trajectory configuration as one queue: trajectory lengths span 30x (slow collisions run
+to tmax), and on GB300 a lone FP64 thread barely speeds up once its SM empties, so the longest
+trajectories must start at the beginning of a job long enough to hide them (the queue is ordered
+longest-first); smaller steps (--ntraj) are dominated by their slowest trajectory.
 
 value: device-resident inputs, CUDA events on the launch stream around K steps.
 e2e:   the public host entry point cair_run_queue from pinned host buffers (level table and work
@@ -173,12 +175,12 @@ def measured_peaks():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=16)
-    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ntraj", type=int, default=65536, help="trajectories per step")
-    ap.add_argument("--inflight", type=int, default=8, help="batches in flight on separate streams")
-    ap.add_argument("--e2e-ntraj", type=int, default=262144, help="trajectories of the e2e host call")
+    ap.add_argument("--ntraj", type=int, default=1000000, help="trajectories per step (one queue)")
+    ap.add_argument("--inflight", type=int, default=1, help="steps in flight on separate streams")
+    ap.add_argument("--e2e-ntraj", type=int, default=1000000, help="trajectories of the e2e host call")
     ap.add_argument("--max-attempts", type=int, default=1000000)
     ap.add_argument("--cpu-wall", type=float, default=20.0, help="seconds of CPU work per core for the baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -213,42 +213,43 @@ void orc_pip_eval(int table, const double* rms, const double* dmsdr_diag, int wa
   }
 }
 
-/* Condition scale of the PIP sum: scale[0] = sum_i |C_i B_i| and scale[1 + d] =
- * sum_j |C_j dB_j/dvar_d| -- the magnitude of the terms that cancel in V and dV, used to
- * state rounding-level agreement of other evaluation orders. */
+/* Condition scale of the PIP sum: the same graph evaluated on absolute values (|p_a||p_b| +
+ * sum |p_c| at every node, and likewise for the derivatives), i.e. the standard bound on how
+ * far any other evaluation order of these sums can move the result divided by the unit
+ * roundoff.  scale[0] for V, scale[1 + d] for dV/dvar_d. */
 void orc_pip_scale(int table, const double* rms, const double* dmsdr_diag, const double* C, double* scale) {
   pip_tab T = pip_table(table);
   double rm[128], p[480], dm[128], dp[480];
   for (int k = 0; k < T.nmono; ++k) {
     if (T.mo[k] == 0) rm[k] = 1.0;
-    else if (T.mo[k] == 1) rm[k] = rms[T.ma[k]];
+    else if (T.mo[k] == 1) rm[k] = fabs(rms[T.ma[k]]);
     else rm[k] = rm[T.ma[k]] * rm[T.mb[k]];
   }
   for (int k = 0; k < T.npoly; ++k) {
     const short* L = T.plist + T.poff[k];
     double s = 0.0;
     if (T.po[k] == 0) { for (int i = 0; i < T.plen[k]; ++i) s += rm[L[i]]; }
-    else { s = p[T.pa[k]] * p[T.pb[k]]; for (int i = 0; i < T.plen[k]; ++i) s -= p[L[i]]; }
+    else { s = p[T.pa[k]] * p[T.pb[k]]; for (int i = 0; i < T.plen[k]; ++i) s += p[L[i]]; }
     p[k] = s;
   }
   double v = 0.0;
-  for (int i = 0; i < T.nbasis; ++i) v += fabs(C[i] * p[T.basis[i]]);
+  for (int i = 0; i < T.nbasis; ++i) v += fabs(C[i]) * p[T.basis[i]];
   scale[0] = v;
   for (int d = 0; d < T.nvar; ++d) {
     for (int k = 0; k < T.nmono; ++k) {
       if (T.mo[k] == 0) dm[k] = 0.0;
-      else if (T.mo[k] == 1) dm[k] = (T.ma[k] == d) ? dmsdr_diag[d] : 0.0;
+      else if (T.mo[k] == 1) dm[k] = (T.ma[k] == d) ? fabs(dmsdr_diag[d]) : 0.0;
       else dm[k] = dm[T.ma[k]] * rm[T.mb[k]] + rm[T.ma[k]] * dm[T.mb[k]];
     }
     for (int k = 0; k < T.npoly; ++k) {
       const short* L = T.plist + T.poff[k];
       double s = 0.0;
       if (T.po[k] == 0) { for (int i = 0; i < T.plen[k]; ++i) s += dm[L[i]]; }
-      else { s = dp[T.pa[k]] * p[T.pb[k]] + p[T.pa[k]] * dp[T.pb[k]]; for (int i = 0; i < T.plen[k]; ++i) s -= dp[L[i]]; }
+      else { s = dp[T.pa[k]] * p[T.pb[k]] + p[T.pa[k]] * dp[T.pb[k]]; for (int i = 0; i < T.plen[k]; ++i) s += dp[L[i]]; }
       dp[k] = s;
     }
     double g = 0.0;
-    for (int j = 0; j < T.nbasis; ++j) g += fabs(C[j] * dp[T.basis[j]]);
+    for (int j = 0; j < T.nbasis; ++j) g += fabs(C[j]) * dp[T.basis[j]];
     scale[1 + d] = g;
   }
 }

@@ -55,25 +55,33 @@ def test_surface_energy_and_gradient_parity(gpu_lib, oracle_lib, name):
     R, Qall = np.concatenate([R, R2]), np.concatenate([Qall, Q2])
     V_o, g_o, m_o = o.compute(R, Qall)
     V_g, g_g, m_g = api.PES(H).Compute(R, Qall)
-    # 1e-12 relative to max(|V|, 0.1 Eh) (V crosses zero), or 100 rounding units of the condition
-    # scale (sum of the magnitudes of the terms the fit adds, which reaches 10^4..10^6 |V| for O3 at
-    # short range, where any other evaluation order of the same sum moves V by that much)
-    cs = o.condition_scale(R)
-    vs = np.maximum(1e-12 * np.maximum(np.abs(V_o), 0.1), 100 * 2.2e-16 * cs[:, 0])
-    err = np.abs(V_g - V_o)
-    assert np.all(err <= vs), (err / vs).max()
-    gs = np.maximum(1e-12 * np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2), 100 * 2.2e-16 * cs[:, 1:])
-    assert np.all(np.abs(g_g - g_o) <= gs), (np.abs(g_g - g_o) / gs).max()
-    ms = np.maximum(np.abs(m_o).max(axis=1, keepdims=True), 1e-2)
-    mt = np.maximum(1e-12 * ms, 100 * 2.2e-16 * cs[:, 1:].max(axis=1, keepdims=True))
-    assert np.all(np.abs(m_g - m_o) <= mt), (np.abs(m_g - m_o) / mt).max()
-    # energy-only path (PES%Potential)
     Ve = api.PES(H).Potential(R, Qall)
-    assert np.all(np.abs(Ve - V_o) <= vs)
-    # the plain relative agreement, for the record
-    print("%s: max |dV|/max(|V|,0.1) = %.2e, max |dg|/|g|max = %.2e" %
-          (name, (err / np.maximum(np.abs(V_o), 0.1)).max(),
-           (np.abs(g_g - g_o) / np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2)).max()))
+    _check_rounding_level(o, R, V_o, g_o, [(V_g, g_g), (Ve, None)], name)
+    ms = np.maximum(np.abs(m_o).max(axis=1, keepdims=True), 1e-2)
+    bound = np.maximum(1e-12 * ms, 2.2e-16 * o.condition_scale(R)[:, 1:].max(axis=1, keepdims=True))
+    assert np.all(np.abs(m_g - m_o) <= bound)
+
+
+def _check_rounding_level(o, R, V_o, g_o, candidates, name, frac=0.98):
+    """1e-12 relative (energies to max(|V|, 0.1 Eh) since V crosses zero, gradients to the row's
+    largest component) on at least `frac` of the points, and everywhere within the rounding-error
+    bound of the fitted sums: unit roundoff x the surface graph evaluated on absolute values.  The
+    O3 UMN fit cancels terms up to 10^8 times |V| at short range, where no evaluation order other
+    than the reference's own reproduces V to 1e-12."""
+    cs = o.condition_scale(R)
+    vs = np.maximum(np.abs(V_o), 0.1)
+    gs = np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2)
+    for V, g in candidates:
+        ev = np.abs(V - V_o)
+        assert np.all(ev <= np.maximum(1e-12 * vs, 2.2e-16 * cs[:, 0]))
+        assert np.mean(ev <= 1e-12 * vs) >= frac, np.mean(ev <= 1e-12 * vs)
+        if g is not None:
+            eg = np.abs(g - g_o)
+            assert np.all(eg <= np.maximum(1e-12 * gs, 2.2e-16 * cs[:, 1:]))
+            assert np.mean(np.all(eg <= 1e-12 * gs, axis=1)) >= frac
+            print("%s: max |dV|/max(|V|,0.1) = %.2e (%.4f within 1e-12), max |dg|/|g|max = %.2e (%.4f within 1e-12)" %
+                  (name, (ev / vs).max(), np.mean(ev <= 1e-12 * vs), (eg / gs).max(),
+                   np.mean(np.all(eg <= 1e-12 * gs, axis=1))))
 
 
 @pytest.mark.parametrize("name", ["O3", "N3"])
@@ -85,12 +93,12 @@ def test_rhs_and_hamiltonian_parity(gpu_lib, oracle_lib, name):
     yp_g = api.Collision(H).EvaluateRHS(y)
     R, _ = o.rp(y[:, 6:])
     cs = o.condition_scale(R)
-    sc = np.maximum(1e-12 * np.abs(yp_o).max(axis=1, keepdims=True),
-                    100 * 2.2e-16 * cs[:, 1:].max(axis=1, keepdims=True))
-    assert np.all(np.abs(yp_g - yp_o) <= sc), (np.abs(yp_g - yp_o) / sc).max()
+    sc = np.maximum(1e-12 * np.abs(yp_o).max(axis=1, keepdims=True), 2.2e-16 * cs[:, 1:].max(axis=1, keepdims=True))
+    assert np.all(np.abs(yp_g - yp_o) <= sc)
+    assert np.mean(np.all(np.abs(yp_g - yp_o) <= 1e-12 * np.abs(yp_o).max(axis=1, keepdims=True), axis=1)) >= 0.98
     h_o, r_o = o.hamiltonian(y)
     h_g, r_g = api.Collision(H).Hamiltonian(y)
-    hs = np.maximum(1e-12 * np.maximum(np.abs(h_o), 0.1), 100 * 2.2e-16 * cs[:, 0])
+    hs = np.maximum(1e-12 * np.maximum(np.abs(h_o), 0.1), 2.2e-16 * cs[:, 0])
     assert np.all(np.abs(h_g - h_o) <= hs)
     assert np.allclose(r_g, r_o, rtol=4e-16, atol=0)
     assert np.allclose(api.Collision(H).ApplyTransformation(y), o.apply_transformation(y), rtol=1e-14, atol=1e-300)
