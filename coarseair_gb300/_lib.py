@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcair_gpu.so")
 CAIR_MAX_PES = 8
 CAIR_ABI_VERSION = 1
+CAIR_STATIC_QUEUE_MAX_TRAJ = 16384
 
 STATUS = {0: "CAIR_OK", 1: "CAIR_EINVAL", 2: "CAIR_ECUDA", 3: "CAIR_ETIMEOUT", 4: "CAIR_ENONFINITE",
           5: "CAIR_EUNSUPPORTED"}
@@ -81,6 +82,7 @@ SIGNATURES = [
     ("cair_run_queue", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P]),
     ("cair_run_queue_dev", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, _P, _P]),
     ("cair_queue_workspace_bytes", C.c_int64, [C.c_int64]),
+    ("cair_run_queue_static_dev", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, _P]),
     ("cair_flop_model", C.c_int, [_P, C.c_int32, _D, _D, _D, _D]),
     ("cair_last_counters", C.c_int, [_P, _L]),
     ("cair_fp64_peak_probe", C.c_int, [_P, _D]),

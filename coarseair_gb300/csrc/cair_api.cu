@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -645,9 +646,9 @@ struct BatchBufs {
   int32_t *irej, *iste, *status, *ipes, *item_of, *order;
 };
 
-size_t batch_bytes(int64_t n) {
-  size_t per = sizeof(double) * (12 * 3 + 9 + kDraws) + sizeof(int32_t) * 6;
-  return (size_t)n * per + 40 * 256 + sizeof(unsigned long long) * (8 + 2 * 256);
+constexpr size_t batch_bytes(int64_t n) {
+  return (size_t)n * (sizeof(double) * (12 * 3 + 9 + kDraws) + sizeof(int32_t) * 6) + 40 * 256 +
+         sizeof(unsigned long long) * (8 + 2 * 256);
 }
 
 void carve_into(char* base, int64_t n, BatchBufs& B) {
@@ -781,6 +782,50 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
   if (!workspace)
     CUDA_TRY(h, cudaMemcpyAsync(h->d_ctl + 1, B.ctl + 1, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToDevice, st));
   return 0;
+}
+
+}  // extern "C"
+
+// -----------------------------------------------------------------------------------------
+// Allocation-free variant of the queue path.  The batch state of up to
+// CAIR_STATIC_QUEUE_MAX_TRAJ trajectories lives in this file-scope device array, which every
+// GPU that loads the library holds until the process exits.  In host code the array's name is
+// only a host-side stand-in, so its device address is looked up once per device with
+// cudaGetSymbolAddress (on the first call made with that device current) and passed to the
+// kernels like any workspace.  Every call shares the array: the queue head and counters are
+// cleared at the start of each call, and calls that overlap on the GPU race.
+// -----------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_cair_static_queue_ws[batch_bytes(CAIR_STATIC_QUEUE_MAX_TRAJ)];
+static std::mutex g_static_ws_mutex;
+static void* g_static_ws_ptr[64] = {nullptr};
+
+extern "C" {
+
+int cair_run_queue_static_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                              const cair_work_item* items, int64_t ntot, int64_t max_attempts,
+                              cair_traj_result* results, void* stream) {
+  if (!h) return CAIR_EINVAL;
+  if (ntot < 0 || ntot > CAIR_STATIC_QUEUE_MAX_TRAJ)
+    return fail(h, CAIR_EINVAL, "cair_run_queue_static_dev: ntot exceeds the static workspace (at most " +
+                                    std::to_string(CAIR_STATIC_QUEUE_MAX_TRAJ) + " trajectories per call)");
+  int dev = -1;
+  CUDA_TRY(h, cudaGetDevice(&dev));
+  if (dev != h->device || dev < 0 || dev >= 64)
+    return fail(h, CAIR_EINVAL, "cair_run_queue_static_dev: the current device is not the handle's device");
+  void* ws = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_ws_mutex);
+    if (!g_static_ws_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_cair_static_queue_ws);
+      if (e != cudaSuccess || !p)
+        return fail(h, CAIR_ECUDA, std::string("cudaGetSymbolAddress of the static workspace: ") +
+                                       cudaGetErrorString(e));
+      g_static_ws_ptr[dev] = p;
+    }
+    ws = g_static_ws_ptr[dev];
+  }
+  return cair_run_queue_dev(h, nlevels, levels, nitems, items, ntot, max_attempts, results, ws, stream);
 }
 
 int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,

@@ -255,6 +255,20 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
                        void* workspace, void* stream);
 int64_t cair_queue_workspace_bytes(int64_t ntot);
 
+/* No counterpart in the reference.  cair_run_queue_dev for callers that cannot allocate device
+ * memory once they are running (a host whose GPU memory is handed out by its own pool at
+ * start-up, or code that must not trigger cudaMalloc's implicit synchronisation while it
+ * runs): the batch state lives in a file-scope static device array of
+ * CAIR_STATIC_QUEUE_MAX_TRAJ trajectories (about 7 MB that every GPU loading the library
+ * keeps until exit), and the call allocates nothing.  ntot > CAIR_STATIC_QUEUE_MAX_TRAJ is
+ * rejected with CAIR_EINVAL.  The first call on a device looks up the array's device address,
+ * so make it before any stream capture; the handle's device must be current.  All calls share
+ * the array, so calls that overlap on the GPU race; the array keeps the last call's contents. */
+#define CAIR_STATIC_QUEUE_MAX_TRAJ 16384
+int cair_run_queue_static_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                              const cair_work_item* items, int64_t ntot, int64_t max_attempts,
+                              cair_traj_result* results, void* stream);
+
 /* Algorithmic FP64 operation counts the library's kernels execute per PES energy+gradient
  * evaluation, per energy-only evaluation and per BS attempt (excluding the PES), for
  * roofline accounting.  `exp_per_eval` counts exponentials separately. */
