@@ -115,50 +115,62 @@ __global__ void __launch_bounds__(64) k_integrate3(DevSys S, IntegrateArgs A) {
   unsigned long long c_att = 0, c_acc = 0, c_rej = 0;
   const bool incstp = S.incstp != 0;
   const int ncall = S.ncall;
-  for (;;) {
+  // Lane state.  A lane takes a new trajectory only at an ncall-block boundary, where the whole
+  // warp meets (__syncwarp), so the warp's active lanes always run their attempts in lockstep;
+  // each trajectory still gets its end check after every ncall attempts of its own.
+  unsigned long long k = 0;
+  bool active = false;
+  int ip = 0, irej = 0, iste = 0, irej0 = 0, iste0 = 0;
+  int64_t att = 0;
+  double y[12], x = 0.0, h = 0.0, smax = 0.0, smin = 0.0, H = 0.0;
+  auto take = [&]() {
     const unsigned long long q = atomicAdd(A.queue, 1ull);
-    if (q >= (unsigned long long)A.n) break;
-    const unsigned long long k = A.order ? (unsigned long long)A.order[q] : q;
-    const int ip = A.ipes ? A.ipes[k] : 0;
-    const DevPes& P = S.pes[ip];
-    Rhs3<MODEL> f(S, P);
-    double y[12];
+    active = q < (unsigned long long)A.n;
+    if (!active) return;
+    k = A.order ? (unsigned long long)A.order[q] : q;
+    ip = A.ipes ? A.ipes[k] : 0;
 #pragma unroll
     for (int i = 0; i < 12; ++i) y[i] = A.paq[12 * k + i];
-    double x = A.t[k], h = A.dt[k], smax = A.smax[k], smin = A.smin[k], H = 0.0;
-    int irej = A.irej[k], iste = A.iste[k];
-    const int irej0 = irej, iste0 = iste;
-    int64_t att = 0;
-    int st = CAIR_TRAJ_ATTEMPT_CAP;
-    const double* yscal = A.erra + 12 * k;
+    x = A.t[k]; h = A.dt[k]; smax = A.smax[k]; smin = A.smin[k]; H = 0.0;
+    irej = irej0 = A.irej[k];
+    iste = iste0 = A.iste[k];
+    att = 0;
+  };
+  take();
 #pragma unroll 1
-    for (;;) {
+  for (;;) {
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active) {
+      const DevPes& P = S.pes[ip];
+      Rhs3<MODEL> f(S, P);
       int bad = 0;
 #pragma unroll 1
-      for (int c = 0; c < ncall; ++c) bad |= bs_attempt<12, NS>(f, y, x, h, yscal, S.relax, incstp, smax, smin, irej, iste);
+      for (int c = 0; c < ncall; ++c)
+        bad |= bs_attempt<12, NS>(f, y, x, h, A.erra + 12 * k, S.relax, incstp, smax, smin, irej, iste);
       att += ncall;
       double rpi[3];
       H = hamiltonian3<MODEL>(S, P, y, rpi);
-      if (bad) { st = CAIR_TRAJ_NONFINITE; break; }
       bool conv = x > S.tmax;
 #pragma unroll
       for (int p = 0; p < 3; ++p) conv = conv || (rpi[p] < S.rpimax);
-      if (conv) { st = CAIR_TRAJ_DONE; break; }
-      if (att >= A.max_attempts) break;
-    }
+      if (bad || conv || att >= A.max_attempts) {
 #pragma unroll
-    for (int i = 0; i < 12; ++i) A.paq[12 * k + i] = y[i];
-    A.t[k] = x;
-    A.dt[k] = h;
-    A.H[k] = H;
-    A.smax[k] = smax;
-    A.smin[k] = smin;
-    A.irej[k] = irej;
-    A.iste[k] = iste;
-    A.status[k] = st;
-    c_att += att;
-    c_acc += iste - iste0;
-    c_rej += irej - irej0;
+        for (int i = 0; i < 12; ++i) A.paq[12 * k + i] = y[i];
+        A.t[k] = x;
+        A.dt[k] = h;
+        A.H[k] = H;
+        A.smax[k] = smax;
+        A.smin[k] = smin;
+        A.irej[k] = irej;
+        A.iste[k] = iste;
+        A.status[k] = bad ? CAIR_TRAJ_NONFINITE : (conv ? CAIR_TRAJ_DONE : CAIR_TRAJ_ATTEMPT_CAP);
+        c_att += att;
+        c_acc += iste - iste0;
+        c_rej += irej - irej0;
+        take();
+      }
+    }
+    __syncwarp();
   }
   if (c_att) {
     atomicAdd(A.counters + 0, c_att);
