@@ -20,6 +20,7 @@ Fortran cannot be built here) on the host cores, one process per core, on a boun
 same work items.
 """
 import argparse
+import ctypes
 import json
 import math
 import multiprocessing as mp
@@ -32,6 +33,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
+
+# DRAM bytes per trajectory of the persistent integrator, measured with ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum = 62.16 MB for a 98,304-trajectory launch of this workload); the state is read
+# and written once per trajectory, so the full launch's traffic scales with the trajectory count
+DRAM_BYTES_PER_TRAJ = 632.0
 
 TEMPS = (5000.0, 10000.0, 20000.0)
 
@@ -268,7 +274,7 @@ def main():
                     else "/tmp/bench_clocks.csv")
     ev0 = torch.cuda.Event(enable_timing=True)
     ev_end = [torch.cuda.Event(enable_timing=True) for _ in streams]
-    attempts = 0
+    H.check(lib.cair_set_integrate_timing(H.h, 1), "cair_set_integrate_timing")
     with clocks:
         torch.cuda.synchronize()
         ev0.record(streams[0])
@@ -280,6 +286,12 @@ def main():
             e.record(st)
         torch.cuda.synchronize()
     ms = max(ev0.elapsed_time(e) for e in ev_end)
+    # the persistent integrator's own launches, timed by the library with events on their stream
+    kt = (ctypes.c_float * max(1, args.steps))()
+    nk = ctypes.c_int32(0)
+    H.check(lib.cair_integrate_timings(H.h, kt, args.steps, ctypes.byref(nk)), "cair_integrate_timings")
+    H.check(lib.cair_set_integrate_timing(H.h, 0), "cair_set_integrate_timing")
+    integ_ms = float(np.mean(list(kt)[:nk.value]))
     if world > 1:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -313,14 +325,18 @@ def main():
     # dominant kernel: the persistent integrator; its share of the step is measured in profiles/
     peak_fp64 = fp64_peak_probe(lib, H)
     ms_step = ms / args.steps
-    achieved = flops_step / (ms_step / 1e3) / 1e12
+    achieved = flops_step / (integ_ms / 1e3) / 1e12
     line = {"metric": metric, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg_json,
             "gpu_launches": 8 * args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_fp64["tflops"], "unit": "TFLOP/s",
-                         "frac": achieved / peak_fp64["tflops"], "traffic": None,
+                         "frac": achieved / peak_fp64["tflops"], "traffic": DRAM_BYTES_PER_TRAJ * n,
+                         "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of a "
+                                           "98,304-trajectory launch (632 B per trajectory), scaled by trajectories",
                          "peak_source": peak_fp64["source"],
+                         "kernel": "k_integrate3 (persistent Bulirsch-Stoer integrator)",
+                         "kernel_ms_per_launch": integ_ms, "kernel_share_of_step": integ_ms * args.steps / ms,
                          "work": "executed FP64 operations of the pruned formulation per step "
                                  "(exp, division and sqrt counted as one operation each)"},
             "pes_evals_per_s": counters["grad_evals"] / (ms_step / 1e3),

@@ -86,6 +86,8 @@ SIGNATURES = [
     ("cair_flop_model", C.c_int, [_P, C.c_int32, _D, _D, _D, _D]),
     ("cair_last_counters", C.c_int, [_P, _L]),
     ("cair_fp64_peak_probe", C.c_int, [_P, _D]),
+    ("cair_set_integrate_timing", C.c_int, [_P, C.c_int32]),
+    ("cair_integrate_timings", C.c_int, [_P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_int32)]),
 ]
 
 _lib = None

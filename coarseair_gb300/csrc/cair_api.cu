@@ -34,6 +34,9 @@ struct cair_handle {
   unsigned long long* d_ctl = nullptr;   // [0] queue, [1..5] counters
   long long last_counters[5] = {0, 0, 0, 0, 0};
   double watchdog_s = 0.0;
+  bool time_integrate = false;              // bracket every integrator launch with events
+  std::vector<cudaEvent_t> tev;             // pairs (start, end), reused across calls
+  size_t ntev = 0;                          // pairs recorded since the last read
 };
 
 namespace {
@@ -393,6 +396,7 @@ void cair_destroy(cair_handle* h) {
   if (h->d_work) cudaFree(h->d_work);
   if (h->d_ctl) cudaFree(h->d_ctl);
   if (h->stream) cudaStreamDestroy(h->stream);
+  for (cudaEvent_t e : h->tev) cudaEventDestroy(e);
   delete h;
 }
 
@@ -533,8 +537,23 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A, cudaStream_t
   int64_t need = (A.n + block - 1) / block;
   if (g > need) g = need;
   if (g < 1) g = 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (h->time_integrate) {
+    if (2 * h->ntev + 2 > h->tev.size()) {
+      for (int k = 0; k < 2; ++k) {
+        cudaEvent_t e;
+        CUDA_TRY(h, cudaEventCreate(&e));
+        h->tev.push_back(e);
+      }
+    }
+    e0 = h->tev[2 * h->ntev];
+    e1 = h->tev[2 * h->ntev + 1];
+    ++h->ntev;
+    CUDA_TRY(h, cudaEventRecord(e0, st));
+  }
   if (m == CAIR_PES_O3_UMN) k_integrate3<CAIR_PES_O3_UMN, 3><<<(int)g, block, 0, st>>>(h->sys, A);
   else k_integrate3<CAIR_PES_N3_UMN, 3><<<(int)g, block, 0, st>>>(h->sys, A);
+  if (e1) CUDA_TRY(h, cudaEventRecord(e1, st));
   return check_launch(h);
 }
 
@@ -856,13 +875,18 @@ int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, in
 int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, double* fa, double* ex) {
   if (!h || ipes < 0 || ipes >= h->sys.npes) return CAIR_EINVAL;
   // FP64 operations of the executed formulation, counted from the device code (an FMA counts
-  // two, exp / division / sqrt one each): PIP part from the generator's counts; per pair the
+  // two, exp / division / sqrt one each): PIP part from the generator's counts of the gradient
+  // formulation compiled in (adjoint sweep unless CAIR_PIP_FORWARD); per pair the
   // diatomic (O2 UMN 107 with gradient, 64 energy only; N2 UMN_ForN4 64 / 40) and the MEG
   // variable (11 / 7); pair distances 36, TransToCart 46, Hamilton's equations 18, assembly 15.
   const int m = h->sys.pes[ipes].model;
   const bool o2 = h->sys.diat == CAIR_DIAT_O2_UMN;
   const double diat_g = o2 ? 107 : 64, diat_e = o2 ? 64 : 40, meg_g = 11, meg_e = 7;
+#ifdef CAIR_PIP_FORWARD
   const double pip_g = m == CAIR_PES_O3_UMN ? PIP_O3_EVAL_FLOPS : PIP_N3_EVAL_FLOPS;
+#else
+  const double pip_g = m == CAIR_PES_O3_UMN ? PIP_O3_EVAL_REV_FLOPS : PIP_N3_EVAL_REV_FLOPS;
+#endif
   const double pip_e = m == CAIR_PES_O3_UMN ? PIP_O3_VALUE_FLOPS : PIP_N3_VALUE_FLOPS;
   if (fg) *fg = pip_g + 3 * (diat_g + meg_g) + 36 + 46 + 18 + 15;
   if (fe) *fe = pip_e + 3 * (diat_e + meg_e) + 36 + 30 + 8;
@@ -870,6 +894,25 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
   // extrapolation (297), error norms and step control (82)
   if (fa) *fa = 811;
   if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1);
+  return 0;
+}
+
+int cair_set_integrate_timing(cair_handle* h, int32_t on) {
+  if (!h) return CAIR_EINVAL;
+  h->time_integrate = on != 0;
+  h->ntev = 0;
+  return 0;
+}
+
+int cair_integrate_timings(cair_handle* h, float* ms, int32_t cap, int32_t* count) {
+  if (!h || !count || cap < 0 || (cap > 0 && !ms)) return CAIR_EINVAL;
+  const int32_t n = (int32_t)h->ntev;
+  for (int32_t k = 0; k < n && k < cap; ++k) {
+    CUDA_TRY(h, cudaEventSynchronize(h->tev[2 * k + 1]));
+    CUDA_TRY(h, cudaEventElapsedTime(&ms[k], h->tev[2 * k], h->tev[2 * k + 1]));
+  }
+  *count = n;
+  h->ntev = 0;
   return 0;
 }
 

@@ -9,6 +9,8 @@ This module reads the same data the reference reads at start-up:
   ``a, ab, ra, rb, Eref, totdiss``, 143 lines of three coefficients, then ``C(430)``;
 * N3 UMN: the 276 coefficients the reference keeps inline (N3_UMN_PES_Class.F90:108-201),
   stored here as ``data/N3_UMN.dat``;
+* O3 NN surfaces: ``dtb/Systems/O3/PESs/NN/<Model>/<NHL1>_<NHL2>/`` (O3_NN_PES_Class.F90:74-232):
+  ``ScalingValues.csv`` and ``CalibratedParams/{Lambda,re,W1,b1,W2,b2,W3,b3}.csv``;
 * level lists ``vqn jqn eint egam rmin rmax vmin vmax tau ri ro`` (LevelsContainer_Class.F90).
 
 and fills the input-file keys of the hot path with the values of the reference's own input
@@ -24,7 +26,7 @@ import numpy as np
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
 AMU_TO_AU = 1822.888486209          # [amu] -> electron masses (kgm_To_au / 1000)
-PES_O3_UMN, PES_N3_UMN, PES_O4_UMN = 1, 2, 3
+PES_O3_UMN, PES_N3_UMN, PES_O4_UMN, PES_O3_NN = 1, 2, 3, 4
 DIAT_O2_UMN, DIAT_N2_UMN_FORN4 = 1, 2
 
 _FNUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[dDeE][-+]?\d+)?")
@@ -78,6 +80,37 @@ def load_n3_umn():
 
 
 LEVEL_COLS = ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax", "tau", "ri", "ro")
+
+
+def load_o3_nn(model="NN_11A1_MPE", hidden=(20, 10)):
+    """O3 NN surface as the reference reads it (O3_NN_PES_Class.F90:139-230), packed into one
+    coefficient array: NHL1, NHL2, Lambda, re, Scaling_MEAN(3), Scaling_SD(3), y_Scaling,
+    W1(6, NHL1), b1, W2(NHL1, NHL2), b2, W3, b3, matrices column-major."""
+    h1, h2 = hidden
+    d = os.path.join(DATA, "O3_NN", model, "%d_%d" % (h1, h2))
+    cp = os.path.join(d, "CalibratedParams")
+
+    def rows(name):
+        with open(os.path.join(cp, name)) as f:
+            return [[float(x) for x in ln.replace(",", " ").split()] for ln in f if ln.strip()]
+
+    with open(os.path.join(d, "ScalingValues.csv")) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip()]
+    mean = [float(x) for x in lines[1].split(",")]
+    sd = [float(x) for x in lines[2].split(",")]
+    ysc = float(lines[3].split(",")[0])
+    lam, re_ = rows("Lambda.csv")[0][0], rows("re.csv")[0][0]
+    W1 = np.array(rows("W1.csv"))                  # row i = W1(i, 1:NHL1)
+    W2 = np.array(rows("W2.csv"))                  # row i = W2(i, 1:NHL2)
+    b1 = np.array(rows("b1.csv")).ravel()
+    b2 = np.array(rows("b2.csv")).ravel()
+    W3 = np.array(rows("W3.csv")).ravel()
+    b3 = rows("b3.csv")[0][0]
+    assert W1.shape == (6, h1) and W2.shape == (h1, h2) and b1.size == h1 and b2.size == h2 and W3.size == h2
+    coef = np.concatenate([[h1, h2, lam, re_], mean, sd, [ysc], W1.ravel(order="F"), b1, W2.ravel(order="F"),
+                           b2, W3, [b3]]).astype(np.float64)
+    assert coef.size == 12 + 7 * h1 + h1 * h2 + 2 * h2
+    return Surface(PES_O3_NN, coef, name="O3 " + model)
 
 
 def load_levels(name):
@@ -143,6 +176,12 @@ def o3_config(model="UMN_11A1", mass_amu=15.9994, **kw):
     """O2 + O on one O3 UMN surface (the ground state UMN_11A1 by default)."""
     m = mass_amu * AMU_TO_AU
     return SystemConfig("O2+O " + model, 3, (m, m, m), [load_o3_umn(model)], DIAT_O2_UMN, **kw)
+
+
+def o3nn_config(model="NN_11A1_MPE", mass_amu=15.9994, **kw):
+    """O2 + O on an O3 NN surface with the O2 UMN diatomic."""
+    m = mass_amu * AMU_TO_AU
+    return SystemConfig("O2+O " + model, 3, (m, m, m), [load_o3_nn(model)], DIAT_O2_UMN, **kw)
 
 
 def n3_config(mass_amu=14.0067, **kw):

@@ -279,6 +279,14 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* flops_grad, doub
  * measured with a register-resident DFMA kernel; the denominator of the FP64 roofline. */
 int cair_fp64_peak_probe(cair_handle* h, double* gflops);
 
+/* Kernel timing for roofline accounting (no counterpart in the reference).  While on, every
+ * launch of the persistent integrator made by cair_integrate* / cair_run_queue* is bracketed by
+ * CUDA events on the stream it runs on.  cair_integrate_timings waits for the recorded launches,
+ * writes the first `cap` durations [ms] in launch order, sets *count to the number recorded and
+ * starts a new record.  cair_set_integrate_timing also starts a new record. */
+int cair_set_integrate_timing(cair_handle* h, int32_t on);
+int cair_integrate_timings(cair_handle* h, float* ms, int32_t cap, int32_t* count);
+
 /* Device counters of the last cair_integrate*: total BS attempts, accepted, rejected,
  * PES gradient evaluations, PES energy evaluations. */
 int cair_last_counters(cair_handle* h, int64_t* counters5);

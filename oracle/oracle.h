@@ -28,13 +28,15 @@
 extern "C" {
 #endif
 
-enum { ORC_PES_O3_UMN = 1, ORC_PES_N3_UMN = 2, ORC_PES_O4_UMN = 3 };
+enum { ORC_PES_O3_UMN = 1, ORC_PES_N3_UMN = 2, ORC_PES_O4_UMN = 3, ORC_PES_O3_NN = 4 };
 enum { ORC_DIAT_O2_UMN = 1, ORC_DIAT_N2_UMN_FORN4 = 2 };
 
 typedef struct orc_pes {
   int model;
   int ncoef;
-  const double* coef;           /* C(1:ncoef) [kcal/mol] */
+  const double* coef;           /* UMN: C(1:ncoef) [kcal/mol].  O3 NN: NHL1, NHL2, Lambda, re,
+                                   Scaling_MEAN(3), Scaling_SD(3), y_Scaling, W1(6,NHL1), b1, W2(NHL1,NHL2),
+                                   b2, W3, b3 (column-major, as read by O3_NN_PES_Class.F90:74-232) */
   double a, ab, ra, rb;         /* MEG parameters (O3, O4) */
   double eref, totdiss;         /* O4 */
 } orc_pes;
@@ -66,6 +68,7 @@ void   orc_diat_VdV(int model, double r, double* v, double* dv);
 void   orc_pes_compute(const orc_sys* s, int ipes, const double* R, const double* Qall,
                        double* V, double* dVdR, double* dVdQ);
 double orc_pes_potential(const orc_sys* s, int ipes, const double* R);
+int    orc_o3nn_ncoef(int nhl1, int nhl2);
 /* PIP part only (kcal/mol, derivatives wrt R in Angstrom), all six/three directions */
 void   orc_pip_eval(int table, const double* rms, const double* dmsdr_diag, int want_grad,
                     const double* C, double V0, double* V, double* dV);

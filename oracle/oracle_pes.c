@@ -256,9 +256,15 @@ void orc_pip_scale(int table, const double* rms, const double* dmsdr_diag, const
 
 /* Condition scale of a 3-atom surface evaluation at distances R [bohr]: scale[0] for V [Eh],
  * scale[1..3] for dV/dR [Eh/bohr] (PIP terms plus the diatomic terms' magnitudes). */
+static void o3nn_scale(const orc_sys* s, const orc_pes* P, const double* R, double* scale);
+
 void orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale) {
   const orc_pes* P = &s->pes[ipes];
   double rms[6] = {0}, dms[6] = {0}, sc[7];
+  if (P->model == ORC_PES_O3_NN) {
+    o3nn_scale(s, P, R, scale);
+    return;
+  }
   if (P->model == ORC_PES_O3_UMN) {
     for (int i = 0; i < 3; ++i) {
       double r = R[i] * B_TO_ANG, d1 = r - P->ra, d2 = r - P->rb;
@@ -408,12 +414,190 @@ static void o4_compute(const orc_sys* s, const orc_pes* P, const double* R, cons
   trans_to_cart_4(s->mMiMn, R, Qall, dVdR, dVdQ);
 }
 
+
+/* O3 NN (O3_NN_PES_Class.F90).  Compute (357-477) evaluates the six symmetric features
+ * G = [sum p_i p_j, p1 p2 p3, sum p_i^2 p_j, sum p_i^3 p_j, p1 p2 p3 sum p_i, sum p_i^2 p_j^2] of
+ * p = exp(-Lambda (R - re)) through the tanh-tanh-linear network; Potential (250-297), which the
+ * Hamiltonian calls, evaluates three features, scaled by Scaling_MEAN/SD, through
+ * dgemm(..., W1, 3, ...), i.e. on the leading 3 x NHL1 block of W1's storage read with leading
+ * dimension 3.  The two therefore differ; both are kept as the reference has them. */
+#define EV_TO_HARTREE (1.0 / 27.2113839712790)
+typedef struct {
+  int h1, h2;
+  double lam, re, mean[3], sd[3], ysc, b3;
+  const double *W1, *b1, *W2, *b2, *W3;
+} nn_view;
+
+static nn_view nn_unpack(const double* c) {
+  nn_view v;
+  v.h1 = (int)c[0]; v.h2 = (int)c[1];
+  v.lam = c[2]; v.re = c[3];
+  for (int i = 0; i < 3; ++i) { v.mean[i] = c[4 + i]; v.sd[i] = c[7 + i]; }
+  v.ysc = c[10];
+  const double* q = c + 11;
+  v.W1 = q; q += 6 * v.h1;
+  v.b1 = q; q += v.h1;
+  v.W2 = q; q += v.h1 * v.h2;
+  v.b2 = q; q += v.h2;
+  v.W3 = q; q += v.h2;
+  v.b3 = *q;
+  return v;
+}
+
+int orc_o3nn_ncoef(int h1, int h2) { return 12 + 7 * h1 + h1 * h2 + 2 * h2; }
+
+static void o3nn_compute(const orc_sys* s, const orc_pes* P, const double* R, const double* Qall, double* V,
+                         double* dVdR, double* dVdQ) {
+  const nn_view n = nn_unpack(P->coef);
+  double vd[3], dvd[3], p[3];
+  for (int i = 0; i < 3; ++i) orc_diat_VdV(s->diat, R[i], &vd[i], &dvd[i]);
+  for (int i = 0; i < 3; ++i) p[i] = exp(-(n.lam * (R[i] - n.re)));
+  const double gvp[3] = {p[0] * p[1], p[1] * p[2], p[2] * p[0]};
+  const double gvs[3] = {p[1] + p[2], p[2] + p[0], p[0] + p[1]};
+  const double gc[6] = {gvp[0] * p[0], gvp[0] * p[1], gvp[1] * p[1], gvp[1] * p[2], gvp[2] * p[0], gvp[2] * p[2]};
+  const double gprod = (p[0] * p[1]) * p[2];
+  double G[6];
+  G[0] = (gvp[0] + gvp[1]) + gvp[2];
+  G[1] = gprod;
+  G[2] = ((((gc[0] + gc[1]) + gc[2]) + gc[3]) + gc[4]) + gc[5];
+  G[3] = ((((gc[0] * p[0] + gc[1] * p[1]) + gc[2] * p[1]) + gc[3] * p[2]) + gc[4] * p[0]) + gc[5] * p[2];
+  G[4] = (gc[0] * p[2] + gc[2] * p[0]) + gc[5] * p[1];
+  G[5] = (gc[0] * p[1] + gc[2] * p[2]) + gc[4] * p[2];
+  double psq[3], pcu[3];
+  for (int i = 0; i < 3; ++i) { psq[i] = n.lam * (p[i] * p[i]); pcu[i] = n.lam * ((p[i] * p[i]) * p[i]); }
+  const double psqs[3] = {psq[1] + psq[2], psq[2] + psq[0], psq[0] + psq[1]};
+  const double pcus[3] = {pcu[1] + pcu[2], pcu[2] + pcu[0], pcu[0] + pcu[1]};
+  const double gvps[3] = {-(n.lam * (gvp[0] + gvp[2])), -(n.lam * (gvp[1] + gvp[0])), -(n.lam * (gvp[2] + gvp[1]))};
+  double dG[3][6];
+  for (int r = 0; r < 3; ++r) {
+    dG[r][0] = gvps[r];
+    dG[r][1] = -(n.lam * gprod);
+    dG[r][2] = -((2.0 * gvs[r]) * psq[r] + p[r] * psqs[r]);
+    dG[r][3] = -((3.0 * gvs[r]) * pcu[r] + p[r] * pcus[r]);
+    dG[r][4] = -((n.lam * gprod) * (2.0 * p[r] + gvs[r]));
+    dG[r][5] = -(((2.0 * psq[r]) * psqs[r]) / n.lam);
+  }
+  double z1[64], y1[64], z2[64], y2[64];
+  for (int j = 0; j < n.h1; ++j) {
+    double acc = 0.0;
+    for (int i = 0; i < 6; ++i) acc = acc + G[i] * n.W1[i + 6 * j];
+    z1[j] = acc + n.b1[j];
+    y1[j] = tanh(z1[j]);
+  }
+  for (int k = 0; k < n.h2; ++k) {
+    double acc = 0.0;
+    for (int j = 0; j < n.h1; ++j) acc = acc + y1[j] * n.W2[j + n.h1 * k];
+    z2[k] = acc + n.b2[k];
+    y2[k] = tanh(z2[k]);
+  }
+  double v = 0.0;
+  for (int k = 0; k < n.h2; ++k) v = v + y2[k] * n.W3[k];
+  v = v + n.b3;
+  *V = (v - n.ysc) * EV_TO_HARTREE + ((vd[0] + vd[1]) + vd[2]);
+  if (!dVdR) return;
+  for (int r = 0; r < 3; ++r) {
+    double dy1[64];
+    for (int j = 0; j < n.h1; ++j) {
+      double acc = 0.0;
+      for (int i = 0; i < 6; ++i) acc = acc + dG[r][i] * n.W1[i + 6 * j];
+      dy1[j] = (1.0 - y1[j] * y1[j]) * acc;
+    }
+    double sum = 0.0;
+    for (int k = 0; k < n.h2; ++k) {
+      double acc = 0.0;
+      for (int j = 0; j < n.h1; ++j) acc = acc + n.W2[j + n.h1 * k] * dy1[j];
+      sum = sum + (n.W3[k] * (1.0 - y2[k] * y2[k])) * acc;
+    }
+    dVdR[r] = sum * EV_TO_HARTREE + dvd[r];
+  }
+  trans_to_cart_3(s->mMiMn, R, Qall, dVdR, dVdQ);
+}
+
+static double o3nn_potential(const orc_sys* s, const orc_pes* P, const double* R) {
+  const nn_view n = nn_unpack(P->coef);
+  double vd[3], dvd[3], p[3];
+  for (int i = 0; i < 3; ++i) orc_diat_VdV(s->diat, R[i], &vd[i], &dvd[i]);
+  for (int i = 0; i < 3; ++i) p[i] = exp(-(n.lam * (R[i] - n.re)));
+  const double gvp[3] = {p[0] * p[1], p[1] * p[2], p[2] * p[0]};
+  const double gvs[3] = {p[0] + p[1], p[1] + p[2], p[2] + p[0]};
+  double G[3];
+  G[0] = (gvp[0] + gvp[1]) + gvp[2];
+  G[1] = (p[0] * p[1]) * p[2];
+  G[2] = (gvp[0] * gvs[0] + gvp[1] * gvs[1]) + gvp[2] * gvs[2];
+  for (int i = 0; i < 3; ++i) G[i] = (G[i] - n.mean[i]) / n.sd[i];
+  /* reference BLAS dgemm, alpha = beta = 1: C(1,j) += B(l,j) * A(1,l), l ascending */
+  double y1[64];
+  for (int j = 0; j < n.h1; ++j) {
+    double z = n.b1[j];
+    for (int l = 0; l < 3; ++l) z = z + n.W1[l + 3 * j] * G[l];
+    y1[j] = tanh(z);
+  }
+  double v = 0.0;
+  for (int k = 0; k < n.h2; ++k) {
+    double z = n.b2[k];
+    for (int j = 0; j < n.h1; ++j) z = z + n.W2[j + n.h1 * k] * y1[j];
+    v = v + tanh(z) * n.W3[k];
+  }
+  v = v + n.b3;
+  return (v - n.ysc) * EV_TO_HARTREE + ((vd[0] + vd[1]) + vd[2]);
+}
+
+/* Rounding-level scale of the O3 NN evaluation: the network evaluated on absolute values, with
+ * the absolute error of each pre-activation carried through tanh (|tanh'| <= 1). */
+static void o3nn_scale(const orc_sys* s, const orc_pes* P, const double* R, double* scale) {
+  const nn_view n = nn_unpack(P->coef);
+  double p[3];
+  for (int i = 0; i < 3; ++i) p[i] = exp(-(n.lam * (R[i] - n.re)));
+  double G[6] = {p[0] * p[1] + p[1] * p[2] + p[2] * p[0], p[0] * p[1] * p[2], 0, 0, 0, 0};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (i != j) { G[2] += p[i] * p[i] * p[j]; G[3] += p[i] * p[i] * p[i] * p[j]; }
+  G[4] = G[1] * (p[0] + p[1] + p[2]);
+  G[5] = p[0] * p[0] * p[1] * p[1] + p[1] * p[1] * p[2] * p[2] + p[0] * p[0] * p[2] * p[2];
+  double a1[64], a2[64], w1g[6] = {0};
+  for (int j = 0; j < n.h1; ++j) {
+    double z = fabs(n.b1[j]);
+    for (int i = 0; i < 6; ++i) z += fabs(G[i] * n.W1[i + 6 * j]);
+    a1[j] = 1.0 + z;
+  }
+  double sv = fabs(n.b3) + fabs(n.ysc);
+  for (int k = 0; k < n.h2; ++k) {
+    double z = fabs(n.b2[k]);
+    for (int j = 0; j < n.h1; ++j) z += fabs(n.W2[j + n.h1 * k]) * a1[j];
+    a2[k] = 1.0 + z;
+    sv += fabs(n.W3[k]) * a2[k];
+  }
+  /* gradient: |dG| |W1| (|W2| |W3| a2) with every factor on absolute values */
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < n.h1; ++j) {
+      double t = 0.0;
+      for (int k = 0; k < n.h2; ++k) t += fabs(n.W2[j + n.h1 * k]) * fabs(n.W3[k]) * a2[k];
+      w1g[i] += fabs(n.W1[i + 6 * j]) * a1[j] * t;
+    }
+  scale[0] = sv * EV_TO_HARTREE;
+  for (int r = 0; r < 3; ++r) {
+    double lp = fabs(n.lam) * 4.0 * (1.0 + p[r]) * (1.0 + p[r]) * (1.0 + p[r]);
+    double t = 0.0;
+    for (int i = 0; i < 6; ++i) t += lp * w1g[i];
+    scale[1 + r] = t * EV_TO_HARTREE;
+  }
+  for (int i = 0; i < 3; ++i) {
+    double v, dv;
+    orc_diat_VdV(s->diat, R[i], &v, &dv);
+    scale[0] += fabs(v);
+    scale[1 + i] += fabs(dv);
+  }
+}
+
 void orc_pes_compute(const orc_sys* s, int ipes, const double* R, const double* Qall, double* V, double* dVdR,
                      double* dVdQ) {
   const orc_pes* P = &s->pes[ipes];
   if (P->model == ORC_PES_O3_UMN) o3_compute(s, P, R, Qall, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_N3_UMN) n3_compute(s, P, R, Qall, V, dVdR, dVdQ);
-  else o4_compute(s, P, R, Qall, V, dVdR, dVdQ);
+  else if (P->model == ORC_PES_O3_NN) {
+    if (dVdR) o3nn_compute(s, P, R, Qall, V, dVdR, dVdQ);
+    else *V = o3nn_potential(s, P, R);
+  } else o4_compute(s, P, R, Qall, V, dVdR, dVdQ);
 }
 
 double orc_pes_potential(const orc_sys* s, int ipes, const double* R) {

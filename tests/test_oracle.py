@@ -114,6 +114,95 @@ def test_o3_dissociation_limit(oracle_lib):
         assert abs(v - vd) < 1e-10
 
 
+def _o3nn_numpy(coef, R):
+    """Independent numpy restatement of the O3 NN network part (O3_NN_PES_Class.F90): the Compute
+    features and network with its gradient by the chain rule, and the Potential variant (three
+    scaled features, W1's storage read as a 3 x NHL1 matrix by dgemm with leading dimension 3)."""
+    h1, h2 = int(coef[0]), int(coef[1])
+    lam, re_ = coef[2], coef[3]
+    mean, sd, ysc = coef[4:7], coef[7:10], coef[10]
+    q = 11
+    W1f = coef[q:q + 6 * h1]; q += 6 * h1
+    b1 = coef[q:q + h1]; q += h1
+    W2 = coef[q:q + h1 * h2].reshape(h2, h1).T; q += h1 * h2
+    b2 = coef[q:q + h2]; q += h2
+    W3 = coef[q:q + h2]; q += h2
+    b3 = coef[q]
+    W1 = W1f.reshape(h1, 6).T
+    p = np.exp(-lam * (R - re_))
+    p1, p2, p3 = p.T
+    G = np.stack([p1 * p2 + p2 * p3 + p3 * p1, p1 * p2 * p3,
+                  p1 * p1 * p2 + p1 * p2 * p2 + p2 * p2 * p3 + p2 * p3 * p3 + p1 * p1 * p3 + p1 * p3 * p3,
+                  p1 ** 3 * p2 + p1 * p2 ** 3 + p2 ** 3 * p3 + p2 * p3 ** 3 + p1 ** 3 * p3 + p1 * p3 ** 3,
+                  p1 * p2 * p3 * (p1 + p2 + p3),
+                  p1 * p1 * p2 * p2 + p2 * p2 * p3 * p3 + p1 * p1 * p3 * p3], axis=1)
+    y1 = np.tanh(G @ W1 + b1)
+    y2 = np.tanh(y1 @ W2 + b2)
+    V = (y2 @ W3 + b3 - ysc) / 27.2113839712790
+    # chain rule: dV/dG then dG/dp by symbolic partials, dp/dR = -lam p
+    d2 = W3 * (1 - y2 ** 2)
+    d1 = (d2 @ W2.T) * (1 - y1 ** 2)
+    dVdG = d1 @ W1.T
+    dGdp = np.zeros((len(R), 6, 3))
+    P = [p1, p2, p3]
+    for a in range(3):
+        b, c = [x for x in range(3) if x != a]
+        pa, pb, pc = P[a], P[b], P[c]
+        dGdp[:, 0, a] = pb + pc
+        dGdp[:, 1, a] = pb * pc
+        dGdp[:, 2, a] = 2 * pa * (pb + pc) + pb * pb + pc * pc
+        dGdp[:, 3, a] = 3 * pa * pa * (pb + pc) + pb ** 3 + pc ** 3
+        dGdp[:, 4, a] = pb * pc * (2 * pa + pb + pc)
+        dGdp[:, 5, a] = 2 * pa * (pb * pb + pc * pc)
+    dV = np.einsum("ni,nia->na", dVdG, dGdp) * (-lam * p) / 27.2113839712790
+    Gp = np.stack([p1 * p2 + p2 * p3 + p3 * p1, p1 * p2 * p3,
+                   p1 * p2 * (p1 + p2) + p2 * p3 * (p2 + p3) + p3 * p1 * (p3 + p1)], axis=1)
+    Gp = (Gp - mean) / sd
+    W1p = W1f[:3 * h1].reshape(h1, 3).T
+    Vp = (np.tanh(np.tanh(Gp @ W1p + b1) @ W2 + b2) @ W3 + b3 - ysc) / 27.2113839712790
+    return V, dV, Vp
+
+
+def test_o3nn_surface_pins(oracle_lib):
+    """O3 NN: Compute and Potential against an independent numpy restatement, the analytic
+    gradient against finite differences of Compute's energy, permutation invariance."""
+    from oracle import Oracle
+    L = oracle_lib.lib()
+    cfg = systems.o3nn_config()
+    o = Oracle(cfg)
+    rng = np.random.default_rng(11)
+    Q = _random_geometry(rng, 3, 200)
+    R, Qall = o.rp(Q)
+    keep = np.all((R > 1.6) & (R < 8.0), axis=1)
+    R, Qall = R[keep][:40], Qall[keep][:40]
+    V, g, _ = o.compute(R, Qall)
+    Vd = np.array([[L.orc_diat_V(1, r) for r in row] for row in R]).sum(axis=1)
+    dVd = np.zeros_like(R)
+    import ctypes
+    for n, row in enumerate(R):
+        for i, r in enumerate(row):
+            v, dv = ctypes.c_double(), ctypes.c_double()
+            L.orc_diat_VdV(1, r, ctypes.byref(v), ctypes.byref(dv))
+            dVd[n, i] = dv.value
+    Vn, dVn, Vpn = _o3nn_numpy(cfg.surfaces[0].coef, R)
+    assert np.allclose(V, Vn + Vd, rtol=1e-12, atol=1e-13)
+    assert np.allclose(g, dVn + dVd, rtol=1e-10, atol=1e-12)
+    assert np.allclose(o.potential(R), Vpn + Vd, rtol=1e-12, atol=1e-13)
+    # the two energy routines of the reference differ (Potential is not Compute's energy)
+    assert np.max(np.abs(o.potential(R) - V)) > 1e-3
+    h = 1e-4
+    for i in range(3):
+        def f(dx):
+            Rs = R.copy()
+            Rs[:, i] += dx
+            return o.compute(Rs, Qall)[0]
+        fd = (8 * (f(h) - f(-h)) - (f(2 * h) - f(-2 * h))) / (12 * h)
+        assert np.all(np.abs(fd - g[:, i]) < 1e-8 * np.maximum(np.abs(g).max(axis=1), 1e-3))
+    for perm in ([0, 2, 1], [2, 1, 0], [1, 0, 2]):
+        Vp, _, _ = o.compute(R[:, perm], Qall)
+        assert np.allclose(Vp, V, rtol=1e-12, atol=1e-13)
+
+
 def _rand12_bigint(digits):
     """Independent restatement of rand12 (RandomVector_Module.F90:166-229) on base-256 digits."""
     ia = [45, 127, 149, 76, 45, 244, 81, 88]
