@@ -49,6 +49,15 @@ TRAJ_POINT_DTYPE = np.dtype([("ipair0", "i4"), ("itype0", "i4"), ("eint0", "f8")
                              ("angmom1", "f8"), ("viba1", "f8"), ("b", "f8"), ("xkin", "f8"),
                              ("vrel", "f8", (3,)), ("nmol", "i4"), ("pad", "i4")])
 
+class StatsParams(C.Structure):
+    _fields_ = [("qn_max", C.c_int32), ("iskip", C.c_int32 * 3), ("pres_even_odd", C.c_int32 * 3),
+                ("pad", C.c_int32), ("ham_abs_tol", C.c_double), ("xmu", C.c_double)]
+
+
+FINAL_STATE_DTYPE = np.dtype([("item", "i4"), ("fin", "i4", 3), ("ini", "i4", 3), ("pad", "i4"), ("count", "i8"),
+                              ("nrows", "i8"), ("cross", "f8"), ("cross_sd", "f8"), ("rate", "f8"),
+                              ("rate_sd", "f8")])
+
 LEVEL_DTYPE = np.dtype([("vqn", "i4"), ("jqn", "i4"), ("eint", "f8"), ("egam", "f8"), ("rmin", "f8"),
                         ("rmax", "f8"), ("vmin", "f8"), ("vmax", "f8"), ("tau", "f8"), ("ri", "f8"), ("ro", "f8")])
 ITEM_DTYPE = np.dtype([("ilevel", "i4"), ("ipes", "i4"), ("first", "i8"), ("ntraj", "i8"), ("seed", "i8"),
@@ -86,6 +95,12 @@ SIGNATURES = [
     ("cair_flop_model", C.c_int, [_P, C.c_int32, _D, _D, _D, _D]),
     ("cair_last_counters", C.c_int, [_P, _L]),
     ("cair_fp64_peak_probe", C.c_int, [_P, _D]),
+    ("cair_statistics", C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L]),
+    ("cair_statistics_dev", C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L,
+                                      _P]),
+    ("cair_format_rows", C.c_int, [_P, C.c_int64, C.c_int64, C.c_int32, C.c_char_p, C.c_int64, _L]),
+    ("cair_write_trajectories", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_double, _L]),
+    ("cair_write_trajectories_bin", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_double]),
     ("cair_set_integrate_timing", C.c_int, [_P, C.c_int32]),
     ("cair_integrate_timings", C.c_int, [_P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_int32)]),
 ]

@@ -302,7 +302,75 @@ class RunTrajectories:
         return out
 
 
+def _nint(x):
+    """Fortran nint: nearest integer, halves away from zero."""
+    x = np.asarray(x, dtype=np.float64)
+    return (np.sign(x) * np.floor(np.abs(x) + 0.5)).astype(np.int64)
+
+
 def histogram_assign(j, v, arr):
     """Final (J, v, arrangement) integers of the histogram method (Statistics_Class.F90:626-656)."""
-    return (np.rint(np.asarray(j) - 0.5).astype(np.int64), np.rint(np.asarray(v) - 0.5).astype(np.int64),
-            np.rint(np.asarray(arr) - 0.5).astype(np.int64))
+    return _nint(np.asarray(j) - 0.5), _nint(np.asarray(v) - 0.5), _nint(np.asarray(arr) - 0.5)
+
+
+def format_rows(rows, idx_offset=0, header=True):
+    """trajectories.out text of result rows (Integrator_Class.F90:884-933)."""
+    lib = _lib.load()
+    rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+    n = C.c_int64(0)
+    lib.cair_format_rows(rw.ctypes.data, len(rw), int(idx_offset), int(header), None, 0, C.byref(n))
+    buf = C.create_string_buffer(n.value + 1)
+    rc = lib.cair_format_rows(rw.ctypes.data, len(rw), int(idx_offset), int(header), buf, n.value, C.byref(n))
+    if rc != 0:
+        raise CairError("cair_format_rows: %s" % _lib.STATUS.get(rc, rc))
+    return buf.raw[:n.value].decode()
+
+
+def write_trajectories(directory, rows, ham_abs_tol, idx_offset=0, binary=None):
+    """Write trajectories.out and trajectories_HNotCons.out (and trajectories.bin if `binary` is a
+    path); returns (rows in trajectories.out, rows in trajectories_HNotCons.out)."""
+    lib = _lib.load()
+    rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+    cnt = (C.c_int64 * 2)()
+    rc = lib.cair_write_trajectories(str(directory).encode(), rw.ctypes.data, len(rw), int(idx_offset),
+                                     float(ham_abs_tol), cnt)
+    if rc != 0:
+        raise CairError("cair_write_trajectories: %s" % _lib.STATUS.get(rc, rc))
+    if binary is not None:
+        rc = lib.cair_write_trajectories_bin(str(binary).encode(), rw.ctypes.data, len(rw), int(idx_offset),
+                                             float(ham_abs_tol))
+        if rc != 0:
+            raise CairError("cair_write_trajectories_bin: %s" % _lib.STATUS.get(rc, rc))
+    return cnt[0], cnt[1]
+
+
+class Statistics:
+    """TrajectoriesStats for state-specific runs (Statistics_Class.F90, Histogram assignment,
+    conditions J, v, arrangement): final-state cross sections [bohr^2] and rate coefficients
+    [cm^3/s] per work item, counted on the GPU.  Defaults are the reference's (QuantumNumberMax 300)
+    and its N3 input (Iskip 1, even/oddness preserved for J only: pres_even_odd=(1, 0, 0))."""
+
+    def __init__(self, handle, qn_max=300, iskip=(1, 1, 1), pres_even_odd=(0, 0, 0), ham_abs_tol=None, xmu=None):
+        self.H = handle
+        cfg = handle.cfg
+        m = cfg.masses
+        p = _lib.StatsParams()
+        p.qn_max = int(qn_max)
+        for i in range(3):
+            p.iskip[i] = int(iskip[i])
+            p.pres_even_odd[i] = int(bool(pres_even_odd[i]))
+        p.ham_abs_tol = float(cfg.ham_abs_tol if ham_abs_tol is None else ham_abs_tol)
+        # RedMass of the relative translation: diatom (atoms 1, 2) against atom 3
+        p.xmu = float(xmu if xmu is not None else (m[0] + m[1]) * m[2] / (m[0] + m[1] + m[2]))
+        self.params = p
+
+    def compute(self, items, rows, cap=None):
+        H = self.H
+        it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+        rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+        cap = int(cap if cap is not None else max(64, len(rw)))
+        out = np.zeros(cap, dtype=_lib.FINAL_STATE_DTYPE)
+        n = C.c_int64(0)
+        H.check(H.lib.cair_statistics(H.h, len(it), it.ctypes.data, len(rw), rw.ctypes.data, C.byref(self.params),
+                                      out.ctypes.data, cap, C.byref(n)), "cair_statistics")
+        return out[:n.value].copy()

@@ -13,7 +13,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcair_gpu.so")
 
-SOURCES = ["cair_api.cu"]
+# (source, object, extra flags): the API translation unit, and cair_model.cu once per surface
+# model so the per-model kernels compile in parallel
+SOURCES = [("cair_api.cu", "cair_api.o", []), ("cair_output.cpp", "cair_output.o", [])] + [
+    ("cair_model.cu", "cair_model_%s.o" % name, ["-DCAIR_MODEL_ID=%d" % mid])
+    for name, mid in (("o3_umn", 1), ("n3_umn", 2), ("o4_umn", 3), ("o3_nn", 4))]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177",
                      "-I", os.path.join(HERE, "..", "include")]
@@ -37,7 +41,7 @@ def _deps():
     out = []
     for root, _, files in os.walk(CSRC):
         for f in files:
-            if f.endswith((".cu", ".cuh", ".h")):
+            if f.endswith((".cu", ".cuh", ".h", ".cpp")):
                 out.append(os.path.join(root, f))
     out.append(os.path.join(HERE, "..", "include", "cair_gpu.h"))
     return out
@@ -51,9 +55,10 @@ def build(force=False, verbose=False, extra_flags=()):
     cc = nvcc()
     objs = []
 
-    def compile_one(src):
-        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [cc] + NVCC_FLAGS + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
+    def compile_one(entry):
+        src, objname, flags = entry
+        obj = os.path.join(BUILD, objname)
+        cmd = [cc] + NVCC_FLAGS + flags + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s" % (src, r.stderr[-4000:]))

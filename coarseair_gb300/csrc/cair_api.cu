@@ -13,6 +13,11 @@
 #include <vector>
 
 #include "cair_ic.cuh"
+#include "cair_launch.h"
+#include "cair_stats.cuh"
+
+#include <algorithm>
+#include <climits>
 
 using namespace cair;
 
@@ -34,6 +39,8 @@ struct cair_handle {
   unsigned long long* d_ctl = nullptr;   // [0] queue, [1..5] counters
   long long last_counters[5] = {0, 0, 0, 0, 0};
   double watchdog_s = 0.0;
+  void* d_stats = nullptr;                  // statistics table and its compaction
+  size_t stats_bytes = 0;
   bool time_integrate = false;              // bracket every integrator launch with events
   std::vector<cudaEvent_t> tev;             // pairs (start, end), reused across calls
   size_t ntev = 0;                          // pairs recorded since the last read
@@ -162,6 +169,59 @@ int check_launch(cair_handle* h) {
 bool three_atoms(const cair_handle* h) { return h->sys.natoms == 3; }
 
 int model_of(const cair_handle* h) { return h->sys.pes[0].model; }
+
+// Run f(ModelLaunch<model>{}) for the handle's surface model, then check the launch.
+template <class F>
+int with_model(cair_handle* h, F&& f) {
+  switch (model_of(h)) {
+#define CAIR_CASE(M) \
+  case M:            \
+    f(ModelLaunch<M>{}); \
+    break;
+    CAIR_FOR_EACH_MODEL(CAIR_CASE)
+#undef CAIR_CASE
+    default:
+      return fail(h, CAIR_EUNSUPPORTED, "no kernels for this surface model in this library");
+  }
+  return check_launch(h);
+}
+
+// O3 NN: the reference's arrays (Initialize_O3_NN_PES, O3_NN_PES_Class.F90:139-230, packed as the
+// header states) -> the kernels' fixed 20 x 10 layout (CAIR_NN_* offsets in cair_device.cuh),
+// padded with zeros, plus W1's storage as Potential's dgemm reads it: a 3 x NHL1 matrix with
+// leading dimension 3 (O3_NN_PES_Class.F90:281).
+int pack_o3nn(const double* c, int32_t ncoef, std::vector<double>& out) {
+  const double fh1 = c[0], fh2 = c[1];
+  if (!(fh1 >= 1 && fh1 <= CAIR_NN_H1 && fh2 >= 1 && fh2 <= CAIR_NN_H2)) return CAIR_EINVAL;
+  const int h1 = (int)fh1, h2 = (int)fh2;
+  if (h1 != fh1 || h2 != fh2 || ncoef != 12 + 7 * h1 + h1 * h2 + 2 * h2) return CAIR_EINVAL;
+  const double* W1 = c + 11;
+  const double* b1 = W1 + 6 * h1;
+  const double* W2 = b1 + h1;
+  const double* b2 = W2 + h1 * h2;
+  const double* W3 = b2 + h2;
+  const double b3 = W3[h2];
+  out.assign(CAIR_NN_NCOEF, 0.0);
+  out[CAIR_NN_LAM] = c[2];
+  out[CAIR_NN_RE] = c[3];
+  for (int i = 0; i < 3; ++i) {
+    out[CAIR_NN_MEAN + i] = c[4 + i];
+    out[CAIR_NN_SD + i] = c[7 + i];
+  }
+  out[CAIR_NN_YSC] = c[10];
+  out[CAIR_NN_B3] = b3;
+  for (int j = 0; j < h1; ++j) {
+    for (int i = 0; i < 6; ++i) out[CAIR_NN_W1 + i + 6 * j] = W1[i + 6 * j];
+    for (int l = 0; l < 3; ++l) out[CAIR_NN_W1P + l + 3 * j] = W1[l + 3 * j];
+    out[CAIR_NN_B1 + j] = b1[j];
+    for (int k = 0; k < h2; ++k) out[CAIR_NN_W2 + j + CAIR_NN_H1 * k] = W2[j + h1 * k];
+  }
+  for (int k = 0; k < h2; ++k) {
+    out[CAIR_NN_B2 + k] = b2[k];
+    out[CAIR_NN_W3 + k] = W3[k];
+  }
+  return 0;
+}
 
 int check_ipes(cair_handle* h, int64_t n, const int32_t* ipes) {
   if (!ipes) return 0;
@@ -323,20 +383,29 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
   for (int p = 0; p < d->npes; ++p) {
     const cair_pes_desc& src = d->pes[p];
     int expect = src.model == CAIR_PES_O3_UMN ? 56 : src.model == CAIR_PES_N3_UMN ? 276
-                 : src.model == CAIR_PES_O4_UMN ? 430 : -1;
+                 : src.model == CAIR_PES_O4_UMN ? 430 : src.model == CAIR_PES_O3_NN ? 0 : -1;
     if (expect < 0) return bad(CAIR_EINVAL, "unknown surface model");
-    if (src.ncoef != expect || !src.coef) return bad(CAIR_EINVAL, "wrong coefficient count for surface");
+    std::vector<double> packed;
+    if (src.model == CAIR_PES_O3_NN) {
+      if (!src.coef || src.ncoef < 12) return bad(CAIR_EINVAL, "O3 NN: coefficient array too short");
+      if (int e = pack_o3nn(src.coef, src.ncoef, packed)) return bad(e, "O3 NN: hidden layers must be 1..20 and 1..10 "
+                                                                       "neurons and ncoef = 12 + 7 NHL1 + NHL1 NHL2 + 2 NHL2");
+      if (d->natoms != 3) return bad(CAIR_EINVAL, "surface/atom count mismatch");
+    } else if (src.ncoef != expect || !src.coef) {
+      return bad(CAIR_EINVAL, "wrong coefficient count for surface");
+    } else {
+      packed.assign(src.coef, src.coef + src.ncoef);
+    }
     if (src.model != d->pes[0].model) return bad(CAIR_EUNSUPPORTED, "all surfaces of a handle must share a model");
     if ((src.model == CAIR_PES_O4_UMN) != (d->natoms == 4)) return bad(CAIR_EINVAL, "surface/atom count mismatch");
-    if (src.model == CAIR_PES_O4_UMN) return bad(CAIR_EUNSUPPORTED, "O4 UMN kernels are not built in this library");
     DevPes& P = S.pes[p];
     P.model = src.model;
-    P.ncoef = src.ncoef;
+    P.ncoef = (int32_t)packed.size();
     P.a = src.a; P.ab = src.ab; P.ra = src.ra; P.rb = src.rb;
     P.inv_a = (src.a != 0.0) ? 1.0 / src.a : 0.0;
     P.inv_ab = (src.ab != 0.0) ? 1.0 / src.ab : 0.0;
-    if (cudaMalloc(&h->d_coef[p], sizeof(double) * src.ncoef) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
-    if (cudaMemcpy(h->d_coef[p], src.coef, sizeof(double) * src.ncoef, cudaMemcpyHostToDevice) != cudaSuccess)
+    if (cudaMalloc(&h->d_coef[p], sizeof(double) * packed.size()) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
+    if (cudaMemcpy(h->d_coef[p], packed.data(), sizeof(double) * packed.size(), cudaMemcpyHostToDevice) != cudaSuccess)
       return bad(CAIR_ECUDA, "cudaMemcpy coefficients");
     P.coef = h->d_coef[p];
   }
@@ -395,6 +464,7 @@ void cair_destroy(cair_handle* h) {
   if (h->d_scratch) cudaFree(h->d_scratch);
   if (h->d_work) cudaFree(h->d_work);
   if (h->d_ctl) cudaFree(h->d_ctl);
+  if (h->d_stats) cudaFree(h->d_stats);
   if (h->stream) cudaStreamDestroy(h->stream);
   for (cudaEvent_t e : h->tev) cudaEventDestroy(e);
   delete h;
@@ -422,11 +492,10 @@ int cair_pes_eval(cair_handle* h, int64_t n, const int32_t* ipes, const double* 
                   double* dVdR, double* dVdQ) {
   if (!h || n < 0 || !R || !Qall || !V) return fail(h, CAIR_EINVAL, "cair_pes_eval: bad argument");
   if (n == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_pes_eval: 4-atom surfaces not built");
   if (int e = check_ipes(h, n, ipes)) return e;
   bool grad = dVdR != nullptr;
   if (grad && !dVdQ) return fail(h, CAIR_EINVAL, "cair_pes_eval: dVdQ required with dVdR");
-  const int np = 3, na3 = 9, nv = 6;
+  const int np = h->sys.npairs, na3 = 3 * h->sys.natoms, nv = h->sys.nv;
   size_t bytes = n * (sizeof(int32_t) + sizeof(double) * (np + na3 + 1 + np + nv)) + 8 * 256;
   if (int e = ensure_scratch(h, bytes)) return e;
   Carver c{(char*)h->d_scratch};
@@ -437,15 +506,8 @@ int cair_pes_eval(cair_handle* h, int64_t n, const int32_t* ipes, const double* 
   CUDA_TRY(h, cudaMemcpyAsync(d_R, R, n * np * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(d_Q, Qall, n * na3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   int g = grid_for(h, n);
-  int m = model_of(h);
-  if (m == CAIR_PES_O3_UMN) {
-    if (grad) k_pes_eval3<CAIR_PES_O3_UMN, true><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
-    else k_pes_eval3<CAIR_PES_O3_UMN, false><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
-  } else {
-    if (grad) k_pes_eval3<CAIR_PES_N3_UMN, true><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
-    else k_pes_eval3<CAIR_PES_N3_UMN, false><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m);
-  }
-  if (int e = check_launch(h)) return e;
+  if (int e = with_model(h, [&](auto L) { L.pes_eval(grad, g, h->stream, h->sys, n, d_ip, d_R, d_Q, d_V, d_g, d_m); }))
+    return e;
   CUDA_TRY(h, cudaMemcpyAsync(V, d_V, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (grad) {
     CUDA_TRY(h, cudaMemcpyAsync(dVdR, d_g, n * np * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -457,40 +519,36 @@ int cair_pes_eval(cair_handle* h, int64_t n, const int32_t* ipes, const double* 
 int cair_rhs(cair_handle* h, int64_t n, const int32_t* ipes, const double* y, double* yp) {
   if (!h || n < 0 || !y || !yp) return fail(h, CAIR_EINVAL, "cair_rhs: bad argument");
   if (n == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_rhs: 4-atom systems not built");
   if (int e = check_ipes(h, n, ipes)) return e;
-  if (int e = ensure_scratch(h, n * (4 + 24 * 8) + 1024)) return e;
+  const int ne = h->sys.ne;
+  if (int e = ensure_scratch(h, n * (4 + 2 * ne * 8) + 1024)) return e;
   Carver c{(char*)h->d_scratch};
   int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
-  double *d_y = c.take<double>(n * 12), *d_yp = c.take<double>(n * 12);
+  double *d_y = c.take<double>(n * ne), *d_yp = c.take<double>(n * ne);
   if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(d_y, y, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_y, y, n * ne * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   int g = grid_for(h, n);
-  if (model_of(h) == CAIR_PES_O3_UMN) k_rhs3<CAIR_PES_O3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_yp);
-  else k_rhs3<CAIR_PES_N3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_yp);
-  if (int e = check_launch(h)) return e;
-  CUDA_TRY(h, cudaMemcpyAsync(yp, d_yp, n * 12 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (int e = with_model(h, [&](auto L) { L.rhs(g, h->stream, h->sys, n, d_ip, d_y, d_yp); })) return e;
+  CUDA_TRY(h, cudaMemcpyAsync(yp, d_yp, n * ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   return wait_stream(h);
 }
 
 int cair_hamiltonian(cair_handle* h, int64_t n, const int32_t* ipes, const double* paq, double* H, double* Rpi) {
   if (!h || n < 0 || !paq || !H) return fail(h, CAIR_EINVAL, "cair_hamiltonian: bad argument");
   if (n == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_hamiltonian: 4-atom systems not built");
   if (int e = check_ipes(h, n, ipes)) return e;
-  if (int e = ensure_scratch(h, n * (4 + 16 * 8) + 1024)) return e;
+  const int ne = h->sys.ne, np = h->sys.npairs;
+  if (int e = ensure_scratch(h, n * (4 + (ne + 1 + np) * 8) + 1024)) return e;
   Carver c{(char*)h->d_scratch};
   int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
-  double *d_y = c.take<double>(n * 12), *d_H = c.take<double>(n), *d_r = c.take<double>(n * 3);
+  double *d_y = c.take<double>(n * ne), *d_H = c.take<double>(n), *d_r = c.take<double>(n * np);
   if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(d_y, paq, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_y, paq, n * ne * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   int g = grid_for(h, n);
-  if (model_of(h) == CAIR_PES_O3_UMN)
-    k_hamiltonian3<CAIR_PES_O3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_H, d_r);
-  else k_hamiltonian3<CAIR_PES_N3_UMN><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_H, d_r);
-  if (int e = check_launch(h)) return e;
+  if (int e = with_model(h, [&](auto L) { L.hamiltonian(g, h->stream, h->sys, n, d_ip, d_y, d_H, d_r); }))
+    return e;
   CUDA_TRY(h, cudaMemcpyAsync(H, d_H, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  if (Rpi) CUDA_TRY(h, cudaMemcpyAsync(Rpi, d_r, n * 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (Rpi) CUDA_TRY(h, cudaMemcpyAsync(Rpi, d_r, n * np * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   return wait_stream(h);
 }
 
@@ -499,39 +557,33 @@ int cair_bs_steps(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, d
   if (!h || n < 0 || !paq || !t || !dt || !erra || nattempts < 0)
     return fail(h, CAIR_EINVAL, "cair_bs_steps: bad argument");
   if (n == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_bs_steps: 4-atom systems not built");
   if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_bs_steps: only NSteps = 3 is built");
   if (int e = check_ipes(h, n, ipes)) return e;
-  if (int e = ensure_scratch(h, n * (4 + 26 * 8) + 2048)) return e;
+  const int ne = h->sys.ne;
+  if (int e = ensure_scratch(h, n * (4 + (2 * ne + 2) * 8) + 2048)) return e;
   Carver c{(char*)h->d_scratch};
   int32_t* d_ip = ipes ? c.take<int32_t>(n) : nullptr;
-  double *d_y = c.take<double>(n * 12), *d_t = c.take<double>(n), *d_dt = c.take<double>(n),
-         *d_e = c.take<double>(n * 12);
+  double *d_y = c.take<double>(n * ne), *d_t = c.take<double>(n), *d_dt = c.take<double>(n),
+         *d_e = c.take<double>(n * ne);
   if (d_ip) CUDA_TRY(h, cudaMemcpyAsync(d_ip, ipes, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(d_y, paq, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_y, paq, n * ne * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(d_t, t, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(d_dt, dt, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(d_e, erra, n * 12 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(d_e, erra, n * ne * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   int g = grid_for(h, n);
-  if (model_of(h) == CAIR_PES_O3_UMN)
-    k_bs_steps3<CAIR_PES_O3_UMN, 3><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_t, d_dt, d_e, nattempts);
-  else k_bs_steps3<CAIR_PES_N3_UMN, 3><<<g, 128, 0, h->stream>>>(h->sys, n, d_ip, d_y, d_t, d_dt, d_e, nattempts);
-  if (int e = check_launch(h)) return e;
-  CUDA_TRY(h, cudaMemcpyAsync(paq, d_y, n * 12 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (int e = with_model(h, [&](auto L) { L.bs_steps(g, h->stream, h->sys, n, d_ip, d_y, d_t, d_dt, d_e, nattempts); }))
+    return e;
+  CUDA_TRY(h, cudaMemcpyAsync(paq, d_y, n * ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(t, d_t, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(dt, d_dt, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   return wait_stream(h);
 }
 
 static int launch_integrate(cair_handle* h, const IntegrateArgs& A, cudaStream_t st) {
-  int m = model_of(h);
   // 64-thread blocks: a block holding one long trajectory frees the rest of its SM for the
   // next batch on another stream
   int block = 64, per_sm = 0;
-  if (m == CAIR_PES_O3_UMN)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate3<CAIR_PES_O3_UMN, 3>, block, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate3<CAIR_PES_N3_UMN, 3>, block, 0);
+  if (int e = with_model(h, [&](auto L) { per_sm = L.integrate_blocks_per_sm(block); })) return e;
   if (per_sm < 1) per_sm = 1;
   int64_t g = (int64_t)h->nsm * per_sm;
   int64_t need = (A.n + block - 1) / block;
@@ -551,10 +603,9 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A, cudaStream_t
     ++h->ntev;
     CUDA_TRY(h, cudaEventRecord(e0, st));
   }
-  if (m == CAIR_PES_O3_UMN) k_integrate3<CAIR_PES_O3_UMN, 3><<<(int)g, block, 0, st>>>(h->sys, A);
-  else k_integrate3<CAIR_PES_N3_UMN, 3><<<(int)g, block, 0, st>>>(h->sys, A);
+  if (int e = with_model(h, [&](auto L) { L.integrate((int)g, block, st, h->sys, A); })) return e;
   if (e1) CUDA_TRY(h, cudaEventRecord(e1, st));
-  return check_launch(h);
+  return 0;
 }
 
 int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
@@ -564,7 +615,6 @@ int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* p
       max_attempts < 1)
     return fail(h, CAIR_EINVAL, "cair_integrate_dev: bad argument");
   if (n == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: 4-atom systems not built");
   if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: only NSteps = 3 is built");
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
@@ -580,7 +630,7 @@ int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, 
       max_attempts < 1)
     return fail(h, CAIR_EINVAL, "cair_integrate: bad argument");
   if (n == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: 4-atom systems not built");
+  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: only NSteps = 3 is built");
   if (int e = check_ipes(h, n, ipes)) return e;
   const int ne = h->sys.ne;
   size_t bytes = n * (3 * sizeof(int32_t) + sizeof(int32_t) + sizeof(double) * (2 * ne + 5)) + 16 * 256;
@@ -694,13 +744,9 @@ int sample_ics_into(cair_handle* h, int32_t nitems, const cair_work_item* d_item
   k_ic_draws<<<(nitems + 63) / 64, 64, 0, st>>>(nitems, d_items, d_levels, draws, item_of);
   if (int e = check_launch(h)) return e;
   int g = grid_for(h, ntot);
-  if (model_of(h) == CAIR_PES_O3_UMN)
-    k_sample_ic3<CAIR_PES_O3_UMN><<<g, 128, 0, st>>>(h->sys, ntot, d_items, d_levels, draws, item_of, paq, paq0,
-                                                     erra, H0, b, ipes, key);
-  else
-    k_sample_ic3<CAIR_PES_N3_UMN><<<g, 128, 0, st>>>(h->sys, ntot, d_items, d_levels, draws, item_of, paq, paq0,
-                                                     erra, H0, b, ipes, key);
-  return check_launch(h);
+  return with_model(h, [&](auto L) {
+    L.sample_ic(g, st, h->sys, ntot, d_items, d_levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key);
+  });
 }
 
 int validate_items(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
@@ -888,6 +934,17 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
   const double pip_g = m == CAIR_PES_O3_UMN ? PIP_O3_EVAL_REV_FLOPS : PIP_N3_EVAL_REV_FLOPS;
 #endif
   const double pip_e = m == CAIR_PES_O3_UMN ? PIP_O3_VALUE_FLOPS : PIP_N3_VALUE_FLOPS;
+  if (m == CAIR_PES_O3_NN) {
+    // pes_o3nn: MEG-like variables 9, features 41, layer 1 20 x 14, layer 2 and output 10 x 47,
+    // output 6, adjoint sweep 20 x 35, dG/dR contraction 148 (tanh counted as one operation);
+    // the energy-only network (Potential) 9 + 21 + 20 x 7 + 10 x 43 + 4.  Diatomics with gradient
+    // in both (Compute_Vd_dVd).
+    if (fg) *fg = 9 + 3 * diat_g + 41 + 280 + 470 + 6 + 700 + 148 + 36 + 46 + 18 + 15;
+    if (fe) *fe = 9 + 3 * diat_g + 21 + 140 + 430 + 4 + 36 + 30 + 8;
+    if (fa) *fa = 811;
+    if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1) + CAIR_NN_H1 + CAIR_NN_H2;
+    return 0;
+  }
   if (fg) *fg = pip_g + 3 * (diat_g + meg_g) + 36 + 46 + 18 + 15;
   if (fe) *fe = pip_e + 3 * (diat_e + meg_e) + 36 + 30 + 8;
   // per attempt outside the right-hand side: modified-midpoint updates (432), rational
@@ -895,6 +952,136 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
   if (fa) *fa = 811;
   if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1);
   return 0;
+}
+
+int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
+                        const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
+                        int64_t cap, int64_t* nout, void* stream) {
+  if (!h || nitems < 1 || !items || ntot < 0 || (ntot > 0 && !results) || !params || cap < 0 || (cap > 0 && !out) ||
+      !nout)
+    return fail(h, CAIR_EINVAL, "cair_statistics: bad argument");
+  const cair_stats_params& P = *params;
+  if (P.qn_max < 2 || P.qn_max > 1625) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max must be 2..1625");
+  *nout = 0;
+  if (ntot == 0) return 0;
+  // table at least twice the rows, so linear probing always finds a slot
+  unsigned long long tsize = 1024;
+  while (tsize < 2ull * (unsigned long long)ntot) tsize <<= 1;
+  const size_t need = tsize * 16 + (size_t)nitems * 16 + (size_t)(cap > 0 ? cap : 1) * 16 + 4 * 256;
+  if (h->stats_bytes < need) {
+    if (h->d_stats) cudaFree(h->d_stats);
+    h->d_stats = nullptr;
+    h->stats_bytes = 0;
+    CUDA_TRY(h, cudaMalloc(&h->d_stats, need));
+    h->stats_bytes = need;
+  }
+  Carver c{(char*)h->d_stats};
+  unsigned long long* keys = c.take<unsigned long long>(tsize);
+  unsigned long long* counts = c.take<unsigned long long>(tsize);
+  unsigned long long* item_rows = c.take<unsigned long long>(nitems);
+  long long* item_ini = c.take<long long>(nitems);
+  unsigned long long* okeys = c.take<unsigned long long>(cap > 0 ? cap : 1);
+  unsigned long long* ocounts = c.take<unsigned long long>(cap > 0 ? cap : 1);
+  unsigned long long* dn = c.take<unsigned long long>(2);
+  int* derr = (int*)(dn + 1);
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(h, cudaMemsetAsync(keys, 0xff, tsize * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(counts, 0, tsize * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(item_rows, 0, (size_t)nitems * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(item_ini, 0x7f, (size_t)nitems * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(dn, 0, 16, st));
+  StatsArgs A{ntot, results, P.qn_max, {P.iskip[0], P.iskip[1], P.iskip[2]},
+              {P.pres_even_odd[0], P.pres_even_odd[1], P.pres_even_odd[2]}, P.ham_abs_tol, keys, counts, tsize - 1,
+              item_rows, item_ini, derr};
+  k_stats_count<<<grid_for(h, ntot), 256, 0, st>>>(A);
+  k_stats_compact<<<grid_for(h, (int64_t)tsize), 256, 0, st>>>(keys, counts, tsize, okeys, ocounts,
+                                                               (unsigned long long)cap, dn);
+  if (int e = check_launch(h)) return e;
+  unsigned long long n = 0;
+  int err = 0;
+  std::vector<unsigned long long> rows(nitems);
+  std::vector<long long> ini(nitems);
+  CUDA_TRY(h, cudaMemcpyAsync(&n, dn, 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(rows.data(), item_rows, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(ini.data(), item_ini, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (err) return fail(h, CAIR_EINVAL, "cair_statistics: a quantum number is at or above qn_max");
+  if ((long long)n > cap)
+    return fail(h, CAIR_EINVAL, "cair_statistics: cap too small, " + std::to_string(n) + " final states");
+  std::vector<unsigned long long> k(n), cnt(n);
+  if (n) {
+    CUDA_TRY(h, cudaMemcpyAsync(k.data(), okeys, n * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaMemcpyAsync(cnt.data(), ocounts, n * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaStreamSynchronize(st));
+  }
+  std::vector<size_t> ord(n);
+  for (size_t i = 0; i < n; ++i) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return k[a] < k[b]; });
+  const long long qn = P.qn_max, ifacts = qn * qn * qn;
+  // Boltzmann mean velocity (Collision_Class.F90:576-595), per bohr^2 -> cm^3/s
+  const double pi = std::acos(-1.0), k_to_h = 1.0 / 3.1577513e5, bohr_cm = 0.5291771e-8;
+  for (size_t o = 0; o < n; ++o) {
+    const size_t i = ord[o];
+    const int item = (int)(k[i] >> 32);
+    const long long code = (long long)(k[i] & 0xffffffffull);
+    if (item < 0 || item >= nitems) return fail(h, CAIR_EINVAL, "cair_statistics: row with an item out of range");
+    cair_final_state& F = out[o];
+    F.item = item;
+    F.count = (int64_t)cnt[i];
+    F.nrows = (int64_t)rows[item];
+    F.pad = 0;
+    // IniState from the smallest initial code of the item (ProcessStatistics, 782-929)
+    long long isum = ini[item], ifact = ifacts;
+    for (int cnd = 2; cnd >= 0; --cnd) {
+      ifact /= qn;
+      const long long t = isum / ifact;
+      F.ini[cnd] = (int)(t - 2);
+      isum -= t * ifact;
+    }
+    // WriteFinStateProbabilities (1288-1440), one ring
+    const double bmax = items[item].bmax;
+    double area = pi * bmax * bmax;
+    if (area == 0.0) area = 1.0;
+    const double per = (double)(F.nrows > 1 ? F.nrows : 1);
+    const double fw = (double)F.count / per;
+    F.cross = area * fw;
+    F.cross_sd = std::sqrt(fw * (1.0 - fw) * area * area / per);
+    const int ini_arr = F.ini[2] / 16;
+    isum = code;
+    ifact = ifacts;
+    int fin_arr = 0;
+    for (int cnd = 2; cnd >= 0; --cnd) {
+      ifact /= qn;
+      long long fc = isum / ifact;
+      if (cnd == 2) fin_arr = (int)((fc - 2) / 16);
+      isum -= fc * ifact;
+      fc -= 2;
+      if (P.pres_even_odd[cnd] && ini_arr == fin_arr) {
+        fc = fc * 2;
+        if (F.ini[cnd] % 2 != 0) fc = fc + 1;
+      }
+      F.fin[cnd] = (int)fc;
+    }
+    const double vp = std::sqrt(2.0 * items[item].ttra * k_to_h / P.xmu);
+    const double vel = 2.0 / std::sqrt(pi) * vp * 4.134137e16 * (bohr_cm * bohr_cm * bohr_cm);
+    F.rate = F.cross * vel;
+    F.rate_sd = F.cross_sd * vel;
+  }
+  *nout = (int64_t)n;
+  return 0;
+}
+
+int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
+                    const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
+                    int64_t cap, int64_t* nout) {
+  if (!h || ntot < 0 || (ntot > 0 && !results)) return fail(h, CAIR_EINVAL, "cair_statistics: bad argument");
+  if (int e = ensure_scratch(h, (size_t)ntot * sizeof(cair_traj_result) + 256)) return e;
+  if (ntot > 0)
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_scratch, results, (size_t)ntot * sizeof(cair_traj_result),
+                                cudaMemcpyHostToDevice, h->stream));
+  return cair_statistics_dev(h, nitems, items, ntot, (const cair_traj_result*)h->d_scratch, params, out, cap, nout,
+                             h->stream);
 }
 
 int cair_set_integrate_timing(cair_handle* h, int32_t on) {

@@ -160,6 +160,7 @@ __device__ __forceinline__ void diat(const DevSys& S, double r, double& v, doubl
 
 #include "generated/pip_n3.cuh"
 #include "generated/pip_o3.cuh"
+#include "generated/pip_o4.cuh"
 // gradient of the PIP part: reverse mode (adjoint sweep) unless CAIR_PIP_FORWARD selects the
 // forward mode, whose operation order is the reference's
 #ifdef CAIR_PIP_FORWARD
@@ -188,11 +189,11 @@ __device__ __forceinline__ void trans_to_cart_3(const DevSys& S, const double* R
   }
 }
 
-__device__ __forceinline__ void trans_to_cart_4(const DevSys& S, const double* R, const double* Q,
+__device__ __forceinline__ void trans_to_cart_4(const DevSys& S, const double* Ri, const double* Q,
                                                 const double* dVdR, double* m) {
   double d[6];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) d[i] = dVdR[i] / R[i];
+  for (int i = 0; i < 6; ++i) d[i] = dVdR[i] * Ri[i];
   double m1 = S.mMiMn[0], m2 = S.mMiMn[1], m3 = S.mMiMn[2];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -271,10 +272,193 @@ __device__ __forceinline__ void pes_n3(const DevSys& S, const DevPes& P, const d
   }
 }
 
+// tanh from the table-driven exponential: tanh|x| = 1 - 2 / (exp(2|x|) + 1), sign restored.
+// Absolute error within a few ulp of 1 (the relative error grows as |x| -> 0, where the network
+// only needs the absolute value); |x| > 20 returns +-1 (1 - tanh(20) < 2^-113).  Inline, so the
+// network keeps its activations in registers instead of spilling them around library calls.
+__device__ __forceinline__ double ftanh(double x) {
+  const double a = fabs(x);
+  const double t = a > 20.0 ? 1.0 : 1.0 - 2.0 / (fexp(2.0 * a) + 1.0);
+  return copysign(t, x);
+}
+
+// O3 NN (O3_NN_PES_Class.F90).  Device layout of the coefficients, repacked from the reference's
+// arrays at cair_create with the hidden layers zero-padded to 20 and 10 neurons (a padded neuron has
+// z = 0, tanh(z) = 0 and zero outgoing weights, so it adds exact zeros):
+#define CAIR_NN_H1 20
+#define CAIR_NN_H2 10
+#define CAIR_NN_LAM 0      // Lambda
+#define CAIR_NN_RE 1       // re
+#define CAIR_NN_MEAN 2     // Scaling_MEAN(3)
+#define CAIR_NN_SD 5       // Scaling_SD(3)
+#define CAIR_NN_YSC 8      // y_Scaling
+#define CAIR_NN_B3 9       // b3
+#define CAIR_NN_W1 10      // W1(6, 20): [i + 6 j]
+#define CAIR_NN_W1P 130    // W1 storage read as 3 x NHL1 (Potential's dgemm): [l + 3 j]
+#define CAIR_NN_B1 190     // b1(20)
+#define CAIR_NN_W2 210     // W2(20, 10): [j + 20 k]
+#define CAIR_NN_B2 410     // b2(10)
+#define CAIR_NN_W3 420     // W3(10)
+#define CAIR_NN_NCOEF 430
+#define CAIR_EV_TO_HARTREE (1.0 / 27.2113839712790)
+
+// GRAD: Compute_O3_NN_PES_1d (357-477): six features G of p = exp(-Lambda (R - re)), network
+// 6 -> tanh(20) -> tanh(10) -> 1, gradient by one adjoint sweep (dV/dG) contracted with dG/dR
+// (the reference builds dG/dR first and carries the three directions forward).
+// !GRAD: O3_NN_Potential_From_R (250-297): three scaled features on W1's storage read as 3 x NHL1.
+template <bool GRAD>
+__device__ __forceinline__ void pes_o3nn(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
+                                         const double* Q, double& V, double* dVdR, double* dVdQ) {
+  const double* __restrict__ c = P.coef;
+  const double lam = c[CAIR_NN_LAM], re = c[CAIR_NN_RE];
+  double p[3], vd[3], dvd[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    p[i] = fexp(-(lam * (R[i] - re)));
+    diat<true>(S, R[i], vd[i], dvd[i]);  // Compute_Vd_dVd in both routines
+  }
+  const double vdiat = (vd[0] + vd[1]) + vd[2];
+  const double gvp[3] = {p[0] * p[1], p[1] * p[2], p[2] * p[0]};
+  if (GRAD) {
+    const double gvs[3] = {p[1] + p[2], p[2] + p[0], p[0] + p[1]};
+    const double gprod = gvp[0] * p[2];
+    double G[6];
+    G[0] = (gvp[0] + gvp[1]) + gvp[2];
+    G[1] = gprod;
+    const double gc0 = gvp[0] * p[0], gc1 = gvp[0] * p[1], gc2 = gvp[1] * p[1], gc3 = gvp[1] * p[2],
+                 gc4 = gvp[2] * p[0], gc5 = gvp[2] * p[2];
+    G[2] = ((((gc0 + gc1) + gc2) + gc3) + gc4) + gc5;
+    G[3] = ((((gc0 * p[0] + gc1 * p[1]) + gc2 * p[1]) + gc3 * p[2]) + gc4 * p[0]) + gc5 * p[2];
+    G[4] = (gc0 * p[2] + gc2 * p[0]) + gc5 * p[1];
+    G[5] = (gc0 * p[1] + gc2 * p[2]) + gc4 * p[2];
+    // forward
+    double y1[CAIR_NN_H1];
+#pragma unroll
+    for (int j = 0; j < CAIR_NN_H1; ++j) {
+      double z = 0.0;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) z += G[i] * c[CAIR_NN_W1 + i + 6 * j];
+      y1[j] = ftanh(z + c[CAIR_NN_B1 + j]);
+    }
+    double v = 0.0, d2[CAIR_NN_H2];
+#pragma unroll
+    for (int k = 0; k < CAIR_NN_H2; ++k) {
+      double z = 0.0;
+#pragma unroll
+      for (int j = 0; j < CAIR_NN_H1; ++j) z += y1[j] * c[CAIR_NN_W2 + j + CAIR_NN_H1 * k];
+      const double y2 = ftanh(z + c[CAIR_NN_B2 + k]);
+      const double w3 = c[CAIR_NN_W3 + k];
+      v += y2 * w3;
+      d2[k] = w3 * (1.0 - y2 * y2);
+    }
+    v += c[CAIR_NN_B3];
+    V = (v - c[CAIR_NN_YSC]) * CAIR_EV_TO_HARTREE + vdiat;
+    // adjoint sweep: dV/dG
+    double gG[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int j = 0; j < CAIR_NN_H1; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < CAIR_NN_H2; ++k) s += c[CAIR_NN_W2 + j + CAIR_NN_H1 * k] * d2[k];
+      s *= 1.0 - y1[j] * y1[j];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) gG[i] += c[CAIR_NN_W1 + i + 6 * j] * s;
+    }
+    // dG/dR (Compute_O3_NN_PES_1d dG(:,1:6)) contracted with dV/dG
+    const double inv_lam = 1.0 / lam;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const double psq = lam * (p[r] * p[r]), pcu = lam * ((p[r] * p[r]) * p[r]);
+      const int a = (r + 1) % 3, b = (r + 2) % 3;
+      const double psqs = lam * (p[a] * p[a]) + lam * (p[b] * p[b]);
+      const double pcus = lam * ((p[a] * p[a]) * p[a]) + lam * ((p[b] * p[b]) * p[b]);
+      const double gvps = -(lam * (gvp[r] + gvp[(r + 2) % 3]));
+      double t = gvps * gG[0];
+      t += -(lam * gprod) * gG[1];
+      t += -((2.0 * gvs[r]) * psq + p[r] * psqs) * gG[2];
+      t += -((3.0 * gvs[r]) * pcu + p[r] * pcus) * gG[3];
+      t += -((lam * gprod) * (2.0 * p[r] + gvs[r])) * gG[4];
+      t += -(((2.0 * psq) * psqs) * inv_lam) * gG[5];
+      dVdR[r] = t * CAIR_EV_TO_HARTREE + dvd[r];
+    }
+    trans_to_cart_3(S, Ri, Q, dVdR, dVdQ);
+  } else {
+    const double gvs[3] = {p[0] + p[1], p[1] + p[2], p[2] + p[0]};
+    double G[3];
+    G[0] = (gvp[0] + gvp[1]) + gvp[2];
+    G[1] = gvp[0] * p[2];
+    G[2] = (gvp[0] * gvs[0] + gvp[1] * gvs[1]) + gvp[2] * gvs[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) G[i] = (G[i] - c[CAIR_NN_MEAN + i]) / c[CAIR_NN_SD + i];
+    double y1[CAIR_NN_H1];
+#pragma unroll
+    for (int j = 0; j < CAIR_NN_H1; ++j) {
+      double z = c[CAIR_NN_B1 + j];
+#pragma unroll
+      for (int l = 0; l < 3; ++l) z += c[CAIR_NN_W1P + l + 3 * j] * G[l];
+      y1[j] = ftanh(z);
+    }
+    double v = 0.0;
+#pragma unroll
+    for (int k = 0; k < CAIR_NN_H2; ++k) {
+      double z = c[CAIR_NN_B2 + k];
+#pragma unroll
+      for (int j = 0; j < CAIR_NN_H1; ++j) z += c[CAIR_NN_W2 + j + CAIR_NN_H1 * k] * y1[j];
+      v += ftanh(z) * c[CAIR_NN_W3 + k];
+    }
+    v += c[CAIR_NN_B3];
+    V = (v - c[CAIR_NN_YSC]) * CAIR_EV_TO_HARTREE + vdiat;
+  }
+}
+
+// O4 UMN (Compute_O4_UMN_PES_1d, O4_UMN_PES_Class.F90:269-298 -> O4pes 310-370): MEG variables
+// of the six pairs, O4 PIP (430 terms, gradient by the generated adjoint sweep), six O2 diatomics.
+template <bool GRAD>
+__device__ __forceinline__ void pes_o4(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
+                                       const double* Q, double& V, double* dVdR, double* dVdQ) {
+  double x[6], dx[6], vd[6], dvd[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double rang = R[i] * CAIR_B_TO_ANG;
+    double d1 = rang - P.ra, d2 = rang - P.rb;
+    double e = fexp(-(d1 * P.inv_a) - (d2 * d2) * P.inv_ab);
+    x[i] = e;
+    if (GRAD) dx[i] = (-((2.0 * d2) * P.inv_ab) - P.inv_a) * e;
+    diat<GRAD>(S, R[i], vd[i], dvd[i]);
+  }
+  double vdiat = 0.0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) vdiat = vdiat + vd[i];
+  double vp;
+  const double* __restrict__ C = P.coef;
+  if (GRAD) {
+    double g[6];
+    pip_o4_eval_rev(x, dx, C, 0.0, vp, g);
+    V = vp * CAIR_KCM_TO_HARTREE + vdiat;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) dVdR[i] = g[i] * CAIR_KCM_TO_HARTREE * CAIR_B_TO_ANG + dvd[i];
+    trans_to_cart_4(S, Ri, Q, dVdR, dVdQ);
+  } else {
+    pip_o4_value(x, C, 0.0, vp);
+    V = vp * CAIR_KCM_TO_HARTREE + vdiat;
+  }
+}
+
+// Sizes of a surface model's system: atoms, NEqtVar, NEqtTot, pairs
+template <int MODEL>
+struct Traits {
+  static constexpr int NA = MODEL == CAIR_PES_O4_UMN ? 4 : 3;
+  static constexpr int NV = 3 * (NA - 1);
+  static constexpr int NE = 2 * NV;
+  static constexpr int NP = NA * (NA - 1) / 2;
+};
+
 template <int MODEL, bool GRAD>
 __device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
                                     const double* Q, double& V, double* dVdR, double* dVdQ) {
   if (MODEL == CAIR_PES_O3_UMN) pes_o3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
+  else if (MODEL == CAIR_PES_O3_NN) pes_o3nn<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
+  else if (MODEL == CAIR_PES_O4_UMN) pes_o4<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else pes_n3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
 }
 
@@ -296,49 +480,76 @@ __device__ __forceinline__ void rp3(const DevSys& S, double* Q, double* Rp, doub
   s2 = a * a + b * b + c * c; Ri[2] = rsqrt(s2); Rp[2] = s2 * Ri[2];
 }
 
+// Compute_Rp_CartCoord_4Atoms (Collision_Class.F90:2279-2316): pairs 1-2, 1-3, 1-4, 2-3, 2-4, 3-4;
+// the fourth atom is written to Q[9..11].
+__device__ __forceinline__ void rp4(const DevSys& S, double* Q, double* Rp, double* Ri) {
+  const double m1 = S.mMiMn[0], m2 = S.mMiMn[1], m3 = S.mMiMn[2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) Q[9 + c] = m1 * Q[c] + m2 * Q[3 + c] + m3 * Q[6 + c];
+  constexpr int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double a = Q[3 * pa[k]] - Q[3 * pb[k]], b = Q[3 * pa[k] + 1] - Q[3 * pb[k] + 1],
+                 c = Q[3 * pa[k] + 2] - Q[3 * pb[k] + 2];
+    const double s2 = a * a + b * b + c * c;
+    Ri[k] = rsqrt(s2);
+    Rp[k] = s2 * Ri[k];
+  }
+}
+
+template <int NA>
+__device__ __forceinline__ void rp(const DevSys& S, double* Q, double* Rp, double* Ri) {
+  if (NA == 3) rp3(S, Q, Rp, Ri);
+  else rp4(S, Q, Rp, Ri);
+}
+
 // ------------------------------------------------------------------------------------------
-// Hamilton's equations (ODE_System.F90:45-96) for 3 atoms: y = [p(6), q(6)]
+// Hamilton's equations (ODE_System.F90:45-96): y = [p(NV), q(NV)]
 // ------------------------------------------------------------------------------------------
 template <int MODEL>
-struct Rhs3 {
+struct Rhs {
+  using T = Traits<MODEL>;
   const DevSys& S;
   const DevPes& P;
-  __device__ Rhs3(const DevSys& s, const DevPes& p) : S(s), P(p) {}
-  __device__ __forceinline__ void operator()(const double (&y)[12], double (&yp)[12]) const {
+  __device__ Rhs(const DevSys& s, const DevPes& p) : S(s), P(p) {}
+  __device__ __forceinline__ void operator()(const double (&y)[T::NE], double (&yp)[T::NE]) const {
     // dq_j/dt = sum_{i = j mod 3, ascending} Tpq(j,i) p_i
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      int i0 = j % 3;
+    for (int j = 0; j < T::NV; ++j) {
+      const int i0 = j % 3;
       double acc = 0.0 + S.Tpq[j + 9 * i0] * y[i0];
-      acc = acc + S.Tpq[j + 9 * (i0 + 3)] * y[i0 + 3];
-      yp[6 + j] = acc;
-    }
-    double Q[9], R[3], Ri[3], V, dVdR[3], dVdQ[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) Q[i] = y[6 + i];
-    rp3(S, Q, R, Ri);
+      for (int i = i0 + 3; i < T::NV; i += 3) acc = acc + S.Tpq[j + 9 * i] * y[i];
+      yp[T::NV + j] = acc;
+    }
+    double Q[3 * T::NA], R[T::NP], Ri[T::NP], V, dVdR[T::NP], dVdQ[T::NV];
+#pragma unroll
+    for (int i = 0; i < T::NV; ++i) Q[i] = y[T::NV + i];
+    rp<T::NA>(S, Q, R, Ri);
     pes<MODEL, true>(S, P, R, Ri, Q, V, dVdR, dVdQ);
 #pragma unroll
-    for (int i = 0; i < 6; ++i) yp[i] = -dVdQ[i];
+    for (int i = 0; i < T::NV; ++i) yp[i] = -dVdQ[i];
   }
 };
 
-// Hamiltonian_1d (Collision_Class.F90:2046-2111) for 3 atoms; returns H, fills Rpi
+// Hamiltonian_1d (Collision_Class.F90:2046-2111); returns H, fills Rpi
 template <int MODEL>
-__device__ __forceinline__ double hamiltonian3(const DevSys& S, const DevPes& P, const double (&y)[12],
-                                               double (&Rpi)[3]) {
+__device__ __forceinline__ double hamiltonian(const DevSys& S, const DevPes& P, const double (&y)[Traits<MODEL>::NE],
+                                              double (&Rpi)[Traits<MODEL>::NP]) {
+  using T = Traits<MODEL>;
   double h = 0.0;
 #pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    int j0 = i % 3;
+  for (int i = 0; i < T::NV; ++i) {
+    const int j0 = i % 3;
     double eki = 0.0 + S.Tpq[j0 + 9 * i] * y[j0];
-    eki = eki + S.Tpq[j0 + 3 + 9 * i] * y[j0 + 3];
+#pragma unroll
+    for (int j = j0 + 3; j < T::NV; j += 3) eki = eki + S.Tpq[j + 9 * i] * y[j];
     h = h + y[i] * eki;
   }
-  double Q[9], R[3], V;
+  double Q[3 * T::NA], R[T::NP], V;
 #pragma unroll
-  for (int i = 0; i < 6; ++i) Q[i] = y[6 + i];
-  rp3(S, Q, R, Rpi);
+  for (int i = 0; i < T::NV; ++i) Q[i] = y[T::NV + i];
+  rp<T::NA>(S, Q, R, Rpi);
   pes<MODEL, false>(S, P, R, Rpi, Q, V, nullptr, nullptr);
   return h * 0.5 + V;
 }

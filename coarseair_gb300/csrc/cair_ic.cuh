@@ -42,6 +42,7 @@ struct Stream {
 
 constexpr int kDraws = 6;  // vibphase, rA, rB, rC, rEr, rb
 
+#ifndef CAIR_MODEL_TU  // model-independent: built once, in the API translation unit
 __global__ void k_ic_draws(int nitems, const cair_work_item* __restrict__ items,
                            const cair_level* __restrict__ levels, double* __restrict__ draws,
                            int32_t* __restrict__ item_of) {
@@ -73,6 +74,7 @@ __global__ void k_ic_draws(int nitems, const cair_work_item* __restrict__ items,
     item_of[g] = it;
   }
 }
+#endif
 
 // BondLength (StateInitDiatomAtom_Module.F90:543-730): FuncRHS of the radial motion
 struct RadialRhs {
@@ -87,7 +89,7 @@ struct RadialRhs {
   }
 };
 
-__device__ double boltzmann_er(double ttra, double randnum) {
+static __device__ double boltzmann_er(double ttra, double randnum) {
   const double kelvin_to_hartree = 1.0 / 3.1577513E+05;
   double betai = ttra * kelvin_to_hartree, er = 1.0;
   randnum = randnum - 1.0;
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(128) k_sample_ic3(DevSys S, int64_t ntot, cons
     for (int ip = 0; ip < 6; ++ip)
       for (int i = 0; i < 6; ++i) y[i] = y[i] + S.Tqp[ip + 9 * i] * dq[ip];
     double rpi[3];
-    const double h0 = hamiltonian3<MODEL>(S, S.pes[W.ipes], y, rpi);
+    const double h0 = hamiltonian<MODEL>(S, S.pes[W.ipes], y, rpi);
     // SetErrorFactor: both halves from the momenta
     double ep = 0.0, eq = 0.0;
     for (int i = 0; i < 6; ++i) { ep = ep + y[i] * y[i]; eq = eq + y[i] * y[i]; }
@@ -203,6 +205,7 @@ __global__ void __launch_bounds__(128) k_sample_ic3(DevSys S, int64_t ntot, cons
 }
 
 // Analyse the initial and final points of each trajectory and assemble its output row.
+#ifndef CAIR_MODEL_TU  // model-independent: built once, in the API translation unit
 __global__ void __launch_bounds__(128) k_results3(DevSys S, FsArgs F, int64_t n, const double* __restrict__ paq0,
                                                   const double* __restrict__ paq, const double* __restrict__ H0,
                                                   const double* __restrict__ H, const double* __restrict__ t,
@@ -246,5 +249,6 @@ __global__ void __launch_bounds__(128) k_results3(DevSys S, FsArgs F, int64_t n,
     out[k] = r;
   }
 }
+#endif
 
 }  // namespace cair

@@ -7,78 +7,82 @@
 namespace cair {
 
 // ------------------------------------------------------------------------------------------
-// Batched PES%Compute / PES%Potential (3 atoms)
+// Batched PES%Compute / PES%Potential.  R[n][NP], Qall[n][3 NA], dVdR[n][NP], dVdQ[n][NV].
 // ------------------------------------------------------------------------------------------
 template <int MODEL, bool GRAD>
-__global__ void __launch_bounds__(128) k_pes_eval3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
-                                                   const double* __restrict__ Rin, const double* __restrict__ Qin,
-                                                   double* __restrict__ V, double* __restrict__ dVdR,
-                                                   double* __restrict__ dVdQ) {
+__global__ void __launch_bounds__(128) k_pes_eval(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                                  const double* __restrict__ Rin, const double* __restrict__ Qin,
+                                                  double* __restrict__ V, double* __restrict__ dVdR,
+                                                  double* __restrict__ dVdQ) {
+  using T = Traits<MODEL>;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     const DevPes& P = S.pes[ipes ? ipes[k] : 0];
-    double R[3], Ri[3], Q[9], v, g[3], m[6];
+    double R[T::NP], Ri[T::NP], Q[3 * T::NA], v, g[T::NP], m[T::NV];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) { R[i] = Rin[3 * k + i]; Ri[i] = 1.0 / R[i]; }
+    for (int i = 0; i < T::NP; ++i) { R[i] = Rin[T::NP * k + i]; Ri[i] = 1.0 / R[i]; }
 #pragma unroll
-    for (int i = 0; i < 9; ++i) Q[i] = Qin[9 * k + i];
+    for (int i = 0; i < 3 * T::NA; ++i) Q[i] = Qin[3 * T::NA * k + i];
     pes<MODEL, GRAD>(S, P, R, Ri, Q, v, g, m);
     V[k] = v;
     if (GRAD) {
 #pragma unroll
-      for (int i = 0; i < 3; ++i) dVdR[3 * k + i] = g[i];
+      for (int i = 0; i < T::NP; ++i) dVdR[T::NP * k + i] = g[i];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) dVdQ[6 * k + i] = m[i];
+      for (int i = 0; i < T::NV; ++i) dVdQ[T::NV * k + i] = m[i];
     }
   }
 }
 
 template <int MODEL>
-__global__ void __launch_bounds__(128) k_rhs3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
-                                              const double* __restrict__ y, double* __restrict__ yp) {
+__global__ void __launch_bounds__(128) k_rhs(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                             const double* __restrict__ y, double* __restrict__ yp) {
+  constexpr int NE = Traits<MODEL>::NE;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    Rhs3<MODEL> f(S, S.pes[ipes ? ipes[k] : 0]);
-    double a[12], b[12];
+    Rhs<MODEL> f(S, S.pes[ipes ? ipes[k] : 0]);
+    double a[NE], b[NE];
 #pragma unroll
-    for (int i = 0; i < 12; ++i) a[i] = y[12 * k + i];
+    for (int i = 0; i < NE; ++i) a[i] = y[NE * k + i];
     f(a, b);
 #pragma unroll
-    for (int i = 0; i < 12; ++i) yp[12 * k + i] = b[i];
+    for (int i = 0; i < NE; ++i) yp[NE * k + i] = b[i];
   }
 }
 
 template <int MODEL>
-__global__ void __launch_bounds__(128) k_hamiltonian3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
-                                                      const double* __restrict__ paq, double* __restrict__ H,
-                                                      double* __restrict__ Rpi) {
+__global__ void __launch_bounds__(128) k_hamiltonian(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                                     const double* __restrict__ paq, double* __restrict__ H,
+                                                     double* __restrict__ Rpi) {
+  using T = Traits<MODEL>;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    double y[12], r[3];
+    double y[T::NE], r[T::NP];
 #pragma unroll
-    for (int i = 0; i < 12; ++i) y[i] = paq[12 * k + i];
-    H[k] = hamiltonian3<MODEL>(S, S.pes[ipes ? ipes[k] : 0], y, r);
+    for (int i = 0; i < T::NE; ++i) y[i] = paq[T::NE * k + i];
+    H[k] = hamiltonian<MODEL>(S, S.pes[ipes ? ipes[k] : 0], y, r);
     if (Rpi) {
 #pragma unroll
-      for (int i = 0; i < 3; ++i) Rpi[3 * k + i] = r[i];
+      for (int i = 0; i < T::NP; ++i) Rpi[T::NP * k + i] = r[i];
     }
   }
 }
 
 template <int MODEL, int NS>
-__global__ void __launch_bounds__(128) k_bs_steps3(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
-                                                   double* __restrict__ paq, double* __restrict__ t,
-                                                   double* __restrict__ dt, const double* __restrict__ erra,
-                                                   int32_t nattempts) {
+__global__ void __launch_bounds__(128) k_bs_steps(DevSys S, int64_t n, const int32_t* __restrict__ ipes,
+                                                  double* __restrict__ paq, double* __restrict__ t,
+                                                  double* __restrict__ dt, const double* __restrict__ erra,
+                                                  int32_t nattempts) {
+  constexpr int NE = Traits<MODEL>::NE;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    Rhs3<MODEL> f(S, S.pes[ipes ? ipes[k] : 0]);
-    double y[12];
+    Rhs<MODEL> f(S, S.pes[ipes ? ipes[k] : 0]);
+    double y[NE];
 #pragma unroll
-    for (int i = 0; i < 12; ++i) y[i] = paq[12 * k + i];
+    for (int i = 0; i < NE; ++i) y[i] = paq[NE * k + i];
     double x = t[k], h = dt[k], smax = 0.0, smin = 0.0;
     int irej = 0, iste = 0;
 #pragma unroll 1
     for (int a = 0; a < nattempts; ++a)
-      bs_attempt<12, NS>(f, y, x, h, erra + 12 * k, S.relax, S.incstp != 0, smax, smin, irej, iste);
+      bs_attempt<NE, NS>(f, y, x, h, erra + NE * k, S.relax, S.incstp != 0, smax, smin, irej, iste);
 #pragma unroll
-    for (int i = 0; i < 12; ++i) paq[12 * k + i] = y[i];
+    for (int i = 0; i < NE; ++i) paq[NE * k + i] = y[i];
     t[k] = x;
     dt[k] = h;
   }
@@ -111,7 +115,8 @@ struct IntegrateArgs {
 };
 
 template <int MODEL, int NS>
-__global__ void __launch_bounds__(64) k_integrate3(DevSys S, IntegrateArgs A) {
+__global__ void __launch_bounds__(64) k_integrate(DevSys S, IntegrateArgs A) {
+  constexpr int NE = Traits<MODEL>::NE, NP = Traits<MODEL>::NP;
   unsigned long long c_att = 0, c_acc = 0, c_rej = 0;
   const bool incstp = S.incstp != 0;
   const int ncall = S.ncall;
@@ -122,7 +127,7 @@ __global__ void __launch_bounds__(64) k_integrate3(DevSys S, IntegrateArgs A) {
   bool active = false;
   int ip = 0, irej = 0, iste = 0, irej0 = 0, iste0 = 0;
   int64_t att = 0;
-  double y[12], x = 0.0, h = 0.0, smax = 0.0, smin = 0.0, H = 0.0;
+  double y[NE], x = 0.0, h = 0.0, smax = 0.0, smin = 0.0, H = 0.0;
   auto take = [&]() {
     const unsigned long long q = atomicAdd(A.queue, 1ull);
     active = q < (unsigned long long)A.n;
@@ -130,7 +135,7 @@ __global__ void __launch_bounds__(64) k_integrate3(DevSys S, IntegrateArgs A) {
     k = A.order ? (unsigned long long)A.order[q] : q;
     ip = A.ipes ? A.ipes[k] : 0;
 #pragma unroll
-    for (int i = 0; i < 12; ++i) y[i] = A.paq[12 * k + i];
+    for (int i = 0; i < NE; ++i) y[i] = A.paq[NE * k + i];
     x = A.t[k]; h = A.dt[k]; smax = A.smax[k]; smin = A.smin[k]; H = 0.0;
     irej = irej0 = A.irej[k];
     iste = iste0 = A.iste[k];
@@ -142,20 +147,20 @@ __global__ void __launch_bounds__(64) k_integrate3(DevSys S, IntegrateArgs A) {
     if (!__any_sync(0xffffffffu, active)) break;
     if (active) {
       const DevPes& P = S.pes[ip];
-      Rhs3<MODEL> f(S, P);
+      Rhs<MODEL> f(S, P);
       int bad = 0;
 #pragma unroll 1
       for (int c = 0; c < ncall; ++c)
-        bad |= bs_attempt<12, NS>(f, y, x, h, A.erra + 12 * k, S.relax, incstp, smax, smin, irej, iste);
+        bad |= bs_attempt<NE, NS>(f, y, x, h, A.erra + NE * k, S.relax, incstp, smax, smin, irej, iste);
       att += ncall;
-      double rpi[3];
-      H = hamiltonian3<MODEL>(S, P, y, rpi);
+      double rpi[NP];
+      H = hamiltonian<MODEL>(S, P, y, rpi);
       bool conv = x > S.tmax;
 #pragma unroll
-      for (int p = 0; p < 3; ++p) conv = conv || (rpi[p] < S.rpimax);
+      for (int p = 0; p < NP; ++p) conv = conv || (rpi[p] < S.rpimax);
       if (bad || conv || att >= A.max_attempts) {
 #pragma unroll
-        for (int i = 0; i < 12; ++i) A.paq[12 * k + i] = y[i];
+        for (int i = 0; i < NE; ++i) A.paq[NE * k + i] = y[i];
         A.t[k] = x;
         A.dt[k] = h;
         A.H[k] = H;
@@ -182,6 +187,7 @@ __global__ void __launch_bounds__(64) k_integrate3(DevSys S, IntegrateArgs A) {
 }
 
 // ApplyTransformation (Collision_Class.F90:2406-2432), any NEqtVar
+#ifndef CAIR_MODEL_TU  // model-independent: built once, in the API translation unit
 __global__ void k_apply_transformation(DevSys S, int64_t n, const double* __restrict__ paq,
                                        double* __restrict__ out) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
@@ -194,6 +200,7 @@ __global__ void k_apply_transformation(DevSys S, int64_t n, const double* __rest
     }
   }
 }
+#endif
 
 // ------------------------------------------------------------------------------------------
 // Final-state analysis (TrajectoryPoint_Class.F90:128-495, MolecularState_Class.F90:61-429,
@@ -216,7 +223,7 @@ __device__ __forceinline__ double eff_pot(const DevSys& S, double r, double vc_r
   return diat_v(S, r) + vc_r2 / (r * r);
 }
 
-__device__ int turning_point(const DevSys& S, double ra, double rc, double vc_r2, double eint, int nbis, int nnew,
+static __device__ int turning_point(const DevSys& S, double ra, double rc, double vc_r2, double eint, int nbis, int nnew,
                              double& rt_out) {
   double rt = 0.0;
   if (nbis > 0) {
@@ -242,7 +249,7 @@ __device__ int turning_point(const DevSys& S, double ra, double rc, double vc_r2
   return 0;
 }
 
-__device__ double action_integral(const DevSys& S, const FsArgs& F, double ri, double ro, double vc_r2,
+static __device__ double action_integral(const DevSys& S, const FsArgs& F, double ri, double ro, double vc_r2,
                                   double eint, double twomu) {
   const int n = F.nquad;
   double rm = (ro - ri) * 0.5;
@@ -257,7 +264,7 @@ __device__ double action_integral(const DevSys& S, const FsArgs& F, double ri, d
   return 2.0 * sqrt(twomu) * act * rm;
 }
 
-__device__ int find_extremum(const DevSys& S, double sig, double re, double rlim, double vc_r2, double tol,
+static __device__ int find_extremum(const DevSys& S, double sig, double re, double rlim, double vc_r2, double tol,
                              double& rout, double& vout) {
   const double factor = 0.3819660115, step = 0.005;
   double vlast = eff_pot(S, re, vc_r2) * sig;
@@ -288,7 +295,7 @@ __device__ int find_extremum(const DevSys& S, double sig, double re, double rlim
   return 0;
 }
 
-__device__ double gamma_fct(double y) {
+static __device__ double gamma_fct(double y) {
   double sum = -1.963510026021423 * y;
   if (y == 0.0) return sum;
   for (int it = 0; it <= 1000000; ++it) {
@@ -300,7 +307,7 @@ __device__ double gamma_fct(double y) {
   return sum;
 }
 
-__device__ void find_state(const DevSys& S, const FsArgs& F, int ipair, int ia, int ib, const double* X,
+static __device__ void find_state(const DevSys& S, const FsArgs& F, int ipair, int ia, int ib, const double* X,
                            const double* XD, cair_mol_state& m) {
   const double PI = 3.141592653589793;
   double xma = F.mass[ia], xmb = F.mass[ib];
@@ -396,7 +403,7 @@ __device__ void find_state(const DevSys& S, const FsArgs& F, int ipair, int ia, 
 }
 
 // Analyze for 3 atoms (the atom-diatom systems); p = velocities + coordinates
-__device__ void analyze3(const DevSys& S, const FsArgs& F, const double* __restrict__ p, cair_traj_point& o) {
+static __device__ void analyze3(const DevSys& S, const FsArgs& F, const double* __restrict__ p, cair_traj_point& o) {
   double xx[3][3], xd[3][3];
   for (int a = 0; a < 2; ++a)
     for (int d = 0; d < 3; ++d) { xd[d][a] = p[d + 3 * a]; xx[d][a] = p[d + 3 * a + 6]; }
@@ -453,6 +460,7 @@ __device__ void analyze3(const DevSys& S, const FsArgs& F, const double* __restr
   o.mol[1].ipair = 0; o.mol[1].itype = 0; o.mol[1].eint = 0.0; o.mol[1].angmom = 0.0; o.mol[1].viba = 0.0;
 }
 
+#ifndef CAIR_MODEL_TU  // model-independent: built once, in the API translation unit
 __global__ void __launch_bounds__(128) k_find_state3(DevSys S, FsArgs F, int64_t n, const double* __restrict__ paq,
                                                      cair_traj_point* __restrict__ out) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
@@ -461,5 +469,6 @@ __global__ void __launch_bounds__(128) k_find_state3(DevSys S, FsArgs F, int64_t
     out[k] = o;
   }
 }
+#endif
 
 }  // namespace cair

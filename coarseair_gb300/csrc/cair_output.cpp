@@ -1,0 +1,141 @@
+// trajectories.out / trajectories_HNotCons.out / trajectories.bin writers (host code).
+//
+// Rows follow Integrator_Class.F90:884-933 for three atoms, format
+//   (I10, A, I5, 2(A, ES11.5), *(A, ES14.8))
+// with iTraj = IdxOverall, iPES 1-based, bmax, b_i, j_i, v_i, arr_i, j_f, v_f, arr_f.  Fortran's
+// formatted output is reproduced field by field: a value wider than its field prints as asterisks
+// (so a negative number in ES14.8 is fourteen '*'), a three-digit exponent drops the 'E', NaN and
+// Infinity are right-justified words.  The binary file is the stream that
+// Statistics_Class.F90:283-314 writes and ReadInputsUnformatted (346-506) reads: NTraj, then per
+// row Idx, iPES, bMax, bSampled, Qini(3), Qfin(3) as 8-byte integers and reals.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/cair_gpu.h"
+
+namespace {
+
+void put_int(std::string& s, long long v, int w) {
+  char b[32];
+  int n = std::snprintf(b, sizeof b, "%lld", v);
+  if (n > w) s.append((size_t)w, '*');
+  else s.append((size_t)(w - n), ' ').append(b, (size_t)n);
+}
+
+// Fortran ESw.d: one nonzero digit, d decimals, exponent E+dd (or +ddd without the E)
+void put_es(std::string& s, double x, int w, int d) {
+  char b[64];
+  int n;
+  if (std::isnan(x)) n = std::snprintf(b, sizeof b, "NaN");
+  else if (std::isinf(x)) n = std::snprintf(b, sizeof b, x > 0 ? (w >= 8 ? "Infinity" : "Inf") : (w >= 9 ? "-Infinity" : "-Inf"));
+  else {
+    n = std::snprintf(b, sizeof b, "%.*E", d, x);
+    char* e = std::strchr(b, 'E');
+    if (e) {
+      int ex = std::atoi(e + 1);
+      if (ex > 99 || ex < -99) {  // three exponent digits: drop the E
+        std::memmove(e, e + 1, std::strlen(e + 1) + 1);
+        n -= 1;
+      }
+    }
+  }
+  if (n > w) s.append((size_t)w, '*');
+  else s.append((size_t)(w - n), ' ').append(b, (size_t)n);
+}
+
+void format_row(std::string& s, const cair_traj_result& r, int64_t idx_offset) {
+  put_int(s, idx_offset + r.idx, 10);
+  s += ',';
+  put_int(s, (long long)r.ipes + 1, 5);
+  s += ',';
+  put_es(s, r.bmax, 11, 5);
+  s += ',';
+  put_es(s, r.b, 11, 5);
+  const double v[6] = {r.j_i, r.v_i, r.arr_i, r.j_f, r.v_f, r.arr_f};
+  for (double x : v) {
+    s += ',';
+    put_es(s, x, 14, 8);
+  }
+  s += '\n';
+}
+
+const char* kHeader =
+    "#    iTraj, iPES,       bmax,        b_i,           j_i,           v_i,         arr_i,           j_f,"
+    "           v_f,         arr_f\n";
+
+bool conserved(const cair_traj_result& r, double tol) {
+  return r.status == CAIR_TRAJ_DONE && std::fabs(r.dH) <= tol;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cair_format_rows(const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t with_header, char* buf,
+                     int64_t cap, int64_t* len) {
+  if (n < 0 || (n > 0 && !rows) || !len || cap < 0 || (cap > 0 && !buf)) return CAIR_EINVAL;
+  std::string s;
+  if (with_header) s += kHeader;
+  for (int64_t k = 0; k < n; ++k) format_row(s, rows[k], idx_offset);
+  *len = (int64_t)s.size();
+  if ((int64_t)s.size() > cap) return CAIR_EINVAL;
+  std::memcpy(buf, s.data(), s.size());
+  return 0;
+}
+
+int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
+                            double ham_abs_tol, int64_t* counts) {
+  if (!dir || n < 0 || (n > 0 && !rows)) return CAIR_EINVAL;
+  const std::string d(dir);
+  FILE* f[2] = {std::fopen((d + "/trajectories.out").c_str(), "w"),
+                std::fopen((d + "/trajectories_HNotCons.out").c_str(), "w")};
+  if (!f[0] || !f[1]) {
+    for (FILE* x : f)
+      if (x) std::fclose(x);
+    return CAIR_EINVAL;
+  }
+  int64_t c[2] = {0, 0};
+  std::string s[2] = {kHeader, kHeader};
+  bool ok = true;
+  for (int64_t k = 0; k < n; ++k) {
+    const int which = conserved(rows[k], ham_abs_tol) ? 0 : 1;
+    format_row(s[which], rows[k], idx_offset);
+    ++c[which];
+    if (s[which].size() > (1u << 20)) {
+      ok = ok && std::fwrite(s[which].data(), 1, s[which].size(), f[which]) == s[which].size();
+      s[which].clear();
+    }
+  }
+  for (int i = 0; i < 2; ++i) {
+    ok = ok && std::fwrite(s[i].data(), 1, s[i].size(), f[i]) == s[i].size();
+    ok = (std::fclose(f[i]) == 0) && ok;
+  }
+  if (counts) {
+    counts[0] = c[0];
+    counts[1] = c[1];
+  }
+  return ok ? 0 : CAIR_EINVAL;
+}
+
+int cair_write_trajectories_bin(const char* path, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
+                                double ham_abs_tol) {
+  if (!path || n < 0 || (n > 0 && !rows)) return CAIR_EINVAL;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return CAIR_EINVAL;
+  int64_t nt = 0;
+  for (int64_t k = 0; k < n; ++k) nt += conserved(rows[k], ham_abs_tol) ? 1 : 0;
+  bool ok = std::fwrite(&nt, 8, 1, f) == 1;
+  for (int64_t k = 0; k < n && ok; ++k) {
+    const cair_traj_result& r = rows[k];
+    if (!conserved(r, ham_abs_tol)) continue;
+    const int64_t ii[2] = {idx_offset + r.idx, (int64_t)r.ipes + 1};
+    const double dd[8] = {r.bmax, r.b, r.j_i, r.v_i, r.arr_i, r.j_f, r.v_f, r.arr_f};
+    ok = std::fwrite(ii, 8, 2, f) == 2 && std::fwrite(dd, 8, 8, f) == 8;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? 0 : CAIR_EINVAL;
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+// Final-state statistics on the device (app/TrajectoriesStats/Statistics_Class.F90, Histogram
+// assignment, three conditions J, v, arrangement): each finished trajectory's row is turned into
+// its initial- and final-state codes where it lies in HBM, and the rows are counted per
+// (work item, final state) in an open-addressing table, so the cross sections need only the table
+// back on the host instead of the million trajectories.out rows.
+#pragma once
+#include "cair_device.cuh"
+
+namespace cair {
+
+struct StatsArgs {
+  int64_t ntot;
+  const cair_traj_result* rows;
+  int32_t qnmax;
+  int32_t iskip[3];
+  int32_t pres[3];
+  double ham_abs_tol;
+  unsigned long long* keys;       // table: (item << 32) | final-state code, ~0 = empty
+  unsigned long long* counts;
+  unsigned long long mask;        // table size - 1 (a power of two)
+  unsigned long long* item_rows;  // rows of each item in the statistics (TrajsPerb)
+  long long* item_inicode;        // smallest initial-state code of each item (IniStateCode(1))
+  int* error;                     // set to 1: a quantum number at or above qnmax
+};
+
+constexpr unsigned long long kStatsEmpty = ~0ull;
+
+// IdentifyInitialStates (Statistics_Class.F90:591-680) for one row and the final-state code of
+// AddFinState's Histogram branch (935-1282).  Fortran nint rounds half away from zero (llround);
+// Fortran mod takes the sign of the dividend, as C's % does.
+__device__ __forceinline__ void stats_codes(const StatsArgs& A, const cair_traj_result& r, long long& ini_code,
+                                            long long& fin_code, bool& bad) {
+  double qi[3] = {r.j_i, r.v_i, r.arr_i}, qf[3] = {r.j_f, r.v_f, r.arr_f};
+  const long long qnmax = A.qnmax;
+  const int ipair_ini = (int)((qi[2] - 0.49) / 16);
+  const int ipair_fin = (int)((qf[2] - 0.49) / 16);
+  long long ifact = 1, isum = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    qi[c] = qi[c] - 0.5;
+    long long ini = llround(qi[c]);
+    if (ini >= qnmax) bad = true;
+    const double fin_raw = qf[c];
+    qf[c] = qf[c] - 0.5;
+    if (A.pres[c] && ipair_ini == ipair_fin) {
+      if (ini % 2 == 1) {
+        qf[c] = qf[c] - 1.0;
+        if (llround(qf[c] * 0.5) < 0 && fin_raw > 0.0) qf[c] = qf[c] + 2.0;
+      }
+      qf[c] = qf[c] * 0.5;
+    }
+    ini = ini + 2;
+    isum = isum + (A.iskip[c] != 0 ? ini : 2) * ifact;
+    ifact = ifact * qnmax;
+  }
+  ini_code = isum;
+  long long fsum = 0;
+  ifact = 1;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    long long iquse = llround(qf[c]) * A.iskip[c];
+    if (iquse + 2 > qnmax) iquse = 0;
+    if (A.iskip[c] != 0 || c == 2) fsum = fsum + (iquse + 2) * ifact;
+    ifact = ifact * qnmax;
+  }
+  fin_code = fsum;
+}
+
+__device__ __forceinline__ unsigned long long stats_hash(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+#ifndef CAIR_MODEL_TU
+// Rows that enter the statistics: finished trajectories whose energy is conserved (the others go
+// to trajectories_HNotCons.out, Integrator_Class.F90:755-776, 884-888).
+__global__ void __launch_bounds__(256) k_stats_count(StatsArgs A) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < A.ntot; k += (int64_t)gridDim.x * blockDim.x) {
+    const cair_traj_result r = A.rows[k];
+    if (r.status != CAIR_TRAJ_DONE || !(fabs(r.dH) <= A.ham_abs_tol)) continue;
+    long long ic, fc;
+    bool bad = false;
+    stats_codes(A, r, ic, fc, bad);
+    if (bad) atomicExch(A.error, 1);
+    atomicAdd(A.item_rows + r.item, 1ull);
+    atomicMin(A.item_inicode + r.item, ic);
+    // fc < qnmax^3 < 2^32 (qnmax <= 1625 is checked on the host)
+    const unsigned long long key = ((unsigned long long)(uint32_t)r.item << 32) | (unsigned long long)fc;
+    unsigned long long h = stats_hash(key) & A.mask;
+    for (unsigned long long probe = 0; probe <= A.mask; ++probe) {  // the table is at least twice the rows
+      const unsigned long long old = atomicCAS(A.keys + h, kStatsEmpty, key);
+      if (old == kStatsEmpty || old == key) {
+        atomicAdd(A.counts + h, 1ull);
+        break;
+      }
+      h = (h + 1) & A.mask;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_stats_compact(const unsigned long long* keys, const unsigned long long* counts,
+                                                       unsigned long long size, unsigned long long* out_keys,
+                                                       unsigned long long* out_counts, unsigned long long cap,
+                                                       unsigned long long* nout) {
+  for (unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; s < size;
+       s += (unsigned long long)gridDim.x * blockDim.x) {
+    if (keys[s] == kStatsEmpty) continue;
+    const unsigned long long i = atomicAdd(nout, 1ull);
+    if (i < cap) {
+      out_keys[i] = keys[s];
+      out_counts[i] = counts[s];
+    }
+  }
+}
+#endif
+
+}  // namespace cair

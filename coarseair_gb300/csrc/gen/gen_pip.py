@@ -601,6 +601,16 @@ def main():
     info = emit_device_reverse(S, "O3", "pip_o3_eval_rev", zero_vars=set(), dirs=[0, 1, 2],
                                path=os.path.join(gen, "pip_o3.cuh"), coeff_symbol="C")
     print("O3 reverse:", info)
+    # O4 on its own PIP (six MEG variables, all live): energy and adjoint-sweep gradient only
+    o4 = os.path.join(gen, "pip_o4.cuh")
+    with open(o4, "w") as f:
+        f.write("/* O4 UMN PIP (O4_UMN_PES_Class.F90 EvMono/EvPoly/evbas). Generated by gen_pip.py, do not edit. */\n")
+    info = emit_device(S, "O4", "pip_o4_value", zero_vars=set(), dirs=[], path=o4, coeff_symbol="C",
+                       value_only=True)
+    print("O4 value:", info)
+    info = emit_device_reverse(S, "O4", "pip_o4_eval_rev", zero_vars=set(), dirs=[0, 1, 2, 3, 4, 5], path=o4,
+                               coeff_symbol="C")
+    print("O4 reverse:", info)
     with open(os.path.join(REPO, "coarseair_gb300", "data", "N3_UMN.dat"), "w") as f:
         f.write("# N3 UMN surface (N4 PIP, MEG variables): 276 linear coefficients [kcal/mol]\n")
         f.write("# a = 1.0 Ang, ab = 1.5 Ang^2, re = 1.098 Ang, totdiss = 457.4 kcal/mol\n")

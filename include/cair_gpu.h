@@ -50,7 +50,8 @@ extern "C" {
 enum cair_pes_model {
   CAIR_PES_O3_UMN = 1, /* O3_UMN_PES_Class.F90  (System O3, Model UMN_*)            */
   CAIR_PES_N3_UMN = 2, /* N3_UMN_PES_Class.F90  (System N3, Model UMN)              */
-  CAIR_PES_O4_UMN = 3  /* O4_UMN_PES_Class.F90  (System O4, Model UMN_Singlet/...)  */
+  CAIR_PES_O4_UMN = 3, /* O4_UMN_PES_Class.F90  (System O4, Model UMN_Singlet/...)  */
+  CAIR_PES_O3_NN = 4   /* O3_NN_PES_Class.F90   (System O3, Model NN_*)             */
 };
 
 /* Diatomic potentials of the pairs (DiatomicPotential_Factory_Class.F90:115-229). */
@@ -77,10 +78,15 @@ enum cair_traj_status {
 
 /* One surface: linear coefficients and MEG parameters.  Replaces the data a
  * PES%Initialize reads (O3_UMN_PES_Class.F90:67-135, O4_UMN_PES_Class.F90:118-210;
- * the N3 coefficients are inline in N3_UMN_PES_Class.F90:108-201). */
+ * the N3 coefficients are inline in N3_UMN_PES_Class.F90:108-201).
+ * CAIR_PES_O3_NN packs what Initialize_O3_NN_PES reads (O3_NN_PES_Class.F90:74-232) into coef:
+ *   NHL1, NHL2, Lambda, re, Scaling_MEAN(3), Scaling_SD(3), y_Scaling, W1(6,NHL1), b1(NHL1),
+ *   W2(NHL1,NHL2), b2(NHL2), W3(NHL2), b3
+ * (matrices column-major as in Fortran), ncoef = 12 + 7 NHL1 + NHL1 NHL2 + 2 NHL2; the kernels
+ * hold NHL1 <= 20, NHL2 <= 10.  The MEG fields are unused. */
 typedef struct cair_pes_desc {
   int32_t model;       /* cair_pes_model                                      */
-  int32_t ncoef;       /* 56 (O3), 276 (N3), 430 (O4)                         */
+  int32_t ncoef;       /* 56 (O3), 276 (N3), 430 (O4), see above (O3 NN)       */
   const double* coef;  /* C(1:ncoef) [kcal/mol], copied at cair_create        */
   double a, ab, ra, rb;/* MEG parameters [Ang, Ang^2, Ang, Ang] (O3, O4)      */
   double eref;         /* O4 file value (unused by the energy, as in the reference) */
@@ -268,6 +274,61 @@ int64_t cair_queue_workspace_bytes(int64_t ntot);
 int cair_run_queue_static_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
                               const cair_work_item* items, int64_t ntot, int64_t max_attempts,
                               cair_traj_result* results, void* stream);
+
+/* Final-state statistics of state-specific runs (app/TrajectoriesStats/Statistics_Class.F90,
+ * "Final States Assigment Mthd = Histogram", three conditions J, v, arrangement, no identical
+ * diatoms) and rate coefficients (Process_Class.F90:122-209 with the Boltzmann mean velocity of
+ * Collision_Class.F90:576-595).  Each work item is one run; its rows are the finished trajectories
+ * whose |dH| <= ham_abs_tol (the rest are the HNotCons rows).  One impact-parameter ring per item. */
+typedef struct cair_stats_params {
+  int32_t qn_max;            /* QuantumNumberMax (300 in the reference), at most 1625          */
+  int32_t iskip[3];          /* "Iskip for Condition 1..3"                                      */
+  int32_t pres_even_odd[3];  /* "Preserving Even / Oddness of Condition 1..3?" (0/1)           */
+  int32_t pad;
+  double ham_abs_tol;        /* "Tolerance on Hamiltonian" [Eh]                                 */
+  double xmu;                /* reduced mass of the relative translation [a.u.] (RedMass)      */
+} cair_stats_params;
+
+/* One line of the statistics output (FinCondVec, IniState, Cross, CrossSD) plus its rate. */
+typedef struct cair_final_state {
+  int32_t item;              /* work item                                                       */
+  int32_t fin[3];            /* FinCondVec: J, v, arrangement code                              */
+  int32_t ini[3];            /* IniState                                                        */
+  int32_t pad;
+  int64_t count;             /* rows that ended in this state                                   */
+  int64_t nrows;             /* rows of the item in the statistics (TrajsPerb)                  */
+  double cross, cross_sd;    /* [bohr^2]                                                        */
+  double rate, rate_sd;      /* cross sections x mean velocity [cm^3/s]                         */
+} cair_final_state;
+
+/* Statistics of `ntot` result rows already on the device (as cair_run_queue_dev leaves them),
+ * counted on the GPU; the final states (at most `cap`, sorted by item then final-state code) and
+ * their count come back to host memory.  Returns CAIR_EINVAL with the needed size in the message
+ * when cap is too small.  `items` is the host copy of the work items. */
+int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
+                        const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
+                        int64_t cap, int64_t* nout, void* stream);
+/* The same from host rows. */
+int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
+                    const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
+                    int64_t cap, int64_t* nout);
+
+/* trajectories.out rows (Integrator_Class.F90:884-933, three atoms): format
+ * (I10, ',', I5, 2(',', ES11.5), 6(',', ES14.8)) with iTraj = idx_offset + idx, iPES 1-based,
+ * bmax, b_i, j_i, v_i, arr_i, j_f, v_f, arr_f; Fortran field overflow prints asterisks.  Host code,
+ * no handle or GPU needed.  cair_format_rows fills buf (not NUL-terminated) and sets *len; it
+ * returns CAIR_EINVAL with *len = the size needed when cap is too small. */
+int cair_format_rows(const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t with_header, char* buf,
+                     int64_t cap, int64_t* len);
+/* <dir>/trajectories.out (finished rows with |dH| <= ham_abs_tol) and <dir>/trajectories_HNotCons.out
+ * (the rest: energy not conserved, and the attempt-capped or non-finite rows, where the reference
+ * stops with an error), each with the reference's header line; counts[0..1] = rows written. */
+int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
+                            double ham_abs_tol, int64_t* counts);
+/* trajectories.bin: the stream Statistics_Class.F90:283-314 writes (NTraj, then per row Idx, iPES,
+ * bMax, bSampled, Qini(3), Qfin(3); 8-byte integers and reals) for the trajectories.out rows. */
+int cair_write_trajectories_bin(const char* path, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
+                                double ham_abs_tol);
 
 /* Algorithmic FP64 operation counts the library's kernels execute per PES energy+gradient
  * evaluation, per energy-only evaluation and per BS attempt (excluding the PES), for

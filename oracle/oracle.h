@@ -63,6 +63,7 @@ int  orc_sys_init(orc_sys* s);   /* fills neqtvar/neqttot/npairs, mMiMn, Tqp, Tp
 /* ---- diatomic potentials ---- */
 double orc_diat_V(int model, double r);
 void   orc_diat_VdV(int model, double r, double* v, double* dv);
+void   orc_diat_scale(int model, double r, double* sv, double* sdv);   /* rounding-level scales */
 
 /* ---- surfaces: V [Eh], dVdR [Eh/bohr], dVdQ (+dV/dq of the NAtoms-1 free atoms) ---- */
 void   orc_pes_compute(const orc_sys* s, int ipes, const double* R, const double* Qall,
@@ -144,6 +145,12 @@ int    orc_turning_point(int diat, double ra, double rc, double vc_r2, double ei
 double orc_action_integral(int diat, double ri, double ro, double vc_r2, double eint, int n, double twomu);
 int    orc_find_extremum(int diat, double sig, double r0, double rlim, double vc_r2, double tol,
                          double* rout, double* vout);
+
+/* ---- statistics of one state-specific run (Histogram assignment) ---- */
+int    orc_statistics(int nrows, int ncond, const int* iskip, const int* pres, int qnmax, const double* bmax,
+                      const double* bsamp, const double* qini, const double* qfin, int cap, long long* codes,
+                      int* fincond, int* inistate, long long* counts, double* cross, double* cross_sd);
+double orc_mean_velocity(double ttra, double xmu);
 
 /* ---- constants ---- */
 double orc_const(const char* name);

@@ -83,6 +83,11 @@ def lib():
         L.orc_pip_eval.argtypes = [C.c_int, _D, _D, C.c_int, _D, C.c_double, _D, _D]
         L.orc_pes_scale.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D]
         L.orc_rp.argtypes = [C.POINTER(OrcSys), _D, _D, _D]
+        _I64 = C.POINTER(C.c_int64)
+        L.orc_statistics.argtypes = [C.c_int, C.c_int, _I, _I, C.c_int, _D, _D, _D, _D, C.c_int, _I64, _I, _I, _I64,
+                                     _D, _D]
+        L.orc_mean_velocity.argtypes = [C.c_double, C.c_double]
+        L.orc_mean_velocity.restype = C.c_double
         L.orc_rhs.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D]
         L.orc_hamiltonian.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D, _D]
         L.orc_bs_attempts.argtypes = [C.POINTER(OrcSys), C.c_int, _I, _D, _D, _D, _D, C.c_int]
@@ -165,10 +170,10 @@ class Oracle:
         return V, g, m
 
     def condition_scale(self, R, ipes=None):
-        """Magnitudes of the terms summed into V (column 0) and dV/dR_i (columns 1..3): the scale at
+        """Magnitudes of the terms summed into V (column 0) and dV/dR_i (columns 1..NPairs): the scale at
         which a different evaluation order of the same surface changes the result."""
         R = np.ascontiguousarray(R, np.float64).reshape(-1, self.npairs)
-        out = np.zeros((R.shape[0], 4))
+        out = np.zeros((R.shape[0], 1 + self.npairs))
         for k in range(R.shape[0]):
             self.L.orc_pes_scale(C.byref(self.s), 0 if ipes is None else int(ipes[k]), dp(R[k]), dp(out[k]))
         return out
@@ -221,7 +226,18 @@ class Oracle:
         self.L.orc_bs_attempts(C.byref(self.s), n, ip(ipe), dp(paq), dp(t), dp(dt), dp(erra), int(nattempts))
         return paq, t, dt
 
-    def integrate(self, paq, erra, dt0=None, ipes=None, max_attempts=None):
+    def integrate(self, paq, erra, dt0=None, ipes=None, max_attempts=None, procs=1):
+        """orc_integrate over a batch; procs > 1 splits it over that many spawned processes
+        (trajectories are independent, so the result is the same)."""
+        n = np.shape(paq)[0]
+        if procs > 1 and n >= 2 * procs:
+            import multiprocessing as mp
+            parts = np.array_split(np.arange(n), procs)
+            args = [(self.cfg, np.asarray(paq)[ix], np.asarray(erra)[ix], dt0,
+                     None if ipes is None else np.asarray(ipes)[ix], max_attempts) for ix in parts]
+            with mp.get_context("spawn").Pool(procs) as pool:
+                outs = pool.starmap(_integrate_part, args)
+            return {k: np.concatenate([o[k] for o in outs]) for k in outs[0]}
         paq = np.ascontiguousarray(paq, np.float64).copy()
         n = paq.shape[0]
         t = np.zeros(n)
@@ -270,3 +286,37 @@ class Oracle:
                             ipair1=p.mol[1].ipair, itype1=p.mol[1].itype, angmom1=p.mol[1].angmom,
                             viba1=p.mol[1].viba))
         return out
+
+
+def _integrate_part(cfg, paq, erra, dt0, ipes, max_attempts):
+    return Oracle(cfg).integrate(paq, erra, dt0=dt0, ipes=ipes, max_attempts=max_attempts)
+
+
+def statistics(bmax, bsamp, qini, qfin, iskip=(1, 1, 1), pres=(0, 0, 0), qnmax=300, cap=4096):
+    """orc_statistics for the rows of one run: list of (fincond tuple, count, cross, cross_sd) in order
+    of first appearance, and IniState."""
+    L = lib()
+    n = len(bmax)
+    qini = np.ascontiguousarray(qini, np.float64).reshape(n, -1)
+    qfin = np.ascontiguousarray(qfin, np.float64).reshape(n, -1)
+    ncond = qini.shape[1]
+    sk = np.ascontiguousarray(iskip, np.int32)
+    pr = np.ascontiguousarray([int(bool(x)) for x in pres], np.int32)
+    codes = np.zeros(cap, np.int64)
+    fin = np.zeros(cap * ncond, np.int32)
+    ini = np.zeros(ncond, np.int32)
+    counts = np.zeros(cap, np.int64)
+    cross, sd = np.zeros(cap), np.zeros(cap)
+    nfs = L.orc_statistics(n, ncond, ip(sk), ip(pr), int(qnmax), dp(np.ascontiguousarray(bmax, np.float64)),
+                           dp(np.ascontiguousarray(bsamp, np.float64)), dp(qini), dp(qfin), cap,
+                           codes.ctypes.data_as(C.POINTER(C.c_int64)), ip(fin), ip(ini),
+                           counts.ctypes.data_as(C.POINTER(C.c_int64)), dp(cross), dp(sd))
+    if nfs < 0:
+        raise ValueError("orc_statistics failed (%d)" % nfs)
+    fin = fin.reshape(cap, ncond)
+    return [(tuple(int(x) for x in fin[i]), int(counts[i]), float(cross[i]), float(sd[i])) for i in range(nfs)], \
+        tuple(int(x) for x in ini)
+
+
+def mean_velocity(ttra, xmu):
+    return lib().orc_mean_velocity(float(ttra), float(xmu))

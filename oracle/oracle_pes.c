@@ -129,6 +129,36 @@ void orc_diat_VdV(int model, double r, double* v, double* dv) {
   }
 }
 
+/* Rounding-level scales of a diatomic evaluation at r [bohr]: the same sums on absolute values
+ * (O2 UMN: the eight Gaussian terms cancel to ~1e-3 of their sum; N2: De (1-u)^2 - De cancels at
+ * large r), for V [Eh] and dV/dr [Eh/bohr]. */
+void orc_diat_scale(int model, double r, double* sv, double* sdv) {
+  double rang = r * B_TO_ANG;
+  if (model == ORC_DIAT_O2_UMN) {
+    double a = 0.0, d = 0.0;
+    for (int k = 0; k <= 7; ++k) {
+      double ab = O2_ALPHA * powi_gf(O2_BETA, k);
+      double e = exp(-(ab * (rang * rang)));
+      a += fabs(O2_A[k]) * e;
+      d += 2.0 * fabs(O2_A[k]) * ab * rang * e * (1.0 + ab * rang * rang);
+    }
+    double rb = rang / B_TO_ANG, e6, e8, e6dr, e8dr;
+    o2_edisp(rb, &e6, &e8, &e6dr, &e8dr);
+    *sv = a * 1.e-3 + e6 + 2.0 * e8;
+    *sdv = (d * 1.e-3) * B_TO_ANG + fabs(e6dr) + 2.0 * fabs(e8dr);
+  } else {
+    double r3 = (rang * rang) * rang, r4 = r3 * rang, ts = r4 + N2_RED4;
+    double y = (r4 - N2_RED4) / ts, fa = 0.0, fy = 0.0, yi = 1.0, dfa = 0.0, yj = 1.0;
+    for (int i = 0; i < 7; ++i) { fa += fabs(N2_CS[i]) * fabs(yi); fy += N2_CS[i] * yi; yi *= y; }
+    for (int i = 1; i < 7; ++i) { dfa += i * fabs(N2_CS[i]) * fabs(yj); yj *= y; }
+    double dydr = 8.0 * r3 * N2_RED4 / (ts * ts);
+    double u = exp(-(fy * (rang - N2_RED))), minu = 1.0 - u, dr = fabs(rang - N2_RED);
+    double arg = fa * dr * (1.0 + fabs(fy * (rang - N2_RED)));   /* error of u is u times this (relative) */
+    *sv = (N2_DE * (minu * minu) + N2_DE + 2.0 * N2_DE * fabs(minu) * u * arg) * KCM_TO_HARTREE;
+    *sdv = 2.0 * N2_DE * (fabs(minu) + u) * u * (dfa * dydr * dr + fa) * (1.0 + arg) * KCM_TO_HARTREE * B_TO_ANG;
+  }
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* Generic PIP evaluator over the generated tables.  Follows EvMono/EvPoly/evbas and the      */
 /* forward-mode EvdMdR/EvdPdr/evdbdr of N3_UMN_PES_Class.F90:677-2053 (same structure in      */
@@ -265,6 +295,22 @@ void orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale) {
     o3nn_scale(s, P, R, scale);
     return;
   }
+  if (P->model == ORC_PES_O4_UMN) {   /* scale[0] for V, scale[1..6] for the six pairs */
+    for (int i = 0; i < 6; ++i) {
+      double r = R[i] * B_TO_ANG, d1 = r - P->ra, d2 = r - P->rb;
+      double e = exp(-(d1 / P->a) - (d2 * d2) / P->ab);
+      rms[i] = e; dms[i] = (-(2.0 * d2 / P->ab) - 1.0 / P->a) * e;
+    }
+    orc_pip_scale(2, rms, dms, P->coef, sc);
+    scale[0] = sc[0] * KCM_TO_HARTREE;
+    for (int i = 0; i < 6; ++i) {
+      double sv, sdv;
+      orc_diat_scale(s->diat, R[i], &sv, &sdv);
+      scale[0] += sv;
+      scale[1 + i] = sc[1 + i] * KCM_TO_HARTREE * B_TO_ANG + sdv;
+    }
+    return;
+  }
   if (P->model == ORC_PES_O3_UMN) {
     for (int i = 0; i < 3; ++i) {
       double r = R[i] * B_TO_ANG, d1 = r - P->ra, d2 = r - P->rb;
@@ -287,10 +333,10 @@ void orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale) {
     scale[3] = sc[4] * KCM_TO_HARTREE * B_TO_ANG;
   }
   for (int i = 0; i < 3; ++i) {
-    double v, dv;
-    orc_diat_VdV(s->diat, R[i], &v, &dv);
-    scale[0] += fabs(v);
-    scale[1 + i] += fabs(dv);
+    double sv, sdv;
+    orc_diat_scale(s->diat, R[i], &sv, &sdv);
+    scale[0] += sv;
+    scale[1 + i] += sdv;
   }
 }
 
@@ -582,10 +628,10 @@ static void o3nn_scale(const orc_sys* s, const orc_pes* P, const double* R, doub
     scale[1 + r] = t * EV_TO_HARTREE;
   }
   for (int i = 0; i < 3; ++i) {
-    double v, dv;
-    orc_diat_VdV(s->diat, R[i], &v, &dv);
-    scale[0] += fabs(v);
-    scale[1 + i] += fabs(dv);
+    double sv, sdv;
+    orc_diat_scale(s->diat, R[i], &sv, &sdv);
+    scale[0] += sv;
+    scale[1 + i] += sdv;
   }
 }
 

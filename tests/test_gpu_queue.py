@@ -1,5 +1,7 @@
 """GPU tests of the device initial-condition sampler and the end-to-end queue path (cair_run_queue)
 against the oracle on the same work items."""
+import os
+
 import numpy as np
 import pytest
 
@@ -72,7 +74,7 @@ def test_run_queue_matches_oracle_path(gpu_lib, oracle_lib, name):
     same_f, same_i = [], []
     for i, (il, _, nt, seed, T, bmax, dinit) in enumerate(entries):
         ref = o.sample_ics(nt, _oracle_levels(rows[il:il + 1]), seed=seed, ttra=T, bmax=bmax, dinit=dinit)
-        out = o.integrate(ref["paq"], ref["erra"])
+        out = o.integrate(ref["paq"], ref["erra"], procs=min(16, os.cpu_count() or 1))
         fi = o.analyze(ref["paq0"])
         ff = o.analyze(o.apply_transformation(out["paq"]))
         sl = slice(int(items["first"][i]), int(items["first"][i] + nt))

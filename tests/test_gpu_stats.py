@@ -1,0 +1,84 @@
+"""GPU statistics (cair_statistics: final-state counts on the device, cross sections and rates)
+against the oracle's restatement of Statistics_Class.F90 on the same rows: identical final states
+and counts, cross sections and their standard deviations to 1e-14 relative, rates = cross
+sections x the Boltzmann mean velocity."""
+import numpy as np
+import pytest
+
+from coarseair_gb300 import _lib, api, systems
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(H, items, rows, pres, st):
+    import oracle
+    cfg = H.cfg
+    m = cfg.masses
+    xmu = (m[0] + m[1]) * m[2] / sum(m)
+    got = st.compute(items, rows)
+    keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= cfg.ham_abs_tol)
+    for i, it in enumerate(items):
+        sel = keep & (rows["item"] == i)
+        ref, ini = oracle.statistics(np.full(sel.sum(), it["bmax"]), rows["b"][sel],
+                                     np.stack([rows["j_i"][sel], rows["v_i"][sel], rows["arr_i"][sel]], 1),
+                                     np.stack([rows["j_f"][sel], rows["v_f"][sel], rows["arr_f"][sel]], 1),
+                                     pres=pres)
+        g = got[got["item"] == i]
+        assert len(g) == len(ref)
+        gd = {tuple(int(x) for x in r["fin"]): r for r in g}
+        vel = oracle.mean_velocity(it["ttra"], xmu)
+        for fs, n, cross, sd in ref:
+            r = gd[fs]
+            assert tuple(int(x) for x in r["ini"]) == ini
+            assert r["count"] == n and r["nrows"] == sel.sum()
+            assert r["cross"] == pytest.approx(cross, rel=1e-14)
+            assert r["cross_sd"] == pytest.approx(sd, rel=1e-14, abs=1e-300)
+            assert r["rate"] == pytest.approx(cross * vel, rel=1e-13)
+            assert r["rate_sd"] == pytest.approx(sd * vel, rel=1e-13, abs=1e-300)
+    return got
+
+
+def test_statistics_of_a_queue_run(gpu_lib, oracle_lib):
+    cfg = systems.n3_config(rmax=16.0)
+    H = api.Handle(cfg)
+    lv = systems.load_levels("N2")
+    table = api.level_table(lv[[5, 300, 2000]])
+    items = api.work_items([(0, 0, 400, api.process_seed(7, 1), 10000.0, 7.0, 15.0),
+                            (1, 0, 300, api.process_seed(7, 2), 20000.0, 7.0, 15.0),
+                            (2, 0, 300, api.process_seed(7, 3), 5000.0, 7.0, 15.0)])
+    rows = api.RunTrajectories(H).run(table, items)
+    got = _compare(H, items, rows, (1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 0)))
+    # every counted row is in exactly one final state
+    for i in range(len(items)):
+        g = got[got["item"] == i]
+        assert g["count"].sum() == g["nrows"][0]
+    H.close()
+
+
+def test_statistics_on_synthetic_rows(gpu_lib, oracle_lib):
+    """100k rows over 5 items with scattered continuous quantum numbers (many final states,
+    arrangement changes, dissociated rows, a few HNotCons and capped rows)."""
+    cfg = systems.o3_config()
+    H = api.Handle(cfg)
+    rng = np.random.default_rng(21)
+    n, nitems = 100000, 5
+    rows = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    rows["item"] = rng.integers(0, nitems, n)
+    rows["j_i"] = 10.5 + 2.0 * rows["item"]
+    rows["v_i"] = 0.5 + rows["item"] % 2
+    rows["arr_i"] = 16.5
+    rows["j_f"] = rng.uniform(0.0, 60.0, n)
+    rows["v_f"] = rng.uniform(-1.5, 12.0, n)
+    rows["arr_f"] = rng.choice([16.5, 17.5, 18.5, 32.5, 48.5], n)
+    rows["b"] = rng.uniform(0.0, 6.0, n)
+    rows["status"] = np.where(rng.uniform(size=n) < 0.01, 1, 0)
+    rows["dH"] = np.where(rng.uniform(size=n) < 0.01, 1.0, 1e-9)
+    items = np.zeros(nitems, dtype=_lib.ITEM_DTYPE)
+    items["bmax"] = 6.0
+    items["ttra"] = [5000.0, 10000.0, 15000.0, 20000.0, 8000.0]
+    _compare(H, items, rows, (1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 0)))
+    _compare(H, items, rows, (0, 0, 0), api.Statistics(H))
+    # a table that cannot hold every final state is an error, not a truncation
+    with pytest.raises(api.CairError, match="cap too small"):
+        api.Statistics(H).compute(items, rows, cap=8)
+    H.close()

@@ -318,3 +318,27 @@ def test_integration_conserves_energy(oracle_lib):
     res = o.integrate(ic["paq"], ic["erra"])
     assert np.all(res["status"] == 0)
     assert np.max(np.abs(res["H"] - ic["H0"])) < cfg.ham_abs_tol
+
+
+def test_statistics_known_answers(oracle_lib):
+    """Histogram statistics of six hand-made rows (Statistics_Class.F90): J folded by even/oddness
+    within the initial arrangement, arrangement change, dissociated v < 0; Cross = pi bmax^2 n/N,
+    CrossSD = sqrt(w (1 - w) A^2 / N); Boltzmann mean velocity in cm^3/s per bohr^2."""
+    import oracle
+    qini = np.array([[10.5, 0.5, 16.5]] * 6)
+    qfin = np.array([[10.5, 0.5, 16.5], [12.4, 0.6, 16.5], [11.6, 1.2, 16.5], [8.5, 0.5, 32.5],
+                     [20.0, -1.0, 18.5], [10.5, 0.5, 16.5]])
+    res, ini = oracle.statistics(np.full(6, 7.0), np.linspace(1, 6, 6), qini, qfin, pres=(1, 0, 0))
+    assert ini == (10, 0, 16)
+    got = {r[0]: r[1:] for r in res}
+    assert set(got) == {(10, 0, 16), (12, 0, 16), (12, 1, 16), (8, 0, 32), (20, -2, 18)}
+    area = np.pi * 49.0
+    for fs, (n, cross, sd) in got.items():
+        w = n / 6.0
+        assert n == (2 if fs == (10, 0, 16) else 1)
+        assert cross == pytest.approx(area * w, rel=1e-15)
+        assert sd == pytest.approx(np.sqrt(w * (1 - w) * area * area / 6.0), rel=1e-15)
+    xmu = 1822.888486209 * 14.0067 * 2 / 3
+    vp = np.sqrt(2 * 10000.0 / 3.1577513e5 / xmu)
+    assert oracle.mean_velocity(10000.0, xmu) == pytest.approx(2 / np.sqrt(np.pi) * vp * 4.134137e16 * 0.5291771e-8 ** 3,
+                                                               rel=1e-14)

@@ -1,0 +1,56 @@
+"""trajectories.out / trajectories_HNotCons.out / trajectories.bin writers (host code in the
+library; no GPU).  Expected rows are written out by hand from the reference's format
+(I10, A, I5, 2(A, ES11.5), *(A, ES14.8)) (Integrator_Class.F90:933) and Fortran's edit-descriptor
+rules: a field too narrow for its value prints as asterisks, a three-digit exponent drops the E."""
+import numpy as np
+
+from coarseair_gb300 import _lib, api
+
+HEADER = ("#    iTraj, iPES,       bmax,        b_i,           j_i,           v_i,         arr_i,           j_f,"
+          "           v_f,         arr_f\n")
+
+
+def _rows():
+    r = np.zeros(4, dtype=_lib.RESULT_DTYPE)
+    r["idx"] = [7, 8, 9, 10]
+    r["ipes"] = [0, 2, 0, 0]
+    r["bmax"] = 7.0
+    r["b"] = [3.25, 0.0, 6.999999999, 1.0e100]
+    r["j_i"], r["v_i"], r["arr_i"] = 10.5, 0.5, 16.5
+    r["j_f"] = [11.49, 2.0, np.nan, 1.0e-100]
+    r["v_f"] = [-1.0, 3.5, 0.5, 12.25]
+    r["arr_f"] = [32.5, 16.5, 18.5, 48.5]
+    r["status"] = [0, 0, 0, 1]
+    r["dH"] = [1e-9, 2e-5, 0.0, 0.0]
+    return r
+
+
+EXPECTED = [
+    "         7,    1,7.00000E+00,3.25000E+00,1.05000000E+01,5.00000000E-01,1.65000000E+01,1.14900000E+01,"
+    "**************,3.25000000E+01\n",
+    "         8,    3,7.00000E+00,0.00000E+00,1.05000000E+01,5.00000000E-01,1.65000000E+01,2.00000000E+00,"
+    "3.50000000E+00,1.65000000E+01\n",
+    "         9,    1,7.00000E+00,7.00000E+00,1.05000000E+01,5.00000000E-01,1.65000000E+01,           NaN,"
+    "5.00000000E-01,1.85000000E+01\n",
+    "        10,    1,7.00000E+00,1.00000+100,1.05000000E+01,5.00000000E-01,1.65000000E+01,1.00000000-100,"
+    "1.22500000E+01,4.85000000E+01\n",
+]
+
+
+def test_rows_follow_the_reference_format():
+    assert api.format_rows(_rows(), header=False) == "".join(EXPECTED)
+    assert api.format_rows(_rows()[:1], idx_offset=1000, header=True) == HEADER + EXPECTED[0].replace(
+        "         7,", "      1007,")
+
+
+def test_files_split_by_energy_conservation(tmp_path):
+    rows = _rows()
+    n_ok, n_not = api.write_trajectories(tmp_path, rows, ham_abs_tol=1e-5, binary=tmp_path / "trajectories.bin")
+    assert (n_ok, n_not) == (2, 2)
+    assert (tmp_path / "trajectories.out").read_text() == HEADER + EXPECTED[0] + EXPECTED[2]
+    assert (tmp_path / "trajectories_HNotCons.out").read_text() == HEADER + EXPECTED[1] + EXPECTED[3]
+    raw = (tmp_path / "trajectories.bin").read_bytes()
+    assert np.frombuffer(raw[:8], "<i8")[0] == 2
+    recs = np.frombuffer(raw[8:], dtype=[("idx", "<i8"), ("ipes", "<i8"), ("v", "<f8", 8)])
+    assert list(recs["idx"]) == [7, 9] and list(recs["ipes"]) == [1, 1]
+    assert recs["v"][0].tolist() == [7.0, 3.25, 10.5, 0.5, 16.5, 11.49, -1.0, 32.5]
