@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcair_gpu.so")
 CAIR_MAX_PES = 8
-CAIR_ABI_VERSION = 1
+CAIR_ABI_VERSION = 2
 CAIR_STATIC_QUEUE_MAX_TRAJ = 16384
 
 STATUS = {0: "CAIR_OK", 1: "CAIR_EINVAL", 2: "CAIR_ECUDA", 3: "CAIR_ETIMEOUT", 4: "CAIR_ENONFINITE",
@@ -61,11 +61,12 @@ FINAL_STATE_DTYPE = np.dtype([("item", "i4"), ("fin", "i4", 3), ("ini", "i4", 3)
 LEVEL_DTYPE = np.dtype([("vqn", "i4"), ("jqn", "i4"), ("eint", "f8"), ("egam", "f8"), ("rmin", "f8"),
                         ("rmax", "f8"), ("vmin", "f8"), ("vmax", "f8"), ("tau", "f8"), ("ri", "f8"), ("ro", "f8")])
 ITEM_DTYPE = np.dtype([("ilevel", "i4"), ("ipes", "i4"), ("first", "i8"), ("ntraj", "i8"), ("seed", "i8"),
-                       ("ttra", "f8"), ("bmax", "f8"), ("dinit", "f8")])
+                       ("ttra", "f8"), ("bmax", "f8"), ("dinit", "f8"), ("ilevel2", "i4"), ("pad", "i4")])
 RESULT_DTYPE = np.dtype([("idx", "i8"), ("item", "i4"), ("ipes", "i4"), ("status", "i4"), ("iste", "i4"),
                          ("irej", "i4"), ("pad", "i4"),
                          ("bmax", "f8"), ("b", "f8"), ("j_i", "f8"), ("v_i", "f8"), ("arr_i", "f8"),
-                         ("j_f", "f8"), ("v_f", "f8"), ("arr_f", "f8"), ("t", "f8"), ("dH", "f8")])
+                         ("j_f", "f8"), ("v_f", "f8"), ("arr_f", "f8"), ("t", "f8"), ("dH", "f8"),
+                         ("j2_i", "f8"), ("v2_i", "f8"), ("j2_f", "f8"), ("v2_f", "f8")])
 
 # (name, restype, argtypes) of every entry point declared in include/cair_gpu.h
 _P = C.c_void_p

@@ -249,13 +249,15 @@ def level_table(levels):
 
 
 def work_items(entries):
-    """entries: iterable of (ilevel, ipes, ntraj, seed, ttra, bmax, dinit) -> cair_work_item[] tiling
-    the batch in order."""
+    """entries: iterable of (ilevel, ipes, ntraj, seed, ttra, bmax, dinit[, ilevel2]) -> cair_work_item[]
+    tiling the batch in order; ilevel2 is the projectile diatom's level of a diatom + diatom system."""
     entries = list(entries)
     out = np.zeros(len(entries), dtype=_lib.ITEM_DTYPE)
     first = 0
-    for i, (il, ip, nt, seed, ttra, bmax, dinit) in enumerate(entries):
-        out[i] = (il, ip, first, nt, seed, ttra, bmax, dinit)
+    for i, e in enumerate(entries):
+        il, ip, nt, seed, ttra, bmax, dinit = e[:7]
+        il2 = e[7] if len(e) > 7 else 0
+        out[i] = (il, ip, first, nt, seed, ttra, bmax, dinit, il2, 0)
         first += nt
     return out
 
@@ -267,7 +269,7 @@ def process_seed(iseed, iproc, npes=1, inode=1, rndnb=0):
 
 
 class InitialConditions:
-    """SetIniCondForward for diatom + atom work items, on the GPU."""
+    """SetIniCondForward for diatom + atom and diatom + diatom work items, on the GPU."""
 
     def __init__(self, handle):
         self.H = handle

@@ -696,13 +696,14 @@ int cair_apply_transformation(cair_handle* h, int64_t n, const double* paq, doub
 int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_point* out) {
   if (!h || n < 0 || !paq_vel || !out) return fail(h, CAIR_EINVAL, "cair_find_state: bad argument");
   if (n == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_find_state: 4-atom analysis not built");
-  if (int e = ensure_scratch(h, n * (12 * 8 + sizeof(cair_traj_point)) + 1024)) return e;
+  const int ne = h->sys.ne;
+  if (int e = ensure_scratch(h, n * (ne * 8 + sizeof(cair_traj_point)) + 1024)) return e;
   Carver c{(char*)h->d_scratch};
-  double* d_p = c.take<double>(n * 12);
+  double* d_p = c.take<double>(n * ne);
   cair_traj_point* d_o = c.take<cair_traj_point>(n);
-  CUDA_TRY(h, cudaMemcpyAsync(d_p, paq_vel, n * 12 * 8, cudaMemcpyHostToDevice, h->stream));
-  k_find_state3<<<grid_for(h, n), 128, 0, h->stream>>>(h->sys, h->fs, n, d_p, d_o);
+  CUDA_TRY(h, cudaMemcpyAsync(d_p, paq_vel, n * ne * 8, cudaMemcpyHostToDevice, h->stream));
+  if (three_atoms(h)) k_find_state<3><<<grid_for(h, n), 128, 0, h->stream>>>(h->sys, h->fs, n, d_p, d_o);
+  else k_find_state<4><<<grid_for(h, n), 128, 0, h->stream>>>(h->sys, h->fs, n, d_p, d_o);
   if (int e = check_launch(h)) return e;
   CUDA_TRY(h, cudaMemcpyAsync(out, d_o, n * sizeof(cair_traj_point), cudaMemcpyDeviceToHost, h->stream));
   return wait_stream(h);
@@ -715,15 +716,16 @@ struct BatchBufs {
   int32_t *irej, *iste, *status, *ipes, *item_of, *order;
 };
 
-constexpr size_t batch_bytes(int64_t n) {
-  return (size_t)n * (sizeof(double) * (12 * 3 + 9 + kDraws) + sizeof(int32_t) * 6) + 40 * 256 +
+// Batch state of n trajectories of ne equations (12: diatom + atom, 18: diatom + diatom)
+constexpr size_t batch_bytes(int64_t n, int ne) {
+  return (size_t)n * (sizeof(double) * (ne * 3 + 9 + kDraws) + sizeof(int32_t) * 6) + 40 * 256 +
          sizeof(unsigned long long) * (8 + 2 * 256);
 }
 
-void carve_into(char* base, int64_t n, BatchBufs& B) {
+void carve_into(char* base, int64_t n, int ne, BatchBufs& B) {
   Carver c{base};
   B.ctl = c.take<unsigned long long>(8 + 2 * 256);
-  B.paq = c.take<double>(n * 12); B.paq0 = c.take<double>(n * 12); B.erra = c.take<double>(n * 12);
+  B.paq = c.take<double>(n * ne); B.paq0 = c.take<double>(n * ne); B.erra = c.take<double>(n * ne);
   B.t = c.take<double>(n); B.dt = c.take<double>(n); B.H = c.take<double>(n); B.H0 = c.take<double>(n);
   B.smax = c.take<double>(n); B.smin = c.take<double>(n); B.b = c.take<double>(n);
   B.draws = c.take<double>(n * kDraws); B.key = c.take<double>(n);
@@ -733,15 +735,16 @@ void carve_into(char* base, int64_t n, BatchBufs& B) {
 
 int carve_batch(cair_handle* h, int64_t n, bool with_state, BatchBufs& B) {
   (void)with_state;
-  if (int e = ensure_work(h, batch_bytes(n))) return e;
-  carve_into((char*)h->d_work, n, B);
+  if (int e = ensure_work(h, batch_bytes(n, h->sys.ne))) return e;
+  carve_into((char*)h->d_work, n, h->sys.ne, B);
   return 0;
 }
 
 int sample_ics_into(cair_handle* h, int32_t nitems, const cair_work_item* d_items, const cair_level* d_levels,
                     int64_t ntot, double* paq, double* paq0, double* erra, double* H0, double* b, int32_t* ipes,
                     int32_t* item_of, double* draws, cudaStream_t st, double* key = nullptr) {
-  k_ic_draws<<<(nitems + 63) / 64, 64, 0, st>>>(nitems, d_items, d_levels, draws, item_of);
+  k_ic_draws<<<(nitems + 63) / 64, 64, 0, st>>>(nitems, h->sys.natoms == 4 ? 2 : 1, d_items, d_levels, draws,
+                                                item_of);
   if (int e = check_launch(h)) return e;
   int g = grid_for(h, ntot);
   return with_model(h, [&](auto L) {
@@ -755,6 +758,8 @@ int validate_items(cair_handle* h, int32_t nlevels, const cair_level* levels, in
   for (int i = 0; i < nitems; ++i) {
     const cair_work_item& w = items[i];
     if (w.ilevel < 0 || w.ilevel >= nlevels) return fail(h, CAIR_EINVAL, "work item level out of range");
+    if (h->sys.natoms == 4 && (w.ilevel2 < 0 || w.ilevel2 >= nlevels))
+      return fail(h, CAIR_EINVAL, "work item projectile level out of range");
     if (w.ipes < 0 || w.ipes >= h->sys.npes) return fail(h, CAIR_EINVAL, "work item surface out of range");
     if (w.ntraj < 0 || w.first != sum) return fail(h, CAIR_EINVAL, "work items must tile [0, ntot) in order");
     if (!(w.dinit > 0.0) || std::fabs(w.bmax) > w.dinit) return fail(h, CAIR_EINVAL, "impact parameter exceeds Dinit");
@@ -775,7 +780,6 @@ int cair_sample_ics_dev(cair_handle* h, int32_t nlevels, const cair_level* level
       !ipes || !item_of)
     return fail(h, CAIR_EINVAL, "cair_sample_ics_dev: bad argument");
   if (ntot == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "initial conditions: diatom + atom only");
   if (int e = ensure_scratch(h, ntot * kDraws * sizeof(double) + 1024)) return e;
   cudaStream_t st = (cudaStream_t)stream;
   return sample_ics_into(h, nitems, items, levels, ntot, paq, paq0, erra, H0, b, ipes, item_of,
@@ -789,7 +793,6 @@ int cair_sample_ics(cair_handle* h, int32_t nlevels, const cair_level* levels, i
       !ipes)
     return fail(h, CAIR_EINVAL, "cair_sample_ics: bad argument");
   if (ntot == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "initial conditions: diatom + atom only");
   if (int e = validate_items(h, nlevels, levels, nitems, items, ntot)) return e;
   BatchBufs B;
   if (int e = carve_batch(h, ntot, false, B)) return e;
@@ -803,16 +806,17 @@ int cair_sample_ics(cair_handle* h, int32_t nlevels, const cair_level* levels, i
   if (int e = sample_ics_into(h, nitems, d_it, d_lv, ntot, B.paq, B.paq0, B.erra, B.H0, B.b, B.ipes, B.item_of,
                               B.draws, st))
     return e;
-  CUDA_TRY(h, cudaMemcpyAsync(paq, B.paq, ntot * 12 * 8, cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(h, cudaMemcpyAsync(paq0, B.paq0, ntot * 12 * 8, cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(h, cudaMemcpyAsync(erra, B.erra, ntot * 12 * 8, cudaMemcpyDeviceToHost, st));
+  const int ne = h->sys.ne;
+  CUDA_TRY(h, cudaMemcpyAsync(paq, B.paq, ntot * ne * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(paq0, B.paq0, ntot * ne * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(erra, B.erra, ntot * ne * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(H0, B.H0, ntot * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(b, B.b, ntot * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(ipes, B.ipes, ntot * 4, cudaMemcpyDeviceToHost, st));
   return wait_stream(h);
 }
 
-int64_t cair_queue_workspace_bytes(int64_t ntot) { return ntot < 0 ? 0 : (int64_t)batch_bytes(ntot); }
+int64_t cair_queue_workspace_bytes(int64_t ntot) { return ntot < 0 ? 0 : (int64_t)batch_bytes(ntot, 18); }
 
 int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
                        const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results,
@@ -820,11 +824,10 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
   if (!h || nlevels < 1 || nitems < 0 || ntot < 0 || !levels || !items || !results || max_attempts < 1)
     return fail(h, CAIR_EINVAL, "cair_run_queue_dev: bad argument");
   if (ntot == 0) return 0;
-  if (!three_atoms(h)) return fail(h, CAIR_EUNSUPPORTED, "cair_run_queue: diatom + atom only");
   if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_run_queue: only NSteps = 3 is built");
   if (workspace && ((uintptr_t)workspace & 255)) return fail(h, CAIR_EINVAL, "workspace must be 256-byte aligned");
   BatchBufs B;
-  if (workspace) carve_into((char*)workspace, ntot, B);
+  if (workspace) carve_into((char*)workspace, ntot, h->sys.ne, B);
   else if (int e = carve_batch(h, ntot, true, B)) return e;
   cudaStream_t st = (cudaStream_t)stream;
   if (int e = sample_ics_into(h, nitems, items, levels, ntot, B.paq, B.paq0, B.erra, B.H0, B.b, B.ipes, B.item_of,
@@ -841,8 +844,12 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
   IntegrateArgs A{ntot, B.ipes, B.paq, B.t, B.dt, B.erra, B.H, B.smax, B.smin, B.irej, B.iste, B.status,
                   max_attempts, B.ctl, B.ctl + 1, B.order};
   if (int e = launch_integrate(h, A, st)) return e;
-  k_results3<<<g, 128, 0, st>>>(h->sys, h->fs, ntot, B.paq0, B.paq, B.H0, B.H, B.t, B.status, B.iste, B.irej,
-                                  B.item_of, items, results);
+  if (three_atoms(h))
+    k_results<3><<<g, 128, 0, st>>>(h->sys, h->fs, ntot, B.paq0, B.paq, B.H0, B.H, B.t, B.status, B.iste, B.irej,
+                                    B.item_of, items, results);
+  else
+    k_results<4><<<g, 128, 0, st>>>(h->sys, h->fs, ntot, B.paq0, B.paq, B.H0, B.H, B.t, B.status, B.iste, B.irej,
+                                    B.item_of, items, results);
   if (int e = check_launch(h)) return e;
   if (!workspace)
     CUDA_TRY(h, cudaMemcpyAsync(h->d_ctl + 1, B.ctl + 1, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToDevice, st));
@@ -860,7 +867,7 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
 // kernels like any workspace.  Every call shares the array: the queue head and counters are
 // cleared at the start of each call, and calls that overlap on the GPU race.
 // -----------------------------------------------------------------------------------------
-static __device__ __align__(256) unsigned char g_cair_static_queue_ws[batch_bytes(CAIR_STATIC_QUEUE_MAX_TRAJ)];
+static __device__ __align__(256) unsigned char g_cair_static_queue_ws[batch_bytes(CAIR_STATIC_QUEUE_MAX_TRAJ, 12)];
 static std::mutex g_static_ws_mutex;
 static void* g_static_ws_ptr[64] = {nullptr};
 
@@ -870,9 +877,10 @@ int cair_run_queue_static_dev(cair_handle* h, int32_t nlevels, const cair_level*
                               const cair_work_item* items, int64_t ntot, int64_t max_attempts,
                               cair_traj_result* results, void* stream) {
   if (!h) return CAIR_EINVAL;
-  if (ntot < 0 || ntot > CAIR_STATIC_QUEUE_MAX_TRAJ)
+  if (ntot < 0 || batch_bytes(ntot, h->sys.ne) > sizeof(g_cair_static_queue_ws))
     return fail(h, CAIR_EINVAL, "cair_run_queue_static_dev: ntot exceeds the static workspace (at most " +
-                                    std::to_string(CAIR_STATIC_QUEUE_MAX_TRAJ) + " trajectories per call)");
+                                    std::to_string(CAIR_STATIC_QUEUE_MAX_TRAJ) +
+                                    " diatom + atom trajectories per call, fewer of four atoms)");
   int dev = -1;
   CUDA_TRY(h, cudaGetDevice(&dev));
   if (dev != h->device || dev < 0 || dev >= 64)

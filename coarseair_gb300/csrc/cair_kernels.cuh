@@ -460,12 +460,106 @@ static __device__ void analyze3(const DevSys& S, const FsArgs& F, const double* 
   o.mol[1].ipair = 0; o.mol[1].itype = 0; o.mol[1].eint = 0.0; o.mol[1].angmom = 0.0; o.mol[1].viba = 0.0;
 }
 
+// Analyze for 4 atoms (TrajectoryPoint_Class.F90:128-374 with SetPairs 417-495): the closest pair
+// (mapped onto a pair of atom 1) and its opposite pair are the two molecules, unless the third
+// closest squared distance is below rmaxCluster (25 bohr^2, Input_Class.F90:166), a cluster: then
+// both molecules get iPair = -1, itype = -10, viba = AngMom = -1.
+constexpr double kRmaxCluster = 25.0;
+
+static __device__ void analyze4(const DevSys& S, const FsArgs& F, const double* __restrict__ p, cair_traj_point& o) {
+  double xx[3][4], xd[3][4];
+  for (int a = 0; a < 3; ++a)
+    for (int d = 0; d < 3; ++d) { xd[d][a] = p[d + 3 * a]; xx[d][a] = p[d + 3 * a + 9]; }
+  for (int d = 0; d < 3; ++d) {
+    xd[d][3] = ((0.0 + S.mMiMn[0] * p[d]) + S.mMiMn[1] * p[d + 3]) + S.mMiMn[2] * p[d + 6];
+    xx[d][3] = ((0.0 + S.mMiMn[0] * p[d + 9]) + S.mMiMn[1] * p[d + 12]) + S.mMiMn[2] * p[d + 15];
+  }
+  const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+  double rbs[6];
+  int irbs[6];
+  for (int q = 0; q < 6; ++q) {
+    double a = xx[0][pa[q]] - xx[0][pb[q]], b = xx[1][pa[q]] - xx[1][pb[q]], c = xx[2][pa[q]] - xx[2][pb[q]];
+    rbs[q] = a * a + b * b + c * c;
+    irbs[q] = q + 1;
+  }
+  for (int i = 1; i < 6; ++i)  // ascending with index (hpsort, Sorting_Module.F90:20-83)
+    for (int j = i; j > 0 && rbs[j - 1] > rbs[j]; --j) {
+      double t = rbs[j]; rbs[j] = rbs[j - 1]; rbs[j - 1] = t;
+      int k = irbs[j]; irbs[j] = irbs[j - 1]; irbs[j - 1] = k;
+    }
+  o.nmol = 2;
+  o.pad = 0;
+  int ip1;
+  if (rbs[1] > 100.0) {
+    ip1 = irbs[0] <= 3 ? irbs[0] : 7 - irbs[0];
+  } else if (rbs[2] < kRmaxCluster) {
+    o.b = 0.0;
+    o.xkin = 0.0;
+    for (int d = 0; d < 3; ++d) o.vrel[d] = 0.0;
+    for (int im = 0; im < 2; ++im) {
+      o.mol[im].ipair = -1; o.mol[im].itype = -10; o.mol[im].eint = 0.0;
+      o.mol[im].angmom = -1.0; o.mol[im].viba = -1.0;
+    }
+    return;
+  } else {
+    ip1 = irbs[0] < irbs[1] ? irbs[0] : irbs[1];
+    if (ip1 > 3) ip1 = 7 - ip1;
+  }
+  const int ip2 = 7 - ip1;  // opposite pair
+  const int m1a = pa[ip1 - 1], m1b = pb[ip1 - 1];
+  double cm[3][2], cmd[3][2];
+  for (int d = 0; d < 3; ++d) {
+    cm[d][0] = cm[d][1] = cmd[d][0] = cmd[d][1] = 0.0;
+    for (int j = 0; j < 4; ++j) {
+      int w = (j == m1a || j == m1b) ? 0 : 1;
+      cm[d][w] = cm[d][w] + F.mass[j] * xx[d][j];
+      cmd[d][w] = cmd[d][w] + F.mass[j] * xd[d][j];
+    }
+  }
+  double xp = 0.0, xt = 0.0;
+  for (int j = 0; j < 4; ++j) {
+    if (j == m1a || j == m1b) xp = xp + F.mass[j];
+    else xt = xt + F.mass[j];
+  }
+  double xpi = 1.0 / xp, xti = 1.0 / xt, xrel[3], vrel[3];
+  for (int d = 0; d < 3; ++d) {
+    cm[d][0] *= xpi; cm[d][1] *= xti; cmd[d][0] *= xpi; cmd[d][1] *= xti;
+    xrel[d] = cm[d][0] - cm[d][1];
+    vrel[d] = cmd[d][0] - cmd[d][1];
+  }
+  double xnum = xrel[0] * vrel[0] + xrel[1] * vrel[1] + xrel[2] * vrel[2];
+  double v = vrel[0] * vrel[0] + vrel[1] * vrel[1] + vrel[2] * vrel[2];
+  double tt = -xnum / v;
+  double e0 = xrel[0] + tt * vrel[0], e1 = xrel[1] + tt * vrel[1], e2 = xrel[2] + tt * vrel[2];
+  o.b = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+  o.xkin = 0.0;
+  for (int d = 0; d < 3; ++d) o.xkin = o.xkin + 0.5 * xp * (cmd[d][0] * cmd[d][0]) + 0.5 * xt * (cmd[d][1] * cmd[d][1]);
+  for (int d = 0; d < 3; ++d) o.vrel[d] = vrel[d];
+  for (int im = 0; im < 2; ++im) {
+    const int ip = im == 0 ? ip1 : ip2, a = pa[ip - 1], b = pb[ip - 1];
+    double X[6], XD[6];
+    for (int d = 0; d < 3; ++d) {
+      X[2 * d] = xx[d][a]; X[2 * d + 1] = xx[d][b];
+      XD[2 * d] = xd[d][a]; XD[2 * d + 1] = xd[d][b];
+    }
+    find_state(S, F, ip, a, b, X, XD, o.mol[im]);
+  }
+}
+
+template <int NA>
+__device__ __forceinline__ void analyze(const DevSys& S, const FsArgs& F, const double* __restrict__ p,
+                                        cair_traj_point& o) {
+  if (NA == 3) analyze3(S, F, p, o);
+  else analyze4(S, F, p, o);
+}
+
 #ifndef CAIR_MODEL_TU  // model-independent: built once, in the API translation unit
-__global__ void __launch_bounds__(128) k_find_state3(DevSys S, FsArgs F, int64_t n, const double* __restrict__ paq,
-                                                     cair_traj_point* __restrict__ out) {
+template <int NA>
+__global__ void __launch_bounds__(128) k_find_state(DevSys S, FsArgs F, int64_t n, const double* __restrict__ paq,
+                                                    cair_traj_point* __restrict__ out) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     cair_traj_point o;
-    analyze3(S, F, paq + 12 * k, o);
+    analyze<NA>(S, F, paq + 6 * (NA - 1) * k, o);
     out[k] = o;
   }
 }

@@ -55,6 +55,9 @@ void ModelLaunch<MODEL>::sample_ic(int grid, cudaStream_t st, const DevSys& S, i
   if constexpr (Traits<MODEL>::NA == 3)
     k_sample_ic3<MODEL><<<grid, 128, 0, st>>>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes,
                                               key);
+  else
+    k_sample_ic4<MODEL><<<grid, 128, 0, st>>>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes,
+                                              key);
 }
 
 template struct ModelLaunch<CAIR_MODEL_ID>;

@@ -196,5 +196,7 @@ def o4_config(mass_amu=15.9994, **kw):
     m = mass_amu * AMU_TO_AU
     kw.setdefault("bmax", 8.0)
     kw.setdefault("dinit", 18.0)
+    kw.setdefault("rmax", 35.0)     # input/O4/UMN/input/CoarseAIR_StS.inp:228-229
+    kw.setdefault("tmax", 5.0e5)
     surfs = [load_o4_umn(x) for x in ("UMN_Singlet", "UMN_Triplet", "UMN_Quintet")]
     return SystemConfig("O2+O2 UMN", 4, (m, m, m, m), surfs, DIAT_O2_UMN, degeneracy=(1.0, 3.0, 5.0), **kw)

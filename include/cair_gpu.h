@@ -44,7 +44,7 @@ extern "C" {
 #endif
 
 #define CAIR_MAX_PES 8
-#define CAIR_ABI_VERSION 1
+#define CAIR_ABI_VERSION 2
 
 /* Surface models (PES_Factory_Class.F90:46-329, System x PES_Model strings). */
 enum cair_pes_model {
@@ -155,6 +155,8 @@ typedef struct cair_work_item {
   double ttra;      /* translational temperature [K] (Boltzmann model)         */
   double bmax;      /* impact-parameter bound [bohr] (Circles, one ring)       */
   double dinit;     /* initial separation [bohr]                               */
+  int32_t ilevel2;  /* diatom + diatom: row of the projectile's level (atoms 3, 4) */
+  int32_t pad;
 } cair_work_item;
 
 /* One row of trajectories.out (Integrator_Class.F90:884-933) plus diagnostics. */
@@ -171,6 +173,8 @@ typedef struct cair_traj_result {
   double j_f, v_f, arr_f;  /* the same for the final point                             */
   double t;         /* final time [a.u.]                                            */
   double dH;        /* H_final - H0 [Eh]; |dH| > HamAbsTol goes to the HNotCons file */
+  double j2_i, v2_i, j2_f, v2_f;  /* four atoms: the second molecule's AngMom, viba; the
+                                     arrangement is then 16 iPair1 + itype1 + 4 itype2 + 1/2 */
 } cair_traj_result;
 
 typedef struct cair_handle cair_handle;
@@ -265,9 +269,9 @@ int64_t cair_queue_workspace_bytes(int64_t ntot);
  * memory once they are running (a host whose GPU memory is handed out by its own pool at
  * start-up, or code that must not trigger cudaMalloc's implicit synchronisation while it
  * runs): the batch state lives in a file-scope static device array of
- * CAIR_STATIC_QUEUE_MAX_TRAJ trajectories (about 7 MB that every GPU loading the library
- * keeps until exit), and the call allocates nothing.  ntot > CAIR_STATIC_QUEUE_MAX_TRAJ is
- * rejected with CAIR_EINVAL.  The first call on a device looks up the array's device address,
+ * CAIR_STATIC_QUEUE_MAX_TRAJ diatom + atom trajectories (about 8 MB that every GPU loading the
+ * library keeps until exit; it holds about two thirds as many diatom + diatom ones), and the call
+ * allocates nothing.  A batch beyond the array is rejected with CAIR_EINVAL.  The first call on a device looks up the array's device address,
  * so make it before any stream capture; the handle's device must be current.  All calls share
  * the array, so calls that overlap on the GPU race; the array keeps the last call's contents. */
 #define CAIR_STATIC_QUEUE_MAX_TRAJ 16384

@@ -118,6 +118,10 @@ int    orc_sample_ic(const orc_sys* s, orc_rng* rng, const orc_level* levels, in
                      const orc_ic_cfg* cfg, int ipes,
                      double* paq, double* paq0, double* H0, double* erra, double* b, int* ilevel,
                      double* er_out);
+/* diatom (atoms 1, 2; level lev1) + diatom (atoms 3, 4; level lev2), state-specific */
+int    orc_sample_ic4(const orc_sys* s, orc_rng* rng, const orc_level* lev1, const orc_level* lev2,
+                      const orc_ic_cfg* cfg, int ipes, double* paq, double* paq0, double* H0, double* erra,
+                      double* bout, double* er_out);
 void   orc_bond_length(int diat, double xmui, double ro, double tau, double vc_r2, double vibphase,
                        double* r, double* rdot);
 double orc_boltzmann_er(double ttra, double randnum);

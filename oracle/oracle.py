@@ -84,6 +84,8 @@ def lib():
         L.orc_pes_scale.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D]
         L.orc_rp.argtypes = [C.POINTER(OrcSys), _D, _D, _D]
         _I64 = C.POINTER(C.c_int64)
+        L.orc_sample_ic4.argtypes = [C.POINTER(OrcSys), C.POINTER(OrcRng), C.POINTER(OrcLevel), C.POINTER(OrcLevel),
+                                     C.POINTER(OrcIcCfg), C.c_int, _D, _D, _D, _D, _D, _D]
         L.orc_statistics.argtypes = [C.c_int, C.c_int, _I, _I, C.c_int, _D, _D, _D, _D, C.c_int, _I64, _I, _I, _I64,
                                      _D, _D]
         L.orc_mean_velocity.argtypes = [C.c_double, C.c_double]
@@ -273,6 +275,29 @@ class Oracle:
                                  dp(paq0[k]), dp(H0[k:k + 1]), dp(erra[k]), dp(b[k:k + 1]), ip(il[k:k + 1]),
                                  dp(er[k:k + 1]))
         return dict(paq=paq, paq0=paq0, H0=H0, erra=erra, b=b, ilevel=il, er=er)
+
+    def sample_ics4(self, n, level1, level2, ttra=None, bmax=None, dinit=None, seed=None):
+        """Diatom + diatom initial conditions (state-specific, one level per molecule) from one stream."""
+        cfg = self.cfg
+        rng = OrcRng()
+        self.L.orc_rng_seed(C.byref(rng), int(cfg.seed if seed is None else seed))
+        lv = (OrcLevel * 2)()
+        for i, row in enumerate((level1, level2)):
+            L = lv[i]
+            L.vqn, L.jqn = int(row["vqn"]), int(row["jqn"])
+            for c in ("eint", "egam", "rmin", "rmax", "vmin", "vmax", "tau", "ri", "ro"):
+                setattr(L, c, float(row[c]))
+            L.rlim = 0.0
+        ic = OrcIcCfg(cfg.ttra if ttra is None else ttra, cfg.bmax if bmax is None else bmax,
+                      cfg.dinit if dinit is None else dinit, 1)
+        ne = self.ne
+        paq, paq0, erra = np.zeros((n, ne)), np.zeros((n, ne)), np.zeros((n, ne))
+        H0, b, er = np.zeros(n), np.zeros(n), np.zeros(n)
+        for k in range(n):
+            self.L.orc_sample_ic4(C.byref(self.s), C.byref(rng), C.byref(lv[0]), C.byref(lv[1]), C.byref(ic), 0,
+                                  dp(paq[k]), dp(paq0[k]), dp(H0[k:k + 1]), dp(erra[k]), dp(b[k:k + 1]),
+                                  dp(er[k:k + 1]))
+        return dict(paq=paq, paq0=paq0, H0=H0, erra=erra, b=b, er=er)
 
     # -- final states --
     def analyze(self, paq_vel):

@@ -277,6 +277,19 @@ void orc_analyze(const orc_sys* s, const double* paq, orc_traj_point* out) {
   } else {
     if (rbs[1] > 100.0) {
       ip1 = irbs[0] <= 3 ? irbs[0] : 7 - irbs[0];
+    } else if (rbs[2] < 25.0) {   /* rmaxCluster (Input_Class.F90:166): a cluster, SetPairs 456-460 */
+      out->nmol = 2;
+      out->b = 0.0;
+      out->xkin = 0.0;
+      for (int d = 0; d < 3; ++d) out->vrel[d] = 0.0;
+      for (int im = 0; im < 2; ++im) {   /* AnalyzeTrajectoryPoint 355-364 */
+        out->mol[im].ipair = -1;
+        out->mol[im].itype = -10;
+        out->mol[im].eint = 0.0;
+        out->mol[im].angmom = -1.0;
+        out->mol[im].viba = -1.0;
+      }
+      return;
     } else {
       ip1 = irbs[0] < irbs[1] ? irbs[0] : irbs[1];
       if (ip1 > 3) ip1 = 7 - ip1;

@@ -92,6 +92,107 @@ void orc_bond_length(int diat, double xmui, double ro, double tau, double vc_r2,
   *rdot = y[1];
 }
 
+/* ---- One diatom: ComputeKineticEnergy (draws for quasi-bound levels), BondLength (vibrational
+ * phase draw) and Compute_Coordinates_Velocities (three orientation draws), StateInitDiatomAtom_Module.F90
+ * 236-348, 543-833; atoms a, b of masses ma, mb; q, qd [dir][atom] relative to the diatom's centre. */
+static void diatom_ic(const orc_sys* s, orc_rng* rng, const orc_level* L, double ma, double mb, double q[3][2],
+                      double qd[3][2]) {
+  double redmass_d = ma * mb / (ma + mb);
+  double xmui = 1.0 / redmass_d, xmui2 = 0.5 * xmui;
+  double jh = (double)L->jqn + 0.5;
+  double vc_r2 = xmui2 * (jh * jh);
+  if (L->egam != 0.0) {
+    for (int it = 1; it < 100000; ++it) {
+      double ra = orc_rng_draw(rng), rb = orc_rng_draw(rng);
+      double v1 = 2.0 * ra - 1.0, v2 = 2.0 * rb - 1.0, r = v1 * v1 + v2 * v2;
+      if (r >= 1.0) continue;
+      double fac = sqrt(-2.0 * log(r) / r);
+      double g1 = v1 * fac, g2 = v2 * fac;
+      double ek = L->egam * g1 + L->eint;
+      if (ek < 0.0 || ek >= L->vmax) {
+        ek = L->egam * g2 + L->eint;
+        if (ek < 0.0 || ek >= L->vmax) continue;
+      }
+      break;
+    }
+  }
+  double vibphase = orc_rng_draw(rng);
+  double bl, dbl;
+  orc_bond_length(s->diat, xmui, L->ro, L->tau, vc_r2, vibphase, &bl, &dbl);
+  double omega = 2.0 * sqrt(vc_r2 * xmui2) / (bl * bl);
+  double fa = mb / (ma + mb), fb = -ma / (ma + mb);
+  double rA = orc_rng_draw(rng), rB = orc_rng_draw(rng), rC = orc_rng_draw(rng);
+  double twopi = PI_ * 2.0;
+  double gam = rA * twopi, bet = acos(2.0 * (rB - 0.5)), alp = rC * twopi;
+  double cb = cos(bet), sb = sin(bet), ca = cos(alp), sa = sin(alp), cg = cos(gam), sg = sin(gam);
+  double u1 = cb * ca * cg - sa * sg, u2 = -(cb * ca * sg) - sa * cg;
+  double w1 = cb * sa * cg + sg * ca, w2 = -(cb * sa * sg) + ca * cg;
+  double uu1 = -(cb * sg * ca) - sa * cg;
+  double ro_ = bl * omega;
+  q[0][0] = fa * bl * u1;
+  q[1][0] = fa * bl * u2;
+  q[2][0] = fa * bl * sb * ca;
+  q[0][1] = fb * bl * u1;
+  q[1][1] = fb * bl * u2;
+  q[2][1] = fb * bl * sb * ca;
+  qd[0][0] = fa * (dbl * u1 + ro_ * w1);
+  qd[1][0] = fa * (dbl * uu1 + ro_ * w2);
+  qd[2][0] = fa * (dbl * (sb * ca) + ro_ * sb * sa);
+  qd[0][1] = fb * (dbl * u1 + ro_ * w1);
+  qd[1][1] = fb * (dbl * uu1 + ro_ * w2);
+  qd[2][1] = fb * (dbl * (sb * ca) + ro_ * sb * sa);
+}
+
+/* ---- SetIniCondForward (Collision_Class.F90:1065-1211) for diatom (atoms 1,2) + diatom (atoms 3,4):
+ * SetInitialState_DiatomDiatom (StateInitDiatomDiatom_Module.F90:86-219; state-specific: no level
+ * draw) for each molecule, then CoordVeloc_FreeTotAngMom, ComputeCoordinatesVelocities,
+ * ShiftCoordinates and SetPaQ (1216-1314, 1591-1849) with the projectile's atom 4 eliminated. ---- */
+int orc_sample_ic4(const orc_sys* s, orc_rng* rng, const orc_level* lev1, const orc_level* lev2,
+                   const orc_ic_cfg* cfg, int ipes, double* paq, double* paq0, double* H0, double* erra,
+                   double* bout, double* er_out) {
+  const double* m = s->mass;
+  double q1[3][2], qd1[3][2], q2[3][2], qd2[3][2];
+  diatom_ic(s, rng, lev1, m[0], m[1], q1, qd1);
+  diatom_ic(s, rng, lev2, m[2], m[3], q2, qd2);
+  double er = orc_boltzmann_er(cfg->ttra, orc_rng_draw(rng));
+  double b = -cfg->bmax;
+  if (b < 0.0) {
+    double r2 = orc_rng_draw(rng);
+    b = -sqrt(r2) * b;
+  }
+  double mt = m[0] + m[1], mp = m[2] + m[3];
+  double redmass = mt * mp / (mt + mp);
+  double fA = -mp / (mt + mp), fB = mt / (mt + mp);
+  double qx1 = fA * cfg->dinit, qx2 = fB * cfg->dinit;
+  double ver = sqrt(2.0 * er / redmass);
+  double ratio = b / cfg->dinit;
+  double verx = -ver * sqrt(1.0 - ratio * ratio);
+  double verz = -ver * ratio;
+  for (int a = 0; a < 2; ++a) {
+    q1[0][a] = q1[0][a] + qx1; q1[1][a] = q1[1][a] + 0.0; q1[2][a] = q1[2][a] + 0.0;
+    qd1[0][a] = qd1[0][a] + fA * verx; qd1[1][a] = qd1[1][a] + 0.0; qd1[2][a] = qd1[2][a] + fA * verz;
+    q2[0][a] = q2[0][a] + qx2; q2[1][a] = q2[1][a] + 0.0; q2[2][a] = q2[2][a] + 0.0;
+    qd2[0][a] = qd2[0][a] + fB * verx; qd2[1][a] = qd2[1][a] + 0.0; qd2[2][a] = qd2[2][a] + fB * verz;
+  }
+  int nv = s->neqtvar;   /* 9 */
+  double dq[9];
+  for (int d = 0; d < 3; ++d) {
+    paq[nv + d] = q1[d][0]; dq[d] = qd1[d][0];
+    paq[nv + 3 + d] = q1[d][1]; dq[3 + d] = qd1[d][1];
+    paq[nv + 6 + d] = q2[d][0]; dq[6 + d] = qd2[d][0];
+  }
+  for (int i = 0; i < nv; ++i) paq[i] = 0.0;
+  for (int ip = 0; ip < nv; ++ip)
+    for (int i = 0; i < nv; ++i) paq[i] = paq[i] + TQ(s->Tqp, ip, i) * dq[ip];
+  double Rpi[6];
+  orc_hamiltonian(s, ipes, paq, H0, Rpi);
+  orc_error_factor(s, s->eps, paq, erra);
+  for (int i = 0; i < nv; ++i) { paq0[i] = dq[i]; paq0[nv + i] = paq[nv + i]; }
+  *bout = b;
+  if (er_out) *er_out = er;
+  return 0;
+}
+
 /* ---- SetIniCondForward (Collision_Class.F90:1065-1211) for diatom (atoms 1,2) + atom (3) ---- */
 int orc_sample_ic(const orc_sys* s, orc_rng* rng, const orc_level* levels, int nlevels, const orc_ic_cfg* cfg,
                   int ipes, double* paq, double* paq0, double* H0, double* erra, double* bout, int* ilevel,

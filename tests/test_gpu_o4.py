@@ -149,3 +149,92 @@ def test_o4_integrate_to_end(gpu_lib, oracle_lib):
     h_o, _ = o.hamiltonian(tr.paq, ipes=ip)
     assert np.max(np.abs(tr.H - h_o)) < 1e-9
     assert np.max(np.abs(tr.H - o.hamiltonian(y, ipes=ip)[0])) < cfg.ham_abs_tol
+
+
+def _o4_items(lv):
+    from coarseair_gb300 import api as _api
+    rows = lv[[0, 40, 120]]
+    table = _api.level_table(rows)
+    entries = [(0, 0, 12, _api.process_seed(3, 1), 10000.0, 8.0, 18.0, 1),
+               (1, 1, 12, _api.process_seed(3, 2), 10000.0, 8.0, 18.0, 2),
+               (2, 2, 12, _api.process_seed(3, 3), 10000.0, 8.0, 18.0, 0)]
+    return rows, table, entries, _api.work_items(entries)
+
+
+def test_o4_device_initial_conditions_match_oracle(gpu_lib, oracle_lib):
+    """SetIniCondForward for diatom + diatom on the device against the oracle's stream."""
+    cfg, o, H = _setup()
+    lv = systems.load_levels("O2")
+    rows, table, entries, items = _o4_items(lv)
+    ic = api.InitialConditions(H).sample(table, items)
+    for i, e in enumerate(entries):
+        il, ipes, nt, seed, T, bmax, dinit, il2 = e
+        ref = o.sample_ics4(nt, rows[il], rows[il2], ttra=T, bmax=bmax, dinit=dinit, seed=seed)
+        sl = slice(int(items["first"][i]), int(items["first"][i] + nt))
+        for key in ("paq", "paq0", "erra"):
+            sc = np.abs(ref[key]).max(axis=1, keepdims=True)
+            assert np.all(np.abs(ic[key][sl] - ref[key]) <= 1e-10 * sc), key
+        # H0 on the item's surface
+        h_ref, _ = o.hamiltonian(ref["paq"], ipes=np.full(nt, ipes))
+        assert np.all(np.abs(ic["H0"][sl] - h_ref) <= 1e-11 * np.maximum(np.abs(h_ref), 0.1))
+        assert np.allclose(ic["b"][sl], ref["b"], rtol=1e-14, atol=0)
+
+
+def _fs_tuple(f):
+    qn = lambda x: int(np.sign(x) * np.floor(abs(x) + 0.5))
+    return (qn(f["angmom"] - 0.5), qn(f["viba"] - 0.5), qn(f["angmom1"] - 0.5), qn(f["viba1"] - 0.5),
+            16 * f["ipair"] + f["itype"] + 4 * f["itype1"])
+
+
+def test_o4_final_state_analysis_on_identical_points(gpu_lib, oracle_lib):
+    cfg, o, H = _setup()
+    y, erra = _collision_points(o, cfg, 16, 17)
+    ip = np.arange(len(y), dtype=np.int32) % 3
+    res = o.integrate(y, erra, ipes=ip, procs=PROCS)
+    pts = np.concatenate([o.apply_transformation(y), o.apply_transformation(res["paq"])])
+    fo = o.analyze(pts)
+    fg = api.MolecularState(H).FindState(pts)
+    for k, f in enumerate(fo):
+        g = fg[k]
+        gd = dict(angmom=g["angmom0"], viba=g["viba0"], angmom1=g["angmom1"], viba1=g["viba1"],
+                  ipair=g["ipair0"], itype=g["itype0"], itype1=g["itype1"])
+        assert _fs_tuple(gd) == _fs_tuple(f)
+        assert g["ipair1"] == f["ipair1"]
+        assert np.allclose([g["viba0"], g["viba1"]], [f["viba"], f["viba1"]], rtol=1e-9, atol=1e-12)
+        assert np.allclose([g["angmom0"], g["angmom1"]], [f["angmom"], f["angmom1"]], rtol=1e-12, atol=1e-12)
+
+
+def test_o4_run_queue_matches_oracle(gpu_lib, oracle_lib):
+    """cair_run_queue for O2 + O2 on the three surfaces: final (J1, v1, J2, v2, arrangement) equal
+    to the oracle's on the trajectories whose oracle outcome is stable under a 1e-14 perturbation."""
+    cfg, o, H = _setup()
+    lv = systems.load_levels("O2")
+    rows, table, entries, items = _o4_items(lv)
+    res = api.RunTrajectories(H).run(table, items)
+    assert np.all(res["status"] == 0)
+    assert np.max(np.abs(res["dH"])) < cfg.ham_abs_tol
+    same, stable = [], []
+    for i, e in enumerate(entries):
+        il, ipes, nt, seed, T, bmax, dinit, il2 = e
+        ref = o.sample_ics4(nt, rows[il], rows[il2], ttra=T, bmax=bmax, dinit=dinit, seed=seed)
+        ipv = np.full(nt, ipes, np.int32)
+        a = o.integrate(ref["paq"], ref["erra"], ipes=ipv, procs=PROCS)
+        b = o.integrate(ref["paq"] * (1 + 1e-14), ref["erra"], ipes=ipv, procs=PROCS)
+        fa = [_fs_tuple(f) for f in o.analyze(o.apply_transformation(a["paq"]))]
+        fb = [_fs_tuple(f) for f in o.analyze(o.apply_transformation(b["paq"]))]
+        sl = slice(int(items["first"][i]), int(items["first"][i] + nt))
+        r = res[sl]
+        qn = lambda x: (np.sign(x) * np.floor(np.abs(x) + 0.5)).astype(int)
+        fg = list(zip(qn(r["j_f"] - 0.5), qn(r["v_f"] - 0.5), qn(r["j2_f"] - 0.5), qn(r["v2_f"] - 0.5),
+                      qn(r["arr_f"] - 0.5)))
+        same += [tuple(int(x) for x in g) == f for g, f in zip(fg, fa)]
+        stable += [x == y for x, y in zip(fa, fb)]
+        fi = [_fs_tuple(f) for f in o.analyze(ref["paq0"])]
+        gi = list(zip(qn(r["j_i"] - 0.5), qn(r["v_i"] - 0.5), qn(r["j2_i"] - 0.5), qn(r["v2_i"] - 0.5),
+                      qn(r["arr_i"] - 0.5)))
+        assert [tuple(int(x) for x in g) for g in gi] == fi
+    same, stable = np.array(same), np.array(stable)
+    print("O4 queue: GPU vs oracle %.4f overall, %.4f on oracle-stable (%d of %d stable)" %
+          (same.mean(), same[stable].mean(), stable.sum(), len(stable)))
+    assert stable.sum() >= len(stable) // 2
+    assert same[stable].mean() >= 0.995

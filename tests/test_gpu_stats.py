@@ -22,7 +22,7 @@ def _compare(H, items, rows, pres, st):
         ref, ini = oracle.statistics(np.full(sel.sum(), it["bmax"]), rows["b"][sel],
                                      np.stack([rows["j_i"][sel], rows["v_i"][sel], rows["arr_i"][sel]], 1),
                                      np.stack([rows["j_f"][sel], rows["v_f"][sel], rows["arr_f"][sel]], 1),
-                                     pres=pres)
+                                     pres=pres, cap=max(64, int(sel.sum())))
         g = got[got["item"] == i]
         assert len(g) == len(ref)
         gd = {tuple(int(x) for x in r["fin"]): r for r in g}
