@@ -60,31 +60,86 @@ def workload(ntraj, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=15.0):
     return table, api.work_items(entries)
 
 
-def config():
-    """N3 system of the workload.  The end-of-collision criterion is the one stated for the
-    atom-diatom configurations (any pair beyond 16 bohr, attempt cap 1e6)."""
+def workload_o3(ntraj):
+    """O2(v=0, J=1) + O on UMN_11A1: one state-specific run, seed 1, 10,000 K, b = 6 sqrt(U) bohr."""
+    from coarseair_gb300 import api, systems
+    lv = systems.load_levels("O2")
+    row = lv[(lv["vqn"] == 0) & (lv["jqn"] == 1)]
+    return api.level_table(row), api.work_items([(0, 0, ntraj, api.process_seed(1, 1), 10000.0, 6.0, 15.0)])
+
+
+def workload_o4(ntraj, npairs=64, seed_levels=3):
+    """O2 + O2 on the three O4 UMN surfaces: 64 (level, level) pairs drawn uniformly (seed 3) from the
+    first 200 O2 levels, 10,000 K, b = 8 sqrt(U) bohr, Dinit 18 bohr; each pair's trajectories are
+    split over the singlet, triplet and quintet surfaces in proportion to their degeneracies 1:3:5
+    (contiguous blocks per surface, Collision_Class.F90:2468-2507)."""
+    from coarseair_gb300 import api, systems
+    lv = systems.load_levels("O2")[:200]
+    rng = np.random.default_rng(seed_levels)
+    pairs = rng.integers(0, 200, size=(npairs, 2))
+    table = api.level_table(lv)
+    per_pair = [ntraj // npairs + (1 if k < ntraj % npairs else 0) for k in range(npairs)]
+    entries = []
+    for k, (a, b) in enumerate(pairs):
+        n = per_pair[k]
+        split = [n * 1 // 9, n * 3 // 9]
+        split.append(n - split[0] - split[1])
+        for ip in range(3):
+            entries.append((int(a), ip, split[ip], api.process_seed(3, 3 * k + ip + 1), 10000.0, 8.0, 18.0, int(b)))
+    return table, api.work_items(entries)
+
+
+def config(system="n3"):
+    """System of the workload.  N3 and O3 use the end-of-collision criterion stated for the atom-diatom
+    configurations (any pair beyond 16 bohr, attempt cap 1e6); O4 the reference's O4 input
+    (35 bohr, tmax 5e5)."""
     from coarseair_gb300 import systems
+    if system == "o3":
+        return systems.o3_config(dinit=15.0, bmax=6.0, rmax=16.0)
+    if system == "o4":
+        return systems.o4_config()
     return systems.n3_config(dinit=15.0, bmax=7.0, rmax=16.0, tmax=4.0e5)
+
+
+SYSTEMS = {
+    "n3": dict(workload=workload, ntraj=1000000,
+               text="N2+N on N3 UMN (N4 PIP), plain FP64: 64 levels (seed 2) x {5000,10000,20000} K, "
+                    "b = 7 sqrt(U) bohr, Dinit 15 bohr, rmax 16 bohr, m = 14.0067 amu"),
+    "o3": dict(workload=workload_o3, ntraj=10000,
+               text="O2(v=0,J=1)+O on O3 UMN_11A1, plain FP64: seed 1, 10000 K, b = 6 sqrt(U) bohr, Dinit 15 bohr, "
+                    "rmax 16 bohr, m = 15.9994 amu"),
+    "o4": dict(workload=workload_o4, ntraj=500000,
+               text="O2+O2 on O4 UMN singlet/triplet/quintet (1:3:5), plain FP64: 64 level pairs from the first 200 "
+                    "O2 levels (seed 3), 10000 K, b = 8 sqrt(U) bohr, Dinit 18 bohr, rmax 35 bohr, m = 15.9994 amu"),
+}
 
 
 # ------------------------------------------------------------------------------------------------
 # CPU side: the oracle on host cores (one process per core, spawned before any GPU work)
 # ------------------------------------------------------------------------------------------------
+def _oracle_level(table, il):
+    lv = table[il:il + 1]
+    lvs = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax",
+                                                   "tau", "ri", "ro", "rlim")])
+    for c in lvs.dtype.names:
+        lvs[c] = lv[c] if c in lv.dtype.names else 0.0
+    return lvs
+
+
 def _cpu_worker(args):
-    items, table, wall = args
+    items, table, wall, system = args
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
-    o = Oracle(config())
+    o = Oracle(config(system))
     done, t0 = 0, time.perf_counter()
-    for (il, ntraj, seed, ttra, bmax, dinit) in items:
-        lv = table[il:il + 1]
-        lvs = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax",
-                                                       "tau", "ri", "ro", "rlim")])
-        for c in lvs.dtype.names:
-            lvs[c] = lv[c] if c in lv.dtype.names else 0.0
-        ic = o.sample_ics(ntraj, lvs, seed=seed, ttra=ttra, bmax=bmax, dinit=dinit)
+    for (il, ntraj, seed, ttra, bmax, dinit, ipes, il2) in items:
+        if system == "o4":
+            ic = o.sample_ics4(ntraj, _oracle_level(table, il)[0], _oracle_level(table, il2)[0], ttra=ttra,
+                               bmax=bmax, dinit=dinit, seed=seed)
+        else:
+            ic = o.sample_ics(ntraj, _oracle_level(table, il), seed=seed, ttra=ttra, bmax=bmax, dinit=dinit)
         for k in range(ntraj):
-            res = o.integrate(ic["paq"][k:k + 1], ic["erra"][k:k + 1])
+            res = o.integrate(ic["paq"][k:k + 1], ic["erra"][k:k + 1], ipes=np.array([ipes], np.int32))
             o.analyze(ic["paq0"][k:k + 1])
             o.analyze(o.apply_transformation(res["paq"]))
             done += 1
@@ -93,19 +148,25 @@ def _cpu_worker(args):
     return done, time.perf_counter() - t0
 
 
-def cpu_baseline(table, items, cores, wall):
+def cpu_baseline(table, items, cores, wall, system="n3"):
     """Trajectories/s of the oracle on `cores` processes, each running trajectories of its own
     work items for about `wall` seconds (a bounded sample of the same workload)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
     per = [[] for _ in range(cores)]
-    for k, it in enumerate(items):
-        per[k % cores].append((int(it["ilevel"]), int(it["ntraj"]), int(it["seed"]), float(it["ttra"]),
-                               float(it["bmax"]), float(it["dinit"])))
+    if len(items) >= cores:
+        for k, it in enumerate(items):
+            per[k % cores].append((int(it["ilevel"]), int(it["ntraj"]), int(it["seed"]), float(it["ttra"]),
+                                   float(it["bmax"]), float(it["dinit"]), int(it["ipes"]), int(it["ilevel2"])))
+    else:  # fewer items than cores: every process runs the first item's stream from its own seed
+        it = items[0]
+        for k in range(cores):
+            per[k].append((int(it["ilevel"]), int(it["ntraj"]), int(it["seed"]) + 2 * k, float(it["ttra"]),
+                           float(it["bmax"]), float(it["dinit"]), int(it["ipes"]), int(it["ilevel2"])))
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        out = pool.map(_cpu_worker, [(p, table, wall) for p in per])
+        out = pool.map(_cpu_worker, [(p, table, wall, system) for p in per])
     n = sum(o[0] for o in out)
     t = max(o[1] for o in out)
     return n / t, n, t
@@ -184,24 +245,30 @@ def main():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ntraj", type=int, default=1000000, help="trajectories per step (one queue)")
+    ap.add_argument("--system", default="n3", choices=sorted(SYSTEMS),
+                    help="n3: N2+N 1M (the headline); o3: O2+O 10k; o4: O2+O2 500k")
+    ap.add_argument("--ntraj", type=int, default=None, help="trajectories per step (one queue)")
     ap.add_argument("--inflight", type=int, default=1, help="steps in flight on separate streams")
-    ap.add_argument("--e2e-ntraj", type=int, default=1000000, help="trajectories of the e2e host call")
+    ap.add_argument("--e2e-ntraj", type=int, default=None, help="trajectories of the e2e host call")
     ap.add_argument("--max-attempts", type=int, default=1000000)
     ap.add_argument("--cpu-wall", type=float, default=20.0, help="seconds of CPU work per core for the baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    spec = SYSTEMS[args.system]
+    if args.ntraj is None:
+        args.ntraj = spec["ntraj"]
+    if args.e2e_ntraj is None:
+        args.e2e_ntraj = args.ntraj
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
-    table, items = workload(args.ntraj)
+    table, items = spec["workload"](args.ntraj)
     cores = host_cores()
     metric = "trajectories/s"
-    cfg_json = {"workload": "N2+N on N3 UMN (N4 PIP), plain FP64: 64 levels (seed 2) x {5000,10000,20000} K, "
-                            "b = 7 sqrt(U) bohr, Dinit 15 bohr, rmax 16 bohr, m = 14.0067 amu",
+    cfg_json = {"workload": spec["text"],
                 "trajectories_per_step": int(args.ntraj), "work_items": int(len(items)),
-                "full_config_trajectories": 1000000, "parallelism": "replicas" if world > 1 else "single",
+                "full_config_trajectories": spec["ntraj"], "parallelism": "replicas" if world > 1 else "single",
                 "l2": "inputs stay resident; each step re-samples initial conditions and rewrites all state "
                       "(state per step %.0f MB, above the 129 MB L2 from 1M trajectories)" % (args.ntraj * 0.4e-3)}
 
@@ -211,7 +278,7 @@ def main():
         K, W = args.steps, args.warmup
         times, total = [], 0
         for s in range(W + K):
-            rate, n, t = cpu_baseline(table, items, cores, max(2.0, args.cpu_wall / 4))
+            rate, n, t = cpu_baseline(table, items, cores, max(2.0, args.cpu_wall / 4), args.system)
             if s >= W:
                 times.append(t)
                 total += n
@@ -230,7 +297,7 @@ def main():
     # CPU baseline first (spawned processes before any GPU call)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, n, t = cpu_baseline(table, items, cores, args.cpu_wall)
+        rate, n, t = cpu_baseline(table, items, cores, args.cpu_wall, args.system)
         cpu = {"value": rate, "unit": "trajectories/s", "cores": cores, "kind": "port",
                "sample": "%d trajectories of the same work items in %.1f s on %d processes "
                          "(C restatement of the reference CPU path, -O2 no FMA)" % (n, t, cores)}
@@ -242,7 +309,7 @@ def main():
         dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     dev = torch.device("cuda", torch.cuda.current_device())
-    cfg = config()
+    cfg = config(args.system)
     H = api.Handle(cfg)
     lib = H.lib
     n = int(items["ntraj"].sum())
@@ -308,7 +375,7 @@ def main():
     # e2e through the host entry point with pinned buffers
     e2e = None
     if not args.no_e2e:
-        etab, eitems = workload(args.e2e_ntraj)
+        etab, eitems = spec["workload"](args.e2e_ntraj)
         ne = int(eitems["ntraj"].sum())
         pin_res = torch.empty(ne * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
         pin_lv = torch.from_numpy(etab.view(np.uint8).copy()).pin_memory()
@@ -331,9 +398,11 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg_json,
             "gpu_launches": 8 * args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_fp64["tflops"], "unit": "TFLOP/s",
-                         "frac": achieved / peak_fp64["tflops"], "traffic": DRAM_BYTES_PER_TRAJ * n,
+                         "frac": achieved / peak_fp64["tflops"],
+                         "traffic": DRAM_BYTES_PER_TRAJ * n if args.system == "n3" else None,
                          "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of a "
-                                           "98,304-trajectory launch (632 B per trajectory), scaled by trajectories",
+                                           "98,304-trajectory launch (632 B per trajectory), scaled by trajectories"
+                                           if args.system == "n3" else "not captured for this system",
                          "peak_source": peak_fp64["source"],
                          "kernel": "k_integrate3 (persistent Bulirsch-Stoer integrator)",
                          "kernel_ms_per_launch": integ_ms, "kernel_share_of_step": integ_ms * args.steps / ms,

@@ -953,6 +953,15 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
     if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1) + CAIR_NN_H1 + CAIR_NN_H2;
     return 0;
   }
+  if (m == CAIR_PES_O4_UMN) {
+    // six pairs: distances 72, TransToCart_4 110, Hamilton's equations 45, assembly 15; BS
+    // bookkeeping scales with the 18 equations
+    if (fg) *fg = PIP_O4_EVAL_REV_FLOPS + 6 * (diat_g + meg_g) + 72 + 110 + 45 + 15;
+    if (fe) *fe = PIP_O4_VALUE_FLOPS + 6 * (diat_e + meg_e) + 72 + 45 + 8;
+    if (fa) *fa = 811.0 * 18.0 / 12.0;
+    if (ex) *ex = 6.0 * ((o2 ? 8 : 1) + 1);
+    return 0;
+  }
   if (fg) *fg = pip_g + 3 * (diat_g + meg_g) + 36 + 46 + 18 + 15;
   if (fe) *fe = pip_e + 3 * (diat_e + meg_e) + 36 + 30 + 8;
   // per attempt outside the right-hand side: modified-midpoint updates (432), rational
