@@ -82,3 +82,56 @@ def test_statistics_on_synthetic_rows(gpu_lib, oracle_lib):
     with pytest.raises(api.CairError, match="cap too small"):
         api.Statistics(H).compute(items, rows, cap=8)
     H.close()
+
+
+def test_rate_coefficients_within_two_sigma_of_the_oracle_path(gpu_lib, oracle_lib):
+    """The same 600 initial conditions (one N2 + N run) propagated and analysed by the GPU path and
+    by the oracle: every final state's rate coefficient agrees within twice the combined Monte-Carlo
+    standard deviation (the acceptance criterion for rates), and the totals match."""
+    import os
+    import oracle
+    from oracle import Oracle
+    cfg = systems.n3_config(rmax=16.0)
+    H = api.Handle(cfg)
+    o = Oracle(cfg)
+    lv = systems.load_levels("N2")
+    rows_lv = lv[[300]]
+    table = api.level_table(rows_lv)
+    nt, seed, T = 600, api.process_seed(9, 1), 10000.0
+    items = api.work_items([(0, 0, nt, seed, T, 7.0, 15.0)])
+    rows = api.RunTrajectories(H).run(table, items)
+    # oracle path on the same stream
+    lvo = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax", "tau",
+                                                   "ri", "ro", "rlim")])
+    for c in lvo.dtype.names:
+        lvo[c] = rows_lv[c] if c in rows_lv.dtype.names else 0.0
+    ic = o.sample_ics(nt, lvo, seed=seed, ttra=T, bmax=7.0, dinit=15.0)
+    res = o.integrate(ic["paq"], ic["erra"], procs=min(16, os.cpu_count() or 1))
+    fi = o.analyze(ic["paq0"])
+    ff = o.analyze(o.apply_transformation(res["paq"]))
+    keep = (res["status"] == 0) & (np.abs(res["H"] - ic["H0"]) <= cfg.ham_abs_tol)
+    col = lambda fs, k: np.array([f[k] for f in fs])
+    qi = np.stack([col(fi, "angmom"), col(fi, "viba"), 16 * col(fi, "ipair") + col(fi, "itype") + 0.5], 1)
+    qf = np.stack([col(ff, "angmom"), col(ff, "viba"), 16 * col(ff, "ipair") + col(ff, "itype") + 0.5], 1)
+    ref, _ = oracle.statistics(np.full(keep.sum(), 7.0), ic["b"][keep], qi[keep], qf[keep], pres=(1, 0, 0),
+                               cap=nt)
+    m = cfg.masses
+    vel = oracle.mean_velocity(T, (m[0] + m[1]) * m[2] / sum(m))
+    got = api.Statistics(H, pres_even_odd=(1, 0, 0)).compute(items, rows)
+    g = {tuple(int(x) for x in r["fin"]): (r["rate"], r["rate_sd"]) for r in got}
+    r = {fs: (cross * vel, sd * vel) for fs, n, cross, sd in ref}
+    worst = 0.0
+    for fs in set(g) | set(r):
+        kg, sg = g.get(fs, (0.0, 0.0))
+        ko, so = r.get(fs, (0.0, 0.0))
+        sig = np.hypot(sg, so)
+        if sig == 0.0:
+            assert kg == ko
+            continue
+        worst = max(worst, abs(kg - ko) / sig)
+    tot_g, tot_o = sum(v[0] for v in g.values()), sum(v[0] for v in r.values())
+    print("rates: %d final states (GPU) / %d (oracle), worst |dk|/sigma %.3f, total %.6e vs %.6e" %
+          (len(g), len(r), worst, tot_g, tot_o))
+    assert worst <= 2.0
+    assert tot_g == pytest.approx(tot_o, rel=1e-12)
+    H.close()
