@@ -42,8 +42,10 @@ DRAM_BYTES_PER_TRAJ = 632.0
 TEMPS = (5000.0, 10000.0, 20000.0)
 
 
-def workload(ntraj, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=15.0):
-    """Level table and work items of the N2 + N configuration."""
+def workload(ntraj, rank=0, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=15.0):
+    """Level table and work items of the N2 + N configuration.  Replica `rank` draws its streams as
+    processes rank * nitems + 1 ... of the run (Collision_Class.F90:295-296), so replicas never repeat
+    each other's trajectories."""
     from coarseair_gb300 import api, systems
     lv = systems.load_levels("N2")
     rng = np.random.default_rng(seed_levels)
@@ -56,19 +58,19 @@ def workload(ntraj, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=15.0):
         for it, T in enumerate(TEMPS):
             k = il * len(TEMPS) + it
             n = base + (1 if k < extra else 0)
-            entries.append((il, 0, n, api.process_seed(iseed, k + 1), T, bmax, dinit))
+            entries.append((il, 0, n, api.process_seed(iseed, rank * nitems + k + 1), T, bmax, dinit))
     return table, api.work_items(entries)
 
 
-def workload_o3(ntraj):
+def workload_o3(ntraj, rank=0):
     """O2(v=0, J=1) + O on UMN_11A1: one state-specific run, seed 1, 10,000 K, b = 6 sqrt(U) bohr."""
     from coarseair_gb300 import api, systems
     lv = systems.load_levels("O2")
     row = lv[(lv["vqn"] == 0) & (lv["jqn"] == 1)]
-    return api.level_table(row), api.work_items([(0, 0, ntraj, api.process_seed(1, 1), 10000.0, 6.0, 15.0)])
+    return api.level_table(row), api.work_items([(0, 0, ntraj, api.process_seed(1, rank + 1), 10000.0, 6.0, 15.0)])
 
 
-def workload_o4(ntraj, npairs=64, seed_levels=3):
+def workload_o4(ntraj, rank=0, npairs=64, seed_levels=3):
     """O2 + O2 on the three O4 UMN surfaces: 64 (level, level) pairs drawn uniformly (seed 3) from the
     first 200 O2 levels, 10,000 K, b = 8 sqrt(U) bohr, Dinit 18 bohr; each pair's trajectories are
     split over the singlet, triplet and quintet surfaces in proportion to their degeneracies 1:3:5
@@ -85,7 +87,8 @@ def workload_o4(ntraj, npairs=64, seed_levels=3):
         split = [n * 1 // 9, n * 3 // 9]
         split.append(n - split[0] - split[1])
         for ip in range(3):
-            entries.append((int(a), ip, split[ip], api.process_seed(3, 3 * k + ip + 1), 10000.0, 8.0, 18.0, int(b)))
+            entries.append((int(a), ip, split[ip], api.process_seed(3, rank * 3 * npairs + 3 * k + ip + 1), 10000.0,
+                            8.0, 18.0, int(b)))
     return table, api.work_items(entries)
 
 
@@ -263,7 +266,7 @@ def main():
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
-    table, items = spec["workload"](args.ntraj)
+    table, items = spec["workload"](args.ntraj, rank)
     cores = host_cores()
     metric = "trajectories/s"
     cfg_json = {"workload": spec["text"],
@@ -360,10 +363,8 @@ def main():
     H.check(lib.cair_set_integrate_timing(H.h, 0), "cair_set_integrate_timing")
     integ_ms = float(np.mean(list(kt)[:nk.value]))
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * args.steps * world / (ms / 1e3)
+        ms = max_over_ranks(ms, dist, torch.tensor([0.0], device=dev))
+    value = aggregate_rate(n, args.steps, world, ms)
     res = np.frombuffer(res_bufs[(args.steps - 1) % len(streams)].cpu().numpy().tobytes(), dtype=_lib.RESULT_DTYPE)
     per_traj = res["iste"].astype(np.int64) + res["irej"]
     att = int(np.sum(per_traj))
@@ -375,7 +376,7 @@ def main():
     # e2e through the host entry point with pinned buffers
     e2e = None
     if not args.no_e2e:
-        etab, eitems = spec["workload"](args.e2e_ntraj)
+        etab, eitems = spec["workload"](args.e2e_ntraj, rank)
         ne = int(eitems["ntraj"].sum())
         pin_res = torch.empty(ne * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
         pin_lv = torch.from_numpy(etab.view(np.uint8).copy()).pin_memory()
@@ -426,6 +427,19 @@ def main():
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def max_over_ranks(value, dist, buf):
+    """The slowest replica's time: all_reduce(MAX) of one number through the tensor `buf` (a CUDA tensor
+    under NCCL, a CPU tensor under gloo)."""
+    buf.fill_(float(value))
+    dist.all_reduce(buf, op=dist.ReduceOp.MAX)
+    return float(buf.item())
+
+
+def aggregate_rate(ntraj_per_rank, steps, world, ms):
+    """Whole-job trajectories/s: every replica's trajectories over the slowest replica's time."""
+    return ntraj_per_rank * steps * world / (ms / 1e3)
 
 
 def fp64_peak_probe(lib, H):

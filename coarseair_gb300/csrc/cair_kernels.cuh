@@ -114,8 +114,14 @@ struct IntegrateArgs {
   const int32_t* order;         // queue position -> trajectory (NULL: identity)
 };
 
+// Minimum resident 64-thread blocks per SM the register allocation must allow (1: up to 255
+// registers per thread, 4 blocks fit; 6: at most 168 registers, more warps to hide FP64 latency).
+#ifndef CAIR_INTEGRATE_MIN_BLOCKS
+#define CAIR_INTEGRATE_MIN_BLOCKS 1
+#endif
+
 template <int MODEL, int NS>
-__global__ void __launch_bounds__(64) k_integrate(DevSys S, IntegrateArgs A) {
+__global__ void __launch_bounds__(64, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(DevSys S, IntegrateArgs A) {
   constexpr int NE = Traits<MODEL>::NE, NP = Traits<MODEL>::NP;
   unsigned long long c_att = 0, c_acc = 0, c_rej = 0;
   const bool incstp = S.incstp != 0;
