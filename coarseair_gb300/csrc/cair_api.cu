@@ -1101,6 +1101,59 @@ int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items,
                              h->stream);
 }
 
+struct cair_queue_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+int cair_queue_graph_create(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                            const cair_work_item* items, int64_t ntot, int64_t max_attempts,
+                            cair_traj_result* results, void* workspace, cair_queue_graph** out) {
+  if (!h || !out || !workspace) return fail(h, CAIR_EINVAL, "cair_queue_graph_create: bad argument (workspace required)");
+  *out = nullptr;
+  cudaStream_t st = nullptr;
+  CUDA_TRY(h, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  const bool timing = h->time_integrate;
+  h->time_integrate = false;  // event pairs are per call, not per replay
+  cudaGraph_t graph = nullptr;
+  int rc = 0;
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    rc = fail(h, CAIR_ECUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+  } else {
+    rc = cair_run_queue_dev(h, nlevels, levels, nitems, items, ntot, max_attempts, results, workspace, st);
+    e = cudaStreamEndCapture(st, &graph);  // always ends the capture, also after a failed call
+    if (rc == 0 && e != cudaSuccess) rc = fail(h, CAIR_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+  }
+  h->time_integrate = timing;
+  cudaGraphExec_t exec = nullptr;
+  if (rc == 0) {
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) rc = fail(h, CAIR_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  cudaStreamDestroy(st);
+  if (rc != 0) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc;
+  }
+  *out = new cair_queue_graph{graph, exec};
+  return 0;
+}
+
+int cair_queue_graph_launch(cair_handle* h, cair_queue_graph* g, void* stream) {
+  if (!h || !g || !g->exec) return fail(h, CAIR_EINVAL, "cair_queue_graph_launch: bad argument");
+  CUDA_TRY(h, cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  return 0;
+}
+
+void cair_queue_graph_destroy(cair_queue_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+}
+
 int cair_set_integrate_timing(cair_handle* h, int32_t on) {
   if (!h) return CAIR_EINVAL;
   h->time_integrate = on != 0;

@@ -279,6 +279,20 @@ int cair_run_queue_static_dev(cair_handle* h, int32_t nlevels, const cair_level*
                               const cair_work_item* items, int64_t ntot, int64_t max_attempts,
                               cair_traj_result* results, void* stream);
 
+/* CUDA graph of the queue path (no counterpart in the reference): cair_queue_graph_create captures
+ * cair_run_queue_dev(h, ..., workspace, stream) -- the eight kernel launches and the memsets between
+ * them -- once and instantiates it; cair_queue_graph_launch replays it on `stream`, reading the level
+ * table and work items and writing the result rows through the same device pointers every time
+ * (refill them between replays to run other batches of the same size).  The workspace is required
+ * (nothing may be allocated while capturing); replays on one workspace must not overlap.  The graph
+ * does not record cair_set_integrate_timing events. */
+typedef struct cair_queue_graph cair_queue_graph;
+int cair_queue_graph_create(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                            const cair_work_item* items, int64_t ntot, int64_t max_attempts,
+                            cair_traj_result* results, void* workspace, cair_queue_graph** graph);
+int cair_queue_graph_launch(cair_handle* h, cair_queue_graph* graph, void* stream);
+void cair_queue_graph_destroy(cair_queue_graph* graph);
+
 /* Final-state statistics of state-specific runs (app/TrajectoriesStats/Statistics_Class.F90,
  * "Final States Assigment Mthd = Histogram", three conditions J, v, arrangement, no identical
  * diatoms) and rate coefficients (Process_Class.F90:122-209 with the Boltzmann mean velocity of
