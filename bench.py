@@ -405,7 +405,7 @@ def main():
                                            "98,304-trajectory launch (632 B per trajectory), scaled by trajectories"
                                            if args.system == "n3" else "not captured for this system",
                          "peak_source": peak_fp64["source"],
-                         "kernel": "k_integrate3 (persistent Bulirsch-Stoer integrator)",
+                         "kernel": "k_integrate (persistent Bulirsch-Stoer integrator)",
                          "kernel_ms_per_launch": integ_ms, "kernel_share_of_step": integ_ms * args.steps / ms,
                          "work": "executed FP64 operations of the pruned formulation per step "
                                  "(exp, division and sqrt counted as one operation each)"},

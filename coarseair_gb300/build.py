@@ -51,6 +51,8 @@ def build(force=False, verbose=False, extra_flags=()):
     os.makedirs(BUILD, exist_ok=True)
     deps = _deps()
     if not force and not _newer(LIB, deps):
+        if _newer(EXAMPLE, [os.path.join(HERE, "examples", "cair_run.c"), LIB]):
+            build_example()
         return LIB
     cc = nvcc()
     objs = []
@@ -74,7 +76,26 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr[-4000:])
     os.replace(tmp, LIB)
+    build_example()
     return LIB
+
+
+EXAMPLE = os.path.join(HERE, "examples", "cair_run")
+
+
+def build_example():
+    """The C caller examples/cair_run.c, linked against the library with the host compiler."""
+    src = os.path.join(HERE, "examples", "cair_run.c")
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc or not os.path.exists(src):
+        return None
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
+    cmd = [cc, "-O2", "-std=c11", "-I", os.path.join(HERE, "..", "include"), src, "-o", EXAMPLE, "-L", HERE,
+           "-lcair_gpu", "-Wl,-rpath," + HERE, "-L", cuda_lib, "-lcudart", "-Wl,-rpath," + cuda_lib]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("example build failed:\n" + r.stderr[-4000:])
+    return EXAMPLE
 
 
 if __name__ == "__main__":
