@@ -262,6 +262,15 @@ def work_items(entries):
     return out
 
 
+def degeneracy_blocks(ntraj, degeneracies):
+    """Trajectories per surface of a batch, as SetPESIndx assigns them (Collision_Class.F90:2468-2507):
+    contiguous blocks of int(g_k / sum(g) * ntraj) for every surface but the last, which takes the rest."""
+    g = np.asarray(degeneracies, dtype=np.float64)
+    g = g / g.sum()
+    counts = [int(x * ntraj) for x in g[:-1]]
+    return counts + [ntraj - sum(counts)]
+
+
 def process_seed(iseed, iproc, npes=1, inode=1, rndnb=0):
     """Stream seed of process iProc (Collision_Class.F90:295-296)."""
     return int(iseed * (1 + (iproc - 1) * (npes + 1) + (inode - 1) * 200.0 * (npes + 1)) +

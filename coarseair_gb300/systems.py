@@ -178,6 +178,18 @@ def o3_config(model="UMN_11A1", mass_amu=15.9994, **kw):
     return SystemConfig("O2+O " + model, 3, (m, m, m), [load_o3_umn(model)], DIAT_O2_UMN, **kw)
 
 
+# input/O3/UMN/input/CoarseAIR.inp:116-134: the nine O3 UMN surfaces and their degeneracies
+O3_MIX = (("UMN_11A1", 1.0), ("UMN_11A2", 1.0), ("UMN_13A1", 3.0), ("UMN_13A2", 3.0), ("UMN_15A1", 5.0),
+          ("UMN_15A2", 5.0), ("UMN_21A1", 1.0), ("UMN_23A1", 3.0), ("UMN_25A1", 5.0))
+
+
+def o3_mix_config(mass_amu=15.9994, **kw):
+    """O2 + O on the nine O3 UMN surfaces of the reference's O3 input, degeneracies 1/1/3/3/5/5/1/3/5."""
+    m = mass_amu * AMU_TO_AU
+    return SystemConfig("O2+O UMN 9 surfaces", 3, (m, m, m), [load_o3_umn(name) for name, _ in O3_MIX], DIAT_O2_UMN,
+                        degeneracy=tuple(d for _, d in O3_MIX), **kw)
+
+
 def o3nn_config(model="NN_11A1_MPE", mass_amu=15.9994, **kw):
     """O2 + O on an O3 NN surface with the O2 UMN diatomic."""
     m = mass_amu * AMU_TO_AU

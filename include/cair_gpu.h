@@ -43,8 +43,8 @@
 extern "C" {
 #endif
 
-#define CAIR_MAX_PES 8
-#define CAIR_ABI_VERSION 2
+#define CAIR_MAX_PES 16
+#define CAIR_ABI_VERSION 3
 
 /* Surface models (PES_Factory_Class.F90:46-329, System x PES_Model strings). */
 enum cair_pes_model {
