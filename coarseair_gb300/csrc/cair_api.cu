@@ -382,7 +382,7 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
   }
   for (int p = 0; p < d->npes; ++p) {
     const cair_pes_desc& src = d->pes[p];
-    int expect = src.model == CAIR_PES_O3_UMN ? 56 : src.model == CAIR_PES_N3_UMN ? 276
+    int expect = src.model == CAIR_PES_O3_UMN ? 56 : (src.model == CAIR_PES_N3_UMN || src.model == CAIR_PES_N4_UMN) ? 276
                  : src.model == CAIR_PES_O4_UMN ? 430 : src.model == CAIR_PES_O3_NN ? 0 : -1;
     if (expect < 0) return bad(CAIR_EINVAL, "unknown surface model");
     std::vector<double> packed;
@@ -397,7 +397,8 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
       packed.assign(src.coef, src.coef + src.ncoef);
     }
     if (src.model != d->pes[0].model) return bad(CAIR_EUNSUPPORTED, "all surfaces of a handle must share a model");
-    if ((src.model == CAIR_PES_O4_UMN) != (d->natoms == 4)) return bad(CAIR_EINVAL, "surface/atom count mismatch");
+    if ((src.model == CAIR_PES_O4_UMN || src.model == CAIR_PES_N4_UMN) != (d->natoms == 4))
+      return bad(CAIR_EINVAL, "surface/atom count mismatch");
     DevPes& P = S.pes[p];
     P.model = src.model;
     P.ncoef = (int32_t)packed.size();
@@ -953,11 +954,13 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
     if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1) + CAIR_NN_H1 + CAIR_NN_H2;
     return 0;
   }
-  if (m == CAIR_PES_O4_UMN) {
+  if (m == CAIR_PES_O4_UMN || m == CAIR_PES_N4_UMN) {
     // six pairs: distances 72, TransToCart_4 110, Hamilton's equations 45, assembly 15; BS
     // bookkeeping scales with the 18 equations
-    if (fg) *fg = PIP_O4_EVAL_REV_FLOPS + 6 * (diat_g + meg_g) + 72 + 110 + 45 + 15;
-    if (fe) *fe = PIP_O4_VALUE_FLOPS + 6 * (diat_e + meg_e) + 72 + 45 + 8;
+    const double pg = m == CAIR_PES_O4_UMN ? PIP_O4_EVAL_REV_FLOPS : PIP_N4_EVAL_REV_FLOPS;
+    const double pe = m == CAIR_PES_O4_UMN ? PIP_O4_VALUE_FLOPS : PIP_N4_VALUE_FLOPS;
+    if (fg) *fg = pg + 6 * (diat_g + meg_g) + 72 + 110 + 45 + 15;
+    if (fe) *fe = pe + 6 * (diat_e + meg_e) + 72 + 45 + 8;
     if (fa) *fa = 811.0 * 18.0 / 12.0;
     if (ex) *ex = 6.0 * ((o2 ? 8 : 1) + 1);
     return 0;

@@ -161,6 +161,7 @@ __device__ __forceinline__ void diat(const DevSys& S, double r, double& v, doubl
 #include "generated/pip_n3.cuh"
 #include "generated/pip_o3.cuh"
 #include "generated/pip_o4.cuh"
+#include "generated/pip_n4.cuh"
 // gradient of the PIP part: reverse mode (adjoint sweep) unless CAIR_PIP_FORWARD selects the
 // forward mode, whose operation order is the reference's
 #ifdef CAIR_PIP_FORWARD
@@ -444,10 +445,43 @@ __device__ __forceinline__ void pes_o4(const DevSys& S, const DevPes& P, const d
   }
 }
 
+// N4 UMN (Compute_N4_UMN_PES_1d, N4_UMN_PES_Class.F90:329-361 -> n4pes 373-417): the N4 PIP on all
+// six MEG variables (the N3 surface is the same fit with three pairs pinned), six N2 diatomics.
+template <bool GRAD>
+__device__ __forceinline__ void pes_n4(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
+                                       const double* Q, double& V, double* dVdR, double* dVdQ) {
+  double x[6], dx[6], vd[6], dvd[6];
+  const double inv_ab = 1.0 / 1.5;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double d = R[i] * CAIR_B_TO_ANG - 1.098;
+    double e = fexp(-d - (d * d) * inv_ab);
+    x[i] = e;
+    if (GRAD) dx[i] = (-((2.0 * d) * inv_ab) - 1.0) * e;
+    diat<GRAD>(S, R[i], vd[i], dvd[i]);
+  }
+  double vdiat = 0.0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) vdiat = vdiat + vd[i];
+  double vp;
+  const double* __restrict__ C = P.coef;
+  if (GRAD) {
+    double g[6];
+    pip_n4_eval_rev(x, dx, C, 457.4, vp, g);
+    V = (vp * CAIR_KCM_TO_HARTREE + 0.0) + vdiat;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) dVdR[i] = g[i] * CAIR_KCM_TO_HARTREE * CAIR_B_TO_ANG + dvd[i];
+    trans_to_cart_4(S, Ri, Q, dVdR, dVdQ);
+  } else {
+    pip_n4_value(x, C, 457.4, vp);
+    V = (vp * CAIR_KCM_TO_HARTREE + 0.0) + vdiat;
+  }
+}
+
 // Sizes of a surface model's system: atoms, NEqtVar, NEqtTot, pairs
 template <int MODEL>
 struct Traits {
-  static constexpr int NA = MODEL == CAIR_PES_O4_UMN ? 4 : 3;
+  static constexpr int NA = (MODEL == CAIR_PES_O4_UMN || MODEL == CAIR_PES_N4_UMN) ? 4 : 3;
   static constexpr int NV = 3 * (NA - 1);
   static constexpr int NE = 2 * NV;
   static constexpr int NP = NA * (NA - 1) / 2;
@@ -459,6 +493,7 @@ __device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const doub
   if (MODEL == CAIR_PES_O3_UMN) pes_o3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else if (MODEL == CAIR_PES_O3_NN) pes_o3nn<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else if (MODEL == CAIR_PES_O4_UMN) pes_o4<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
+  else if (MODEL == CAIR_PES_N4_UMN) pes_n4<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else pes_n3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
 }
 

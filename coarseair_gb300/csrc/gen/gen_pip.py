@@ -252,6 +252,15 @@ def load_surfaces(ref):
     assert len(nums) == 276, len(nums)
     out["N3_C"] = [float(x.replace("D", "e").replace("d", "e")) for x in nums]
     out["N3_C_text"] = nums
+    # N4 UMN (N2 + N2): the same N4 PIP routines with its own inline coefficients
+    t = read(os.path.join(ref, "src/PESs/N4_UMN_PES_Class.F90"))
+    for sub in ("EvMono", "EvPoly", "evbas"):
+        assert subroutine_body(t, sub) == subroutine_body(read(os.path.join(ref, "src/PESs/N3_UMN_PES_Class.F90")),
+                                                            sub), "N4 UMN %s differs from the N3 file's" % sub
+    g = re.search(r"dimension\(276\)\s*,parameter\s*::\s*C\s*=\s*\(/(.*?)/\)", t, re.S | re.I)
+    nums = re.findall(r"[-+]?\d+\.\d*D[-+]?\d+", g.group(1), re.I)
+    assert len(nums) == 276, len(nums)
+    out["N4_C_text"] = nums
     return out
 
 
@@ -611,6 +620,18 @@ def main():
     info = emit_device_reverse(S, "O4", "pip_o4_eval_rev", zero_vars=set(), dirs=[0, 1, 2, 3, 4, 5], path=o4,
                                coeff_symbol="C")
     print("O4 reverse:", info)
+    # N4 UMN on the full N4 PIP (all six MEG variables live): energy and adjoint-sweep gradient
+    n4 = os.path.join(gen, "pip_n4.cuh")
+    with open(n4, "w") as f:
+        f.write("/* N4 UMN PIP (N4_UMN_PES_Class.F90 EvMono/EvPoly/evbas). Generated by gen_pip.py, do not edit. */\n")
+    info = emit_device(S, "N4", "pip_n4_value", zero_vars=set(), dirs=[], path=n4, coeff_symbol="C",
+                       value_only=True)
+    print("N4 value:", info)
+    info = emit_device_reverse(S, "N4", "pip_n4_eval_rev", zero_vars=set(), dirs=[0, 1, 2, 3, 4, 5], path=n4,
+                               coeff_symbol="C")
+    print("N4 reverse:", info)
+    # the N3 surface is this fit with three pairs pinned: one coefficient file serves both
+    assert S["N4_C_text"] == S["N3_C_text"], "N4 UMN coefficients differ from the N3 UMN ones"
     with open(os.path.join(REPO, "coarseair_gb300", "data", "N3_UMN.dat"), "w") as f:
         f.write("# N3 UMN surface (N4 PIP, MEG variables): 276 linear coefficients [kcal/mol]\n")
         f.write("# a = 1.0 Ang, ab = 1.5 Ang^2, re = 1.098 Ang, totdiss = 457.4 kcal/mol\n")

@@ -26,7 +26,7 @@ import numpy as np
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
 AMU_TO_AU = 1822.888486209          # [amu] -> electron masses (kgm_To_au / 1000)
-PES_O3_UMN, PES_N3_UMN, PES_O4_UMN, PES_O3_NN = 1, 2, 3, 4
+PES_O3_UMN, PES_N3_UMN, PES_O4_UMN, PES_O3_NN, PES_N4_UMN = 1, 2, 3, 4, 5
 DIAT_O2_UMN, DIAT_N2_UMN_FORN4 = 1, 2
 
 _FNUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[dDeE][-+]?\d+)?")
@@ -201,6 +201,22 @@ def n3_config(mass_amu=14.0067, **kw):
     m = mass_amu * AMU_TO_AU
     kw.setdefault("bmax", 7.0)
     return SystemConfig("N2+N UMN", 3, (m, m, m), [load_n3_umn()], DIAT_N2_UMN_FORN4, **kw)
+
+
+def load_n4_umn():
+    """N4 UMN (N4_UMN_PES_Class.F90): the N4 PIP on all six pairs with the same 276 coefficients as N3 UMN."""
+    n3 = load_n3_umn()
+    return Surface(PES_N4_UMN, n3.coef, 1.0, 1.5, 1.098, 1.098, 0.0, 457.4, name="N4 UMN")
+
+
+def n4_config(mass_amu=14.0067, **kw):
+    """N2 + N2 on the N4 UMN surface with the UMN_ForN4 N2 diatomic (Dinit 23 bohr and Stratified rings
+    up to 8 bohr as input/N4/UMN/input/CoarseAIR_VS_UMNDiat.inp; one ring of 8 bohr here)."""
+    m = mass_amu * AMU_TO_AU
+    kw.setdefault("bmax", 8.0)
+    kw.setdefault("dinit", 23.0)
+    kw.setdefault("rmax", 30.0)
+    return SystemConfig("N2+N2 UMN", 4, (m, m, m, m), [load_n4_umn()], DIAT_N2_UMN_FORN4, **kw)
 
 
 def o4_config(mass_amu=15.9994, **kw):

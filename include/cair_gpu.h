@@ -51,7 +51,8 @@ enum cair_pes_model {
   CAIR_PES_O3_UMN = 1, /* O3_UMN_PES_Class.F90  (System O3, Model UMN_*)            */
   CAIR_PES_N3_UMN = 2, /* N3_UMN_PES_Class.F90  (System N3, Model UMN)              */
   CAIR_PES_O4_UMN = 3, /* O4_UMN_PES_Class.F90  (System O4, Model UMN_Singlet/...)  */
-  CAIR_PES_O3_NN = 4   /* O3_NN_PES_Class.F90   (System O3, Model NN_*)             */
+  CAIR_PES_O3_NN = 4,  /* O3_NN_PES_Class.F90   (System O3, Model NN_*)             */
+  CAIR_PES_N4_UMN = 5  /* N4_UMN_PES_Class.F90  (System N4, Model UMN; 4 atoms)     */
 };
 
 /* Diatomic potentials of the pairs (DiatomicPotential_Factory_Class.F90:115-229). */
@@ -86,7 +87,7 @@ enum cair_traj_status {
  * hold NHL1 <= 20, NHL2 <= 10.  The MEG fields are unused. */
 typedef struct cair_pes_desc {
   int32_t model;       /* cair_pes_model                                      */
-  int32_t ncoef;       /* 56 (O3), 276 (N3), 430 (O4), see above (O3 NN)       */
+  int32_t ncoef;       /* 56 (O3), 276 (N3, N4), 430 (O4), see above (O3 NN)   */
   const double* coef;  /* C(1:ncoef) [kcal/mol], copied at cair_create        */
   double a, ab, ra, rb;/* MEG parameters [Ang, Ang^2, Ang, Ang] (O3, O4)      */
   double eref;         /* O4 file value (unused by the energy, as in the reference) */

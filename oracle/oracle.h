@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-enum { ORC_PES_O3_UMN = 1, ORC_PES_N3_UMN = 2, ORC_PES_O4_UMN = 3, ORC_PES_O3_NN = 4 };
+enum { ORC_PES_O3_UMN = 1, ORC_PES_N3_UMN = 2, ORC_PES_O4_UMN = 3, ORC_PES_O3_NN = 4, ORC_PES_N4_UMN = 5 };
 enum { ORC_DIAT_O2_UMN = 1, ORC_DIAT_N2_UMN_FORN4 = 2 };
 
 typedef struct orc_pes {

@@ -295,14 +295,17 @@ void orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale) {
     o3nn_scale(s, P, R, scale);
     return;
   }
-  if (P->model == ORC_PES_O4_UMN) {   /* scale[0] for V, scale[1..6] for the six pairs */
+  if (P->model == ORC_PES_O4_UMN || P->model == ORC_PES_N4_UMN) {   /* scale[0] for V, scale[1..6] per pair */
+    const int n4 = P->model == ORC_PES_N4_UMN;
     for (int i = 0; i < 6; ++i) {
-      double r = R[i] * B_TO_ANG, d1 = r - P->ra, d2 = r - P->rb;
-      double e = exp(-(d1 / P->a) - (d2 * d2) / P->ab);
-      rms[i] = e; dms[i] = (-(2.0 * d2 / P->ab) - 1.0 / P->a) * e;
+      double r = R[i] * B_TO_ANG;
+      double d1 = n4 ? r - 1.098 : r - P->ra, d2 = n4 ? r - 1.098 : r - P->rb;
+      double ia = n4 ? 1.0 : 1.0 / P->a, iab = n4 ? 1.0 / 1.5 : 1.0 / P->ab;
+      double e = exp(-(d1 * ia) - (d2 * d2) * iab);
+      rms[i] = e; dms[i] = (-(2.0 * d2 * iab) - ia) * e;
     }
-    orc_pip_scale(2, rms, dms, P->coef, sc);
-    scale[0] = sc[0] * KCM_TO_HARTREE;
+    orc_pip_scale(n4 ? 1 : 2, rms, dms, P->coef, sc);
+    scale[0] = (sc[0] + (n4 ? 457.4 : 0.0)) * KCM_TO_HARTREE;
     for (int i = 0; i < 6; ++i) {
       double sv, sdv;
       orc_diat_scale(s->diat, R[i], &sv, &sdv);
@@ -433,6 +436,32 @@ static void n3_compute(const orc_sys* s, const orc_pes* P, const double* R, cons
   dVdR[1] = dd[1] + dvp[1];
   dVdR[2] = dd[2] + dvp[3];
   trans_to_cart_3(s->mMiMn, R, Qall, dVdR, dVdQ);
+}
+
+/* N4 UMN: Compute_N4_UMN_PES_1d (N4_UMN_PES_Class.F90:329-361) -> n4pes (373-417): the N4 PIP on
+ * all six MEG variables, Eref = 0 (line 102), V = VTriat + VDiat. */
+static void n4_compute(const orc_sys* s, const orc_pes* P, const double* R, const double* Qall, double* V,
+                       double* dVdR, double* dVdQ) {
+  const double a = 1.0, ab = 1.5, re = 1.098, totdiss = 457.4, eref = 0.0;
+  double rms[6], dms[6], vp, dvp[6], vdiat = 0.0, dd[6];
+  for (int i = 0; i < 6; ++i) {
+    double v;
+    if (dVdR) orc_diat_VdV(s->diat, R[i], &v, &dd[i]);
+    else v = orc_diat_V(s->diat, R[i]);
+    vdiat = vdiat + v;
+  }
+  for (int i = 0; i < 6; ++i) {
+    double r = R[i] * B_TO_ANG, d = r - re;
+    double e = exp(-(d / a) - (d * d) / ab);          /* EvMorse 551-568 */
+    rms[i] = e;
+    dms[i] = (-(2.0 * d / ab) - 1.0 / a) * e;          /* EvdMsdR 573-599 */
+  }
+  orc_pip_eval(1, rms, dms, dVdR != 0, P->coef, totdiss, &vp, dvp);
+  double vt = vp * KCM_TO_HARTREE + eref;
+  *V = vt + vdiat;
+  if (!dVdR) return;
+  for (int i = 0; i < 6; ++i) dVdR[i] = dvp[i] * KCM_TO_HARTREE * B_TO_ANG + dd[i];
+  trans_to_cart_4(s->mMiMn, R, Qall, dVdR, dVdQ);
 }
 
 /* O4 UMN: Compute_O4_UMN_PES_1d (O4_UMN_PES_Class.F90:269-298) -> O4pes (310-370) */
@@ -640,6 +669,7 @@ void orc_pes_compute(const orc_sys* s, int ipes, const double* R, const double* 
   const orc_pes* P = &s->pes[ipes];
   if (P->model == ORC_PES_O3_UMN) o3_compute(s, P, R, Qall, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_N3_UMN) n3_compute(s, P, R, Qall, V, dVdR, dVdQ);
+  else if (P->model == ORC_PES_N4_UMN) n4_compute(s, P, R, Qall, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_O3_NN) {
     if (dVdR) o3nn_compute(s, P, R, Qall, V, dVdR, dVdQ);
     else *V = o3nn_potential(s, P, R);

@@ -13,7 +13,7 @@ from coarseair_gb300 import systems
 
 
 def _cfgs():
-    return [systems.o3_config(), systems.n3_config(), systems.o4_config()]
+    return [systems.o3_config(), systems.n3_config(), systems.o4_config(), systems.n4_config()]
 
 
 def _random_geometry(rng, natoms, n):
@@ -25,7 +25,7 @@ def _random_geometry(rng, natoms, n):
     return np.array(out)
 
 
-@pytest.mark.parametrize("idx", [0, 1, 2])
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
 def test_surface_gradient_matches_finite_differences(oracle_lib, idx):
     from oracle import Oracle
     cfg = _cfgs()[idx]
@@ -80,10 +80,11 @@ def test_three_atom_surfaces_are_permutation_invariant(oracle_lib, idx):
         assert np.allclose(o.potential(R[:, perm]), v, rtol=1e-12, atol=1e-13)
 
 
-def test_four_atom_surface_is_permutation_invariant(oracle_lib):
-    """O4: swapping atoms 1 <-> 2 maps pairs (12,13,14,23,24,34) -> (12,23,24,13,14,34)."""
+@pytest.mark.parametrize("idx", [2, 3])
+def test_four_atom_surface_is_permutation_invariant(oracle_lib, idx):
+    """O4, N4: swapping atoms 1 <-> 2 maps pairs (12,13,14,23,24,34) -> (12,23,24,13,14,34)."""
     from oracle import Oracle
-    o = Oracle(_cfgs()[2])
+    o = Oracle(_cfgs()[idx])
     R = np.array([[2.3, 3.1, 4.2, 3.6, 3.9, 2.4], [2.2, 5.0, 5.5, 4.7, 5.2, 2.3]])
     v = o.potential(R)
     assert np.allclose(o.potential(R[:, [0, 3, 4, 1, 2, 5]]), v, rtol=1e-11, atol=1e-12)
@@ -91,6 +92,18 @@ def test_four_atom_surface_is_permutation_invariant(oracle_lib):
     assert np.allclose(o.potential(R[:, [0, 2, 1, 4, 3, 5]]), v, rtol=1e-11, atol=1e-12)
     # molecules swapped (1,2) <-> (3,4): (12,13,14,23,24,34) -> (34,13,23,14,24,12)
     assert np.allclose(o.potential(R[:, [5, 1, 3, 2, 4, 0]]), v, rtol=1e-11, atol=1e-12)
+
+
+def test_n4_reduces_to_n3_with_a_distant_atom(oracle_lib):
+    """N4 UMN with atom 4 at 10^3 bohr from the others is the N3 UMN fit (the N3 surface is the N4
+    PIP with those pairs pinned at 10^3 bohr) plus the three far N2 diatomic terms."""
+    from oracle import Oracle
+    L = oracle_lib.lib()
+    o4, o3 = Oracle(systems.n4_config()), Oracle(systems.n3_config())
+    for r in ([2.1, 2.9, 3.7], [2.07, 4.0, 5.5]):
+        v3 = o3.potential(np.array([r]))[0]
+        v4 = o4.potential(np.array([[r[0], r[1], 1.0e3, r[2], 1.0e3, 1.0e3]]))[0]
+        assert abs(v4 - (v3 + 3 * L.orc_diat_V(2, 1.0e3))) < 1e-12
 
 
 def test_n3_dissociation_limit(oracle_lib):
