@@ -35,9 +35,9 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 # DRAM bytes per trajectory of the persistent integrator, measured with ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum = 62.16 MB for a 98,304-trajectory launch of this workload); the state is read
+# dram__bytes_write.sum = 69.13 MB for a 98,304-trajectory launch of this workload); the state is read
 # and written once per trajectory, so the full launch's traffic scales with the trajectory count
-DRAM_BYTES_PER_TRAJ = 632.0
+DRAM_BYTES_PER_TRAJ = 703.0
 
 TEMPS = (5000.0, 10000.0, 20000.0)
 
@@ -402,7 +402,7 @@ def main():
                          "frac": achieved / peak_fp64["tflops"],
                          "traffic": DRAM_BYTES_PER_TRAJ * n if args.system == "n3" else None,
                          "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of a "
-                                           "98,304-trajectory launch (632 B per trajectory), scaled by trajectories"
+                                           "98,304-trajectory launch (703 B per trajectory), scaled by trajectories"
                                            if args.system == "n3" else "not captured for this system",
                          "peak_source": peak_fp64["source"],
                          "kernel": "k_integrate (persistent Bulirsch-Stoer integrator)",
