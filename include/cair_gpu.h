@@ -230,7 +230,8 @@ int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* p
                        const double* erra, double* H, double* smax, double* smin, int32_t* irej, int32_t* iste,
                        int32_t* status, int64_t max_attempts, void* stream);
 
-/* Final-state analysis of n trajectory points (TrajectoryPoint%Analyze + FindState).
+/* Final-state analysis of n trajectory points (TrajectoryPoint%Analyze + SetPairs + FindState);
+ * four-atom points fill both molecules of cair_traj_point (a cluster gives iPair = -1).
  * paq_vel[n][NEqtTot] holds VELOCITIES and coordinates, i.e. PaQ after
  * Collision%ApplyTransformation (Collision_Class.F90:2406-2432) or PaQ0. */
 int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_point* out);
@@ -238,11 +239,13 @@ int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_
 /* ApplyTransformation on device: momenta -> velocities, in place on a copy. */
 int cair_apply_transformation(cair_handle* h, int64_t n, const double* paq, double* paq_vel);
 
-/* Initial conditions of diatom + atom trajectories on the device (SetIniCondForward,
- * Collision_Class.F90:1065-1211: level, BondLength vibrational phase, orientation, Boltzmann
- * translational energy, impact parameter, momenta, H0, error scales).  One device thread
- * per work item runs the item's random-number stream in the reference's draw order; one
- * thread per trajectory does the rest.  Host arrays; ntot = sum of items[].ntraj. */
+/* Initial conditions on the device (SetIniCondForward, Collision_Class.F90:1065-1211: level,
+ * BondLength vibrational phase, orientation, Boltzmann translational energy, impact parameter,
+ * momenta, H0, error scales) for diatom + atom systems (SetInitialState_DiatomAtom,
+ * StateInitDiatomAtom_Module.F90:90-231) and diatom + diatom systems (SetInitialState_DiatomDiatom,
+ * StateInitDiatomDiatom_Module.F90:86-219; the projectile's level is items[].ilevel2).  One device
+ * thread per work item runs the item's random-number stream in the reference's draw order; one
+ * thread per trajectory does the rest.  Host arrays of NEqtTot columns; ntot = sum of items[].ntraj. */
 int cair_sample_ics(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
                     const cair_work_item* items, int64_t ntot, double* paq, double* paq0, double* erra,
                     double* H0, double* b, int32_t* ipes);
@@ -252,7 +255,9 @@ int cair_sample_ics_dev(cair_handle* h, int32_t nlevels, const cair_level* level
 
 /* RunTrajectories for a set of work items, end to end on the GPU: initial conditions,
  * propagation (persistent kernel), ApplyTransformation, analysis of the initial and final
- * points and the trajectories.out rows.  Host arrays: results[ntot]. */
+ * points and the trajectories.out rows.  Host arrays: results[ntot].  Put every (level,
+ * temperature, surface) run of a computation into one call: the queue is ordered longest-first
+ * across all of them, which hides each run's slowest trajectories behind the others' work. */
 int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
                    const cair_work_item* items, int64_t ntot, int64_t max_attempts, cair_traj_result* results);
 /* The same on device pointers (levels, items, results on the device), asynchronous on
