@@ -36,6 +36,33 @@ def _i32(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
 
 
+def system_desc(cfg, tpq=None):
+    """cair_system_desc of a SystemConfig; returns it with the arrays it points into (keep them alive)."""
+    d = _lib.SystemDesc()
+    d.abi_version = _lib.CAIR_ABI_VERSION
+    d.natoms = cfg.natoms
+    d.npes = len(cfg.surfaces)
+    d.diat_model = cfg.diat_model
+    for i, m in enumerate(cfg.masses):
+        d.mass[i] = m
+    keep = []
+    for i, s in enumerate(cfg.surfaces):
+        c = np.ascontiguousarray(s.coef, dtype=np.float64)
+        keep.append(c)
+        p = d.pes[i]
+        p.model, p.ncoef, p.coef = s.model, c.size, dptr(c)
+        p.a, p.ab, p.ra, p.rb, p.eref, p.totdiss = s.a, s.ab, s.ra, s.rb, s.eref, s.totdiss
+    if tpq is not None:
+        t = np.asfortranarray(tpq, dtype=np.float64).ravel(order="F")
+        keep.append(t)
+        d.tpq = dptr(t)
+    d.dt0, d.eps, d.relax, d.rmax, d.tmax, d.ham_abs_tol = (cfg.dt0, cfg.eps, cfg.relax, cfg.rmax, cfg.tmax,
+                                                            cfg.ham_abs_tol)
+    d.nsteps, d.inc_step, d.ncall, d.nquad = cfg.nsteps, cfg.inc_step, cfg.ncall, cfg.nquad
+    d.rsmal, d.rcent, d.rfact, d.tthresau = cfg.rsmal, cfg.rcent, cfg.rfact, cfg.tthresau
+    return d, keep
+
+
 class Handle:
     """Owns one cair_handle (device copies of the surfaces, stream, scratch)."""
 
@@ -43,28 +70,7 @@ class Handle:
         lib = _lib.load()
         self.lib = lib
         self.cfg = cfg
-        d = _lib.SystemDesc()
-        d.abi_version = _lib.CAIR_ABI_VERSION
-        d.natoms = cfg.natoms
-        d.npes = len(cfg.surfaces)
-        d.diat_model = cfg.diat_model
-        for i, m in enumerate(cfg.masses):
-            d.mass[i] = m
-        self._keep = []
-        for i, s in enumerate(cfg.surfaces):
-            c = np.ascontiguousarray(s.coef, dtype=np.float64)
-            self._keep.append(c)
-            p = d.pes[i]
-            p.model, p.ncoef, p.coef = s.model, c.size, dptr(c)
-            p.a, p.ab, p.ra, p.rb, p.eref, p.totdiss = s.a, s.ab, s.ra, s.rb, s.eref, s.totdiss
-        if tpq is not None:
-            t = np.asfortranarray(tpq, dtype=np.float64).ravel(order="F")
-            self._keep.append(t)
-            d.tpq = dptr(t)
-        d.dt0, d.eps, d.relax, d.rmax, d.tmax, d.ham_abs_tol = (cfg.dt0, cfg.eps, cfg.relax, cfg.rmax,
-                                                                cfg.tmax, cfg.ham_abs_tol)
-        d.nsteps, d.inc_step, d.ncall, d.nquad = cfg.nsteps, cfg.inc_step, cfg.ncall, cfg.nquad
-        d.rsmal, d.rcent, d.rfact, d.tthresau = cfg.rsmal, cfg.rcent, cfg.rfact, cfg.tthresau
+        d, self._keep = system_desc(cfg, tpq)
         h = C.c_void_p()
         rc = lib.cair_create(C.byref(h), C.byref(d))
         self.h = h
