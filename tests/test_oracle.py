@@ -321,6 +321,28 @@ def test_initial_conditions_recover_sampled_level(oracle_lib):
             assert abs(f["angmom"] - (j + 0.5)) < 1e-6
 
 
+def test_diatom_diatom_initial_conditions_recover_both_levels(oracle_lib):
+    """Diatom + diatom sampler (SetInitialState_DiatomDiatom for each molecule, relative placement
+    with atom 4 eliminated) + the four-atom analysis on PaQ0: molecule 1 is pair 1-2 in the target's
+    level, molecule 2 the opposite pair 3-4 in the projectile's, and the impact parameter and
+    relative kinetic energy are the sampled ones."""
+    from oracle import Oracle
+    cfg = systems.o4_config(mass_amu=REF_MASS["O2"] / systems.AMU_TO_AU)
+    o = Oracle(cfg)
+    lv = systems.load_levels("O2")
+    for (v1, j1), (v2, j2) in (((0, 1), (0, 1)), ((2, 15), (5, 33))):
+        a = lv[(lv["vqn"] == v1) & (lv["jqn"] == j1)][0]
+        b = lv[(lv["vqn"] == v2) & (lv["jqn"] == j2)][0]
+        ic = o.sample_ics4(5, a, b, ttra=10000.0, bmax=8.0, dinit=18.0, seed=7)
+        for k, f in enumerate(o.analyze(ic["paq0"])):
+            assert (f["ipair"], f["ipair1"]) == (1, 6)
+            assert abs(f["angmom"] - (j1 + 0.5)) < 1e-6 and abs(f["angmom1"] - (j2 + 0.5)) < 1e-6
+            assert abs(f["viba"] - (v1 + 0.5)) < 2e-2 and abs(f["viba1"] - (v2 + 0.5)) < 2e-2
+            assert abs(f["b"] - ic["b"][k]) < 1e-9
+            # kinetic energy of the two centres of mass = the sampled relative translational energy
+            assert abs(f["xkin"] - ic["er"][k]) < 1e-10 * ic["er"][k]
+
+
 def test_integration_conserves_energy(oracle_lib):
     from oracle import Oracle
     cfg = systems.o3_config()
