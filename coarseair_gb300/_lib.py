@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcair_gpu.so")
 CAIR_MAX_PES = 16
-CAIR_ABI_VERSION = 3
+CAIR_ABI_VERSION = 4
 CAIR_STATIC_QUEUE_MAX_TRAJ = 16384
 
 STATUS = {0: "CAIR_OK", 1: "CAIR_EINVAL", 2: "CAIR_ECUDA", 3: "CAIR_ETIMEOUT", 4: "CAIR_ENONFINITE",
@@ -50,11 +50,11 @@ TRAJ_POINT_DTYPE = np.dtype([("ipair0", "i4"), ("itype0", "i4"), ("eint0", "f8")
                              ("vrel", "f8", (3,)), ("nmol", "i4"), ("pad", "i4")])
 
 class StatsParams(C.Structure):
-    _fields_ = [("qn_max", C.c_int32), ("iskip", C.c_int32 * 3), ("pres_even_odd", C.c_int32 * 3),
-                ("pad", C.c_int32), ("ham_abs_tol", C.c_double), ("xmu", C.c_double)]
+    _fields_ = [("qn_max", C.c_int32), ("ncond", C.c_int32), ("iskip", C.c_int32 * 5),
+                ("pres_even_odd", C.c_int32 * 5), ("ham_abs_tol", C.c_double), ("xmu", C.c_double)]
 
 
-FINAL_STATE_DTYPE = np.dtype([("item", "i4"), ("fin", "i4", 3), ("ini", "i4", 3), ("pad", "i4"), ("count", "i8"),
+FINAL_STATE_DTYPE = np.dtype([("item", "i4"), ("fin", "i4", 5), ("ini", "i4", 5), ("pad", "i4"), ("count", "i8"),
                               ("nrows", "i8"), ("cross", "f8"), ("cross_sd", "f8"), ("rate", "f8"),
                               ("rate_sd", "f8")])
 

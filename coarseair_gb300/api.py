@@ -362,23 +362,35 @@ def write_trajectories(directory, rows, ham_abs_tol, idx_offset=0, binary=None):
 
 
 class Statistics:
-    """TrajectoriesStats for state-specific runs (Statistics_Class.F90, Histogram assignment,
-    conditions J, v, arrangement): final-state cross sections [bohr^2] and rate coefficients
-    [cm^3/s] per work item, counted on the GPU.  Defaults are the reference's (QuantumNumberMax 300)
-    and its N3 input (Iskip 1, even/oddness preserved for J only: pres_even_odd=(1, 0, 0))."""
+    """TrajectoriesStats for state-specific runs (Statistics_Class.F90, Histogram assignment):
+    final-state cross sections [bohr^2] and rate coefficients [cm^3/s] per work item, counted on
+    the GPU.  Conditions are J, v, arrangement for diatom + atom and J1, v1, J2, v2, arrangement for
+    diatom + diatom (the reference's N4/O4 inputs, Identical Diatoms = no).  Defaults are the
+    reference's (QuantumNumberMax 300, Iskip 1, no even/oddness preserved); shorter iskip and
+    pres_even_odd tuples are padded with those defaults."""
 
-    def __init__(self, handle, qn_max=300, iskip=(1, 1, 1), pres_even_odd=(0, 0, 0), ham_abs_tol=None, xmu=None):
+    def __init__(self, handle, qn_max=300, iskip=(1, 1, 1, 1, 1), pres_even_odd=(0, 0, 0, 0, 0), ham_abs_tol=None,
+                 xmu=None):
         self.H = handle
         cfg = handle.cfg
         m = cfg.masses
+        ncond = 5 if cfg.natoms == 4 else 3
+        iskip = tuple(iskip) + (1,) * (5 - len(iskip))
+        pres_even_odd = tuple(pres_even_odd) + (0,) * (5 - len(pres_even_odd))
         p = _lib.StatsParams()
         p.qn_max = int(qn_max)
-        for i in range(3):
-            p.iskip[i] = int(iskip[i])
-            p.pres_even_odd[i] = int(bool(pres_even_odd[i]))
+        p.ncond = ncond
+        for i in range(5):
+            p.iskip[i] = int(iskip[i]) if i < ncond else 0
+            p.pres_even_odd[i] = int(bool(pres_even_odd[i])) if i < ncond else 0
         p.ham_abs_tol = float(cfg.ham_abs_tol if ham_abs_tol is None else ham_abs_tol)
-        # RedMass of the relative translation: diatom (atoms 1, 2) against atom 3
-        p.xmu = float(xmu if xmu is not None else (m[0] + m[1]) * m[2] / (m[0] + m[1] + m[2]))
+        # RedMass of the relative translation, target against projectile (Collision_Class.F90:454):
+        # diatom (atoms 1, 2) against atom 3, or against the diatom (atoms 3, 4)
+        if xmu is None:
+            mt, mp = m[0] + m[1], sum(m[2:])
+            xmu = mt * mp / (mt + mp)
+        p.xmu = float(xmu)
+        self.ncond = ncond
         self.params = p
 
     def compute(self, items, rows, cap=None):

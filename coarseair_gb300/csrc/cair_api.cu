@@ -981,7 +981,14 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
       !nout)
     return fail(h, CAIR_EINVAL, "cair_statistics: bad argument");
   const cair_stats_params& P = *params;
-  if (P.qn_max < 2 || P.qn_max > 1625) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max must be 2..1625");
+  const int nc = P.ncond;
+  if (nc != 3 && nc != 5) return fail(h, CAIR_EINVAL, "cair_statistics: ncond must be 3 or 5");
+  if (nc != (h->sys.natoms == 4 ? 5 : 3))
+    return fail(h, CAIR_EINVAL, "cair_statistics: ncond must be 3 for diatom + atom, 5 for diatom + diatom");
+  // codes lie within +-70 qn_max^ncond; with the item folded in they must stay inside a signed 64-bit key
+  double span = 70.0 * (double)nitems;
+  for (int c = 0; c < nc; ++c) span *= (double)P.qn_max;
+  if (P.qn_max < 2 || span >= 4.6e18) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max out of range");
   *nout = 0;
   if (ntot == 0) return 0;
   // table at least twice the rows, so linear probing always finds a slot
@@ -1010,10 +1017,21 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   CUDA_TRY(h, cudaMemsetAsync(item_rows, 0, (size_t)nitems * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(item_ini, 0x7f, (size_t)nitems * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(dn, 0, 16, st));
-  StatsArgs A{ntot, results, P.qn_max, {P.iskip[0], P.iskip[1], P.iskip[2]},
-              {P.pres_even_odd[0], P.pres_even_odd[1], P.pres_even_odd[2]}, P.ham_abs_tol, keys, counts, tsize - 1,
-              item_rows, item_ini, derr};
-  k_stats_count<<<grid_for(h, ntot), 256, 0, st>>>(A);
+  StatsArgs A{ntot,
+              results,
+              P.qn_max,
+              {P.iskip[0], P.iskip[1], P.iskip[2], P.iskip[3], P.iskip[4]},
+              {P.pres_even_odd[0], P.pres_even_odd[1], P.pres_even_odd[2], P.pres_even_odd[3], P.pres_even_odd[4]},
+              P.ham_abs_tol,
+              (unsigned long long)nitems,
+              keys,
+              counts,
+              tsize - 1,
+              item_rows,
+              item_ini,
+              derr};
+  if (nc == 3) k_stats_count<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
+  else k_stats_count<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
   k_stats_compact<<<grid_for(h, (int64_t)tsize), 256, 0, st>>>(keys, counts, tsize, okeys, ocounts,
                                                                (unsigned long long)cap, dn);
   if (int e = check_launch(h)) return e;
@@ -1026,7 +1044,8 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   CUDA_TRY(h, cudaMemcpyAsync(rows.data(), item_rows, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(ini.data(), item_ini, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaStreamSynchronize(st));
-  if (err) return fail(h, CAIR_EINVAL, "cair_statistics: a quantum number is at or above qn_max");
+  if (err == 1) return fail(h, CAIR_EINVAL, "cair_statistics: a quantum number is at or above qn_max");
+  if (err) return fail(h, CAIR_EINVAL, "cair_statistics: a final-state code of -1 on the last item");
   if ((long long)n > cap)
     return fail(h, CAIR_EINVAL, "cair_statistics: cap too small, " + std::to_string(n) + " final states");
   std::vector<unsigned long long> k(n), cnt(n);
@@ -1037,23 +1056,35 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   }
   std::vector<size_t> ord(n);
   for (size_t i = 0; i < n; ++i) ord[i] = i;
-  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return k[a] < k[b]; });
-  const long long qn = P.qn_max, ifacts = qn * qn * qn;
+  // key = code x nitems + item, with the code possibly negative: decode as a signed number
+  std::vector<long long> kitem(n), kcode(n);
+  for (size_t i = 0; i < n; ++i) {
+    const long long ks = (long long)k[i], ni = nitems;
+    kitem[i] = ((ks % ni) + ni) % ni;
+    kcode[i] = (ks - kitem[i]) / ni;
+  }
+  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+    return kitem[a] != kitem[b] ? kitem[a] < kitem[b] : kcode[a] < kcode[b];
+  });
+  const long long qn = P.qn_max;
+  long long ifacts = 1;
+  for (int c = 0; c < nc; ++c) ifacts *= qn;
   // Boltzmann mean velocity (Collision_Class.F90:576-595), per bohr^2 -> cm^3/s
   const double pi = std::acos(-1.0), k_to_h = 1.0 / 3.1577513e5, bohr_cm = 0.5291771e-8;
   for (size_t o = 0; o < n; ++o) {
     const size_t i = ord[o];
-    const int item = (int)(k[i] >> 32);
-    const long long code = (long long)(k[i] & 0xffffffffull);
+    const int item = (int)kitem[i];
+    const long long code = kcode[i];
     if (item < 0 || item >= nitems) return fail(h, CAIR_EINVAL, "cair_statistics: row with an item out of range");
     cair_final_state& F = out[o];
     F.item = item;
     F.count = (int64_t)cnt[i];
     F.nrows = (int64_t)rows[item];
     F.pad = 0;
+    for (int c = 0; c < 5; ++c) F.ini[c] = F.fin[c] = 0;
     // IniState from the smallest initial code of the item (ProcessStatistics, 782-929)
     long long isum = ini[item], ifact = ifacts;
-    for (int cnd = 2; cnd >= 0; --cnd) {
+    for (int cnd = nc - 1; cnd >= 0; --cnd) {
       ifact /= qn;
       const long long t = isum / ifact;
       F.ini[cnd] = (int)(t - 2);
@@ -1067,14 +1098,14 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
     const double fw = (double)F.count / per;
     F.cross = area * fw;
     F.cross_sd = std::sqrt(fw * (1.0 - fw) * area * area / per);
-    const int ini_arr = F.ini[2] / 16;
+    const int ini_arr = F.ini[nc - 1] / 16;
     isum = code;
     ifact = ifacts;
     int fin_arr = 0;
-    for (int cnd = 2; cnd >= 0; --cnd) {
+    for (int cnd = nc - 1; cnd >= 0; --cnd) {
       ifact /= qn;
       long long fc = isum / ifact;
-      if (cnd == 2) fin_arr = (int)((fc - 2) / 16);
+      if (cnd == nc - 1) fin_arr = (int)((fc - 2) / 16);
       isum -= fc * ifact;
       fc -= 2;
       if (P.pres_even_odd[cnd] && ini_arr == fin_arr) {

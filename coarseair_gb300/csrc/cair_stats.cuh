@@ -1,5 +1,5 @@
 // Final-state statistics on the device (app/TrajectoriesStats/Statistics_Class.F90, Histogram
-// assignment, three conditions J, v, arrangement): each finished trajectory's row is turned into
+// assignment, conditions J, v, arrangement or J1, v1, J2, v2, arrangement): each finished trajectory's row is turned into
 // its initial- and final-state codes where it lies in HBM, and the rows are counted per
 // (work item, final state) in an open-addressing table, so the cross sections need only the table
 // back on the host instead of the million trajectories.out rows.
@@ -12,31 +12,46 @@ struct StatsArgs {
   int64_t ntot;
   const cair_traj_result* rows;
   int32_t qnmax;
-  int32_t iskip[3];
-  int32_t pres[3];
+  int32_t iskip[5];
+  int32_t pres[5];
   double ham_abs_tol;
-  unsigned long long* keys;       // table: (item << 32) | final-state code, ~0 = empty
+  unsigned long long nitems;      // table key = final-state code x nitems + item
+  unsigned long long* keys;       // ~0 = empty
   unsigned long long* counts;
   unsigned long long mask;        // table size - 1 (a power of two)
   unsigned long long* item_rows;  // rows of each item in the statistics (TrajsPerb)
   long long* item_inicode;        // smallest initial-state code of each item (IniStateCode(1))
-  int* error;                     // set to 1: a quantum number at or above qnmax
+  int* error;                     // 1: a quantum number at or above qnmax; 2: an unrepresentable key
 };
 
 constexpr unsigned long long kStatsEmpty = ~0ull;
 
+// The NC conditions of a row, in trajectories.csv order: J, v, arr (3 atoms) or J1, v1, J2, v2, arr.
+template <int NC>
+__device__ __forceinline__ void stats_conditions(const cair_traj_result& r, double (&qi)[NC], double (&qf)[NC]) {
+  if (NC == 3) {
+    qi[0] = r.j_i; qi[1] = r.v_i; qi[NC - 1] = r.arr_i;
+    qf[0] = r.j_f; qf[1] = r.v_f; qf[NC - 1] = r.arr_f;
+  } else {
+    qi[0] = r.j_i; qi[1] = r.v_i; qi[2 % NC] = r.j2_i; qi[3 % NC] = r.v2_i; qi[NC - 1] = r.arr_i;
+    qf[0] = r.j_f; qf[1] = r.v_f; qf[2 % NC] = r.j2_f; qf[3 % NC] = r.v2_f; qf[NC - 1] = r.arr_f;
+  }
+}
+
 // IdentifyInitialStates (Statistics_Class.F90:591-680) for one row and the final-state code of
 // AddFinState's Histogram branch (935-1282).  Fortran nint rounds half away from zero (llround);
 // Fortran mod takes the sign of the dividend, as C's % does.
+template <int NC>
 __device__ __forceinline__ void stats_codes(const StatsArgs& A, const cair_traj_result& r, long long& ini_code,
                                             long long& fin_code, bool& bad) {
-  double qi[3] = {r.j_i, r.v_i, r.arr_i}, qf[3] = {r.j_f, r.v_f, r.arr_f};
+  double qi[NC], qf[NC];
+  stats_conditions<NC>(r, qi, qf);
   const long long qnmax = A.qnmax;
-  const int ipair_ini = (int)((qi[2] - 0.49) / 16);
-  const int ipair_fin = (int)((qf[2] - 0.49) / 16);
+  const int ipair_ini = (int)((qi[NC - 1] - 0.49) / 16);
+  const int ipair_fin = (int)((qf[NC - 1] - 0.49) / 16);
   long long ifact = 1, isum = 0;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
+  for (int c = 0; c < NC; ++c) {
     qi[c] = qi[c] - 0.5;
     long long ini = llround(qi[c]);
     if (ini >= qnmax) bad = true;
@@ -57,10 +72,10 @@ __device__ __forceinline__ void stats_codes(const StatsArgs& A, const cair_traj_
   long long fsum = 0;
   ifact = 1;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
+  for (int c = 0; c < NC; ++c) {
     long long iquse = llround(qf[c]) * A.iskip[c];
     if (iquse + 2 > qnmax) iquse = 0;
-    if (A.iskip[c] != 0 || c == 2) fsum = fsum + (iquse + 2) * ifact;
+    if (A.iskip[c] != 0 || c == NC - 1) fsum = fsum + (iquse + 2) * ifact;
     ifact = ifact * qnmax;
   }
   fin_code = fsum;
@@ -78,18 +93,24 @@ __device__ __forceinline__ unsigned long long stats_hash(unsigned long long k) {
 #ifndef CAIR_MODEL_TU
 // Rows that enter the statistics: finished trajectories whose energy is conserved (the others go
 // to trajectories_HNotCons.out, Integrator_Class.F90:755-776, 884-888).
+template <int NC>
 __global__ void __launch_bounds__(256) k_stats_count(StatsArgs A) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < A.ntot; k += (int64_t)gridDim.x * blockDim.x) {
     const cair_traj_result r = A.rows[k];
     if (r.status != CAIR_TRAJ_DONE || !(fabs(r.dH) <= A.ham_abs_tol)) continue;
     long long ic, fc;
     bool bad = false;
-    stats_codes(A, r, ic, fc, bad);
+    stats_codes<NC>(A, r, ic, fc, bad);
     if (bad) atomicExch(A.error, 1);
     atomicAdd(A.item_rows + r.item, 1ull);
     atomicMin(A.item_inicode + r.item, ic);
-    // fc < qnmax^3 < 2^32 (qnmax <= 1625 is checked on the host)
-    const unsigned long long key = ((unsigned long long)(uint32_t)r.item << 32) | (unsigned long long)fc;
+    // |fc| < 70 qnmax^NC (a cluster's arrangement code is negative), and 70 qnmax^NC x nitems < 2^62
+    // is checked on the host: the key is fc x nitems + item as a two's-complement 64-bit number
+    const unsigned long long key = (unsigned long long)fc * A.nitems + (unsigned long long)r.item;
+    if (key == kStatsEmpty) {  // fc = -1 on the last item: not representable in the table
+      atomicExch(A.error, 2);
+      continue;
+    }
     unsigned long long h = stats_hash(key) & A.mask;
     for (unsigned long long probe = 0; probe <= A.mask; ++probe) {  // the table is at least twice the rows
       const unsigned long long old = atomicCAS(A.keys + h, kStatsEmpty, key);

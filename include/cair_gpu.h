@@ -44,7 +44,7 @@ extern "C" {
 #endif
 
 #define CAIR_MAX_PES 16
-#define CAIR_ABI_VERSION 3
+#define CAIR_ABI_VERSION 4
 
 /* Surface models (PES_Factory_Class.F90:46-329, System x PES_Model strings). */
 enum cair_pes_model {
@@ -300,24 +300,26 @@ int cair_queue_graph_launch(cair_handle* h, cair_queue_graph* graph, void* strea
 void cair_queue_graph_destroy(cair_queue_graph* graph);
 
 /* Final-state statistics of state-specific runs (app/TrajectoriesStats/Statistics_Class.F90,
- * "Final States Assigment Mthd = Histogram", three conditions J, v, arrangement, no identical
- * diatoms) and rate coefficients (Process_Class.F90:122-209 with the Boltzmann mean velocity of
+ * "Final States Assigment Mthd = Histogram", "Identical Diatoms? = no"; three conditions J, v,
+ * arrangement for diatom + atom, five J1, v1, J2, v2, arrangement for diatom + diatom) and rate
+ * coefficients (Process_Class.F90:122-209 with the Boltzmann mean velocity of
  * Collision_Class.F90:576-595).  Each work item is one run; its rows are the finished trajectories
  * whose |dH| <= ham_abs_tol (the rest are the HNotCons rows).  One impact-parameter ring per item. */
 typedef struct cair_stats_params {
-  int32_t qn_max;            /* QuantumNumberMax (300 in the reference), at most 1625          */
-  int32_t iskip[3];          /* "Iskip for Condition 1..3"                                      */
-  int32_t pres_even_odd[3];  /* "Preserving Even / Oddness of Condition 1..3?" (0/1)           */
-  int32_t pad;
+  int32_t qn_max;            /* QuantumNumberMax (300 in the reference)                         */
+  int32_t ncond;             /* "Nb of Final Conditions": 3 (J, v, arr) or 5 (J1, v1, J2, v2, arr) */
+  int32_t iskip[5];          /* "Iskip for Condition 1..ncond"                                  */
+  int32_t pres_even_odd[5];  /* "Preserving Even / Oddness of Condition 1..ncond?" (0/1)       */
   double ham_abs_tol;        /* "Tolerance on Hamiltonian" [Eh]                                 */
   double xmu;                /* reduced mass of the relative translation [a.u.] (RedMass)      */
 } cair_stats_params;
 
-/* One line of the statistics output (FinCondVec, IniState, Cross, CrossSD) plus its rate. */
+/* One line of the statistics output (FinCondVec, IniState, Cross, CrossSD) plus its rate;
+ * conditions beyond ncond are zero. */
 typedef struct cair_final_state {
   int32_t item;              /* work item                                                       */
-  int32_t fin[3];            /* FinCondVec: J, v, arrangement code                              */
-  int32_t ini[3];            /* IniState                                                        */
+  int32_t fin[5];            /* FinCondVec: J, v, arrangement or J1, v1, J2, v2, arrangement    */
+  int32_t ini[5];            /* IniState                                                        */
   int32_t pad;
   int64_t count;             /* rows that ended in this state                                   */
   int64_t nrows;             /* rows of the item in the statistics (TrajsPerb)                  */

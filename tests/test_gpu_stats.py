@@ -10,26 +10,33 @@ from coarseair_gb300 import _lib, api, systems
 pytestmark = pytest.mark.gpu
 
 
+def _conds(rows, sel, natoms, which):
+    names = ("j", "v", "arr") if natoms == 3 else ("j", "v", "j2", "v2", "arr")
+    return np.stack([rows[nm + "_" + which][sel] for nm in names], 1)
+
+
 def _compare(H, items, rows, pres, st):
     import oracle
     cfg = H.cfg
     m = cfg.masses
-    xmu = (m[0] + m[1]) * m[2] / sum(m)
+    nc = 3 if cfg.natoms == 3 else 5
+    mt, mp = m[0] + m[1], sum(m[2:])
+    xmu = mt * mp / (mt + mp)
     got = st.compute(items, rows)
+    assert np.all(got["fin"][:, nc:] == 0) and np.all(got["ini"][:, nc:] == 0)
     keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= cfg.ham_abs_tol)
     for i, it in enumerate(items):
         sel = keep & (rows["item"] == i)
         ref, ini = oracle.statistics(np.full(sel.sum(), it["bmax"]), rows["b"][sel],
-                                     np.stack([rows["j_i"][sel], rows["v_i"][sel], rows["arr_i"][sel]], 1),
-                                     np.stack([rows["j_f"][sel], rows["v_f"][sel], rows["arr_f"][sel]], 1),
-                                     pres=pres, cap=max(64, int(sel.sum())))
+                                     _conds(rows, sel, cfg.natoms, "i"), _conds(rows, sel, cfg.natoms, "f"),
+                                     iskip=(1,) * nc, pres=pres, cap=max(64, int(sel.sum())))
         g = got[got["item"] == i]
         assert len(g) == len(ref)
-        gd = {tuple(int(x) for x in r["fin"]): r for r in g}
+        gd = {tuple(int(x) for x in r["fin"][:nc]): r for r in g}
         vel = oracle.mean_velocity(it["ttra"], xmu)
         for fs, n, cross, sd in ref:
             r = gd[fs]
-            assert tuple(int(x) for x in r["ini"]) == ini
+            assert tuple(int(x) for x in r["ini"][:nc]) == ini
             assert r["count"] == n and r["nrows"] == sel.sum()
             assert r["cross"] == pytest.approx(cross, rel=1e-14)
             assert r["cross_sd"] == pytest.approx(sd, rel=1e-14, abs=1e-300)
@@ -84,6 +91,59 @@ def test_statistics_on_synthetic_rows(gpu_lib, oracle_lib):
     H.close()
 
 
+def test_statistics_on_synthetic_diatom_diatom_rows(gpu_lib, oracle_lib):
+    """Five conditions (J1, v1, J2, v2, arrangement) as for O2 + O2: 100k rows over 4 items with
+    exchange arrangements, one-molecule dissociation and four-atom clusters (arrangement -65.5,
+    a negative final-state code), against the oracle with and without even/oddness preserved."""
+    cfg = systems.o4_config()
+    H = api.Handle(cfg)
+    rng = np.random.default_rng(33)
+    n, nitems = 100000, 4
+    rows = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    rows["item"] = rng.integers(0, nitems, n)
+    rows["j_i"] = 1.5 + 2.0 * rows["item"]
+    rows["v_i"] = 0.5
+    rows["j2_i"] = 3.5 + 4.0 * (rows["item"] % 2)
+    rows["v2_i"] = 0.5 + (rows["item"] >= 2)
+    rows["arr_i"] = 16.0 + 2.0 + 4.0 * 2.0 + 0.5       # iPair 1, both molecules bound (itype 2)
+    rows["j_f"] = rng.uniform(-1.0, 40.0, n)
+    rows["v_f"] = rng.uniform(-1.0, 8.0, n)
+    rows["j2_f"] = rng.uniform(-1.0, 40.0, n)
+    rows["v2_f"] = rng.uniform(-1.0, 8.0, n)
+    arr = rng.choice([26.5, 42.5, 58.5, 22.5, 18.5, 17.5, -65.5], n)
+    rows["arr_f"] = arr
+    for c in ("j_f", "v_f", "j2_f", "v2_f"):
+        rows[c] = np.where(arr == -65.5, -0.5, rows[c])
+    rows["b"] = rng.uniform(0.0, 8.0, n)
+    rows["status"] = np.where(rng.uniform(size=n) < 0.01, 1, 0)
+    rows["dH"] = np.where(rng.uniform(size=n) < 0.01, 1.0, 1e-9)
+    items = np.zeros(nitems, dtype=_lib.ITEM_DTYPE)
+    items["bmax"] = 8.0
+    items["ttra"] = [5000.0, 10000.0, 15000.0, 20000.0]
+    got = _compare(H, items, rows, (1, 0, 1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 1, 0, 0)))
+    assert np.any(got["fin"][:, 4] < 0)
+    _compare(H, items, rows, (0, 0, 0, 0, 0), api.Statistics(H))
+    H.close()
+
+
+def test_statistics_of_an_o2_o2_queue_run(gpu_lib, oracle_lib):
+    """Rows of a real O2 + O2 queue run (two items, the three O4 surfaces) through the device
+    statistics and through the oracle's: identical final states, counts and cross sections."""
+    cfg = systems.o4_config()
+    H = api.Handle(cfg)
+    lv = systems.load_levels("O2")
+    il = [int(np.flatnonzero((lv["vqn"] == 0) & (lv["jqn"] == j))[0]) for j in (1, 3)]
+    table = api.level_table(lv[il])
+    items = api.work_items([(0, 0, 48, api.process_seed(5, 1), 10000.0, 8.0, 18.0, 1),
+                            (1, 1, 48, api.process_seed(5, 2), 20000.0, 8.0, 18.0, 0)])
+    rows = api.RunTrajectories(H).run(table, items)
+    got = _compare(H, items, rows, (0, 0, 0, 0, 0), api.Statistics(H))
+    for i in range(len(items)):
+        g = got[got["item"] == i]
+        assert g["count"].sum() == g["nrows"][0]
+    H.close()
+
+
 def test_rate_coefficients_within_two_sigma_of_the_oracle_path(gpu_lib, oracle_lib):
     """The same 600 initial conditions (one N2 + N run) propagated and analysed by the GPU path and
     by the oracle: every final state's rate coefficient agrees within twice the combined Monte-Carlo
@@ -118,7 +178,7 @@ def test_rate_coefficients_within_two_sigma_of_the_oracle_path(gpu_lib, oracle_l
     m = cfg.masses
     vel = oracle.mean_velocity(T, (m[0] + m[1]) * m[2] / sum(m))
     got = api.Statistics(H, pres_even_odd=(1, 0, 0)).compute(items, rows)
-    g = {tuple(int(x) for x in r["fin"]): (r["rate"], r["rate_sd"]) for r in got}
+    g = {tuple(int(x) for x in r["fin"][:3]): (r["rate"], r["rate_sd"]) for r in got}
     r = {fs: (cross * vel, sd * vel) for fs, n, cross, sd in ref}
     worst = 0.0
     for fs in set(g) | set(r):
@@ -168,7 +228,7 @@ def test_config1_rates_within_two_sigma(gpu_lib, oracle_lib):
     m = cfg.masses
     vel = oracle.mean_velocity(T, (m[0] + m[1]) * m[2] / sum(m))
     got = api.Statistics(H).compute(items, rows)
-    g = {tuple(int(x) for x in r["fin"]): (r["rate"], r["rate_sd"]) for r in got}
+    g = {tuple(int(x) for x in r["fin"][:3]): (r["rate"], r["rate_sd"]) for r in got}
     r = {fs: (cross * vel, sd * vel) for fs, n, cross, sd in ref}
     dev = []
     for fs in set(g) | set(r):
