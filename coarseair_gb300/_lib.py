@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcair_gpu.so")
 CAIR_MAX_PES = 16
-CAIR_ABI_VERSION = 4
+CAIR_ABI_VERSION = 5
 CAIR_STATIC_QUEUE_MAX_TRAJ = 16384
 
 STATUS = {0: "CAIR_OK", 1: "CAIR_EINVAL", 2: "CAIR_ECUDA", 3: "CAIR_ETIMEOUT", 4: "CAIR_ENONFINITE",
@@ -99,9 +99,9 @@ SIGNATURES = [
     ("cair_statistics", C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L]),
     ("cair_statistics_dev", C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L,
                                       _P]),
-    ("cair_format_rows", C.c_int, [_P, C.c_int64, C.c_int64, C.c_int32, C.c_char_p, C.c_int64, _L]),
-    ("cair_write_trajectories", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_double, _L]),
-    ("cair_write_trajectories_bin", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_double]),
+    ("cair_format_rows", C.c_int, [_P, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_char_p, C.c_int64, _L]),
+    ("cair_write_trajectories", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double, _L]),
+    ("cair_write_trajectories_bin", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double]),
     ("cair_queue_graph_create", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, _P,
                                           C.POINTER(C.c_void_p)]),
     ("cair_queue_graph_launch", C.c_int, [_P, _P, _P]),

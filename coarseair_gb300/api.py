@@ -330,32 +330,35 @@ def histogram_assign(j, v, arr):
     return _nint(np.asarray(j) - 0.5), _nint(np.asarray(v) - 0.5), _nint(np.asarray(arr) - 0.5)
 
 
-def format_rows(rows, idx_offset=0, header=True):
-    """trajectories.out text of result rows (Integrator_Class.F90:884-933)."""
+def format_rows(rows, idx_offset=0, header=True, nmol=1):
+    """trajectories.out text of result rows (Integrator_Class.F90:884-933); nmol is NInitMolecules
+    (1: diatom + atom, 2: diatom + diatom)."""
     lib = _lib.load()
     rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
     n = C.c_int64(0)
-    lib.cair_format_rows(rw.ctypes.data, len(rw), int(idx_offset), int(header), None, 0, C.byref(n))
+    lib.cair_format_rows(rw.ctypes.data, len(rw), int(idx_offset), int(nmol), int(header), None, 0, C.byref(n))
     buf = C.create_string_buffer(n.value + 1)
-    rc = lib.cair_format_rows(rw.ctypes.data, len(rw), int(idx_offset), int(header), buf, n.value, C.byref(n))
+    rc = lib.cair_format_rows(rw.ctypes.data, len(rw), int(idx_offset), int(nmol), int(header), buf, n.value,
+                              C.byref(n))
     if rc != 0:
         raise CairError("cair_format_rows: %s" % _lib.STATUS.get(rc, rc))
     return buf.raw[:n.value].decode()
 
 
-def write_trajectories(directory, rows, ham_abs_tol, idx_offset=0, binary=None):
+def write_trajectories(directory, rows, ham_abs_tol, idx_offset=0, binary=None, nmol=1):
     """Write trajectories.out and trajectories_HNotCons.out (and trajectories.bin if `binary` is a
-    path); returns (rows in trajectories.out, rows in trajectories_HNotCons.out)."""
+    path); returns (rows in trajectories.out, rows in trajectories_HNotCons.out).  nmol is
+    NInitMolecules (1: diatom + atom, 2: diatom + diatom)."""
     lib = _lib.load()
     rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
     cnt = (C.c_int64 * 2)()
-    rc = lib.cair_write_trajectories(str(directory).encode(), rw.ctypes.data, len(rw), int(idx_offset),
+    rc = lib.cair_write_trajectories(str(directory).encode(), rw.ctypes.data, len(rw), int(idx_offset), int(nmol),
                                      float(ham_abs_tol), cnt)
     if rc != 0:
         raise CairError("cair_write_trajectories: %s" % _lib.STATUS.get(rc, rc))
     if binary is not None:
         rc = lib.cair_write_trajectories_bin(str(binary).encode(), rw.ctypes.data, len(rw), int(idx_offset),
-                                             float(ham_abs_tol))
+                                             int(nmol), float(ham_abs_tol))
         if rc != 0:
             raise CairError("cair_write_trajectories_bin: %s" % _lib.STATUS.get(rc, rc))
     return cnt[0], cnt[1]

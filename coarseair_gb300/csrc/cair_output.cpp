@@ -1,13 +1,14 @@
 // trajectories.out / trajectories_HNotCons.out / trajectories.bin writers (host code).
 //
-// Rows follow Integrator_Class.F90:884-933 for three atoms, format
-//   (I10, A, I5, 2(A, ES11.5), *(A, ES14.8))
-// with iTraj = IdxOverall, iPES 1-based, bmax, b_i, j_i, v_i, arr_i, j_f, v_f, arr_f.  Fortran's
-// formatted output is reproduced field by field: a value wider than its field prints as asterisks
-// (so a negative number in ES14.8 is fourteen '*'), a three-digit exponent drops the 'E', NaN and
-// Infinity are right-justified words.  The binary file is the stream that
-// Statistics_Class.F90:283-314 writes and ReadInputsUnformatted (346-506) reads: NTraj, then per
-// row Idx, iPES, bMax, bSampled, Qini(3), Qfin(3) as 8-byte integers and reals.
+// Rows follow Integrator_Class.F90:884-920, format (I10, A, I5, 2(A, ES11.5), *(A, ES14.8)) with
+// iTraj = IdxOverall, iPES 1-based, bmax, b_i, then the initial and the final conditions: J, v,
+// arrangement for one initial molecule, J1, v1, J2, v2, arrangement for two (NInitMolecules, with
+// the header line of Integrator_Class.F90:183-189 for each).  Fortran's formatted output is
+// reproduced field by field: a value wider than its field prints as asterisks (so a negative
+// number in ES14.8 is fourteen '*'), a three-digit exponent drops the 'E', NaN and Infinity are
+// right-justified words.  The binary file is the stream that Statistics_Class.F90:283-314 writes
+// and ReadInputsUnformatted (346-506) reads: NTraj, then per row Idx, iPES, bMax, bSampled,
+// Qini(NCond), Qfin(NCond) as 8-byte integers and reals.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -45,7 +46,19 @@ void put_es(std::string& s, double x, int w, int d) {
   else s.append((size_t)(w - n), ' ').append(b, (size_t)n);
 }
 
-void format_row(std::string& s, const cair_traj_result& r, int64_t idx_offset) {
+// The NCond initial then the NCond final conditions of a row (3 or 5 per side).
+int conditions(const cair_traj_result& r, int nmol, double* q) {
+  if (nmol == 1) {
+    const double v[6] = {r.j_i, r.v_i, r.arr_i, r.j_f, r.v_f, r.arr_f};
+    std::memcpy(q, v, sizeof v);
+    return 3;
+  }
+  const double v[10] = {r.j_i, r.v_i, r.j2_i, r.v2_i, r.arr_i, r.j_f, r.v_f, r.j2_f, r.v2_f, r.arr_f};
+  std::memcpy(q, v, sizeof v);
+  return 5;
+}
+
+void format_row(std::string& s, const cair_traj_result& r, int64_t idx_offset, int nmol) {
   put_int(s, idx_offset + r.idx, 10);
   s += ',';
   put_int(s, (long long)r.ipes + 1, 5);
@@ -53,17 +66,23 @@ void format_row(std::string& s, const cair_traj_result& r, int64_t idx_offset) {
   put_es(s, r.bmax, 11, 5);
   s += ',';
   put_es(s, r.b, 11, 5);
-  const double v[6] = {r.j_i, r.v_i, r.arr_i, r.j_f, r.v_f, r.arr_f};
-  for (double x : v) {
+  double q[10];
+  const int nc = conditions(r, nmol, q);
+  for (int c = 0; c < 2 * nc; ++c) {
     s += ',';
-    put_es(s, x, 14, 8);
+    put_es(s, q[c], 14, 8);
   }
   s += '\n';
 }
 
-const char* kHeader =
+const char* kHeader1 =
     "#    iTraj, iPES,       bmax,        b_i,           j_i,           v_i,         arr_i,           j_f,"
     "           v_f,         arr_f\n";
+const char* kHeader2 =
+    "#    iTraj, iPES,       bmax,        b_i,          j1_i,          v1_i,          j2_i,          v2_i,"
+    "         arr_i,          j1_f,          v1_f,          j2_f,          v2_f,         arr_f\n";
+
+const char* header(int nmol) { return nmol == 1 ? kHeader1 : kHeader2; }
 
 bool conserved(const cair_traj_result& r, double tol) {
   return r.status == CAIR_TRAJ_DONE && std::fabs(r.dH) <= tol;
@@ -73,21 +92,22 @@ bool conserved(const cair_traj_result& r, double tol) {
 
 extern "C" {
 
-int cair_format_rows(const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t with_header, char* buf,
-                     int64_t cap, int64_t* len) {
-  if (n < 0 || (n > 0 && !rows) || !len || cap < 0 || (cap > 0 && !buf)) return CAIR_EINVAL;
+int cair_format_rows(const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t nmol, int32_t with_header,
+                     char* buf, int64_t cap, int64_t* len) {
+  if (n < 0 || (n > 0 && !rows) || !len || cap < 0 || (cap > 0 && !buf) || (nmol != 1 && nmol != 2))
+    return CAIR_EINVAL;
   std::string s;
-  if (with_header) s += kHeader;
-  for (int64_t k = 0; k < n; ++k) format_row(s, rows[k], idx_offset);
+  if (with_header) s += header(nmol);
+  for (int64_t k = 0; k < n; ++k) format_row(s, rows[k], idx_offset, nmol);
   *len = (int64_t)s.size();
   if ((int64_t)s.size() > cap) return CAIR_EINVAL;
   std::memcpy(buf, s.data(), s.size());
   return 0;
 }
 
-int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
+int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t nmol,
                             double ham_abs_tol, int64_t* counts) {
-  if (!dir || n < 0 || (n > 0 && !rows)) return CAIR_EINVAL;
+  if (!dir || n < 0 || (n > 0 && !rows) || (nmol != 1 && nmol != 2)) return CAIR_EINVAL;
   const std::string d(dir);
   FILE* f[2] = {std::fopen((d + "/trajectories.out").c_str(), "w"),
                 std::fopen((d + "/trajectories_HNotCons.out").c_str(), "w")};
@@ -97,11 +117,11 @@ int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64
     return CAIR_EINVAL;
   }
   int64_t c[2] = {0, 0};
-  std::string s[2] = {kHeader, kHeader};
+  std::string s[2] = {header(nmol), header(nmol)};
   bool ok = true;
   for (int64_t k = 0; k < n; ++k) {
     const int which = conserved(rows[k], ham_abs_tol) ? 0 : 1;
-    format_row(s[which], rows[k], idx_offset);
+    format_row(s[which], rows[k], idx_offset, nmol);
     ++c[which];
     if (s[which].size() > (1u << 20)) {
       ok = ok && std::fwrite(s[which].data(), 1, s[which].size(), f[which]) == s[which].size();
@@ -120,8 +140,8 @@ int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64
 }
 
 int cair_write_trajectories_bin(const char* path, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
-                                double ham_abs_tol) {
-  if (!path || n < 0 || (n > 0 && !rows)) return CAIR_EINVAL;
+                                int32_t nmol, double ham_abs_tol) {
+  if (!path || n < 0 || (n > 0 && !rows) || (nmol != 1 && nmol != 2)) return CAIR_EINVAL;
   FILE* f = std::fopen(path, "wb");
   if (!f) return CAIR_EINVAL;
   int64_t nt = 0;
@@ -131,8 +151,9 @@ int cair_write_trajectories_bin(const char* path, const cair_traj_result* rows, 
     const cair_traj_result& r = rows[k];
     if (!conserved(r, ham_abs_tol)) continue;
     const int64_t ii[2] = {idx_offset + r.idx, (int64_t)r.ipes + 1};
-    const double dd[8] = {r.bmax, r.b, r.j_i, r.v_i, r.arr_i, r.j_f, r.v_f, r.arr_f};
-    ok = std::fwrite(ii, 8, 2, f) == 2 && std::fwrite(dd, 8, 8, f) == 8;
+    double dd[12] = {r.bmax, r.b};
+    const size_t nd = 2 + 2 * (size_t)conditions(r, nmol, dd + 2);
+    ok = std::fwrite(ii, 8, 2, f) == 2 && std::fwrite(dd, 8, nd, f) == nd;
   }
   ok = (std::fclose(f) == 0) && ok;
   return ok ? 0 : CAIR_EINVAL;

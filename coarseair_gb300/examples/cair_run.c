@@ -90,7 +90,7 @@ int main(int argc, char** argv) {
   rc = cair_run_queue(h, nl, lv, nl, items, ntot, 1000000, rows);
   if (rc) return fail(h, rc, "cair_run_queue");
   int64_t counts[2] = {0, 0};
-  rc = cair_write_trajectories(argv[3], rows, ntot, 0, sys.ham_abs_tol, counts);
+  rc = cair_write_trajectories(argv[3], rows, ntot, 0, 1, sys.ham_abs_tol, counts);
   if (rc) return fail(h, rc, "cair_write_trajectories");
   int64_t att[5];
   cair_last_counters(h, att);

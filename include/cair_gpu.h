@@ -44,7 +44,7 @@ extern "C" {
 #endif
 
 #define CAIR_MAX_PES 16
-#define CAIR_ABI_VERSION 4
+#define CAIR_ABI_VERSION 5
 
 /* Surface models (PES_Factory_Class.F90:46-329, System x PES_Model strings). */
 enum cair_pes_model {
@@ -339,22 +339,25 @@ int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items,
                     const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
                     int64_t cap, int64_t* nout);
 
-/* trajectories.out rows (Integrator_Class.F90:884-933, three atoms): format
- * (I10, ',', I5, 2(',', ES11.5), 6(',', ES14.8)) with iTraj = idx_offset + idx, iPES 1-based,
- * bmax, b_i, j_i, v_i, arr_i, j_f, v_f, arr_f; Fortran field overflow prints asterisks.  Host code,
- * no handle or GPU needed.  cair_format_rows fills buf (not NUL-terminated) and sets *len; it
- * returns CAIR_EINVAL with *len = the size needed when cap is too small. */
-int cair_format_rows(const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t with_header, char* buf,
-                     int64_t cap, int64_t* len);
+/* trajectories.out rows (Integrator_Class.F90:884-933): format
+ * (I10, ',', I5, 2(',', ES11.5), *(',', ES14.8)) with iTraj = idx_offset + idx, iPES 1-based, bmax,
+ * b_i, then for nmol = 1 (NInitMolecules, diatom + atom) j_i, v_i, arr_i, j_f, v_f, arr_f and for
+ * nmol = 2 (diatom + diatom) j1_i, v1_i, j2_i, v2_i, arr_i, j1_f, v1_f, j2_f, v2_f, arr_f; the header
+ * line is the reference's for each (Integrator_Class.F90:183-189).  Fortran field overflow prints
+ * asterisks.  Host code, no handle or GPU needed.  cair_format_rows fills buf (not NUL-terminated)
+ * and sets *len; it returns CAIR_EINVAL with *len = the size needed when cap is too small. */
+int cair_format_rows(const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t nmol, int32_t with_header,
+                     char* buf, int64_t cap, int64_t* len);
 /* <dir>/trajectories.out (finished rows with |dH| <= ham_abs_tol) and <dir>/trajectories_HNotCons.out
  * (the rest: energy not conserved, and the attempt-capped or non-finite rows, where the reference
  * stops with an error), each with the reference's header line; counts[0..1] = rows written. */
-int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
+int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64_t n, int64_t idx_offset, int32_t nmol,
                             double ham_abs_tol, int64_t* counts);
 /* trajectories.bin: the stream Statistics_Class.F90:283-314 writes (NTraj, then per row Idx, iPES,
- * bMax, bSampled, Qini(3), Qfin(3); 8-byte integers and reals) for the trajectories.out rows. */
+ * bMax, bSampled, Qini(NCond), Qfin(NCond); NCond = 3 for nmol = 1, 5 for nmol = 2; 8-byte integers
+ * and reals) for the trajectories.out rows. */
 int cair_write_trajectories_bin(const char* path, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
-                                double ham_abs_tol);
+                                int32_t nmol, double ham_abs_tol);
 
 /* Algorithmic FP64 operation counts the library's kernels execute per PES energy+gradient
  * evaluation, per energy-only evaluation and per BS attempt (excluding the PES), for

@@ -54,3 +54,56 @@ def test_files_split_by_energy_conservation(tmp_path):
     recs = np.frombuffer(raw[8:], dtype=[("idx", "<i8"), ("ipes", "<i8"), ("v", "<f8", 8)])
     assert list(recs["idx"]) == [7, 9] and list(recs["ipes"]) == [1, 1]
     assert recs["v"][0].tolist() == [7.0, 3.25, 10.5, 0.5, 16.5, 11.49, -1.0, 32.5]
+
+
+HEADER2 = ("#    iTraj, iPES,       bmax,        b_i,          j1_i,          v1_i,          j2_i,          v2_i,"
+           "         arr_i,          j1_f,          v1_f,          j2_f,          v2_f,         arr_f\n")
+
+
+def _rows2():
+    """Two diatom + diatom rows: a four-atom cluster (negative J2, arrangement -65.5) and an exchange."""
+    r = np.zeros(2, dtype=_lib.RESULT_DTYPE)
+    r["idx"] = [3, 4]
+    r["ipes"] = [1, 0]
+    r["bmax"] = 8.0
+    r["b"] = [2.5, 0.125]
+    r["j_i"], r["v_i"], r["j2_i"], r["v2_i"], r["arr_i"] = 1.5, 0.5, 3.5, 1.5, 26.5
+    r["j_f"] = [12.25, 40.0]
+    r["v_f"] = [0.5, 3.0]
+    r["j2_f"] = [-0.5, 7.0]
+    r["v2_f"] = [2.5, 0.0]
+    r["arr_f"] = [-65.5, 58.5]
+    r["status"] = [0, 0]
+    r["dH"] = [1e-9, 1e-3]
+    return r
+
+
+EXPECTED2 = [
+    "         3,    2,8.00000E+00,2.50000E+00,1.50000000E+00,5.00000000E-01,3.50000000E+00,1.50000000E+00,"
+    "2.65000000E+01,1.22500000E+01,5.00000000E-01,**************,2.50000000E+00,**************\n",
+    "         4,    1,8.00000E+00,1.25000E-01,1.50000000E+00,5.00000000E-01,3.50000000E+00,1.50000000E+00,"
+    "2.65000000E+01,4.00000000E+01,3.00000000E+00,7.00000000E+00,0.00000000E+00,5.85000000E+01\n",
+]
+
+
+def test_two_molecule_rows_follow_the_reference_format():
+    assert api.format_rows(_rows2(), header=True, nmol=2) == HEADER2 + "".join(EXPECTED2)
+
+
+def test_two_molecule_files(tmp_path):
+    n_ok, n_not = api.write_trajectories(tmp_path, _rows2(), ham_abs_tol=1e-5, binary=tmp_path / "trajectories.bin",
+                                         nmol=2)
+    assert (n_ok, n_not) == (1, 1)
+    assert (tmp_path / "trajectories.out").read_text() == HEADER2 + EXPECTED2[0]
+    assert (tmp_path / "trajectories_HNotCons.out").read_text() == HEADER2 + EXPECTED2[1]
+    raw = (tmp_path / "trajectories.bin").read_bytes()
+    assert np.frombuffer(raw[:8], "<i8")[0] == 1
+    recs = np.frombuffer(raw[8:], dtype=[("idx", "<i8"), ("ipes", "<i8"), ("v", "<f8", 12)])
+    assert list(recs["idx"]) == [3] and list(recs["ipes"]) == [2]
+    assert recs["v"][0].tolist() == [8.0, 2.5, 1.5, 0.5, 3.5, 1.5, 26.5, 12.25, 0.5, -0.5, 2.5, -65.5]
+
+
+def test_bad_molecule_count_is_refused():
+    import pytest
+    with pytest.raises(api.CairError):
+        api.format_rows(_rows2(), nmol=3)
