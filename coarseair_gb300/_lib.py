@@ -102,6 +102,7 @@ SIGNATURES = [
     ("cair_format_rows", C.c_int, [_P, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_char_p, C.c_int64, _L]),
     ("cair_write_trajectories", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double, _L]),
     ("cair_write_trajectories_bin", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double]),
+    ("cair_merge_trajectories", C.c_int, [C.c_int32, C.POINTER(C.c_char_p), C.c_char_p, _L]),
     ("cair_queue_graph_create", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, _P,
                                           C.POINTER(C.c_void_p)]),
     ("cair_queue_graph_launch", C.c_int, [_P, _P, _P]),

@@ -364,6 +364,20 @@ def write_trajectories(directory, rows, ham_abs_tol, idx_offset=0, binary=None, 
     return cnt[0], cnt[1]
 
 
+def merge_trajectories(src_dirs, out_dir):
+    """MergeTrajectories (ComputeRates.sh:406-472): append each directory's trajectories.out and
+    trajectories_HNotCons.out to out_dir/trajectories.csv and out_dir/trajectories_HNotCons.out
+    (one header line), write out_dir/NConvTraj.dat; returns the merged row count."""
+    lib = _lib.load()
+    src = [str(d).encode() for d in src_dirs]
+    arr = (C.c_char_p * max(1, len(src)))(*src)
+    n = C.c_int64(0)
+    rc = lib.cair_merge_trajectories(len(src), arr, str(out_dir).encode(), C.byref(n))
+    if rc != 0:
+        raise CairError("cair_merge_trajectories: %s" % _lib.STATUS.get(rc, rc))
+    return n.value
+
+
 class Statistics:
     """TrajectoriesStats for state-specific runs (Statistics_Class.F90, Histogram assignment):
     final-state cross sections [bohr^2] and rate coefficients [cm^3/s] per work item, counted on

@@ -159,4 +159,72 @@ int cair_write_trajectories_bin(const char* path, const cair_traj_result* rows, 
   return ok ? 0 : CAIR_EINVAL;
 }
 
+// MergeTrajectories (scripts/executing/ComputeRates.sh:406-472), for each source directory that
+// holds a trajectories.out: while <out>/trajectories.csv does not exist, the source's
+// trajectories.out and trajectories_HNotCons.out are copied whole over <out>/trajectories.csv and
+// <out>/trajectories_HNotCons.out; after that they are appended without their header line.  Then
+// NConvTraj.dat = lines of trajectories.csv - 1.
+int cair_merge_trajectories(int32_t nsrc, const char* const* src_dirs, const char* out_dir, int64_t* ntraj) {
+  if (nsrc < 0 || (nsrc > 0 && !src_dirs) || !out_dir) return CAIR_EINVAL;
+  const std::string out(out_dir);
+  const std::string csv = out + "/trajectories.csv", hnc = out + "/trajectories_HNotCons.out";
+  auto exists = [](const std::string& p) {
+    FILE* f = std::fopen(p.c_str(), "rb");
+    if (f) std::fclose(f);
+    return f != nullptr;
+  };
+  // the first source is copied whole over dst (the script's `cat >`); later ones are appended
+  // without their first line (`tail -n+2 >>`)
+  auto append = [](const std::string& src, const std::string& dst, bool skip_header) {
+    FILE* in = std::fopen(src.c_str(), "rb");
+    if (!in) return false;
+    FILE* o = std::fopen(dst.c_str(), skip_header ? "ab" : "wb");
+    if (!o) {
+      std::fclose(in);
+      return false;
+    }
+    bool ok = true, at_body = !skip_header;
+    char buf[1 << 16];
+    size_t n;
+    while (ok && (n = std::fread(buf, 1, sizeof buf, in)) > 0) {
+      size_t from = 0;
+      if (!at_body) {
+        const char* nl = (const char*)std::memchr(buf, '\n', n);
+        if (!nl) continue;
+        from = (size_t)(nl - buf) + 1;
+        at_body = true;
+      }
+      ok = std::fwrite(buf + from, 1, n - from, o) == n - from;
+    }
+    ok = !std::ferror(in) && ok;
+    std::fclose(in);
+    return (std::fclose(o) == 0) && ok;
+  };
+  bool ok = true;
+  for (int32_t i = 0; i < nsrc && ok; ++i) {
+    if (!src_dirs[i]) return CAIR_EINVAL;
+    const std::string d(src_dirs[i]);
+    if (!exists(d + "/trajectories.out")) continue;
+    const bool first = !exists(csv);
+    ok = append(d + "/trajectories.out", csv, !first);
+    if (ok && exists(d + "/trajectories_HNotCons.out")) ok = append(d + "/trajectories_HNotCons.out", hnc, !first);
+  }
+  if (!ok) return CAIR_EINVAL;
+  int64_t lines = 0;
+  if (FILE* f = std::fopen(csv.c_str(), "rb")) {
+    char buf[1 << 16];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof buf, f)) > 0)
+      for (size_t k = 0; k < n; ++k) lines += buf[k] == '\n';
+    std::fclose(f);
+  }
+  const int64_t nt = lines > 0 ? lines - 1 : 0;
+  FILE* f = std::fopen((out + "/NConvTraj.dat").c_str(), "w");
+  if (!f) return CAIR_EINVAL;
+  ok = std::fprintf(f, "%lld\n", (long long)nt) > 0;
+  ok = (std::fclose(f) == 0) && ok;
+  if (ntraj) *ntraj = nt;
+  return ok ? 0 : CAIR_EINVAL;
+}
+
 }  // extern "C"

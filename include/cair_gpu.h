@@ -359,6 +359,14 @@ int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64
 int cair_write_trajectories_bin(const char* path, const cair_traj_result* rows, int64_t n, int64_t idx_offset,
                                 int32_t nmol, double ham_abs_tol);
 
+/* MergeTrajectories (scripts/executing/ComputeRates.sh:406-472): the trajectories.out of each
+ * source directory (one per process or replica, in order) is appended to <out_dir>/trajectories.csv
+ * -- whole when that file does not exist yet, without its header line otherwise -- and its
+ * trajectories_HNotCons.out to <out_dir>/trajectories_HNotCons.out alike; directories without a
+ * trajectories.out are skipped.  Writes <out_dir>/NConvTraj.dat (rows in trajectories.csv) and
+ * sets *ntraj to that count.  Host code, no handle or GPU needed. */
+int cair_merge_trajectories(int32_t nsrc, const char* const* src_dirs, const char* out_dir, int64_t* ntraj);
+
 /* Algorithmic FP64 operation counts the library's kernels execute per PES energy+gradient
  * evaluation, per energy-only evaluation and per BS attempt (excluding the PES), for
  * roofline accounting.  `exp_per_eval` counts exponentials separately. */

@@ -107,3 +107,25 @@ def test_bad_molecule_count_is_refused():
     import pytest
     with pytest.raises(api.CairError):
         api.format_rows(_rows2(), nmol=3)
+
+
+def test_merge_follows_merge_trajectories(tmp_path):
+    """Two replicas' outputs (plus a directory without output) merge into one trajectories.csv with
+    the first header only, HNotCons likewise, and NConvTraj.dat holds the row count."""
+    rows = _rows()
+    dirs = [tmp_path / "Proc_1", tmp_path / "Proc_2", tmp_path / "Proc_3"]
+    for d in dirs:
+        d.mkdir()
+    api.write_trajectories(dirs[0], rows, ham_abs_tol=1e-5)
+    api.write_trajectories(dirs[2], rows[:3], ham_abs_tol=1e-5, idx_offset=1000)
+    out = tmp_path / "merged"
+    out.mkdir()
+    (out / "trajectories_HNotCons.out").write_text("stale\n")
+    n = api.merge_trajectories(dirs, out)
+    second = [e.replace("         %d," % i, "      %d," % (1000 + i), 1) for e, i in zip(EXPECTED, (7, 8, 9, 10))]
+    assert n == 4
+    assert (out / "trajectories.csv").read_text() == HEADER + EXPECTED[0] + EXPECTED[2] + second[0] + second[2]
+    assert (out / "trajectories_HNotCons.out").read_text() == HEADER + EXPECTED[1] + EXPECTED[3] + second[1]
+    assert (out / "NConvTraj.dat").read_text() == "4\n"
+    # a later merge appends to the existing trajectories.csv, as the script does
+    assert api.merge_trajectories(dirs[:1], out) == 6
