@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcair_gpu.so")
 CAIR_MAX_PES = 16
-CAIR_ABI_VERSION = 5
+CAIR_ABI_VERSION = 6
 CAIR_STATIC_QUEUE_MAX_TRAJ = 16384
 
 STATUS = {0: "CAIR_OK", 1: "CAIR_EINVAL", 2: "CAIR_ECUDA", 3: "CAIR_ETIMEOUT", 4: "CAIR_ENONFINITE",
@@ -54,14 +54,15 @@ class StatsParams(C.Structure):
                 ("pres_even_odd", C.c_int32 * 5), ("ham_abs_tol", C.c_double), ("xmu", C.c_double)]
 
 
-FINAL_STATE_DTYPE = np.dtype([("item", "i4"), ("fin", "i4", 5), ("ini", "i4", 5), ("pad", "i4"), ("count", "i8"),
+FINAL_STATE_DTYPE = np.dtype([("run", "i4"), ("fin", "i4", 5), ("ini", "i4", 5), ("nrings", "i4"), ("count", "i8"),
                               ("nrows", "i8"), ("cross", "f8"), ("cross_sd", "f8"), ("rate", "f8"),
                               ("rate_sd", "f8")])
 
 LEVEL_DTYPE = np.dtype([("vqn", "i4"), ("jqn", "i4"), ("eint", "f8"), ("egam", "f8"), ("rmin", "f8"),
                         ("rmax", "f8"), ("vmin", "f8"), ("vmax", "f8"), ("tau", "f8"), ("ri", "f8"), ("ro", "f8")])
 ITEM_DTYPE = np.dtype([("ilevel", "i4"), ("ipes", "i4"), ("first", "i8"), ("ntraj", "i8"), ("seed", "i8"),
-                       ("ttra", "f8"), ("bmax", "f8"), ("dinit", "f8"), ("ilevel2", "i4"), ("pad", "i4")])
+                       ("ttra", "f8"), ("bmax", "f8"), ("dinit", "f8"), ("ilevel2", "i4"), ("b_mode", "i4"),
+                       ("bmin", "f8"), ("skip", "i8")])
 RESULT_DTYPE = np.dtype([("idx", "i8"), ("item", "i4"), ("ipes", "i4"), ("status", "i4"), ("iste", "i4"),
                          ("irej", "i4"), ("pad", "i4"),
                          ("bmax", "f8"), ("b", "f8"), ("j_i", "f8"), ("v_i", "f8"), ("arr_i", "f8"),
@@ -96,8 +97,8 @@ SIGNATURES = [
     ("cair_flop_model", C.c_int, [_P, C.c_int32, _D, _D, _D, _D]),
     ("cair_last_counters", C.c_int, [_P, _L]),
     ("cair_fp64_peak_probe", C.c_int, [_P, _D]),
-    ("cair_statistics", C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L]),
-    ("cair_statistics_dev", C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L,
+    ("cair_statistics", C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L]),
+    ("cair_statistics_dev", C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L,
                                       _P]),
     ("cair_format_rows", C.c_int, [_P, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_char_p, C.c_int64, _L]),
     ("cair_write_trajectories", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double, _L]),

@@ -255,16 +255,44 @@ def level_table(levels):
 
 
 def work_items(entries):
-    """entries: iterable of (ilevel, ipes, ntraj, seed, ttra, bmax, dinit[, ilevel2]) -> cair_work_item[]
-    tiling the batch in order; ilevel2 is the projectile diatom's level of a diatom + diatom system."""
+    """entries: iterable of (ilevel, ipes, ntraj, seed, ttra, bmax, dinit[, ilevel2[, b_mode, bmin, skip]])
+    -> cair_work_item[] tiling the batch in order; ilevel2 is the projectile diatom's level of a
+    diatom + diatom system; b_mode, bmin, skip describe an impact-parameter ring (ring_entries)."""
     entries = list(entries)
     out = np.zeros(len(entries), dtype=_lib.ITEM_DTYPE)
     first = 0
     for i, e in enumerate(entries):
         il, ip, nt, seed, ttra, bmax, dinit = e[:7]
         il2 = e[7] if len(e) > 7 else 0
-        out[i] = (il, ip, first, nt, seed, ttra, bmax, dinit, il2, 0)
+        mode, bmin, skip = (e[8], e[9], e[10]) if len(e) > 8 else (0, 0.0, 0)
+        out[i] = (il, ip, first, nt, seed, ttra, bmax, dinit, il2, mode, bmin, skip)
         first += nt
+    return out
+
+
+STRATA = {"Circles": 0, "Rings": 1, "Segments": 2}
+
+
+def ring_entries(ilevel, ipes, ntraj, seed, ttra, dinit, bring, ntring, strata="Circles", ilevel2=0):
+    """Work-item entries for one stream of `ntraj` trajectories stratified in impact-parameter rings,
+    as InitializeImpactParameter and GetImpactParamValue split it (ImpactParameter_Class.F90:55-221):
+    ring r gets int(ntring_r x ntraj / sum(ntring)) trajectories, the first ring the remainder,
+    and draws its impact parameter from the ring's input value bring_r (negative: sampled by the
+    strata type up to |bring_r|; positive: that fixed value) with the previous ring's value as
+    bmin.  The rings continue one random-number stream (skip = trajectories of the earlier rings)."""
+    bring, ntring = list(bring), [int(x) for x in ntring]
+    if len(bring) != len(ntring) or not bring:
+        raise ValueError("one weight per ring")
+    if any(w < 0 for w in ntring):
+        raise ValueError("negative ring weights leave the reference's rings without trajectories")
+    total = sum(ntring)
+    counts = [int(float(w * ntraj) / total) for w in ntring]
+    counts[0] += ntraj - sum(counts)
+    out, skip = [], 0
+    for r, (b, n) in enumerate(zip(bring, counts)):
+        bmin = -bring[r - 1] if r > 0 else 0.0
+        out.append((ilevel, ipes, n, seed, ttra, -float(b), dinit, ilevel2, STRATA[strata], float(bmin), skip))
+        skip += n
     return out
 
 
@@ -410,13 +438,20 @@ class Statistics:
         self.ncond = ncond
         self.params = p
 
-    def compute(self, items, rows, cap=None):
+    def compute(self, items, rows, runs=None, cap=None):
+        """Final states of every run.  runs[i] is the run of work item i: the items (surfaces,
+        impact-parameter rings) whose rows the reference's statistics read together for one
+        initial state and temperature; None makes each item its own run."""
         H = self.H
         it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
         rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+        rn = None if runs is None else np.ascontiguousarray(runs, dtype=np.int32)
+        if rn is not None and len(rn) != len(it):
+            raise ValueError("runs must have one entry per work item")
         cap = int(cap if cap is not None else max(64, len(rw)))
         out = np.zeros(cap, dtype=_lib.FINAL_STATE_DTYPE)
         n = C.c_int64(0)
-        H.check(H.lib.cair_statistics(H.h, len(it), it.ctypes.data, len(rw), rw.ctypes.data, C.byref(self.params),
-                                      out.ctypes.data, cap, C.byref(n)), "cair_statistics")
+        H.check(H.lib.cair_statistics(H.h, len(it), it.ctypes.data, None if rn is None else rn.ctypes.data, len(rw),
+                                      rw.ctypes.data, C.byref(self.params), out.ctypes.data, cap, C.byref(n)),
+                "cair_statistics")
         return out[:n.value].copy()

@@ -17,6 +17,7 @@
 #include "cair_stats.cuh"
 
 #include <algorithm>
+#include <limits>
 #include <climits>
 
 using namespace cair;
@@ -763,7 +764,10 @@ int validate_items(cair_handle* h, int32_t nlevels, const cair_level* levels, in
       return fail(h, CAIR_EINVAL, "work item projectile level out of range");
     if (w.ipes < 0 || w.ipes >= h->sys.npes) return fail(h, CAIR_EINVAL, "work item surface out of range");
     if (w.ntraj < 0 || w.first != sum) return fail(h, CAIR_EINVAL, "work items must tile [0, ntot) in order");
-    if (!(w.dinit > 0.0) || std::fabs(w.bmax) > w.dinit) return fail(h, CAIR_EINVAL, "impact parameter exceeds Dinit");
+    if (!(w.dinit > 0.0) || std::fabs(w.bmax) > w.dinit || std::fabs(w.bmin) > w.dinit)
+      return fail(h, CAIR_EINVAL, "impact parameter exceeds Dinit");
+    if (w.b_mode < 0 || w.b_mode > 2) return fail(h, CAIR_EINVAL, "b_mode must be 0 (Circles), 1 (Rings) or 2 (Segments)");
+    if (w.skip < 0) return fail(h, CAIR_EINVAL, "work item skip must be >= 0");
     if (!(w.ttra > 0.0)) return fail(h, CAIR_EINVAL, "translational temperature must be positive");
     sum += w.ntraj;
   }
@@ -974,9 +978,9 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
   return 0;
 }
 
-int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
-                        const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
-                        int64_t cap, int64_t* nout, void* stream) {
+int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                        int64_t ntot, const cair_traj_result* results, const cair_stats_params* params,
+                        cair_final_state* out, int64_t cap, int64_t* nout, void* stream) {
   if (!h || nitems < 1 || !items || ntot < 0 || (ntot > 0 && !results) || !params || cap < 0 || (cap > 0 && !out) ||
       !nout)
     return fail(h, CAIR_EINVAL, "cair_statistics: bad argument");
@@ -985,16 +989,28 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   if (nc != 3 && nc != 5) return fail(h, CAIR_EINVAL, "cair_statistics: ncond must be 3 or 5");
   if (nc != (h->sys.natoms == 4 ? 5 : 3))
     return fail(h, CAIR_EINVAL, "cair_statistics: ncond must be 3 for diatom + atom, 5 for diatom + diatom");
-  // codes lie within +-70 qn_max^ncond; with the item folded in they must stay inside a signed 64-bit key
-  double span = 70.0 * (double)nitems;
-  for (int c = 0; c < nc; ++c) span *= (double)P.qn_max;
-  if (P.qn_max < 2 || span >= 4.6e18) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max out of range");
+  std::vector<int32_t> run_of(nitems);
+  int32_t nruns = 0;
+  for (int i = 0; i < nitems; ++i) {
+    run_of[i] = item_run ? item_run[i] : i;
+    if (run_of[i] < 0 || run_of[i] >= nitems) return fail(h, CAIR_EINVAL, "cair_statistics: run out of range");
+    nruns = std::max(nruns, run_of[i] + 1);
+  }
+  std::vector<double> run_ttra(nruns, -1.0);
+  for (int i = 0; i < nitems; ++i) {
+    double& t = run_ttra[run_of[i]];
+    if (t < 0.0) t = items[i].ttra;
+    else if (std::fabs(t - items[i].ttra) > 1e-12 * t)
+      return fail(h, CAIR_EINVAL, "cair_statistics: items of one run differ in temperature");
+  }
+  if (P.qn_max < 2) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max out of range");
   *nout = 0;
   if (ntot == 0) return 0;
   // table at least twice the rows, so linear probing always finds a slot
   unsigned long long tsize = 1024;
   while (tsize < 2ull * (unsigned long long)ntot) tsize <<= 1;
-  const size_t need = tsize * 16 + (size_t)nitems * 16 + (size_t)(cap > 0 ? cap : 1) * 16 + 4 * 256;
+  const size_t per_run = (size_t)kMaxRings * 16 + 16;
+  const size_t need = tsize * 32 + (size_t)nitems * 24 + (size_t)nruns * per_run + 8 * 256;
   if (h->stats_bytes < need) {
     if (h->d_stats) cudaFree(h->d_stats);
     h->d_stats = nullptr;
@@ -1005,10 +1021,14 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   Carver c{(char*)h->d_stats};
   unsigned long long* keys = c.take<unsigned long long>(tsize);
   unsigned long long* counts = c.take<unsigned long long>(tsize);
+  unsigned long long* okeys = c.take<unsigned long long>(tsize);
+  unsigned long long* ocounts = c.take<unsigned long long>(tsize);
   unsigned long long* item_rows = c.take<unsigned long long>(nitems);
   long long* item_ini = c.take<long long>(nitems);
-  unsigned long long* okeys = c.take<unsigned long long>(cap > 0 ? cap : 1);
-  unsigned long long* ocounts = c.take<unsigned long long>(cap > 0 ? cap : 1);
+  double* ring_b = c.take<double>((size_t)nruns * kMaxRings);
+  unsigned long long* ring_rows = c.take<unsigned long long>((size_t)nruns * kMaxRings);
+  int32_t* d_run = c.take<int32_t>(nitems);
+  int32_t* d_nring = c.take<int32_t>(nruns);
   unsigned long long* dn = c.take<unsigned long long>(2);
   int* derr = (int*)(dn + 1);
   cudaStream_t st = (cudaStream_t)stream;
@@ -1016,6 +1036,7 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   CUDA_TRY(h, cudaMemsetAsync(counts, 0, tsize * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(item_rows, 0, (size_t)nitems * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(item_ini, 0x7f, (size_t)nitems * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(ring_rows, 0, (size_t)nruns * kMaxRings * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(dn, 0, 16, st));
   StatsArgs A{ntot,
               results,
@@ -1023,81 +1044,149 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
               {P.iskip[0], P.iskip[1], P.iskip[2], P.iskip[3], P.iskip[4]},
               {P.pres_even_odd[0], P.pres_even_odd[1], P.pres_even_odd[2], P.pres_even_odd[3], P.pres_even_odd[4]},
               P.ham_abs_tol,
-              (unsigned long long)nitems,
+              d_run,
+              ring_b,
+              d_nring,
+              nruns,
+              1,
               keys,
               counts,
               tsize - 1,
               item_rows,
               item_ini,
+              ring_rows,
               derr};
-  if (nc == 3) k_stats_count<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
-  else k_stats_count<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
-  k_stats_compact<<<grid_for(h, (int64_t)tsize), 256, 0, st>>>(keys, counts, tsize, okeys, ocounts,
-                                                               (unsigned long long)cap, dn);
+  if (nc == 3) k_stats_items<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
+  else k_stats_items<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
   if (int e = check_launch(h)) return e;
-  unsigned long long n = 0;
   int err = 0;
   std::vector<unsigned long long> rows(nitems);
   std::vector<long long> ini(nitems);
-  CUDA_TRY(h, cudaMemcpyAsync(&n, dn, 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(rows.data(), item_rows, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(ini.data(), item_ini, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaStreamSynchronize(st));
   if (err == 1) return fail(h, CAIR_EINVAL, "cair_statistics: a quantum number is at or above qn_max");
-  if (err) return fail(h, CAIR_EINVAL, "cair_statistics: a final-state code of -1 on the last item");
-  if ((long long)n > cap)
-    return fail(h, CAIR_EINVAL, "cair_statistics: cap too small, " + std::to_string(n) + " final states");
+  // SetRings per run: the distinct |bMax| (within 1e-3) of the items with counted rows, ascending;
+  // IniState from the smallest initial code of the run
+  std::vector<double> rb((size_t)nruns * kMaxRings, 0.0);
+  std::vector<int32_t> nring(nruns, 0);
+  std::vector<long long> run_ini(nruns, std::numeric_limits<long long>::max());
+  for (int i = 0; i < nitems; ++i) {
+    if (rows[i] == 0) continue;
+    const int r = run_of[i];
+    run_ini[r] = std::min(run_ini[r], ini[i]);
+    double* e = rb.data() + (size_t)r * kMaxRings;
+    const double b = std::fabs(items[i].bmax);
+    bool dup = false;
+    for (int q = 0; q < nring[r]; ++q) dup = dup || std::fabs(b - e[q]) < 1.0e-3;
+    if (dup) continue;
+    if (nring[r] == kMaxRings) return fail(h, CAIR_EINVAL, "cair_statistics: more than 64 rings in a run");
+    e[nring[r]++] = b;
+  }
+  int R = 1;
+  for (int r = 0; r < nruns; ++r) {
+    std::sort(rb.begin() + (size_t)r * kMaxRings, rb.begin() + (size_t)r * kMaxRings + nring[r]);
+    R = std::max(R, (int)nring[r]);
+  }
+  // codes lie within +-70 qn_max^ncond; with the run and ring folded in they must fit a signed 64-bit key
+  double span = 70.0 * (double)nruns * (double)R;
+  for (int q = 0; q < nc; ++q) span *= (double)P.qn_max;
+  if (span >= 4.6e18) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max^ncond x runs x rings too large");
+  A.R = R;
+  CUDA_TRY(h, cudaMemcpyAsync(ring_b, rb.data(), rb.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_nring, nring.data(), (size_t)nruns * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_run, run_of.data(), (size_t)nitems * 4, cudaMemcpyHostToDevice, st));
+  if (nc == 3) k_stats_count<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
+  else k_stats_count<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
+  k_stats_compact<<<grid_for(h, (int64_t)tsize), 256, 0, st>>>(keys, counts, tsize, okeys, ocounts, tsize, dn);
+  if (int e = check_launch(h)) return e;
+  unsigned long long n = 0;
+  std::vector<unsigned long long> perb((size_t)nruns * kMaxRings);
+  CUDA_TRY(h, cudaMemcpyAsync(&n, dn, 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(perb.data(), ring_rows, perb.size() * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (err) return fail(h, CAIR_EINVAL, "cair_statistics: a final-state key of -1 (not representable)");
   std::vector<unsigned long long> k(n), cnt(n);
   if (n) {
     CUDA_TRY(h, cudaMemcpyAsync(k.data(), okeys, n * 8, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(h, cudaMemcpyAsync(cnt.data(), ocounts, n * 8, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(h, cudaStreamSynchronize(st));
   }
-  std::vector<size_t> ord(n);
-  for (size_t i = 0; i < n; ++i) ord[i] = i;
-  // key = code x nitems + item, with the code possibly negative: decode as a signed number
-  std::vector<long long> kitem(n), kcode(n);
+  // key = (code x nruns + run) x R + ring with a possibly negative code: decode with floor division
+  struct Entry {
+    long long code;
+    int run, ring;
+    unsigned long long count;
+  };
+  auto floordiv = [](long long a, long long b) { return a / b - ((a % b != 0) && ((a < 0) != (b < 0))); };
+  std::vector<Entry> ent(n);
   for (size_t i = 0; i < n; ++i) {
-    const long long ks = (long long)k[i], ni = nitems;
-    kitem[i] = ((ks % ni) + ni) % ni;
-    kcode[i] = (ks - kitem[i]) / ni;
+    const long long ks = (long long)k[i];
+    const long long rest = floordiv(ks, R);
+    ent[i].ring = (int)(ks - rest * R);
+    ent[i].code = floordiv(rest, nruns);
+    ent[i].run = (int)(rest - ent[i].code * nruns);
+    ent[i].count = cnt[i];
   }
-  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
-    return kitem[a] != kitem[b] ? kitem[a] < kitem[b] : kcode[a] < kcode[b];
+  std::sort(ent.begin(), ent.end(), [](const Entry& a, const Entry& b) {
+    return a.run != b.run ? a.run < b.run : (a.code != b.code ? a.code < b.code : a.ring < b.ring);
   });
   const long long qn = P.qn_max;
   long long ifacts = 1;
-  for (int c = 0; c < nc; ++c) ifacts *= qn;
-  // Boltzmann mean velocity (Collision_Class.F90:576-595), per bohr^2 -> cm^3/s
+  for (int q = 0; q < nc; ++q) ifacts *= qn;
   const double pi = std::acos(-1.0), k_to_h = 1.0 / 3.1577513e5, bohr_cm = 0.5291771e-8;
-  for (size_t o = 0; o < n; ++o) {
-    const size_t i = ord[o];
-    const int item = (int)kitem[i];
-    const long long code = kcode[i];
-    if (item < 0 || item >= nitems) return fail(h, CAIR_EINVAL, "cair_statistics: row with an item out of range");
-    cair_final_state& F = out[o];
-    F.item = item;
-    F.count = (int64_t)cnt[i];
-    F.nrows = (int64_t)rows[item];
-    F.pad = 0;
-    for (int c = 0; c < 5; ++c) F.ini[c] = F.fin[c] = 0;
-    // IniState from the smallest initial code of the item (ProcessStatistics, 782-929)
-    long long isum = ini[item], ifact = ifacts;
+  int64_t o = 0;
+  for (size_t i = 0; i < n;) {
+    size_t j = i;
+    while (j < n && ent[j].run == ent[i].run && ent[j].code == ent[i].code) ++j;
+    if (o == cap) {
+      int64_t lines = o;
+      for (size_t a = i; a < n;) {
+        size_t b = a;
+        while (b < n && ent[b].run == ent[a].run && ent[b].code == ent[a].code) ++b;
+        ++lines;
+        a = b;
+      }
+      return fail(h, CAIR_EINVAL, "cair_statistics: cap too small, " + std::to_string(lines) + " final states");
+    }
+    const int run = ent[i].run;
+    const long long code = ent[i].code;
+    cair_final_state& F = out[o++];
+    F.run = run;
+    F.nrings = nring[run];
+    F.count = 0;
+    for (size_t a = i; a < j; ++a) F.count += (int64_t)ent[a].count;
+    F.nrows = 0;
+    for (int q = 0; q < nring[run]; ++q) F.nrows += (int64_t)perb[(size_t)run * kMaxRings + q];
+    for (int q = 0; q < 5; ++q) F.ini[q] = F.fin[q] = 0;
+    // IniState from the smallest initial code of the run (ProcessStatistics, 782-929)
+    long long isum = run_ini[run], ifact = ifacts;
     for (int cnd = nc - 1; cnd >= 0; --cnd) {
       ifact /= qn;
       const long long t = isum / ifact;
       F.ini[cnd] = (int)(t - 2);
       isum -= t * ifact;
     }
-    // WriteFinStateProbabilities (1288-1440), one ring
-    const double bmax = items[item].bmax;
-    double area = pi * bmax * bmax;
-    if (area == 0.0) area = 1.0;
-    const double per = (double)(F.nrows > 1 ? F.nrows : 1);
-    const double fw = (double)F.count / per;
-    F.cross = area * fw;
-    F.cross_sd = std::sqrt(fw * (1.0 - fw) * area * area / per);
+    // WriteFinStateProbabilities (1288-1440): ring areas, then Cross and CrossSD over the rings
+    const double* e = rb.data() + (size_t)run * kMaxRings;
+    double cr = 0.0, sd = 0.0, prev = 0.0;
+    for (int q = 0; q < nring[run]; ++q) {
+      const double t = pi * e[q] * e[q];
+      double area = t - prev;
+      prev = t;
+      if (nring[run] == 1 && area == 0.0) area = 1.0;
+      unsigned long long w = 0;
+      for (size_t a = i; a < j; ++a)
+        if (ent[a].ring == q) w += ent[a].count;
+      const double pb = (double)std::max<unsigned long long>(perb[(size_t)run * kMaxRings + q], 1ull);
+      const double fw = (double)w / pb;
+      cr = cr + area * fw;
+      sd = sd + fw * (1.0 - fw) * area * area / pb;
+    }
+    F.cross = cr;
+    F.cross_sd = std::sqrt(sd);
     const int ini_arr = F.ini[nc - 1] / 16;
     isum = code;
     ifact = ifacts;
@@ -1114,16 +1203,17 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
       }
       F.fin[cnd] = (int)fc;
     }
-    const double vp = std::sqrt(2.0 * items[item].ttra * k_to_h / P.xmu);
+    const double vp = std::sqrt(2.0 * run_ttra[run] * k_to_h / P.xmu);
     const double vel = 2.0 / std::sqrt(pi) * vp * 4.134137e16 * (bohr_cm * bohr_cm * bohr_cm);
     F.rate = F.cross * vel;
     F.rate_sd = F.cross_sd * vel;
+    i = j;
   }
-  *nout = (int64_t)n;
+  *nout = o;
   return 0;
 }
 
-int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
+int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run, int64_t ntot,
                     const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
                     int64_t cap, int64_t* nout) {
   if (!h || ntot < 0 || (ntot > 0 && !results)) return fail(h, CAIR_EINVAL, "cair_statistics: bad argument");
@@ -1131,8 +1221,8 @@ int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items,
   if (ntot > 0)
     CUDA_TRY(h, cudaMemcpyAsync(h->d_scratch, results, (size_t)ntot * sizeof(cair_traj_result),
                                 cudaMemcpyHostToDevice, h->stream));
-  return cair_statistics_dev(h, nitems, items, ntot, (const cair_traj_result*)h->d_scratch, params, out, cap, nout,
-                             h->stream);
+  return cair_statistics_dev(h, nitems, items, item_run, ntot, (const cair_traj_result*)h->d_scratch, params, out,
+                             cap, nout, h->stream);
 }
 
 struct cair_queue_graph {

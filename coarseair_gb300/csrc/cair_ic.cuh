@@ -55,9 +55,11 @@ __global__ void k_ic_draws(int nitems, int nmol, const cair_work_item* __restric
   const cair_work_item W = items[it];
   Stream st;
   st.seed(W.seed);
-  for (int64_t k = 0; k < W.ntraj; ++k) {
+  double skipped[kDraws];
+  // the earlier rings of the stream (k < 0) are drawn and dropped
+  for (int64_t k = -W.skip; k < W.ntraj; ++k) {
     const int64_t g = W.first + k;
-    double* d = draws + kDraws * g;
+    double* d = k < 0 ? skipped : draws + kDraws * g;
     if (nmol == 1) st.draw();  // level pick (state-specific: the draw is made and the item's level used)
     for (int mol = 0; mol < nmol; ++mol) {
       const cair_level L = levels[mol == 0 ? W.ilevel : W.ilevel2];
@@ -78,11 +80,22 @@ __global__ void k_ic_draws(int nitems, int nmol, const cair_work_item* __restric
       for (int j = 0; j < 4; ++j) d[4 * mol + j] = st.draw();
     }
     d[4 * nmol] = st.draw();
-    d[4 * nmol + 1] = st.draw();
-    item_of[g] = it;
+    // a fixed impact parameter (bmax < 0) draws no random number (Collision_Class.F90:1280-1281)
+    d[4 * nmol + 1] = W.bmax > 0.0 ? st.draw() : 0.0;
+    if (k >= 0) item_of[g] = it;
   }
 }
 #endif
+
+// The impact parameter of one trajectory (Collision_Class.F90:1276-1296): the ring's input b is
+// -bmax; a negative one is sampled by the strata type, a positive one is used as it is.
+__device__ __forceinline__ double impact_parameter(const cair_work_item& W, double u) {
+  const double bring = -W.bmax, bmin = -W.bmin;
+  if (bring >= 0.0) return bring;
+  if (W.b_mode == 1) return sqrt(bmin * bmin + u * (bring * bring - bmin * bmin));
+  if (W.b_mode == 2) return bmin + u * (-bring - bmin);
+  return -sqrt(u) * bring;
+}
 
 // BondLength (StateInitDiatomAtom_Module.F90:543-730): FuncRHS of the radial motion
 struct RadialRhs {
@@ -199,10 +212,9 @@ __global__ void __launch_bounds__(128) k_sample_ic3(DevSys S, int64_t ntot, cons
     const double* m = S.mass;
     double q[3][2], qd[3][2];
     diatom_ic(S, levels[W.ilevel], m[0], m[1], dr, q, qd);
-    // CoordVeloc_FreeTotAngMom: Boltzmann energy and the impact parameter (Circles, one ring)
+    // CoordVeloc_FreeTotAngMom: Boltzmann energy and the impact parameter
     const double er = boltzmann_er(W.ttra, dr[4]);
-    double b = -W.bmax;
-    if (b < 0.0) b = -sqrt(dr[5]) * b;
+    const double b = impact_parameter(W, dr[5]);
     // ComputeCoordinatesVelocities + ShiftCoordinates (the atom sits at the origin of its frame)
     const double mt = m[0] + m[1], mp = m[2];
     const double redmass = mt * mp / (mt + mp);
@@ -245,8 +257,7 @@ __global__ void __launch_bounds__(128) k_sample_ic4(DevSys S, int64_t ntot, cons
     diatom_ic(S, levels[W.ilevel], m[0], m[1], dr, q1, qd1);
     diatom_ic(S, levels[W.ilevel2], m[2], m[3], dr + 4, q2, qd2);
     const double er = boltzmann_er(W.ttra, dr[8]);
-    double b = -W.bmax;
-    if (b < 0.0) b = -sqrt(dr[9]) * b;
+    const double b = impact_parameter(W, dr[9]);
     const double mt = m[0] + m[1], mp = m[2] + m[3];
     const double redmass = mt * mp / (mt + mp);
     const double fA = -mp / (mt + mp), fB = mt / (mt + mp);
@@ -304,7 +315,7 @@ __global__ void __launch_bounds__(128) k_results(DevSys S, FsArgs F, int64_t n, 
     cair_traj_result r;
     const int it = item_of ? item_of[k] : 0;
     r.item = it;
-    r.idx = item_of ? (k - items[it].first + 1) : (k + 1);
+    r.idx = item_of ? (items[it].skip + k - items[it].first + 1) : (k + 1);
     r.ipes = item_of ? items[it].ipes : 0;
     r.status = status[k];
     r.iste = iste[k];

@@ -1,12 +1,15 @@
 // Final-state statistics on the device (app/TrajectoriesStats/Statistics_Class.F90, Histogram
-// assignment, conditions J, v, arrangement or J1, v1, J2, v2, arrangement): each finished trajectory's row is turned into
-// its initial- and final-state codes where it lies in HBM, and the rows are counted per
-// (work item, final state) in an open-addressing table, so the cross sections need only the table
-// back on the host instead of the million trajectories.out rows.
+// assignment, conditions J, v, arrangement or J1, v1, J2, v2, arrangement): each finished
+// trajectory's row is turned into its initial- and final-state codes where it lies in HBM, and the
+// rows are counted per (run, final state, impact-parameter ring) in an open-addressing table, so
+// the cross sections need only the table back on the host instead of the million
+// trajectories.out rows.
 #pragma once
 #include "cair_device.cuh"
 
 namespace cair {
+
+constexpr int kMaxRings = 64;  // impact-parameter rings per run
 
 struct StatsArgs {
   int64_t ntot;
@@ -15,12 +18,16 @@ struct StatsArgs {
   int32_t iskip[5];
   int32_t pres[5];
   double ham_abs_tol;
-  unsigned long long nitems;      // table key = final-state code x nitems + item
+  const int32_t* item_run;        // run of each work item
+  const double* ring_b;           // ascending ring bounds of each run, kMaxRings per run
+  const int32_t* nring;           // rings of each run
+  long long nruns, R;             // table key = (final-state code x nruns + run) x R + ring
   unsigned long long* keys;       // ~0 = empty
   unsigned long long* counts;
   unsigned long long mask;        // table size - 1 (a power of two)
-  unsigned long long* item_rows;  // rows of each item in the statistics (TrajsPerb)
+  unsigned long long* item_rows;  // counted rows of each item
   long long* item_inicode;        // smallest initial-state code of each item (IniStateCode(1))
+  unsigned long long* ring_rows;  // rows of each (run, ring): TrajsPerb
   int* error;                     // 1: a quantum number at or above qnmax; 2: an unrepresentable key
 };
 
@@ -91,23 +98,52 @@ __device__ __forceinline__ unsigned long long stats_hash(unsigned long long k) {
 }
 
 #ifndef CAIR_MODEL_TU
-// Rows that enter the statistics: finished trajectories whose energy is conserved (the others go
-// to trajectories_HNotCons.out, Integrator_Class.F90:755-776, 884-888).
+__device__ __forceinline__ bool stats_counted(const StatsArgs& A, const cair_traj_result& r) {
+  // finished trajectories whose energy is conserved (the others go to trajectories_HNotCons.out,
+  // Integrator_Class.F90:755-776, 884-888)
+  return r.status == CAIR_TRAJ_DONE && fabs(r.dH) <= A.ham_abs_tol;
+}
+
+// Pass 1: rows and the initial-state code of each item (the rings of a run are the bMax values
+// its rows carry, SetRings, Statistics_Class.F90:511-586).
 template <int NC>
-__global__ void __launch_bounds__(256) k_stats_count(StatsArgs A) {
+__global__ void __launch_bounds__(256) k_stats_items(StatsArgs A) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < A.ntot; k += (int64_t)gridDim.x * blockDim.x) {
     const cair_traj_result r = A.rows[k];
-    if (r.status != CAIR_TRAJ_DONE || !(fabs(r.dH) <= A.ham_abs_tol)) continue;
+    if (!stats_counted(A, r)) continue;
     long long ic, fc;
     bool bad = false;
     stats_codes<NC>(A, r, ic, fc, bad);
     if (bad) atomicExch(A.error, 1);
     atomicAdd(A.item_rows + r.item, 1ull);
     atomicMin(A.item_inicode + r.item, ic);
-    // |fc| < 70 qnmax^NC (a cluster's arrangement code is negative), and 70 qnmax^NC x nitems < 2^62
-    // is checked on the host: the key is fc x nitems + item as a two's-complement 64-bit number
-    const unsigned long long key = (unsigned long long)fc * A.nitems + (unsigned long long)r.item;
-    if (key == kStatsEmpty) {  // fc = -1 on the last item: not representable in the table
+  }
+}
+
+// Pass 2: each row's ring from its sampled b (AddFinState: ring iR + 1 when
+// bRings(iR) < b <= bRings(iR+1), else the first) and its (run, final state, ring) count.
+template <int NC>
+__global__ void __launch_bounds__(256) k_stats_count(StatsArgs A) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < A.ntot; k += (int64_t)gridDim.x * blockDim.x) {
+    const cair_traj_result r = A.rows[k];
+    if (!stats_counted(A, r)) continue;
+    long long ic, fc;
+    bool bad = false;
+    stats_codes<NC>(A, r, ic, fc, bad);
+    const int run = A.item_run[r.item];
+    const double* e = A.ring_b + (size_t)run * kMaxRings;
+    const int nr = A.nring[run];
+    int ring = 0;
+    for (int q = 0; q < nr - 1; ++q)
+      if (!(r.b > e[q + 1] || r.b <= e[q])) {
+        ring = q + 1;
+        break;
+      }
+    atomicAdd(A.ring_rows + (size_t)run * kMaxRings + ring, 1ull);
+    // |fc| < 70 qnmax^NC (a cluster's arrangement code is negative) and 70 qnmax^NC x nruns x R < 2^62
+    // is checked on the host: the key is a two's-complement 64-bit number
+    const unsigned long long key = (unsigned long long)((fc * A.nruns + run) * A.R + ring);
+    if (key == kStatsEmpty) {  // the key -1: not representable in the table
       atomicExch(A.error, 2);
       continue;
     }

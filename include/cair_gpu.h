@@ -44,7 +44,7 @@ extern "C" {
 #endif
 
 #define CAIR_MAX_PES 16
-#define CAIR_ABI_VERSION 5
+#define CAIR_ABI_VERSION 6
 
 /* Surface models (PES_Factory_Class.F90:46-329, System x PES_Model strings). */
 enum cair_pes_model {
@@ -154,15 +154,23 @@ typedef struct cair_work_item {
   int64_t ntraj;    /* number of trajectories                                   */
   int64_t seed;     /* stream seed ("Initial Random Nb Seed" mapped per process) */
   double ttra;      /* translational temperature [K] (Boltzmann model)         */
-  double bmax;      /* impact-parameter bound [bohr] (Circles, one ring)       */
+  double bmax;      /* the ring's bound [bohr] = -(the ring's input "b"): > 0 sampled by b_mode,
+                       < 0 the fixed impact parameter -bmax (no random number drawn) */
   double dinit;     /* initial separation [bohr]                               */
   int32_t ilevel2;  /* diatom + diatom: row of the projectile's level (atoms 3, 4) */
-  int32_t pad;
+  int32_t b_mode;   /* "Impact Parameter Strata Type" (Collision_Class.F90:1276-1296), U uniform:
+                       0 Circles:  b = sqrt(U) bmax
+                       1 Rings:    b = sqrt(bmin^2 + U (bmax^2 - bmin^2))
+                       2 Segments: b = -bmin + U (bmax + bmin)                              */
+  double bmin;      /* -(the previous ring's input "b"), 0 for the first ring (GetImpactParamValue) */
+  int64_t skip;     /* trajectories of the same stream before this item's first: the earlier rings
+                       of a stratified run (Ring%iTrajMax of the previous ring); the item's stream
+                       is drawn through them and its rows are numbered from skip + 1 */
 } cair_work_item;
 
 /* One row of trajectories.out (Integrator_Class.F90:884-933) plus diagnostics. */
 typedef struct cair_traj_result {
-  int64_t idx;      /* trajectory index within its item, 1-based (Traj%Idx)          */
+  int64_t idx;      /* index in its item's stream, 1-based: skip + k + 1 (Traj%Idx)   */
   int32_t item;     /* work item                                                   */
   int32_t ipes;     /* 0-based surface                                              */
   int32_t status;   /* cair_traj_status                                             */
@@ -303,8 +311,12 @@ void cair_queue_graph_destroy(cair_queue_graph* graph);
  * "Final States Assigment Mthd = Histogram", "Identical Diatoms? = no"; three conditions J, v,
  * arrangement for diatom + atom, five J1, v1, J2, v2, arrangement for diatom + diatom) and rate
  * coefficients (Process_Class.F90:122-209 with the Boltzmann mean velocity of
- * Collision_Class.F90:576-595).  Each work item is one run; its rows are the finished trajectories
- * whose |dH| <= ham_abs_tol (the rest are the HNotCons rows).  One impact-parameter ring per item. */
+ * Collision_Class.F90:576-595).  A run is what the reference's statistics read for one initial
+ * state: the rows of every surface and impact-parameter ring of one level and temperature, merged
+ * (item_run maps each work item to its run; NULL makes every item its own run).  Rows counted are
+ * the finished trajectories whose |dH| <= ham_abs_tol (the rest are the HNotCons rows).  The
+ * rings of a run are the distinct |bmax| of its items that have counted rows (SetRings, within
+ * 1e-3), and each row falls in the ring its sampled b lies in, as AddFinState assigns it. */
 typedef struct cair_stats_params {
   int32_t qn_max;            /* QuantumNumberMax (300 in the reference)                         */
   int32_t ncond;             /* "Nb of Final Conditions": 3 (J, v, arr) or 5 (J1, v1, J2, v2, arr) */
@@ -317,25 +329,26 @@ typedef struct cair_stats_params {
 /* One line of the statistics output (FinCondVec, IniState, Cross, CrossSD) plus its rate;
  * conditions beyond ncond are zero. */
 typedef struct cair_final_state {
-  int32_t item;              /* work item                                                       */
+  int32_t run;               /* run (the work item when item_run is NULL)                      */
   int32_t fin[5];            /* FinCondVec: J, v, arrangement or J1, v1, J2, v2, arrangement    */
   int32_t ini[5];            /* IniState                                                        */
-  int32_t pad;
+  int32_t nrings;            /* impact-parameter rings of the run                               */
   int64_t count;             /* rows that ended in this state                                   */
-  int64_t nrows;             /* rows of the item in the statistics (TrajsPerb)                  */
+  int64_t nrows;             /* rows of the run in the statistics (sum of TrajsPerb)            */
   double cross, cross_sd;    /* [bohr^2]                                                        */
   double rate, rate_sd;      /* cross sections x mean velocity [cm^3/s]                         */
 } cair_final_state;
 
 /* Statistics of `ntot` result rows already on the device (as cair_run_queue_dev leaves them),
- * counted on the GPU; the final states (at most `cap`, sorted by item then final-state code) and
+ * counted on the GPU; the final states (at most `cap`, sorted by run then final-state code) and
  * their count come back to host memory.  Returns CAIR_EINVAL with the needed size in the message
- * when cap is too small.  `items` is the host copy of the work items. */
-int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
-                        const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
-                        int64_t cap, int64_t* nout, void* stream);
+ * when cap is too small, and when the items of one run differ in temperature or initial state.
+ * `items` and `item_run` are host arrays. */
+int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                        int64_t ntot, const cair_traj_result* results, const cair_stats_params* params,
+                        cair_final_state* out, int64_t cap, int64_t* nout, void* stream);
 /* The same from host rows. */
-int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items, int64_t ntot,
+int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run, int64_t ntot,
                     const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
                     int64_t cap, int64_t* nout);
 

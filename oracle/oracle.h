@@ -107,9 +107,11 @@ typedef struct orc_level {
 
 typedef struct orc_ic_cfg {
   double ttra;          /* translational temperature [K] (Boltzmann model) */
-  double bmax;          /* impact parameter ring bound [bohr] (Circles, one ring) */
+  double bmax;          /* -(the ring's input b): > 0 sampled, < 0 the fixed value -bmax */
   double dinit;         /* initial separation [bohr] */
   int    state_specific;
+  int    b_mode;        /* ImpParStrataType: 0 Circles, 1 Rings, 2 Segments */
+  double bmin;          /* -(the previous ring's input b), 0 for the first ring */
 } orc_ic_cfg;
 
 /* Sample one trajectory's initial condition from the stream `rng` (draw order as the

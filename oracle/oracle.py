@@ -43,7 +43,37 @@ class OrcLevel(C.Structure):
 
 
 class OrcIcCfg(C.Structure):
-    _fields_ = [("ttra", C.c_double), ("bmax", C.c_double), ("dinit", C.c_double), ("state_specific", C.c_int)]
+    _fields_ = [("ttra", C.c_double), ("bmax", C.c_double), ("dinit", C.c_double), ("state_specific", C.c_int),
+                ("b_mode", C.c_int), ("bmin", C.c_double)]
+
+
+def impact_rings(ntrajtot, bring, ntring):
+    """InitializeImpactParameter (src/Collision/ImpactParameter_Class.F90:55-160): iTrajMax of each
+    ring for NTrajTot trajectories, NTraj = int(dfloat(Weight * NTrajTot) / SumAllWeight) with the
+    remainder added to the first ring; with a negative weight every iTrajMax stays 0."""
+    nr = len(bring)
+    itrajmax = [0] * nr
+    if any(w < 0 for w in ntring):
+        return itrajmax
+    sum_all = sum(ntring)
+    ntraj = [int(float(w * ntrajtot) / sum_all) for w in ntring]
+    if sum(ntraj) != ntrajtot:
+        ntraj[0] = ntraj[0] + ntrajtot - sum(ntraj)
+    acc = 0
+    for r in range(nr):
+        itrajmax[r] = acc + ntraj[r]
+        acc = itrajmax[r]
+    return itrajmax
+
+
+def impact_ring_of(idx, bring, itrajmax):
+    """GetImpactParamValue (ImpactParameter_Class.F90:202-221) for the 1-based trajectory idx:
+    (bmin, b) of the first ring whose iTrajMax reaches idx; None when none does."""
+    for r in range(len(bring)):
+        if idx > itrajmax[r]:
+            continue
+        return (bring[r - 1] if r > 0 else 0.0), bring[r]
+    return None
 
 
 class OrcMol(C.Structure):
@@ -253,8 +283,11 @@ class Oracle:
         return dict(paq=paq, t=t, dt=dt, H=H, smax=smax, smin=smin, irej=irej, iste=iste, status=st)
 
     # -- initial conditions --
-    def sample_ics(self, n, levels, state_specific=True, ttra=None, bmax=None, dinit=None, seed=None, ilevels=None):
-        """Sample n initial conditions from one RNG stream as the reference does for one PES."""
+    def sample_ics(self, n, levels, state_specific=True, ttra=None, bmax=None, dinit=None, seed=None, ilevels=None,
+                   rings=None):
+        """Sample n initial conditions from one RNG stream as the reference does for one PES.
+        rings = (bring, ntring, b_mode): the n trajectories stratified as ImpactParameter_Class
+        splits them (ring input values bring, weights ntring); otherwise one Circles ring bmax."""
         cfg = self.cfg
         rng = OrcRng()
         self.L.orc_rng_seed(C.byref(rng), int(cfg.seed if seed is None else seed))
@@ -270,14 +303,20 @@ class Oracle:
         paq, paq0, erra = np.zeros((n, ne)), np.zeros((n, ne)), np.zeros((n, ne))
         H0, b, er = np.zeros(n), np.zeros(n), np.zeros(n)
         il = np.zeros(n, np.int32)
+        if rings is not None:
+            itm = impact_rings(n, rings[0], rings[1])
         for k in range(n):
+            if rings is not None:
+                bmin_r, b_r = impact_ring_of(k + 1, rings[0], itm)
+                ic.bmax, ic.bmin, ic.b_mode = -b_r, -bmin_r, int(rings[2])
             self.L.orc_sample_ic(C.byref(self.s), C.byref(rng), lv, len(levels), C.byref(ic), 0, dp(paq[k]),
                                  dp(paq0[k]), dp(H0[k:k + 1]), dp(erra[k]), dp(b[k:k + 1]), ip(il[k:k + 1]),
                                  dp(er[k:k + 1]))
         return dict(paq=paq, paq0=paq0, H0=H0, erra=erra, b=b, ilevel=il, er=er)
 
-    def sample_ics4(self, n, level1, level2, ttra=None, bmax=None, dinit=None, seed=None):
-        """Diatom + diatom initial conditions (state-specific, one level per molecule) from one stream."""
+    def sample_ics4(self, n, level1, level2, ttra=None, bmax=None, dinit=None, seed=None, rings=None):
+        """Diatom + diatom initial conditions (state-specific, one level per molecule) from one stream;
+        rings as for sample_ics."""
         cfg = self.cfg
         rng = OrcRng()
         self.L.orc_rng_seed(C.byref(rng), int(cfg.seed if seed is None else seed))
@@ -293,7 +332,12 @@ class Oracle:
         ne = self.ne
         paq, paq0, erra = np.zeros((n, ne)), np.zeros((n, ne)), np.zeros((n, ne))
         H0, b, er = np.zeros(n), np.zeros(n), np.zeros(n)
+        if rings is not None:
+            itm = impact_rings(n, rings[0], rings[1])
         for k in range(n):
+            if rings is not None:
+                bmin_r, b_r = impact_ring_of(k + 1, rings[0], itm)
+                ic.bmax, ic.bmin, ic.b_mode = -b_r, -bmin_r, int(rings[2])
             self.L.orc_sample_ic4(C.byref(self.s), C.byref(rng), C.byref(lv[0]), C.byref(lv[1]), C.byref(ic), 0,
                                   dp(paq[k]), dp(paq0[k]), dp(H0[k:k + 1]), dp(erra[k]), dp(b[k:k + 1]),
                                   dp(er[k:k + 1]))

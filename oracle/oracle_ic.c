@@ -147,6 +147,20 @@ static void diatom_ic(const orc_sys* s, orc_rng* rng, const orc_level* L, double
  * SetInitialState_DiatomDiatom (StateInitDiatomDiatom_Module.F90:86-219; state-specific: no level
  * draw) for each molecule, then CoordVeloc_FreeTotAngMom, ComputeCoordinatesVelocities,
  * ShiftCoordinates and SetPaQ (1216-1314, 1591-1849) with the projectile's atom 4 eliminated. ---- */
+/* SETTING THE IMPACT PARAMETER (Collision_Class.F90:1276-1296): Traj%b is the ring's input value;
+ * a negative one is replaced by a draw according to ImpParStrataType, with bmin the previous
+ * ring's input value (GetImpactParamValue, ImpactParameter_Class.F90:202-221). */
+static double impact_parameter(const orc_ic_cfg* cfg, orc_rng* rng) {
+  double tb = -cfg->bmax, bmin = -cfg->bmin;
+  if (tb < 0.0) {
+    double randnum = orc_rng_draw(rng);
+    if (cfg->b_mode == 0) tb = -sqrt(randnum) * tb;                          /* Circles */
+    else if (cfg->b_mode == 1) tb = sqrt(bmin * bmin + randnum * (tb * tb - bmin * bmin));  /* Rings */
+    else tb = bmin + randnum * (-tb - bmin);                                  /* Segments */
+  }
+  return tb;
+}
+
 int orc_sample_ic4(const orc_sys* s, orc_rng* rng, const orc_level* lev1, const orc_level* lev2,
                    const orc_ic_cfg* cfg, int ipes, double* paq, double* paq0, double* H0, double* erra,
                    double* bout, double* er_out) {
@@ -155,11 +169,7 @@ int orc_sample_ic4(const orc_sys* s, orc_rng* rng, const orc_level* lev1, const 
   diatom_ic(s, rng, lev1, m[0], m[1], q1, qd1);
   diatom_ic(s, rng, lev2, m[2], m[3], q2, qd2);
   double er = orc_boltzmann_er(cfg->ttra, orc_rng_draw(rng));
-  double b = -cfg->bmax;
-  if (b < 0.0) {
-    double r2 = orc_rng_draw(rng);
-    b = -sqrt(r2) * b;
-  }
+  double b = impact_parameter(cfg, rng);
   double mt = m[0] + m[1], mp = m[2] + m[3];
   double redmass = mt * mp / (mt + mp);
   double fA = -mp / (mt + mp), fB = mt / (mt + mp);
@@ -261,11 +271,7 @@ int orc_sample_ic(const orc_sys* s, orc_rng* rng, const orc_level* levels, int n
   for (int d = 0; d < 3; ++d) { q[d][2] = 0.0; qd[d][2] = 0.0; }
   /* CoordVeloc_FreeTotAngMom (1216-1314) */
   double er = orc_boltzmann_er(cfg->ttra, orc_rng_draw(rng));
-  double b = -cfg->bmax;                           /* ring bound (Circles), GetImpactParamValue */
-  if (b < 0.0) {
-    double r2 = orc_rng_draw(rng);
-    b = -sqrt(r2) * b;
-  }
+  double b = impact_parameter(cfg, rng);
   /* ComputeCoordinatesVelocities (1591-1670) */
   double mt = m[0] + m[1], mp = m[2];
   double redmass = mt * mp / (mt + mp);

@@ -54,7 +54,12 @@ int main(void) {
   printf("sizeof.cair_level %zu\n", sizeof(cair_level));
   printf("sizeof.cair_work_item %zu\n", sizeof(cair_work_item));
   printf("sizeof.cair_traj_result %zu\n", sizeof(cair_traj_result));
+  printf("sizeof.cair_final_state %zu\n", sizeof(cair_final_state));
+  printf("sizeof.cair_stats_params %zu\n", sizeof(cair_stats_params));
   P(cair_level, eint); P(cair_level, ro); P(cair_work_item, first); P(cair_work_item, dinit);
+  P(cair_work_item, b_mode); P(cair_work_item, bmin); P(cair_work_item, skip);
+  P(cair_final_state, nrings); P(cair_final_state, count); P(cair_final_state, rate_sd);
+  P(cair_stats_params, pres_even_odd); P(cair_stats_params, ham_abs_tol); P(cair_stats_params, xmu);
   P(cair_traj_result, status); P(cair_traj_result, bmax); P(cair_traj_result, dH);
   return 0;
 }
@@ -76,7 +81,10 @@ def test_struct_layout_matches_c(tmp_path):
     assert int(out["sizeof.cair_level"]) == _lib.LEVEL_DTYPE.itemsize
     assert int(out["sizeof.cair_work_item"]) == _lib.ITEM_DTYPE.itemsize
     assert int(out["sizeof.cair_traj_result"]) == _lib.RESULT_DTYPE.itemsize
-    dt = {"cair_level": _lib.LEVEL_DTYPE, "cair_work_item": _lib.ITEM_DTYPE, "cair_traj_result": _lib.RESULT_DTYPE}
+    assert int(out["sizeof.cair_final_state"]) == _lib.FINAL_STATE_DTYPE.itemsize
+    assert int(out["sizeof.cair_stats_params"]) == ctypes.sizeof(_lib.StatsParams)
+    dt = {"cair_level": _lib.LEVEL_DTYPE, "cair_work_item": _lib.ITEM_DTYPE, "cair_traj_result": _lib.RESULT_DTYPE,
+          "cair_final_state": _lib.FINAL_STATE_DTYPE}
     for key, val in out.items():
         if key.startswith("sizeof"):
             continue
@@ -84,7 +92,8 @@ def test_struct_layout_matches_c(tmp_path):
         if T in dt:
             assert dt[T].fields[F][1] == int(val), key
             continue
-        cls = {"cair_system_desc": _lib.SystemDesc, "cair_pes_desc": _lib.PesDesc, "cair_traj_point": _lib.TrajPoint}[T]
+        cls = {"cair_system_desc": _lib.SystemDesc, "cair_pes_desc": _lib.PesDesc, "cair_traj_point": _lib.TrajPoint,
+               "cair_stats_params": _lib.StatsParams}[T]
         assert getattr(cls, F).offset == int(val), key
 
 

@@ -33,7 +33,7 @@ def test_million_trajectories_properties(gpu_lib):
     assert agree.mean() >= 0.999
     st = api.Statistics(H, pres_even_odd=(1, 0, 0)).compute(items, rows)
     for i in range(len(items)):
-        g = st[st["item"] == i]
+        g = st[st["run"] == i]
         assert g["count"].sum() == g["nrows"][0] == items["ntraj"][i]
         assert g["cross"].sum() == pytest.approx(np.pi * items["bmax"][i] ** 2, rel=1e-12)
     H.close()

@@ -15,29 +15,36 @@ def _conds(rows, sel, natoms, which):
     return np.stack([rows[nm + "_" + which][sel] for nm in names], 1)
 
 
-def _compare(H, items, rows, pres, st):
+def _compare(H, items, rows, pres, st, runs=None):
+    """Device statistics against the oracle's on the counted rows of each run (in row order)."""
     import oracle
     cfg = H.cfg
     m = cfg.masses
     nc = 3 if cfg.natoms == 3 else 5
     mt, mp = m[0] + m[1], sum(m[2:])
     xmu = mt * mp / (mt + mp)
-    got = st.compute(items, rows)
+    got = st.compute(items, rows, runs=runs)
     assert np.all(got["fin"][:, nc:] == 0) and np.all(got["ini"][:, nc:] == 0)
+    run_of = np.arange(len(items)) if runs is None else np.asarray(runs)
+    row_run = run_of[rows["item"]]
     keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= cfg.ham_abs_tol)
-    for i, it in enumerate(items):
-        sel = keep & (rows["item"] == i)
-        ref, ini = oracle.statistics(np.full(sel.sum(), it["bmax"]), rows["b"][sel],
+    for run in np.unique(run_of):
+        sel = keep & (row_run == run)
+        g = got[got["run"] == run]
+        if sel.sum() == 0:
+            assert len(g) == 0
+            continue
+        ref, ini = oracle.statistics(rows["bmax"][sel], rows["b"][sel],
                                      _conds(rows, sel, cfg.natoms, "i"), _conds(rows, sel, cfg.natoms, "f"),
                                      iskip=(1,) * nc, pres=pres, cap=max(64, int(sel.sum())))
-        g = got[got["item"] == i]
         assert len(g) == len(ref)
         gd = {tuple(int(x) for x in r["fin"][:nc]): r for r in g}
-        vel = oracle.mean_velocity(it["ttra"], xmu)
+        vel = oracle.mean_velocity(items["ttra"][run_of == run][0], xmu)
+        nrings = len(np.unique(rows["bmax"][sel]))
         for fs, n, cross, sd in ref:
             r = gd[fs]
             assert tuple(int(x) for x in r["ini"][:nc]) == ini
-            assert r["count"] == n and r["nrows"] == sel.sum()
+            assert r["count"] == n and r["nrows"] == sel.sum() and r["nrings"] == nrings
             assert r["cross"] == pytest.approx(cross, rel=1e-14)
             assert r["cross_sd"] == pytest.approx(sd, rel=1e-14, abs=1e-300)
             assert r["rate"] == pytest.approx(cross * vel, rel=1e-13)
@@ -57,7 +64,7 @@ def test_statistics_of_a_queue_run(gpu_lib, oracle_lib):
     got = _compare(H, items, rows, (1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 0)))
     # every counted row is in exactly one final state
     for i in range(len(items)):
-        g = got[got["item"] == i]
+        g = got[got["run"] == i]
         assert g["count"].sum() == g["nrows"][0]
     H.close()
 
@@ -127,20 +134,61 @@ def test_statistics_on_synthetic_diatom_diatom_rows(gpu_lib, oracle_lib):
 
 
 def test_statistics_of_an_o2_o2_queue_run(gpu_lib, oracle_lib):
-    """Rows of a real O2 + O2 queue run (two items, the three O4 surfaces) through the device
-    statistics and through the oracle's: identical final states, counts and cross sections."""
+    """Rows of a real O2 + O2 queue run through the device statistics and the oracle's: the three
+    surfaces of one level pair (degeneracy blocks 1/3/5) pooled into one run, as the reference's
+    statistics read every surface's rows of a level, and a second level pair on its own."""
     cfg = systems.o4_config()
     H = api.Handle(cfg)
     lv = systems.load_levels("O2")
     il = [int(np.flatnonzero((lv["vqn"] == 0) & (lv["jqn"] == j))[0]) for j in (1, 3)]
     table = api.level_table(lv[il])
-    items = api.work_items([(0, 0, 48, api.process_seed(5, 1), 10000.0, 8.0, 18.0, 1),
-                            (1, 1, 48, api.process_seed(5, 2), 20000.0, 8.0, 18.0, 0)])
+    seed = api.process_seed(5, 1)
+    blocks = api.degeneracy_blocks(72, cfg.degeneracy)
+    entries = [(0, p, nt, seed, 10000.0, 8.0, 18.0, 1) for p, nt in enumerate(blocks)]
+    entries.append((1, 1, 24, api.process_seed(5, 2), 20000.0, 8.0, 18.0, 0))
+    items = api.work_items(entries)
     rows = api.RunTrajectories(H).run(table, items)
-    got = _compare(H, items, rows, (0, 0, 0, 0, 0), api.Statistics(H))
-    for i in range(len(items)):
-        g = got[got["item"] == i]
+    runs = [0, 0, 0, 1]
+    got = _compare(H, items, rows, (0, 0, 0, 0, 0), api.Statistics(H), runs=runs)
+    for run in (0, 1):
+        g = got[got["run"] == run]
         assert g["count"].sum() == g["nrows"][0]
+    assert got[got["run"] == 0]["nrows"][0] == np.sum((rows["item"] < 3) & (rows["status"] == 0) &
+                                                      (np.abs(rows["dH"]) <= cfg.ham_abs_tol))
+    H.close()
+
+
+def test_statistics_pool_rings_and_skip_empty_ones(gpu_lib, oracle_lib):
+    """Impact-parameter rings (SetRings and the ring assignment of AddFinState): 60k synthetic rows in
+    two runs.  Run 0 has items with bmax 2, 4 and 6 bohr (Circles: each samples its whole disc, so
+    rows fall in inner rings too), and the 4-bohr item's rows are all HNotCons, so its ring is not a
+    ring of the statistics; run 1 pools two items of one bmax (two surfaces).  Cross sections sum
+    ring area x probability over the rings, against the oracle on the same rows."""
+    cfg = systems.n3_config()
+    H = api.Handle(cfg)
+    rng = np.random.default_rng(5)
+    bm = [2.0, 4.0, 6.0, 5.0, 5.0]
+    counts = [8000, 12000, 20000, 10000, 10000]
+    items = api.work_items([(0, 0, c, 1, 10000.0, b, 15.0) for c, b in zip(counts, bm)])
+    n = sum(counts)
+    rows = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    rows["item"] = np.repeat(np.arange(5), counts)
+    rows["bmax"] = np.repeat(bm, counts)
+    rows["b"] = rows["bmax"] * np.sqrt(rng.uniform(size=n))
+    rows["j_i"], rows["v_i"], rows["arr_i"] = 20.5, 0.5, 16.5
+    rows["j_f"] = rng.uniform(0.0, 45.0, n)
+    rows["v_f"] = rng.uniform(-0.5, 6.0, n)
+    rows["arr_f"] = rng.choice([16.5, 17.5, 32.5, 48.5], n)
+    rows["status"] = 0
+    rows["dH"] = np.where(rows["item"] == 1, 1.0, 1e-9)
+    runs = [0, 0, 0, 1, 1]
+    got = _compare(H, items, rows, (1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 0)), runs=runs)
+    assert set(got[got["run"] == 0]["nrings"]) == {2} and set(got[got["run"] == 1]["nrings"]) == {1}
+    # items of one run must share the temperature
+    bad = items.copy()
+    bad["ttra"][2] = 20000.0
+    with pytest.raises(api.CairError, match="temperature"):
+        api.Statistics(H).compute(bad, rows, runs=runs)
     H.close()
 
 

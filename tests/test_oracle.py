@@ -377,3 +377,55 @@ def test_statistics_known_answers(oracle_lib):
     vp = np.sqrt(2 * 10000.0 / 3.1577513e5 / xmu)
     assert oracle.mean_velocity(10000.0, xmu) == pytest.approx(2 / np.sqrt(np.pi) * vp * 4.134137e16 * 0.5291771e-8 ** 3,
                                                                rel=1e-14)
+
+
+SCATTERING_RINGS = ([-0.25, -0.5, -1.0, -2.5, -4.0, -7.55], [1, 1, 1, 1, 1, 1])  # CoarseAIR_Scattering.inp:166-178
+RINGS_EXAMPLE = ([-6.0, -14.0], [1, 99])                                          # CoarseAIR_Scattering.inp:181-186
+
+
+def test_impact_parameter_rings_split_like_the_reference(oracle_lib):
+    """InitializeImpactParameter on the reference's own stratified inputs: equal weights give
+    int(N/6) per ring with the remainder in the first; api.ring_entries (the product's helper) and
+    the oracle's restatement agree on counts, stream offsets and (bmin, b) for every weight set."""
+    import oracle
+    from coarseair_gb300 import api
+    assert [e[2] for e in api.ring_entries(0, 0, 100, 1, 1e4, 15.0, *SCATTERING_RINGS)] == [20, 16, 16, 16, 16, 16]
+    assert [e[2] for e in api.ring_entries(0, 0, 100, 1, 1e4, 15.0, *RINGS_EXAMPLE, strata="Rings")] == [1, 99]
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        nr = int(rng.integers(1, 7))
+        bring = list(-rng.uniform(0.5, 9.0, nr))
+        ntring = [int(x) for x in rng.integers(1, 40, nr)]
+        n = int(rng.integers(nr, 5000))
+        ent = api.ring_entries(0, 0, n, 1, 1e4, 15.0, bring, ntring)
+        itm = oracle.impact_rings(n, bring, ntring)
+        assert [e[10] + e[2] for e in ent] == itm
+        for e in ent:
+            for idx in (e[10] + 1, e[10] + e[2]):
+                if e[2] == 0:
+                    continue
+                bmin, b = oracle.impact_ring_of(idx, bring, itm)
+                assert (-e[5], -e[9]) == (b, bmin)
+
+
+@pytest.mark.parametrize("mode,rings", [(0, SCATTERING_RINGS), (1, RINGS_EXAMPLE), (2, RINGS_EXAMPLE)])
+def test_stratified_impact_parameters_stay_in_their_strata(oracle_lib, mode, rings):
+    """Collision_Class.F90:1276-1296 on the oracle's stream: Circles samples each ring's whole disc,
+    Rings the annulus between the previous ring and this one, Segments b = bmin + U (|b| - bmin)
+    with the previous ring's signed input value."""
+    import oracle
+    from oracle import Oracle
+    from coarseair_gb300 import systems
+    o = Oracle(systems.n3_config())
+    lv = systems.load_levels("N2")[[5]]
+    lvo = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax", "tau",
+                                                   "ri", "ro", "rlim")])
+    for c in lvo.dtype.names:
+        lvo[c] = lv[c] if c in lv.dtype.names else 0.0
+    n = 120
+    ic = o.sample_ics(n, lvo, seed=7, ttra=1e4, dinit=15.0, rings=(rings[0], rings[1], mode))
+    itm = oracle.impact_rings(n, *rings)
+    for k in range(n):
+        bmin, b = oracle.impact_ring_of(k + 1, rings[0], itm)
+        lo, hi = {0: (0.0, -b), 1: (-bmin, -b), 2: (bmin, -b)}[mode]
+        assert lo - 1e-12 <= ic["b"][k] <= hi + 1e-12
