@@ -10,7 +10,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcair_gpu.so")
-CAIR_MAX_PES = 16
+CAIR_MAX_PES = 64
 CAIR_ABI_VERSION = 6
 CAIR_STATIC_QUEUE_MAX_TRAJ = 16384
 

@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libcair_gpu.so")
 # model so the per-model kernels compile in parallel
 SOURCES = [("cair_api.cu", "cair_api.o", []), ("cair_output.cpp", "cair_output.o", [])] + [
     ("cair_model.cu", "cair_model_%s.o" % name, ["-DCAIR_MODEL_ID=%d" % mid])
-    for name, mid in (("o3_umn", 1), ("n3_umn", 2), ("o4_umn", 3), ("o3_nn", 4), ("n4_umn", 5))]
+    for name, mid in (("o3_umn", 1), ("n3_umn", 2), ("o4_umn", 3), ("o3_nn", 4), ("n4_umn", 5), ("o3_bnn", 6))]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177",
                      "-I", os.path.join(HERE, "..", "include")]

@@ -191,18 +191,20 @@ int with_model(cair_handle* h, F&& f) {
 // header states) -> the kernels' fixed 20 x 10 layout (CAIR_NN_* offsets in cair_device.cuh),
 // padded with zeros, plus W1's storage as Potential's dgemm reads it: a 3 x NHL1 matrix with
 // leading dimension 3 (O3_NN_PES_Class.F90:281).
-int pack_o3nn(const double* c, int32_t ncoef, std::vector<double>& out) {
+// A BNN sample (BNN_PES_Class.F90) is packed the same way with its Noise appended.
+int pack_o3nn(const double* c, int32_t ncoef, bool bnn, std::vector<double>& out) {
   const double fh1 = c[0], fh2 = c[1];
   if (!(fh1 >= 1 && fh1 <= CAIR_NN_H1 && fh2 >= 1 && fh2 <= CAIR_NN_H2)) return CAIR_EINVAL;
   const int h1 = (int)fh1, h2 = (int)fh2;
-  if (h1 != fh1 || h2 != fh2 || ncoef != 12 + 7 * h1 + h1 * h2 + 2 * h2) return CAIR_EINVAL;
+  if (h1 != fh1 || h2 != fh2 || ncoef != 12 + 7 * h1 + h1 * h2 + 2 * h2 + (bnn ? 1 : 0)) return CAIR_EINVAL;
   const double* W1 = c + 11;
   const double* b1 = W1 + 6 * h1;
   const double* W2 = b1 + h1;
   const double* b2 = W2 + h1 * h2;
   const double* W3 = b2 + h2;
   const double b3 = W3[h2];
-  out.assign(CAIR_NN_NCOEF, 0.0);
+  out.assign(bnn ? CAIR_BNN_NCOEF : CAIR_NN_NCOEF, 0.0);
+  if (bnn) out[CAIR_BNN_NOISE] = W3[h2 + 1];
   out[CAIR_NN_LAM] = c[2];
   out[CAIR_NN_RE] = c[3];
   for (int i = 0; i < 3; ++i) {
@@ -384,13 +386,18 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
   for (int p = 0; p < d->npes; ++p) {
     const cair_pes_desc& src = d->pes[p];
     int expect = src.model == CAIR_PES_O3_UMN ? 56 : (src.model == CAIR_PES_N3_UMN || src.model == CAIR_PES_N4_UMN) ? 276
-                 : src.model == CAIR_PES_O4_UMN ? 430 : src.model == CAIR_PES_O3_NN ? 0 : -1;
+                 : src.model == CAIR_PES_O4_UMN ? 430 : (src.model == CAIR_PES_O3_NN || src.model == CAIR_PES_O3_BNN) ? 0
+                 : -1;
     if (expect < 0) return bad(CAIR_EINVAL, "unknown surface model");
     std::vector<double> packed;
-    if (src.model == CAIR_PES_O3_NN) {
+    if (src.model == CAIR_PES_O3_NN || src.model == CAIR_PES_O3_BNN) {
+      const bool bnn = src.model == CAIR_PES_O3_BNN;
       if (!src.coef || src.ncoef < 12) return bad(CAIR_EINVAL, "O3 NN: coefficient array too short");
-      if (int e = pack_o3nn(src.coef, src.ncoef, packed)) return bad(e, "O3 NN: hidden layers must be 1..20 and 1..10 "
-                                                                       "neurons and ncoef = 12 + 7 NHL1 + NHL1 NHL2 + 2 NHL2");
+      if (int e = pack_o3nn(src.coef, src.ncoef, bnn, packed))
+        return bad(e, bnn ? "O3 BNN: hidden layers must be 1..20 and 1..10 neurons and ncoef = 13 + 7 NHL1 + NHL1 NHL2 "
+                            "+ 2 NHL2"
+                          : "O3 NN: hidden layers must be 1..20 and 1..10 neurons and ncoef = 12 + 7 NHL1 + NHL1 NHL2 "
+                            "+ 2 NHL2");
       if (d->natoms != 3) return bad(CAIR_EINVAL, "surface/atom count mismatch");
     } else if (src.ncoef != expect || !src.coef) {
       return bad(CAIR_EINVAL, "wrong coefficient count for surface");
@@ -947,15 +954,16 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
   const double pip_g = m == CAIR_PES_O3_UMN ? PIP_O3_EVAL_REV_FLOPS : PIP_N3_EVAL_REV_FLOPS;
 #endif
   const double pip_e = m == CAIR_PES_O3_UMN ? PIP_O3_VALUE_FLOPS : PIP_N3_VALUE_FLOPS;
-  if (m == CAIR_PES_O3_NN) {
+  if (m == CAIR_PES_O3_NN || m == CAIR_PES_O3_BNN) {
     // pes_o3nn: MEG-like variables 9, features 41, layer 1 20 x 14, layer 2 and output 10 x 47,
     // output 6, adjoint sweep 20 x 35, dG/dR contraction 148 (tanh counted as one operation);
     // the energy-only network (Potential) 9 + 21 + 20 x 7 + 10 x 43 + 4.  Diatomics with gradient
-    // in both (Compute_Vd_dVd).
-    if (fg) *fg = 9 + 3 * diat_g + 41 + 280 + 470 + 6 + 700 + 148 + 36 + 46 + 18 + 15;
-    if (fe) *fe = 9 + 3 * diat_g + 21 + 140 + 430 + 4 + 36 + 30 + 8;
+    // in both (Compute_Vd_dVd).  BNN: exp(v + Noise) and its factor on the gradient, 2 + 4.
+    const double bo = m == CAIR_PES_O3_BNN ? 1.0 : 0.0;
+    if (fg) *fg = 9 + 3 * diat_g + 41 + 280 + 470 + 6 + 700 + 148 + 36 + 46 + 18 + 15 + 6 * bo;
+    if (fe) *fe = 9 + 3 * diat_g + 21 + 140 + 430 + 4 + 36 + 30 + 8 + 2 * bo;
     if (fa) *fa = 811;
-    if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1) + CAIR_NN_H1 + CAIR_NN_H2;
+    if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1) + CAIR_NN_H1 + CAIR_NN_H2 + bo;
     return 0;
   }
   if (m == CAIR_PES_O4_UMN || m == CAIR_PES_N4_UMN) {

@@ -301,13 +301,18 @@ __device__ __forceinline__ double ftanh(double x) {
 #define CAIR_NN_B2 410     // b2(10)
 #define CAIR_NN_W3 420     // W3(10)
 #define CAIR_NN_NCOEF 430
+#define CAIR_BNN_NOISE 430 // BNN: the sample's Noise
+#define CAIR_BNN_NCOEF 431
 #define CAIR_EV_TO_HARTREE (1.0 / 27.2113839712790)
 
 // GRAD: Compute_O3_NN_PES_1d (357-477): six features G of p = exp(-Lambda (R - re)), network
 // 6 -> tanh(20) -> tanh(10) -> 1, gradient by one adjoint sweep (dV/dG) contracted with dG/dR
 // (the reference builds dG/dR first and carries the three directions forward).
 // !GRAD: O3_NN_Potential_From_R (250-297): three scaled features on W1's storage read as 3 x NHL1.
-template <bool GRAD>
+// BNN (BNN_PES_Class.F90: Compute_BNN_PES_1d 565-640, BNN_Potential_From_R 395-442): the same two
+// networks with the output v taken through VExp = exp(v + Noise): V = (VExp - y_Scaling) eV + the
+// diatomics, dV/dR = VExp dv/dR eV + the diatomics'.
+template <bool GRAD, bool BNN = false>
 __device__ __forceinline__ void pes_o3nn(const DevSys& S, const DevPes& P, const double* R, const double* Ri,
                                          const double* Q, double& V, double* dVdR, double* dVdQ) {
   const double* __restrict__ c = P.coef;
@@ -353,7 +358,9 @@ __device__ __forceinline__ void pes_o3nn(const DevSys& S, const DevPes& P, const
       d2[k] = w3 * (1.0 - y2 * y2);
     }
     v += c[CAIR_NN_B3];
-    V = (v - c[CAIR_NN_YSC]) * CAIR_EV_TO_HARTREE + vdiat;
+    const double vout = BNN ? fexp(v + c[CAIR_BNN_NOISE]) : v;
+    V = (vout - c[CAIR_NN_YSC]) * CAIR_EV_TO_HARTREE + vdiat;
+    const double dscale = BNN ? vout * CAIR_EV_TO_HARTREE : CAIR_EV_TO_HARTREE;
     // adjoint sweep: dV/dG
     double gG[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
@@ -380,7 +387,7 @@ __device__ __forceinline__ void pes_o3nn(const DevSys& S, const DevPes& P, const
       t += -((3.0 * gvs[r]) * pcu + p[r] * pcus) * gG[3];
       t += -((lam * gprod) * (2.0 * p[r] + gvs[r])) * gG[4];
       t += -(((2.0 * psq) * psqs) * inv_lam) * gG[5];
-      dVdR[r] = t * CAIR_EV_TO_HARTREE + dvd[r];
+      dVdR[r] = t * dscale + dvd[r];
     }
     trans_to_cart_3(S, Ri, Q, dVdR, dVdQ);
   } else {
@@ -408,7 +415,8 @@ __device__ __forceinline__ void pes_o3nn(const DevSys& S, const DevPes& P, const
       v += ftanh(z) * c[CAIR_NN_W3 + k];
     }
     v += c[CAIR_NN_B3];
-    V = (v - c[CAIR_NN_YSC]) * CAIR_EV_TO_HARTREE + vdiat;
+    const double vout = BNN ? fexp(v + c[CAIR_BNN_NOISE]) : v;
+    V = (vout - c[CAIR_NN_YSC]) * CAIR_EV_TO_HARTREE + vdiat;
   }
 }
 
@@ -492,6 +500,7 @@ __device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const doub
                                     const double* Q, double& V, double* dVdR, double* dVdQ) {
   if (MODEL == CAIR_PES_O3_UMN) pes_o3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else if (MODEL == CAIR_PES_O3_NN) pes_o3nn<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
+  else if (MODEL == CAIR_PES_O3_BNN) pes_o3nn<GRAD, true>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else if (MODEL == CAIR_PES_O4_UMN) pes_o4<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else if (MODEL == CAIR_PES_N4_UMN) pes_n4<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else pes_n3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);

@@ -30,6 +30,7 @@ struct ModelLaunch {
 };
 
 // Surface models with kernels in this library (one cair_model.cu object each)
-#define CAIR_FOR_EACH_MODEL(X) X(CAIR_PES_O3_UMN) X(CAIR_PES_N3_UMN) X(CAIR_PES_O4_UMN) X(CAIR_PES_O3_NN) X(CAIR_PES_N4_UMN)
+#define CAIR_FOR_EACH_MODEL(X) \
+  X(CAIR_PES_O3_UMN) X(CAIR_PES_N3_UMN) X(CAIR_PES_O4_UMN) X(CAIR_PES_O3_NN) X(CAIR_PES_N4_UMN) X(CAIR_PES_O3_BNN)
 
 }  // namespace cair

@@ -11,6 +11,9 @@ This module reads the same data the reference reads at start-up:
   stored here as ``data/N3_UMN.dat``;
 * O3 NN surfaces: ``dtb/Systems/O3/PESs/NN/<Model>/<NHL1>_<NHL2>/`` (O3_NN_PES_Class.F90:74-232):
   ``ScalingValues.csv`` and ``CalibratedParams/{Lambda,re,W1,b1,W2,b2,W3,b3}.csv``;
+* O3 BNN posterior samples: ``dtb/Systems/O3/PESs/BNN/<Folder>/`` (BNN_PES_Class.F90:95-200,
+  686-770): ``ScalingValues.csv`` and ``CalibratedParams/<name>.csv.<sample>``, packed one line per
+  sample into ``data/O3_BNN/<Folder>/samples.csv.gz`` by ``data/O3_BNN/pack_samples.py``;
 * level lists ``vqn jqn eint egam rmin rmax vmin vmax tau ri ro`` (LevelsContainer_Class.F90).
 
 and fills the input-file keys of the hot path with the values of the reference's own input
@@ -26,7 +29,7 @@ import numpy as np
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
 AMU_TO_AU = 1822.888486209          # [amu] -> electron masses (kgm_To_au / 1000)
-PES_O3_UMN, PES_N3_UMN, PES_O4_UMN, PES_O3_NN, PES_N4_UMN = 1, 2, 3, 4, 5
+PES_O3_UMN, PES_N3_UMN, PES_O4_UMN, PES_O3_NN, PES_N4_UMN, PES_O3_BNN = 1, 2, 3, 4, 5, 6
 DIAT_O2_UMN, DIAT_N2_UMN_FORN4 = 1, 2
 
 _FNUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[dDeE][-+]?\d+)?")
@@ -113,6 +116,36 @@ def load_o3_nn(model="NN_11A1_MPE", hidden=(20, 10)):
     return Surface(PES_O3_NN, coef, name="O3 " + model)
 
 
+def _bnn_samples(folder):
+    with gzip.open(os.path.join(DATA, "O3_BNN", folder, "samples.csv.gz"), "rt") as f:
+        rows = [ln.split(",") for ln in f.read().splitlines() if ln.strip() and not ln.startswith("#")]
+    return {int(r[0]): [float(x) for x in r[1:]] for r in rows}
+
+
+def load_o3_bnn(sample, folder="PES9_Case2_LHS50"):
+    """One posterior sample of the O3 BNN surface as ReadParamPost_BNN reads it
+    (BNN_PES_Class.F90:686-770) with the folder's ScalingValues.csv, packed like load_o3_nn with
+    the sample's Noise appended."""
+    v = _bnn_samples(folder)[int(sample)]
+    h1, h2 = int(v[0]), int(v[1])
+    lam, re_, noise, b3 = v[2:6]
+    q = 6
+    W1 = np.array(v[q:q + 6 * h1]).reshape(6, h1); q += 6 * h1
+    b1 = np.array(v[q:q + h1]); q += h1
+    W2 = np.array(v[q:q + h1 * h2]).reshape(h1, h2); q += h1 * h2
+    b2 = np.array(v[q:q + h2]); q += h2
+    W3 = np.array(v[q:q + h2]); q += h2
+    assert q == len(v)
+    with open(os.path.join(DATA, "O3_BNN", folder, "ScalingValues.csv")) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip()]
+    mean = [float(x) for x in lines[1].split(",")]
+    sd = [float(x) for x in lines[2].split(",")]
+    ysc = float(lines[3].split(",")[0])
+    coef = np.concatenate([[h1, h2, lam, re_], mean, sd, [ysc], W1.ravel(order="F"), b1, W2.ravel(order="F"),
+                           b2, W3, [b3, noise]]).astype(np.float64)
+    return Surface(PES_O3_BNN, coef, name="O3 BNN %s sample %d" % (folder, sample))
+
+
 def load_levels(name):
     """Level list as a structured array (columns LEVEL_COLS)."""
     fn = {"N2": "N2_UMN_ForN4_FromRoss.inp.gz", "O2": "O2_UMN_FromUMN_Sorted.inp.gz"}[name]
@@ -194,6 +227,15 @@ def o3nn_config(model="NN_11A1_MPE", mass_amu=15.9994, **kw):
     """O2 + O on an O3 NN surface with the O2 UMN diatomic."""
     m = mass_amu * AMU_TO_AU
     return SystemConfig("O2+O " + model, 3, (m, m, m), [load_o3_nn(model)], DIAT_O2_UMN, **kw)
+
+
+def o3bnn_config(samples=range(1, 51), folder="PES9_Case2_LHS50", mass_amu=15.9994, **kw):
+    """O2 + O on the O3 BNN with the O2 UMN diatomic, one surface per posterior sample
+    ("Nb of PESs Samples"; with "Initial Random Nb Seed for PES Parameters Sampling = 0" sample i
+    is file .i, Collision_Class.F90:383-394), degeneracy one each (Input_Class.F90:905-923)."""
+    m = mass_amu * AMU_TO_AU
+    surfs = [load_o3_bnn(i, folder) for i in samples]
+    return SystemConfig("O2+O BNN " + folder, 3, (m, m, m), surfs, DIAT_O2_UMN, degeneracy=(1.0,) * len(surfs), **kw)
 
 
 def n3_config(mass_amu=14.0067, **kw):

@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define CAIR_MAX_PES 16
+#define CAIR_MAX_PES 64
 #define CAIR_ABI_VERSION 6
 
 /* Surface models (PES_Factory_Class.F90:46-329, System x PES_Model strings). */
@@ -52,7 +52,9 @@ enum cair_pes_model {
   CAIR_PES_N3_UMN = 2, /* N3_UMN_PES_Class.F90  (System N3, Model UMN)              */
   CAIR_PES_O4_UMN = 3, /* O4_UMN_PES_Class.F90  (System O4, Model UMN_Singlet/...)  */
   CAIR_PES_O3_NN = 4,  /* O3_NN_PES_Class.F90   (System O3, Model NN_*)             */
-  CAIR_PES_N4_UMN = 5  /* N4_UMN_PES_Class.F90  (System N4, Model UMN; 4 atoms)     */
+  CAIR_PES_N4_UMN = 5, /* N4_UMN_PES_Class.F90  (System N4, Model UMN; 4 atoms)     */
+  CAIR_PES_O3_BNN = 6  /* BNN_PES_Class.F90     (System O3, Model BNN; one surface
+                          per posterior sample, StochPESFlg)                        */
 };
 
 /* Diatomic potentials of the pairs (DiatomicPotential_Factory_Class.F90:115-229). */
@@ -84,10 +86,13 @@ enum cair_traj_status {
  *   NHL1, NHL2, Lambda, re, Scaling_MEAN(3), Scaling_SD(3), y_Scaling, W1(6,NHL1), b1(NHL1),
  *   W2(NHL1,NHL2), b2(NHL2), W3(NHL2), b3
  * (matrices column-major as in Fortran), ncoef = 12 + 7 NHL1 + NHL1 NHL2 + 2 NHL2; the kernels
- * hold NHL1 <= 20, NHL2 <= 10.  The MEG fields are unused. */
+ * hold NHL1 <= 20, NHL2 <= 10.  CAIR_PES_O3_BNN packs one posterior sample the same way
+ * (Initialize_BNN_PES and ReadParamPost_BNN, BNN_PES_Class.F90:95-200, 640-760: ScalingValues.csv
+ * and CalibratedParams/<name>.csv.<sample>) followed by its Noise, ncoef one more.  The MEG fields
+ * are unused. */
 typedef struct cair_pes_desc {
   int32_t model;       /* cair_pes_model                                      */
-  int32_t ncoef;       /* 56 (O3), 276 (N3, N4), 430 (O4), see above (O3 NN)   */
+  int32_t ncoef;       /* 56 (O3), 276 (N3, N4), 430 (O4), see above (NN, BNN) */
   const double* coef;  /* C(1:ncoef) [kcal/mol], copied at cair_create        */
   double a, ab, ra, rb;/* MEG parameters [Ang, Ang^2, Ang, Ang] (O3, O4)      */
   double eref;         /* O4 file value (unused by the energy, as in the reference) */

@@ -28,7 +28,8 @@
 extern "C" {
 #endif
 
-enum { ORC_PES_O3_UMN = 1, ORC_PES_N3_UMN = 2, ORC_PES_O4_UMN = 3, ORC_PES_O3_NN = 4, ORC_PES_N4_UMN = 5 };
+enum { ORC_PES_O3_UMN = 1, ORC_PES_N3_UMN = 2, ORC_PES_O4_UMN = 3, ORC_PES_O3_NN = 4, ORC_PES_N4_UMN = 5,
+       ORC_PES_O3_BNN = 6 };
 enum { ORC_DIAT_O2_UMN = 1, ORC_DIAT_N2_UMN_FORN4 = 2 };
 
 typedef struct orc_pes {
@@ -47,7 +48,7 @@ typedef struct orc_sys {
   double mMiMn[3];
   double Tqp[81], Tpq[81];      /* column-major (i,j) -> [i + 9*j], NEqtVar x NEqtVar */
   int npes;
-  orc_pes pes[16];
+  orc_pes pes[64];
   int diat;
   /* integrator (Input keys "Initial time step", "Error control parameter", ...) */
   double dt0, eps, relax, rmax, tmax, hamabstol;

@@ -25,7 +25,7 @@ class OrcPes(C.Structure):
 class OrcSys(C.Structure):
     _fields_ = [("natoms", C.c_int), ("neqtvar", C.c_int), ("neqttot", C.c_int), ("npairs", C.c_int),
                 ("mass", C.c_double * 4), ("mMiMn", C.c_double * 3), ("Tqp", C.c_double * 81),
-                ("Tpq", C.c_double * 81), ("npes", C.c_int), ("pes", OrcPes * 16), ("diat", C.c_int),
+                ("Tpq", C.c_double * 81), ("npes", C.c_int), ("pes", OrcPes * 64), ("diat", C.c_int),
                 ("dt0", C.c_double), ("eps", C.c_double), ("relax", C.c_double), ("rmax", C.c_double),
                 ("tmax", C.c_double), ("hamabstol", C.c_double), ("nsteps", C.c_int), ("incstpsz", C.c_int),
                 ("ncall", C.c_int), ("nquad", C.c_int), ("rsmal", C.c_double), ("rcent", C.c_double),

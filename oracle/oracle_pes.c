@@ -291,7 +291,7 @@ static void o3nn_scale(const orc_sys* s, const orc_pes* P, const double* R, doub
 void orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale) {
   const orc_pes* P = &s->pes[ipes];
   double rms[6] = {0}, dms[6] = {0}, sc[7];
-  if (P->model == ORC_PES_O3_NN) {
+  if (P->model == ORC_PES_O3_NN || P->model == ORC_PES_O3_BNN) {
     o3nn_scale(s, P, R, scale);
     return;
   }
@@ -498,13 +498,18 @@ static void o4_compute(const orc_sys* s, const orc_pes* P, const double* R, cons
  * dimension 3.  The two therefore differ; both are kept as the reference has them. */
 #define EV_TO_HARTREE (1.0 / 27.2113839712790)
 typedef struct {
-  int h1, h2;
-  double lam, re, mean[3], sd[3], ysc, b3;
+  int h1, h2, bnn;
+  double lam, re, mean[3], sd[3], ysc, b3, noise;
   const double *W1, *b1, *W2, *b2, *W3;
 } nn_view;
 
-static nn_view nn_unpack(const double* c) {
+/* BNN_PES_Class.F90: one posterior sample (ReadParamPost_BNN, 686-770) is this layout followed by
+ * its Noise; Compute (565-640) and Potential (395-442) are the NN's two networks with the output
+ * passed through VExp = exp(V + Noise): V = (VExp - y_Scaling) eV_To_Hartree + sum(VDiat) and
+ * dVdR = VExp sum(dVTemp) eV_To_Hartree + dVDiat. */
+static nn_view nn_unpack(const double* c, int bnn) {
   nn_view v;
+  v.bnn = bnn;
   v.h1 = (int)c[0]; v.h2 = (int)c[1];
   v.lam = c[2]; v.re = c[3];
   for (int i = 0; i < 3; ++i) { v.mean[i] = c[4 + i]; v.sd[i] = c[7 + i]; }
@@ -516,14 +521,17 @@ static nn_view nn_unpack(const double* c) {
   v.b2 = q; q += v.h2;
   v.W3 = q; q += v.h2;
   v.b3 = *q;
+  v.noise = bnn ? q[1] : 0.0;
   return v;
 }
+
+int orc_o3bnn_ncoef(int h1, int h2) { return 13 + 7 * h1 + h1 * h2 + 2 * h2; }
 
 int orc_o3nn_ncoef(int h1, int h2) { return 12 + 7 * h1 + h1 * h2 + 2 * h2; }
 
 static void o3nn_compute(const orc_sys* s, const orc_pes* P, const double* R, const double* Qall, double* V,
                          double* dVdR, double* dVdQ) {
-  const nn_view n = nn_unpack(P->coef);
+  const nn_view n = nn_unpack(P->coef, P->model == ORC_PES_O3_BNN);
   double vd[3], dvd[3], p[3];
   for (int i = 0; i < 3; ++i) orc_diat_VdV(s->diat, R[i], &vd[i], &dvd[i]);
   for (int i = 0; i < 3; ++i) p[i] = exp(-(n.lam * (R[i] - n.re)));
@@ -568,7 +576,8 @@ static void o3nn_compute(const orc_sys* s, const orc_pes* P, const double* R, co
   double v = 0.0;
   for (int k = 0; k < n.h2; ++k) v = v + y2[k] * n.W3[k];
   v = v + n.b3;
-  *V = (v - n.ysc) * EV_TO_HARTREE + ((vd[0] + vd[1]) + vd[2]);
+  const double vexp = n.bnn ? exp(v + n.noise) : 1.0;
+  *V = ((n.bnn ? vexp : v) - n.ysc) * EV_TO_HARTREE + ((vd[0] + vd[1]) + vd[2]);
   if (!dVdR) return;
   for (int r = 0; r < 3; ++r) {
     double dy1[64];
@@ -583,13 +592,13 @@ static void o3nn_compute(const orc_sys* s, const orc_pes* P, const double* R, co
       for (int j = 0; j < n.h1; ++j) acc = acc + n.W2[j + n.h1 * k] * dy1[j];
       sum = sum + (n.W3[k] * (1.0 - y2[k] * y2[k])) * acc;
     }
-    dVdR[r] = sum * EV_TO_HARTREE + dvd[r];
+    dVdR[r] = (n.bnn ? vexp * sum * EV_TO_HARTREE : sum * EV_TO_HARTREE) + dvd[r];
   }
   trans_to_cart_3(s->mMiMn, R, Qall, dVdR, dVdQ);
 }
 
 static double o3nn_potential(const orc_sys* s, const orc_pes* P, const double* R) {
-  const nn_view n = nn_unpack(P->coef);
+  const nn_view n = nn_unpack(P->coef, P->model == ORC_PES_O3_BNN);
   double vd[3], dvd[3], p[3];
   for (int i = 0; i < 3; ++i) orc_diat_VdV(s->diat, R[i], &vd[i], &dvd[i]);
   for (int i = 0; i < 3; ++i) p[i] = exp(-(n.lam * (R[i] - n.re)));
@@ -614,13 +623,14 @@ static double o3nn_potential(const orc_sys* s, const orc_pes* P, const double* R
     v = v + tanh(z) * n.W3[k];
   }
   v = v + n.b3;
+  if (n.bnn) v = exp(v + n.noise);
   return (v - n.ysc) * EV_TO_HARTREE + ((vd[0] + vd[1]) + vd[2]);
 }
 
 /* Rounding-level scale of the O3 NN evaluation: the network evaluated on absolute values, with
  * the absolute error of each pre-activation carried through tanh (|tanh'| <= 1). */
 static void o3nn_scale(const orc_sys* s, const orc_pes* P, const double* R, double* scale) {
-  const nn_view n = nn_unpack(P->coef);
+  const nn_view n = nn_unpack(P->coef, P->model == ORC_PES_O3_BNN);
   double p[3];
   for (int i = 0; i < 3; ++i) p[i] = exp(-(n.lam * (R[i] - n.re)));
   double G[6] = {p[0] * p[1] + p[1] * p[2] + p[2] * p[0], p[0] * p[1] * p[2], 0, 0, 0, 0};
@@ -649,12 +659,25 @@ static void o3nn_scale(const orc_sys* s, const orc_pes* P, const double* R, doub
       for (int k = 0; k < n.h2; ++k) t += fabs(n.W2[j + n.h1 * k]) * fabs(n.W3[k]) * a2[k];
       w1g[i] += fabs(n.W1[i + 6 * j]) * a1[j] * t;
     }
+  /* BNN: VExp = exp(v + Noise) turns an absolute error e in v into VExp (e + u), and the gradient
+   * carries VExp as a factor; VExp from the larger of the two networks' outputs */
+  double vexp = 1.0, gfac = 1.0;
+  if (n.bnn) {
+    double vc, vdsum = 0.0, vdi, dvdi;
+    o3nn_compute(s, P, R, 0, &vc, 0, 0);
+    const double vp = o3nn_potential(s, P, R);
+    for (int i = 0; i < 3; ++i) { orc_diat_VdV(s->diat, R[i], &vdi, &dvdi); vdsum += vdi; }
+    const double ec = (vc - vdsum) / EV_TO_HARTREE + n.ysc, ep = (vp - vdsum) / EV_TO_HARTREE + n.ysc;
+    vexp = fmax(fabs(ec), fabs(ep));
+    gfac = vexp * (1.0 + sv);
+    sv = vexp * (sv + fabs(n.noise) + 1.0) + fabs(n.ysc);
+  }
   scale[0] = sv * EV_TO_HARTREE;
   for (int r = 0; r < 3; ++r) {
     double lp = fabs(n.lam) * 4.0 * (1.0 + p[r]) * (1.0 + p[r]) * (1.0 + p[r]);
     double t = 0.0;
     for (int i = 0; i < 6; ++i) t += lp * w1g[i];
-    scale[1 + r] = t * EV_TO_HARTREE;
+    scale[1 + r] = t * gfac * EV_TO_HARTREE;
   }
   for (int i = 0; i < 3; ++i) {
     double sv, sdv;
@@ -670,7 +693,7 @@ void orc_pes_compute(const orc_sys* s, int ipes, const double* R, const double* 
   if (P->model == ORC_PES_O3_UMN) o3_compute(s, P, R, Qall, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_N3_UMN) n3_compute(s, P, R, Qall, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_N4_UMN) n4_compute(s, P, R, Qall, V, dVdR, dVdQ);
-  else if (P->model == ORC_PES_O3_NN) {
+  else if (P->model == ORC_PES_O3_NN || P->model == ORC_PES_O3_BNN) {
     if (dVdR) o3nn_compute(s, P, R, Qall, V, dVdR, dVdQ);
     else *V = o3nn_potential(s, P, R);
   } else o4_compute(s, P, R, Qall, V, dVdR, dVdQ);

@@ -16,11 +16,13 @@ pytestmark = pytest.mark.gpu
 PROCS = min(16, os.cpu_count() or 1)   # oracle integrations run on spawned processes
 
 CFGS = {"O3": lambda: systems.o3_config(), "N3": lambda: systems.n3_config(),
-        "O3NN": lambda: systems.o3nn_config()}
-LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 10), "O3NN": ("O2", 0, 1)}
-# O3 NN: the reference's Hamiltonian evaluates a different network (Potential) from the forces
-# (Compute), so H is not conserved along its trajectories (O3_NN_PES_Class.F90:250-297 vs 357-477)
-CONSERVES_H = {"O3": True, "N3": True, "O3NN": False}
+        "O3NN": lambda: systems.o3nn_config(), "O3BNN": lambda: systems.o3bnn_config(samples=[17])}
+LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 10), "O3NN": ("O2", 0, 1), "O3BNN": ("O2", 0, 1)}
+# O3 NN and BNN: the reference's Hamiltonian evaluates a different network (Potential) from the
+# forces (Compute), so H is not conserved along their trajectories (O3_NN_PES_Class.F90:250-297 vs
+# 357-477; BNN_PES_Class.F90:395-442 vs 565-640)
+CONSERVES_H = {"O3": True, "N3": True, "O3NN": False, "O3BNN": False}
+NAMES = ["O3", "N3", "O3NN", "O3BNN"]
 
 
 def _setup(name, **kw):
@@ -53,7 +55,7 @@ def _geometries(o, n, seed):
     return R, Qall
 
 
-@pytest.mark.parametrize("name", ["O3", "N3", "O3NN"])
+@pytest.mark.parametrize("name", NAMES)
 def test_surface_energy_and_gradient_parity(gpu_lib, oracle_lib, name):
     cfg, o, H = _setup(name)
     R, Qall = _geometries(o, 512, 3)
@@ -111,7 +113,7 @@ def _check_rounding_level(o, R, V_o, g_o, candidates, name):
         assert ok, msg
 
 
-@pytest.mark.parametrize("name", ["O3", "N3", "O3NN"])
+@pytest.mark.parametrize("name", NAMES)
 def test_rhs_and_hamiltonian_parity(gpu_lib, oracle_lib, name):
     cfg, o, H = _setup(name)
     ic = _ics(o, name, 128)
@@ -145,7 +147,7 @@ def _non_chaotic(o, ic, nattempts, thresh=1e-11):
     return dev < thresh, a
 
 
-@pytest.mark.parametrize("name", ["O3", "N3", "O3NN"])
+@pytest.mark.parametrize("name", NAMES)
 def test_phase_space_after_1000_attempts(gpu_lib, oracle_lib, name):
     cfg, o, H = _setup(name)
     ic = _ics(o, name, 24)
@@ -173,7 +175,7 @@ def _gpu_final_qn(fs):
     return J, v, arr
 
 
-@pytest.mark.parametrize("name", ["O3", "N3", "O3NN"])
+@pytest.mark.parametrize("name", NAMES)
 def test_final_state_analysis_parity_on_identical_points(gpu_lib, oracle_lib, name):
     cfg, o, H = _setup(name)
     ic = _ics(o, name, 96)
@@ -189,7 +191,7 @@ def test_final_state_analysis_parity_on_identical_points(gpu_lib, oracle_lib, na
     assert np.allclose(fs_g["b"], [f["b"] for f in fs_o], rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.parametrize("name", ["O3", "N3", "O3NN"])
+@pytest.mark.parametrize("name", NAMES)
 def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
     """Final (v, J, arrangement) from the GPU path against the oracle on the same initial
     conditions.  Rounding differs (FMA, exp), so chaotic trajectories can end differently; the

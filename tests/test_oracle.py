@@ -216,6 +216,53 @@ def test_o3nn_surface_pins(oracle_lib):
         assert np.allclose(Vp, V, rtol=1e-12, atol=1e-13)
 
 
+@pytest.mark.parametrize("sample", [1, 17, 50])
+def test_o3bnn_surface_pins(oracle_lib, sample):
+    """O3 BNN posterior samples (BNN_PES_Class.F90): Compute and Potential against the numpy
+    restatement of the NN networks taken through VExp = exp(v + Noise) (the gradient gains the factor
+    VExp), the gradient against finite differences of Compute's energy, permutation invariance."""
+    import ctypes
+    from oracle import Oracle
+    L = oracle_lib.lib()
+    cfg = systems.o3bnn_config(samples=[sample])
+    coef = cfg.surfaces[0].coef
+    h1, h2 = int(coef[0]), int(coef[1])
+    assert coef.size == 13 + 7 * h1 + h1 * h2 + 2 * h2
+    noise, ysc = coef[-1], coef[10]
+    o = Oracle(cfg)
+    rng = np.random.default_rng(13 + sample)
+    Q = _random_geometry(rng, 3, 200)
+    R, Qall = o.rp(Q)
+    keep = np.all((R > 1.6) & (R < 8.0), axis=1)
+    R, Qall = R[keep][:40], Qall[keep][:40]
+    V, g, _ = o.compute(R, Qall)
+    Vd, dVd = np.zeros(len(R)), np.zeros_like(R)
+    for n, row in enumerate(R):
+        for i, r in enumerate(row):
+            v, dv = ctypes.c_double(), ctypes.c_double()
+            L.orc_diat_VdV(1, r, ctypes.byref(v), ctypes.byref(dv))
+            Vd[n] += v.value
+            dVd[n, i] = dv.value
+    Vn, dVn, Vpn = _o3nn_numpy(coef[:-1], R)
+    ev = 27.2113839712790
+    vexp = np.exp(Vn * ev + ysc + noise)
+    assert np.allclose(V, (vexp - ysc) / ev + Vd, rtol=1e-12, atol=1e-13)
+    assert np.allclose(g, vexp[:, None] * dVn + dVd, rtol=1e-10, atol=1e-12)
+    assert np.allclose(o.potential(R), (np.exp(Vpn * ev + ysc + noise) - ysc) / ev + Vd, rtol=1e-12, atol=1e-13)
+    assert np.max(np.abs(o.potential(R) - V)) > 1e-4
+    h = 1e-4
+    for i in range(3):
+        def f(dx):
+            Rs = R.copy()
+            Rs[:, i] += dx
+            return o.compute(Rs, Qall)[0]
+        fd = (8 * (f(h) - f(-h)) - (f(2 * h) - f(-2 * h))) / (12 * h)
+        assert np.all(np.abs(fd - g[:, i]) < 1e-8 * np.maximum(np.abs(g).max(axis=1), 1e-3))
+    for perm in ([0, 2, 1], [2, 1, 0], [1, 0, 2]):
+        Vp, _, _ = o.compute(R[:, perm], Qall)
+        assert np.allclose(Vp, V, rtol=1e-12, atol=1e-13)
+
+
 def _rand12_bigint(digits):
     """Independent restatement of rand12 (RandomVector_Module.F90:166-229) on base-256 digits."""
     ia = [45, 127, 149, 76, 45, 244, 81, 88]
