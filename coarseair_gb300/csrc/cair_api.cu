@@ -997,21 +997,10 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   if (nc != 3 && nc != 5) return fail(h, CAIR_EINVAL, "cair_statistics: ncond must be 3 or 5");
   if (nc != (h->sys.natoms == 4 ? 5 : 3))
     return fail(h, CAIR_EINVAL, "cair_statistics: ncond must be 3 for diatom + atom, 5 for diatom + diatom");
-  std::vector<int32_t> run_of(nitems);
-  int32_t nruns = 0;
-  for (int i = 0; i < nitems; ++i) {
-    run_of[i] = item_run ? item_run[i] : i;
-    if (run_of[i] < 0 || run_of[i] >= nitems) return fail(h, CAIR_EINVAL, "cair_statistics: run out of range");
-    nruns = std::max(nruns, run_of[i] + 1);
-  }
-  std::vector<double> run_ttra(nruns, -1.0);
-  for (int i = 0; i < nitems; ++i) {
-    double& t = run_ttra[run_of[i]];
-    if (t < 0.0) t = items[i].ttra;
-    else if (std::fabs(t - items[i].ttra) > 1e-12 * t)
-      return fail(h, CAIR_EINVAL, "cair_statistics: items of one run differ in temperature");
-  }
   if (P.qn_max < 2) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max out of range");
+  StatsRuns runs;
+  if (std::string e = stats_runs(nitems, items, item_run, runs); !e.empty()) return fail(h, CAIR_EINVAL, e);
+  const int32_t nruns = runs.nruns;
   *nout = 0;
   if (ntot == 0) return 0;
   // table at least twice the rows, so linear probing always finds a slot
@@ -1064,6 +1053,7 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
               item_ini,
               ring_rows,
               derr};
+  // pass 1: rows and initial-state codes of each item
   if (nc == 3) k_stats_items<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
   else k_stats_items<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
   if (int e = check_launch(h)) return e;
@@ -1075,36 +1065,13 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   CUDA_TRY(h, cudaMemcpyAsync(ini.data(), item_ini, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaStreamSynchronize(st));
   if (err == 1) return fail(h, CAIR_EINVAL, "cair_statistics: a quantum number is at or above qn_max");
-  // SetRings per run: the distinct |bMax| (within 1e-3) of the items with counted rows, ascending;
-  // IniState from the smallest initial code of the run
-  std::vector<double> rb((size_t)nruns * kMaxRings, 0.0);
-  std::vector<int32_t> nring(nruns, 0);
-  std::vector<long long> run_ini(nruns, std::numeric_limits<long long>::max());
-  for (int i = 0; i < nitems; ++i) {
-    if (rows[i] == 0) continue;
-    const int r = run_of[i];
-    run_ini[r] = std::min(run_ini[r], ini[i]);
-    double* e = rb.data() + (size_t)r * kMaxRings;
-    const double b = std::fabs(items[i].bmax);
-    bool dup = false;
-    for (int q = 0; q < nring[r]; ++q) dup = dup || std::fabs(b - e[q]) < 1.0e-3;
-    if (dup) continue;
-    if (nring[r] == kMaxRings) return fail(h, CAIR_EINVAL, "cair_statistics: more than 64 rings in a run");
-    e[nring[r]++] = b;
-  }
-  int R = 1;
-  for (int r = 0; r < nruns; ++r) {
-    std::sort(rb.begin() + (size_t)r * kMaxRings, rb.begin() + (size_t)r * kMaxRings + nring[r]);
-    R = std::max(R, (int)nring[r]);
-  }
-  // codes lie within +-70 qn_max^ncond; with the run and ring folded in they must fit a signed 64-bit key
-  double span = 70.0 * (double)nruns * (double)R;
-  for (int q = 0; q < nc; ++q) span *= (double)P.qn_max;
-  if (span >= 4.6e18) return fail(h, CAIR_EINVAL, "cair_statistics: qn_max^ncond x runs x rings too large");
-  A.R = R;
-  CUDA_TRY(h, cudaMemcpyAsync(ring_b, rb.data(), rb.size() * 8, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(h, cudaMemcpyAsync(d_nring, nring.data(), (size_t)nruns * 4, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(h, cudaMemcpyAsync(d_run, run_of.data(), (size_t)nitems * 4, cudaMemcpyHostToDevice, st));
+  if (std::string e = stats_rings(P, nitems, items, rows.data(), ini.data(), runs); !e.empty())
+    return fail(h, CAIR_EINVAL, e);
+  // pass 2: (run, final state, ring) counts
+  A.R = runs.R;
+  CUDA_TRY(h, cudaMemcpyAsync(ring_b, runs.ring_b.data(), runs.ring_b.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_nring, runs.nring.data(), (size_t)nruns * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_run, runs.run_of.data(), (size_t)nitems * 4, cudaMemcpyHostToDevice, st));
   if (nc == 3) k_stats_count<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
   else k_stats_count<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
   k_stats_compact<<<grid_for(h, (int64_t)tsize), 256, 0, st>>>(keys, counts, tsize, okeys, ocounts, tsize, dn);
@@ -1122,102 +1089,8 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
     CUDA_TRY(h, cudaMemcpyAsync(cnt.data(), ocounts, n * 8, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(h, cudaStreamSynchronize(st));
   }
-  // key = (code x nruns + run) x R + ring with a possibly negative code: decode with floor division
-  struct Entry {
-    long long code;
-    int run, ring;
-    unsigned long long count;
-  };
-  auto floordiv = [](long long a, long long b) { return a / b - ((a % b != 0) && ((a < 0) != (b < 0))); };
-  std::vector<Entry> ent(n);
-  for (size_t i = 0; i < n; ++i) {
-    const long long ks = (long long)k[i];
-    const long long rest = floordiv(ks, R);
-    ent[i].ring = (int)(ks - rest * R);
-    ent[i].code = floordiv(rest, nruns);
-    ent[i].run = (int)(rest - ent[i].code * nruns);
-    ent[i].count = cnt[i];
-  }
-  std::sort(ent.begin(), ent.end(), [](const Entry& a, const Entry& b) {
-    return a.run != b.run ? a.run < b.run : (a.code != b.code ? a.code < b.code : a.ring < b.ring);
-  });
-  const long long qn = P.qn_max;
-  long long ifacts = 1;
-  for (int q = 0; q < nc; ++q) ifacts *= qn;
-  const double pi = std::acos(-1.0), k_to_h = 1.0 / 3.1577513e5, bohr_cm = 0.5291771e-8;
-  int64_t o = 0;
-  for (size_t i = 0; i < n;) {
-    size_t j = i;
-    while (j < n && ent[j].run == ent[i].run && ent[j].code == ent[i].code) ++j;
-    if (o == cap) {
-      int64_t lines = o;
-      for (size_t a = i; a < n;) {
-        size_t b = a;
-        while (b < n && ent[b].run == ent[a].run && ent[b].code == ent[a].code) ++b;
-        ++lines;
-        a = b;
-      }
-      return fail(h, CAIR_EINVAL, "cair_statistics: cap too small, " + std::to_string(lines) + " final states");
-    }
-    const int run = ent[i].run;
-    const long long code = ent[i].code;
-    cair_final_state& F = out[o++];
-    F.run = run;
-    F.nrings = nring[run];
-    F.count = 0;
-    for (size_t a = i; a < j; ++a) F.count += (int64_t)ent[a].count;
-    F.nrows = 0;
-    for (int q = 0; q < nring[run]; ++q) F.nrows += (int64_t)perb[(size_t)run * kMaxRings + q];
-    for (int q = 0; q < 5; ++q) F.ini[q] = F.fin[q] = 0;
-    // IniState from the smallest initial code of the run (ProcessStatistics, 782-929)
-    long long isum = run_ini[run], ifact = ifacts;
-    for (int cnd = nc - 1; cnd >= 0; --cnd) {
-      ifact /= qn;
-      const long long t = isum / ifact;
-      F.ini[cnd] = (int)(t - 2);
-      isum -= t * ifact;
-    }
-    // WriteFinStateProbabilities (1288-1440): ring areas, then Cross and CrossSD over the rings
-    const double* e = rb.data() + (size_t)run * kMaxRings;
-    double cr = 0.0, sd = 0.0, prev = 0.0;
-    for (int q = 0; q < nring[run]; ++q) {
-      const double t = pi * e[q] * e[q];
-      double area = t - prev;
-      prev = t;
-      if (nring[run] == 1 && area == 0.0) area = 1.0;
-      unsigned long long w = 0;
-      for (size_t a = i; a < j; ++a)
-        if (ent[a].ring == q) w += ent[a].count;
-      const double pb = (double)std::max<unsigned long long>(perb[(size_t)run * kMaxRings + q], 1ull);
-      const double fw = (double)w / pb;
-      cr = cr + area * fw;
-      sd = sd + fw * (1.0 - fw) * area * area / pb;
-    }
-    F.cross = cr;
-    F.cross_sd = std::sqrt(sd);
-    const int ini_arr = F.ini[nc - 1] / 16;
-    isum = code;
-    ifact = ifacts;
-    int fin_arr = 0;
-    for (int cnd = nc - 1; cnd >= 0; --cnd) {
-      ifact /= qn;
-      long long fc = isum / ifact;
-      if (cnd == nc - 1) fin_arr = (int)((fc - 2) / 16);
-      isum -= fc * ifact;
-      fc -= 2;
-      if (P.pres_even_odd[cnd] && ini_arr == fin_arr) {
-        fc = fc * 2;
-        if (F.ini[cnd] % 2 != 0) fc = fc + 1;
-      }
-      F.fin[cnd] = (int)fc;
-    }
-    const double vp = std::sqrt(2.0 * run_ttra[run] * k_to_h / P.xmu);
-    const double vel = 2.0 / std::sqrt(pi) * vp * 4.134137e16 * (bohr_cm * bohr_cm * bohr_cm);
-    F.rate = F.cross * vel;
-    F.rate_sd = F.cross_sd * vel;
-    i = j;
-  }
-  *nout = o;
+  if (std::string e = stats_finish(P, runs, (int64_t)n, k.data(), cnt.data(), perb.data(), out, cap, nout); !e.empty())
+    return fail(h, CAIR_EINVAL, e);
   return 0;
 }
 

