@@ -1207,3 +1207,28 @@ int cair_fp64_peak_probe(cair_handle* h, double* gflops) {
 
 }  // extern "C"
 
+
+// Internal (not in include/cair_gpu.h): k_ic_draws' stream code and each trajectory's impact
+// parameter run on the host, so that tests can check the stream order (level pick, diatom draws,
+// the earlier rings' trajectories, a fixed b without a draw) against the oracle without a GPU.
+extern "C" int cair_internal_ic_draws(int32_t natoms, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                                      const cair_work_item* items, int64_t ntot, double* draws, int32_t* item_of,
+                                      double* b) {
+  if ((natoms != 3 && natoms != 4) || nlevels < 1 || !levels || nitems < 1 || !items || !draws || !item_of || !b)
+    return CAIR_EINVAL;
+  int64_t sum = 0;
+  for (int i = 0; i < nitems; ++i) {
+    const cair_work_item& w = items[i];
+    if (w.first != sum || w.ntraj < 0 || w.skip < 0 || w.ilevel < 0 || w.ilevel >= nlevels ||
+        (natoms == 4 && (w.ilevel2 < 0 || w.ilevel2 >= nlevels)))
+      return CAIR_EINVAL;
+    sum += w.ntraj;
+  }
+  if (sum != ntot) return CAIR_EINVAL;
+  const int nmol = natoms == 4 ? 2 : 1;
+  for (int i = 0; i < nitems; ++i)
+    if (!cair::continues_stream(items, i)) cair::stream_draws(items, nitems, i, nmol, levels, draws, item_of);
+  for (int64_t g = 0; g < ntot; ++g)
+    b[g] = cair::impact_parameter(items[item_of[g]], draws[cair::kDraws * g + 4 * nmol + 1]);
+  return 0;
+}

@@ -1,7 +1,8 @@
 // Initial conditions on the device (diatom + atom, diatom + diatom) and the per-trajectory result rows.
 //
-//  k_ic_draws     one thread per work item: the item's random-number stream, drawn in the
-//                 reference's order (RandomVector_Module.F90 RandsetVec/RanddwsVec/rand12)
+//  k_ic_draws     one thread per random-number stream (a work item and the impact-parameter rings
+//                 that continue it), drawn in the reference's order (RandomVector_Module.F90
+//                 RandsetVec/RanddwsVec/rand12)
 //  k_sample_ic3/4 one thread per trajectory: SetIniCondForward (Collision_Class.F90:1065-1211)
 //                 for diatom + atom / diatom + diatom, BondLength as a 1-D Bulirsch-Stoer
 //                 integration on the diatomic
@@ -14,7 +15,7 @@ namespace cair {
 
 // rand12: x <- a x mod 2^64 (the reference multiplies base-256 digits), folded into a double
 // by Horner from the least-significant digit with bi = 1/256.
-__device__ __forceinline__ double rand12(unsigned long long& s) {
+__host__ __device__ __forceinline__ double rand12(unsigned long long& s) {
   s = s * 6364136223846793005ull;
   const double bi = 3.90625E-3;
   double r = (double)(unsigned)(s & 0xFFull);
@@ -26,13 +27,13 @@ __device__ __forceinline__ double rand12(unsigned long long& s) {
 struct Stream {
   unsigned long long s;
   double x[100];
-  __device__ void seed(long long iseed) {
+  __host__ __device__ void seed(long long iseed) {
     long long is = iseed;
     if (is % 2 == 0) is = is - 1;
     s = (unsigned long long)is;
     for (int i = 0; i < 100; ++i) x[i] = rand12(s);
   }
-  __device__ double draw() {
+  __host__ __device__ double draw() {
     int i = (int)(99.0 * x[99]) + 1;
     double v = x[99];
     x[99] = x[i - 1];
@@ -44,22 +45,26 @@ struct Stream {
 // Draws kept per trajectory: per diatom (vibphase, rA, rB, rC), then rEr and rb
 constexpr int kDraws = 10;
 
-#ifndef CAIR_MODEL_TU  // model-independent: built once, in the API translation unit
-// nmol = 1: diatom + atom (SetInitialState_DiatomAtom draws the level pick even when state-specific);
-// nmol = 2: diatom + diatom (SetInitialState_DiatomDiatom, state-specific: no level draw).
-__global__ void k_ic_draws(int nitems, int nmol, const cair_work_item* __restrict__ items,
-                           const cair_level* __restrict__ levels, double* __restrict__ draws,
-                           int32_t* __restrict__ item_of) {
-  int it = blockIdx.x * blockDim.x + threadIdx.x;
-  if (it >= nitems) return;
-  const cair_work_item W = items[it];
+// True when work item it continues the random-number stream of item it - 1: the next impact-parameter
+// ring of the same stream (same seed, skip = the previous item's skip + ntraj), as the reference
+// draws ring after ring from one stream (ImpactParameter_Class.F90:202-221).
+__host__ __device__ inline bool continues_stream(const cair_work_item* items, int it) {
+  if (it == 0 || items[it].skip == 0) return false;
+  const cair_work_item& P = items[it - 1];
+  return P.seed == items[it].seed && P.skip + P.ntraj == items[it].skip;
+}
+
+// One stream, drawn in the reference's order into draws[kDraws * g]: the item `head` and the items
+// that continue its stream, each trajectory with its own item's levels and impact-parameter rule.
+// A head with skip > 0 (its earlier rings are not among the items) first draws and drops skip
+// trajectories under its own rule.  nmol = 1: diatom + atom (SetInitialState_DiatomAtom draws the
+// level pick even when state-specific); nmol = 2: diatom + diatom (SetInitialState_DiatomDiatom,
+// state-specific: no level draw).  Host and device: the library runs it on the GPU (k_ic_draws).
+__host__ __device__ inline void stream_draws(const cair_work_item* items, int nitems, int head, int nmol,
+                                             const cair_level* levels, double* draws, int32_t* item_of) {
   Stream st;
-  st.seed(W.seed);
-  double skipped[kDraws];
-  // the earlier rings of the stream (k < 0) are drawn and dropped
-  for (int64_t k = -W.skip; k < W.ntraj; ++k) {
-    const int64_t g = W.first + k;
-    double* d = k < 0 ? skipped : draws + kDraws * g;
+  st.seed(items[head].seed);
+  auto one = [&](const cair_work_item& W, double* d) {
     if (nmol == 1) st.draw();  // level pick (state-specific: the draw is made and the item's level used)
     for (int mol = 0; mol < nmol; ++mol) {
       const cair_level L = levels[mol == 0 ? W.ilevel : W.ilevel2];
@@ -82,14 +87,34 @@ __global__ void k_ic_draws(int nitems, int nmol, const cair_work_item* __restric
     d[4 * nmol] = st.draw();
     // a fixed impact parameter (bmax < 0) draws no random number (Collision_Class.F90:1280-1281)
     d[4 * nmol + 1] = W.bmax > 0.0 ? st.draw() : 0.0;
-    if (k >= 0) item_of[g] = it;
+  };
+  double skipped[kDraws];
+  for (int64_t k = 0; k < items[head].skip; ++k) one(items[head], skipped);
+  for (int it = head; it < nitems && (it == head || continues_stream(items, it)); ++it) {
+    const cair_work_item& W = items[it];
+    for (int64_t k = 0; k < W.ntraj; ++k) {
+      const int64_t g = W.first + k;
+      one(W, draws + kDraws * g);
+      item_of[g] = it;
+    }
   }
+}
+
+#ifndef CAIR_MODEL_TU  // model-independent: built once, in the API translation unit
+// One thread per stream: the thread of an item that continues the previous item's stream has nothing
+// to do (the stream's head draws it).
+__global__ void k_ic_draws(int nitems, int nmol, const cair_work_item* __restrict__ items,
+                           const cair_level* __restrict__ levels, double* __restrict__ draws,
+                           int32_t* __restrict__ item_of) {
+  int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nitems || continues_stream(items, it)) return;
+  stream_draws(items, nitems, it, nmol, levels, draws, item_of);
 }
 #endif
 
 // The impact parameter of one trajectory (Collision_Class.F90:1276-1296): the ring's input b is
 // -bmax; a negative one is sampled by the strata type, a positive one is used as it is.
-__device__ __forceinline__ double impact_parameter(const cair_work_item& W, double u) {
+__host__ __device__ __forceinline__ double impact_parameter(const cair_work_item& W, double u) {
   const double bring = -W.bmax, bmin = -W.bmin;
   if (bring >= 0.0) return bring;
   if (W.b_mode == 1) return sqrt(bmin * bmin + u * (bring * bring - bmin * bmin));

@@ -169,8 +169,11 @@ typedef struct cair_work_item {
                        2 Segments: b = -bmin + U (bmax + bmin)                              */
   double bmin;      /* -(the previous ring's input "b"), 0 for the first ring (GetImpactParamValue) */
   int64_t skip;     /* trajectories of the same stream before this item's first: the earlier rings
-                       of a stratified run (Ring%iTrajMax of the previous ring); the item's stream
-                       is drawn through them and its rows are numbered from skip + 1 */
+                       of a stratified run (Ring%iTrajMax of the previous ring); rows are numbered
+                       from skip + 1.  An item with the previous item's seed and skip = that item's
+                       skip + ntraj continues its stream (one thread draws the rings in order, each
+                       with its own b rule); any other item with skip > 0 draws and drops skip
+                       trajectories under its own b rule first */
 } cair_work_item;
 
 /* One row of trajectories.out (Integrator_Class.F90:884-933) plus diagnostics. */
