@@ -1232,3 +1232,52 @@ extern "C" int cair_internal_ic_draws(int32_t natoms, int32_t nlevels, const cai
     b[g] = cair::impact_parameter(items[item_of[g]], draws[cair::kDraws * g + 4 * nmol + 1]);
   return 0;
 }
+
+// Internal (not in include/cair_gpu.h): the statistics' per-row device code (stats_counted,
+// stats_codes, stats_key, as k_stats_items and k_stats_count run them) on the host, with the rings
+// from the host half, so that tests can check each row's codes, ring and key without a GPU.
+extern "C" int cair_internal_stats_rows(const cair_stats_params* P, int32_t nitems, const cair_work_item* items,
+                                        const int32_t* item_run, const unsigned long long* item_rows,
+                                        const long long* item_ini, int64_t n, const cair_traj_result* rows,
+                                        int32_t* counted, long long* ic, long long* fc, int32_t* ring,
+                                        unsigned long long* key) {
+  if (!P || (P->ncond != 3 && P->ncond != 5) || nitems < 1 || !items || n < 0 || (n > 0 && !rows)) return CAIR_EINVAL;
+  cair::StatsRuns runs;
+  if (!cair::stats_runs(nitems, items, item_run, runs).empty()) return CAIR_EINVAL;
+  if (!cair::stats_rings(*P, nitems, items, item_rows, item_ini, runs).empty()) return CAIR_EINVAL;
+  int err = 0;
+  cair::StatsArgs A{n,
+                    rows,
+                    P->qn_max,
+                    {P->iskip[0], P->iskip[1], P->iskip[2], P->iskip[3], P->iskip[4]},
+                    {P->pres_even_odd[0], P->pres_even_odd[1], P->pres_even_odd[2], P->pres_even_odd[3],
+                     P->pres_even_odd[4]},
+                    P->ham_abs_tol,
+                    runs.run_of.data(),
+                    runs.ring_b.data(),
+                    runs.nring.data(),
+                    runs.nruns,
+                    runs.R,
+                    nullptr,
+                    nullptr,
+                    0,
+                    nullptr,
+                    nullptr,
+                    nullptr,
+                    &err};
+  for (int64_t k = 0; k < n; ++k) {
+    const cair_traj_result& r = rows[k];
+    counted[k] = cair::stats_counted(A, r) ? 1 : 0;
+    ic[k] = fc[k] = 0;
+    ring[k] = 0;
+    key[k] = 0;
+    if (!counted[k]) continue;
+    bool bad = false;
+    if (P->ncond == 3) cair::stats_codes<3>(A, r, ic[k], fc[k], bad);
+    else cair::stats_codes<5>(A, r, ic[k], fc[k], bad);
+    if (bad) return CAIR_EINVAL;
+    int run;
+    key[k] = cair::stats_key(A, r, fc[k], run, ring[k]);
+  }
+  return 0;
+}

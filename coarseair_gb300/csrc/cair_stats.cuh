@@ -36,7 +36,7 @@ constexpr unsigned long long kStatsEmpty = ~0ull;
 
 // The NC conditions of a row, in trajectories.csv order: J, v, arr (3 atoms) or J1, v1, J2, v2, arr.
 template <int NC>
-__device__ __forceinline__ void stats_conditions(const cair_traj_result& r, double (&qi)[NC], double (&qf)[NC]) {
+__host__ __device__ __forceinline__ void stats_conditions(const cair_traj_result& r, double (&qi)[NC], double (&qf)[NC]) {
   if (NC == 3) {
     qi[0] = r.j_i; qi[1] = r.v_i; qi[NC - 1] = r.arr_i;
     qf[0] = r.j_f; qf[1] = r.v_f; qf[NC - 1] = r.arr_f;
@@ -50,7 +50,7 @@ __device__ __forceinline__ void stats_conditions(const cair_traj_result& r, doub
 // AddFinState's Histogram branch (935-1282).  Fortran nint rounds half away from zero (llround);
 // Fortran mod takes the sign of the dividend, as C's % does.
 template <int NC>
-__device__ __forceinline__ void stats_codes(const StatsArgs& A, const cair_traj_result& r, long long& ini_code,
+__host__ __device__ __forceinline__ void stats_codes(const StatsArgs& A, const cair_traj_result& r, long long& ini_code,
                                             long long& fin_code, bool& bad) {
   double qi[NC], qf[NC];
   stats_conditions<NC>(r, qi, qf);
@@ -98,12 +98,31 @@ __device__ __forceinline__ unsigned long long stats_hash(unsigned long long k) {
   return k;
 }
 
-#ifndef CAIR_MODEL_TU
-__device__ __forceinline__ bool stats_counted(const StatsArgs& A, const cair_traj_result& r) {
+__host__ __device__ __forceinline__ bool stats_counted(const StatsArgs& A, const cair_traj_result& r) {
   // finished trajectories whose energy is conserved (the others go to trajectories_HNotCons.out,
   // Integrator_Class.F90:755-776, 884-888)
   return r.status == CAIR_TRAJ_DONE && fabs(r.dH) <= A.ham_abs_tol;
 }
+
+// A counted row's ring from its sampled b (AddFinState: ring iR + 1 when
+// bRings(iR) < b <= bRings(iR+1), else the first) and its table key (code x nruns + run) x R + ring.
+// |fc| < 70 qnmax^NC (a cluster's arrangement code is negative) and 70 qnmax^NC x nruns x R < 2^62 is
+// checked on the host: the key is a two's-complement 64-bit number.
+__host__ __device__ __forceinline__ unsigned long long stats_key(const StatsArgs& A, const cair_traj_result& r,
+                                                                 long long fc, int& run, int& ring) {
+  run = A.item_run[r.item];
+  const double* e = A.ring_b + (size_t)run * kMaxRings;
+  const int nr = A.nring[run];
+  ring = 0;
+  for (int q = 0; q < nr - 1; ++q)
+    if (!(r.b > e[q + 1] || r.b <= e[q])) {
+      ring = q + 1;
+      break;
+    }
+  return (unsigned long long)((fc * A.nruns + run) * A.R + ring);
+}
+
+#ifndef CAIR_MODEL_TU
 
 // Pass 1: rows and the initial-state code of each item (the rings of a run are the bMax values
 // its rows carry, SetRings, Statistics_Class.F90:511-586).
@@ -131,19 +150,9 @@ __global__ void __launch_bounds__(256) k_stats_count(StatsArgs A) {
     long long ic, fc;
     bool bad = false;
     stats_codes<NC>(A, r, ic, fc, bad);
-    const int run = A.item_run[r.item];
-    const double* e = A.ring_b + (size_t)run * kMaxRings;
-    const int nr = A.nring[run];
-    int ring = 0;
-    for (int q = 0; q < nr - 1; ++q)
-      if (!(r.b > e[q + 1] || r.b <= e[q])) {
-        ring = q + 1;
-        break;
-      }
+    int run, ring;
+    const unsigned long long key = stats_key(A, r, fc, run, ring);
     atomicAdd(A.ring_rows + (size_t)run * kMaxRings + ring, 1ull);
-    // |fc| < 70 qnmax^NC (a cluster's arrangement code is negative) and 70 qnmax^NC x nruns x R < 2^62
-    // is checked on the host: the key is a two's-complement 64-bit number
-    const unsigned long long key = (unsigned long long)((fc * A.nruns + run) * A.R + ring);
     if (key == kStatsEmpty) {  // the key -1: not representable in the table
       atomicExch(A.error, 2);
       continue;

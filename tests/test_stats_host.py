@@ -1,9 +1,11 @@
-"""The host half of the device statistics (coarseair_gb300/csrc/cair_stats_host.cpp: SetRings per
-run, key decoding, WriteFinStateProbabilities over the rings) on the CPU, without a GPU.  The two
-device passes are restated here in numpy from Statistics_Class.F90 -- IdentifyInitialStates
-(591-680), AddFinState's Histogram codes (935-1282) and its ring assignment -- and their counted
-(run, final state, ring) keys go through the library's host code; the lines must equal the oracle's
-statistics of each run's rows.  The same rows as the GPU statistics tests, plus pooled runs."""
+"""The device statistics' logic on the CPU, without a GPU.  The two device passes are restated here in
+numpy from Statistics_Class.F90 -- IdentifyInitialStates (591-680), AddFinState's Histogram codes
+(935-1282) and its ring assignment.  The library's own per-row device code (stats_counted,
+stats_codes, stats_key, run on the host through an internal hook) must give the same codes, rings
+and keys, and the counted (run, final state, ring) keys go through the library's host half
+(coarseair_gb300/csrc/cair_stats_host.cpp: SetRings per run, key decoding, WriteFinStateProbabilities
+over the rings); the lines must equal the oracle's statistics of each run's rows.  The same rows as
+the GPU statistics tests, plus pooled runs."""
 import ctypes as C
 
 import numpy as np
@@ -21,6 +23,9 @@ def _load(path):
     L.cair_internal_stats_rings.restype = C.c_int
     L.cair_internal_stats_rings.argtypes = [C.POINTER(_lib.StatsParams), _I32, _P, _P, _P, _P, _P, _P,
                                             C.POINTER(_I32), C.POINTER(_I32), C.c_char_p, C.c_int]
+    L.cair_internal_stats_rows.restype = C.c_int
+    L.cair_internal_stats_rows.argtypes = [C.POINTER(_lib.StatsParams), _I32, _P, _P, _P, _P, _I64, _P, _P, _P, _P,
+                                           _P, _P]
     L.cair_internal_stats_finish.restype = C.c_int
     L.cair_internal_stats_finish.argtypes = [C.POINTER(_lib.StatsParams), _I32, _P, _P, _P, _P, _I64, _P, _P, _P, _P,
                                              _I64, C.POINTER(_I64), C.c_char_p, C.c_int]
@@ -90,7 +95,20 @@ def _host_statistics(L, P, items, rows, runs, keep, nc):
             if not (rows["b"][k] > e[q + 1] or rows["b"][k] <= e[q]):
                 ring[k] = q + 1
                 break
-    key = ((fc * nruns + rr) * R + ring)[keep]
+    # the library's per-row device code (run on the host) gives the same codes, rings and keys
+    rws = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+    d_cnt, d_ic, d_fc = np.zeros(len(rows), np.int32), np.zeros(len(rows), np.int64), np.zeros(len(rows), np.int64)
+    d_ring, d_key = np.zeros(len(rows), np.int32), np.zeros(len(rows), np.uint64)
+    assert L.cair_internal_stats_rows(C.byref(P), nitems, itc.ctypes.data,
+                                      None if run_arr is None else run_arr.ctypes.data, item_rows.ctypes.data,
+                                      item_ini.ctypes.data, len(rws), rws.ctypes.data, d_cnt.ctypes.data,
+                                      d_ic.ctypes.data, d_fc.ctypes.data, d_ring.ctypes.data, d_key.ctypes.data) == 0
+    full_key = (fc * nruns + rr) * R + ring
+    assert np.array_equal(d_cnt.astype(bool), keep)
+    assert np.array_equal(d_ic[keep], ic[keep]) and np.array_equal(d_fc[keep], fc[keep])
+    assert np.array_equal(d_ring[keep], ring[keep])
+    assert np.array_equal(d_key[keep], full_key[keep].astype(np.int64).view(np.uint64))
+    key = full_key[keep]
     uk, cnt = np.unique(key, return_counts=True)
     ring_rows = np.bincount((rr * MAXR + ring)[keep], minlength=nruns * MAXR).astype(np.uint64)
     ukc = np.ascontiguousarray(uk.astype(np.int64).view(np.uint64))
