@@ -476,3 +476,36 @@ def test_stratified_impact_parameters_stay_in_their_strata(oracle_lib, mode, rin
         bmin, b = oracle.impact_ring_of(k + 1, rings[0], itm)
         lo, hi = {0: (0.0, -b), 1: (-bmin, -b), 2: (bmin, -b)}[mode]
         assert lo - 1e-12 <= ic["b"][k] <= hi + 1e-12
+
+
+@pytest.mark.parametrize("name", ["Singlet", "Triplet", "Quintet"])
+def test_o4_against_the_original_umn_source(oracle_lib, name):
+    """The O4 surfaces against the original UMN Fortran the reference ships beside its fits
+    (dtb/Systems/O4/PESs/UMN/ReCheck, golden values made by tests/golden/make_o4_original_umn.py):
+    the same 430 coefficients and MEG parameters as the dtb/ .dat files, the same 466-polynomial
+    basis, and the oracle's sum C(i) B(i) equal to the original module's own statements evaluated at
+    the same geometries, to the rounding scale of that sum."""
+    import json
+    import os
+    from oracle import Oracle
+    with open(os.path.join(os.path.dirname(__file__), "golden", "o4_original_umn.json")) as f:
+        g = json.load(f)[name]
+    s = systems.load_o4_umn("UMN_" + name)
+    assert np.array_equal(s.coef, np.array(g["C"]))
+    assert (s.a, s.ab, s.ra, s.rb) == (g["a"], g["ab"], g["ra"], g["rb"])
+    assert (g["n_monomials"], g["n_polynomials"], g["n_basis"]) == (112, 466, 430)
+    import ctypes
+    L = oracle_lib.lib()
+    L.orc_const.restype, L.orc_const.argtypes = ctypes.c_double, [ctypes.c_char_p]
+    kcm = L.orc_const(b"Kcm_To_Hartree")
+    assert kcm == g["Econv"] and L.orc_const(b"B_To_Ang") == g["Cconv"]
+    cfg = systems.o4_config()
+    cfg.surfaces = [s]
+    o = Oracle(cfg)
+    R = np.array(g["R_bohr"])
+    V = o.potential(R)
+    vd = np.array([sum(L.orc_diat_V(1, r) for r in row) for row in R])
+    sum_cb = (V - vd) / kcm
+    ref, scale = np.array(g["sum_cb_kcal"]), np.array(g["abs_sum_cb_kcal"])
+    err = np.abs(sum_cb - ref)
+    assert np.all(err <= 2 * 630 * 1.1102230246251565e-16 * scale + 1e-9), (err / scale).max()
