@@ -3,7 +3,10 @@ its fit files (dtb/Systems/O4/PESs/UMN/ReCheck/PES_O4_{singlet_umn_v1,triplet_um
 the module's inline C(430), a, ab, ra, rb, Eref, totdiss and unit constants, and sum_i C(i) B(i)
 [kcal/mol] at seeded geometries, evaluated by interpreting the module's own EvMorse/EvMono/EvPoly/evbas
 statements (parsed with the parsers of coarseair_gb300/csrc/gen/gen_pip.py) in double precision, in
-statement order, together with the same sum on absolute values (the rounding scale).
+statement order, together with the same sum on absolute values (the rounding scale); and the module's
+O2 diatomic (ev2gm2 with its D3 dispersion, constants read from the module) on a grid of distances,
+in the module's units (kcal/mol, its own autoang and autokcal) and in the units the reference's
+O2_UMN_DiatomicPotential_Class keeps (hartree, B_To_Ang).
 
 This is an independent second source for the O4 surfaces: the oracle and the library follow
 O4_UMN_PES_Class.F90 and the dtb/ .dat files instead.
@@ -85,6 +88,56 @@ def geometries(n, seed):
     return out
 
 
+def diatomic(text):
+    """ev2gm2's Gaussian sum and d3disp/edisp's two-body D3 term of the module, for O2 (imol = 4):
+    v(r) = 0.627509523475149 sum_k as(k) exp(-alpha beta^k r^2) + (-s6 e6 - s8 e8) autokcal [kcal/mol],
+    r in Angstrom, e6 = c6 / (d^6 + (rs6 sqrt(c8/c6) + rs8)^6), e8 likewise, d = r / autoang,
+    c8 = 3 c6 r2r4(O)^2."""
+    ev = "\n".join(gen_pip.subroutine_body(text, "ev2gm2"))
+    alpha = fnum(re.search(r"alpha\s*=\s*([-+0-9.dDeE]+)", ev).group(1))
+    beta = fnum(re.search(r"beta\s*=\s*([-+0-9.dDeE]+)", ev).group(1))
+    as_ = [fnum(re.search(r"as\(%d\)\s*=\s*([-+0-9.dDeE]+)" % k, ev).group(1)) for k in range(8)]
+    fac = fnum(re.search(r"v\s*=\s*v\s*\*\s*([-+0-9.dDeE]+)", ev).group(1))
+    d3 = "\n".join(gen_pip.subroutine_body(text, "d3disp"))
+    get = lambda name, body: fnum(re.search(r"%s\s*=\s*([-+0-9.dDeE]+)" % name, body).group(1))
+    autoang, autokcal = get("autoang", d3), get("autokcal", d3)
+    s6, s8, rs6, rs8 = get("s6", d3), get("s8", d3), get("rs6", d3), get("rs8", d3)
+    c6 = get(r"c6\(1\)", d3)
+    ed = re.search(r"subroutine edisp.*?r2r4\(1:94\)\s*=\s*\(/(.*?)/\)", text, re.I | re.S).group(1)
+    r2r4 = [fnum(x) for x in re.sub(r"!.*", "", ed).replace("&", " ").replace(",", " ").split()]
+    assert len(r2r4) == 94
+    c8 = 3.0 * c6 * r2r4[7] * r2r4[7]
+    tmp = math.sqrt(c8 / c6)
+
+    def v(r_ang):
+        g = 0.0
+        for k in range(8):
+            g = g + as_[k] * math.exp(-alpha * beta ** k * r_ang ** 2)
+        g = g * fac
+        d = r_ang / autoang
+        e6 = c6 / (d ** 6 + (rs6 * tmp + rs8) ** 6)
+        e8 = c8 / (d ** 8 + (rs6 * tmp + rs8) ** 8)
+        return g + (-s6 * e6 - s8 * e8) * autokcal
+
+    def v_hartree(r_bohr, b_to_ang):
+        """The same terms in the units O2_UMN_DiatomicPotential_Class.F90:134-381 keeps: the Gaussian
+        sum x 1e-3 [Eh], the dispersion [Eh] at d = (r B_To_Ang) / B_To_Ang."""
+        r_ang = r_bohr * b_to_ang
+        g = 0.0
+        for k in range(8):
+            g = g + as_[k] * math.exp(-alpha * beta ** k * r_ang ** 2)
+        g = g * 1.0e-3
+        d = r_ang / b_to_ang
+        e6 = c6 / (d ** 6 + (rs6 * tmp + rs8) ** 6)
+        e8 = c8 / (d ** 8 + (rs6 * tmp + rs8) ** 8)
+        return g + (-s6 * e6 - s8 * e8)
+
+    v.hartree = v_hartree
+    consts = {"alpha": alpha, "beta": beta, "as": as_, "factor": fac, "autoang": autoang, "autokcal": autokcal,
+              "s6": s6, "s8": s8, "rs6": rs6, "rs8": rs8, "c6": c6, "r2r4_O": r2r4[7]}
+    return v, consts
+
+
 def main(ref):
     src = os.path.join(ref, "dtb", "Systems", "O4", "PESs", "UMN", "ReCheck")
     out = {}
@@ -104,6 +157,13 @@ def main(ref):
                      "totdiss": parameter(text, "totdiss"), "Cconv": cconv, "Econv": parameter(text, "Econv"),
                      "n_monomials": len(mono), "n_polynomials": len(poly), "n_basis": len(basis),
                      "R_bohr": R, "sum_cb_kcal": vals, "abs_sum_cb_kcal": scales}
+    text = open(os.path.join(src, FILES["Quintet"])).read()
+    v, consts = diatomic(text)
+    cconv = parameter(text, "Cconv")
+    r_bohr = [1.6 + 0.2 * i for i in range(60)]
+    out["O2"] = {"file": FILES["Quintet"], "constants": consts, "r_bohr": r_bohr,
+                 "v_kcal": [v(r * cconv) for r in r_bohr],
+                 "v_hartree_reference_units": [v.hartree(r, cconv) for r in r_bohr]}
     with open(os.path.join(HERE, "o4_original_umn.json"), "w") as f:
         json.dump(out, f, indent=1)
 

@@ -509,3 +509,21 @@ def test_o4_against_the_original_umn_source(oracle_lib, name):
     ref, scale = np.array(g["sum_cb_kcal"]), np.array(g["abs_sum_cb_kcal"])
     err = np.abs(sum_cb - ref)
     assert np.all(err <= 2 * 630 * 1.1102230246251565e-16 * scale + 1e-9), (err / scale).max()
+
+
+def test_o2_diatomic_against_the_original_umn_source(oracle_lib):
+    """The O2 UMN diatomic (the oracle's, as O2_UMN_DiatomicPotential_Class.F90 has it) against ev2gm2
+    and its D3 dispersion in the original UMN O4 module, constants read from the module: equal to
+    rounding (the Gaussian terms reach ~53 Eh) in the units the reference's class keeps, and within
+    1e-6 relative of the module's own kcal/mol values, the difference being the module's autoang and
+    autokcal against the reference's B_To_Ang and hartree."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "o4_original_umn.json")) as f:
+        g = json.load(f)["O2"]
+    L = oracle_lib.lib()
+    r = np.array(g["r_bohr"])
+    v = np.array([L.orc_diat_V(1, x) for x in r])
+    assert np.all(np.abs(v - np.array(g["v_hartree_reference_units"])) <= 2e-14)
+    vk = np.array(g["v_kcal"]) * 0.159360144e-2
+    assert np.all(np.abs(v - vk) <= 1e-6 * np.maximum(np.abs(vk), 1e-2))
