@@ -12,13 +12,18 @@
  * the CoarseAIR tree).  Operation order follows the Fortran (left-to-right
  * sums, no fused multiply-add: build with -ffp-contract=off).
  *
- * Parity pins: the reference ships no golden values for these surfaces or the
- * integrator.  The oracle is pinned by (1) the structural check of the PIP tables
- * against the reference's own derivative routines (gen_pip.py), (2) the shipped
- * level lists read as known-answer tests of the final-state chain (turning points,
- * action integral -> v+1/2), (3) finite-difference, permutation-symmetry and
- * dissociation-limit checks of every surface, (4) energy conservation and time
- * reversibility of the integrator.
+ * Parity pinned in part.  The reference ships no golden values for these surfaces
+ * or the integrator; its one independent source, the original UMN Fortran of the O4
+ * surfaces and their O2 diatomic (dtb/Systems/O4/PESs/UMN/ReCheck), pins the O4 and
+ * O2 evaluations here (tests/golden/o4_original_umn.json, made by the script beside
+ * it).  Everything else is parity unpinned against reference outputs and checked by
+ * (1) the structural check of the PIP tables against the reference's own derivative
+ * routines (gen_pip.py), (2) the shipped level lists read as known-answer tests of the
+ * final-state chain (turning points, action integral -> v+1/2), (3) finite-difference,
+ * permutation-symmetry and dissociation-limit checks of every surface, independent
+ * numpy restatements of the NN and BNN networks, the random-number generator and the
+ * impact-parameter rings, (4) energy conservation and time reversibility of the
+ * integrator.
  */
 #ifndef CAIR_ORACLE_H
 #define CAIR_ORACLE_H
