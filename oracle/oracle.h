@@ -13,10 +13,11 @@
  * sums, no fused multiply-add: build with -ffp-contract=off).
  *
  * Parity pinned in part.  The reference ships no golden values for these surfaces
- * or the integrator; its one independent source, the original UMN Fortran of the O4
- * surfaces and their O2 diatomic (dtb/Systems/O4/PESs/UMN/ReCheck), pins the O4 and
- * O2 evaluations here (tests/golden/o4_original_umn.json, made by the script beside
- * it).  Everything else is parity unpinned against reference outputs and checked by
+ * or the integrator; its one independent source, the original UMN Fortran modules of
+ * the O4, N4 (hence N3) and O3 2 5A' surfaces and their O2 and N2 diatomics (under
+ * dtb/Systems/), pins the UMN evaluations here (tests/golden/umn_originals.json, made by
+ * the script beside it).  Everything else is parity unpinned against reference outputs
+ * and checked by
  * (1) the structural check of the PIP tables against the reference's own derivative
  * routines (gen_pip.py), (2) the shipped level lists read as known-answer tests of the
  * final-state chain (turning points, action integral -> v+1/2), (3) finite-difference,

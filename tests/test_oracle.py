@@ -478,52 +478,79 @@ def test_stratified_impact_parameters_stay_in_their_strata(oracle_lib, mode, rin
         assert lo - 1e-12 <= ic["b"][k] <= hi + 1e-12
 
 
-@pytest.mark.parametrize("name", ["Singlet", "Triplet", "Quintet"])
-def test_o4_against_the_original_umn_source(oracle_lib, name):
-    """The O4 surfaces against the original UMN Fortran the reference ships beside its fits
-    (dtb/Systems/O4/PESs/UMN/ReCheck, golden values made by tests/golden/make_o4_original_umn.py):
-    the same 430 coefficients and MEG parameters as the dtb/ .dat files, the same 466-polynomial
-    basis, and the oracle's sum C(i) B(i) equal to the original module's own statements evaluated at
-    the same geometries, to the rounding scale of that sum."""
+def _umn_originals():
     import json
     import os
-    from oracle import Oracle
-    with open(os.path.join(os.path.dirname(__file__), "golden", "o4_original_umn.json")) as f:
-        g = json.load(f)[name]
-    s = systems.load_o4_umn("UMN_" + name)
-    assert np.array_equal(s.coef, np.array(g["C"]))
-    assert (s.a, s.ab, s.ra, s.rb) == (g["a"], g["ab"], g["ra"], g["rb"])
-    assert (g["n_monomials"], g["n_polynomials"], g["n_basis"]) == (112, 466, 430)
+    with open(os.path.join(os.path.dirname(__file__), "golden", "umn_originals.json")) as f:
+        return json.load(f)
+
+
+# golden key -> (system config with that one surface, the surface, totdiss the oracle adds, diatomic id)
+def _umn_case(key):
+    if key.startswith("O4_"):
+        s = systems.load_o4_umn("UMN_" + key[3:])
+        cfg = systems.o4_config()
+        cfg.surfaces = [s]
+        return cfg, s, 0.0, 1
+    if key == "O3_25A1":
+        s = systems.load_o3_umn("UMN_25A1")
+        cfg = systems.o3_config()
+        cfg.surfaces = [s]
+        return cfg, s, 0.0, 1
+    if key == "N4":
+        cfg = systems.n4_config()
+        return cfg, cfg.surfaces[0], 457.4, 2
+    cfg = systems.n3_config()
+    return cfg, cfg.surfaces[0], 457.4, 2
+
+
+@pytest.mark.parametrize("key", ["O4_Singlet", "O4_Triplet", "O4_Quintet", "N4", "N3", "O3_25A1"])
+def test_umn_surfaces_against_the_original_umn_modules(oracle_lib, key):
+    """The UMN surfaces against the original UMN Fortran modules the reference ships beside its fits
+    (golden values made by tests/golden/make_umn_originals.py): the same coefficients and MEG
+    parameters as the fit files the reference reads (the N3 coefficients it keeps inline equal the
+    N4 module's), the same polynomial bases, and the oracle's sum C(i) B(i) equal to the module's own
+    statements evaluated at the same geometries, to the rounding scale of that sum (N3: the N4
+    module at the same three distances with the pairs to the fourth atom at 10^3 bohr)."""
     import ctypes
+    from oracle import Oracle
+    g = _umn_originals()[key]
+    cfg, s, totdiss, diat = _umn_case(key)
+    assert np.array_equal(s.coef, np.array(g["C"]))
+    if key not in ("N4", "N3"):   # the N3/N4 classes hold a, ab, re inline (1, 1.5, 1.098), as the module does
+        assert (s.a, s.ab, s.ra, s.rb) == (g["a"], g["ab"], g["ra"], g["rb"])
+    else:
+        assert (g["a"], g["ab"], g["ra"], g["rb"], g["totdiss"]) == (1.0, 1.5, 1.098, 1.098, totdiss)
     L = oracle_lib.lib()
     L.orc_const.restype, L.orc_const.argtypes = ctypes.c_double, [ctypes.c_char_p]
     kcm = L.orc_const(b"Kcm_To_Hartree")
     assert kcm == g["Econv"] and L.orc_const(b"B_To_Ang") == g["Cconv"]
-    cfg = systems.o4_config()
-    cfg.surfaces = [s]
     o = Oracle(cfg)
-    R = np.array(g["R_bohr"])
+    R = np.array(g["R3_bohr"] if key == "N3" else g["R_bohr"])
     V = o.potential(R)
-    vd = np.array([sum(L.orc_diat_V(1, r) for r in row) for row in R])
-    sum_cb = (V - vd) / kcm
+    vd = np.array([sum(L.orc_diat_V(diat, r) for r in row) for row in R])
+    sum_cb = (V - vd) / kcm - totdiss
     ref, scale = np.array(g["sum_cb_kcal"]), np.array(g["abs_sum_cb_kcal"])
-    err = np.abs(sum_cb - ref)
-    assert np.all(err <= 2 * 630 * 1.1102230246251565e-16 * scale + 1e-9), (err / scale).max()
+    depth = 630 if key.startswith("O4") else 110
+    assert np.all(np.abs(sum_cb - ref) <= 2 * depth * 1.1102230246251565e-16 * (scale + totdiss) + 1e-9)
 
 
-def test_o2_diatomic_against_the_original_umn_source(oracle_lib):
-    """The O2 UMN diatomic (the oracle's, as O2_UMN_DiatomicPotential_Class.F90 has it) against ev2gm2
-    and its D3 dispersion in the original UMN O4 module, constants read from the module: equal to
-    rounding (the Gaussian terms reach ~53 Eh) in the units the reference's class keeps, and within
-    1e-6 relative of the module's own kcal/mol values, the difference being the module's autoang and
-    autokcal against the reference's B_To_Ang and hartree."""
-    import json
-    import os
-    with open(os.path.join(os.path.dirname(__file__), "golden", "o4_original_umn.json")) as f:
-        g = json.load(f)["O2"]
+def test_diatomics_against_the_original_umn_modules(oracle_lib):
+    """The O2 and N2 UMN diatomics (the oracle's, as the reference's O2_UMN and N2_UMN_ForN4 classes have
+    them) against ev2gm2 of the original modules, constants read from the modules.  O2: equal to
+    rounding (its Gaussian terms reach ~53 Eh) in the units the reference's class keeps, and within
+    1e-6 relative of the module's kcal/mol values, the gap being the module's autoang and autokcal
+    against the reference's B_To_Ang and hartree.  N2: the module's kcal/mol values x Econv to 1e-9
+    relative (the reference's class writes re^4 as the literal 1.4534810048)."""
+    g = _umn_originals()
     L = oracle_lib.lib()
-    r = np.array(g["r_bohr"])
+    o2 = g["O2"]
+    r = np.array(o2["r_bohr"])
     v = np.array([L.orc_diat_V(1, x) for x in r])
-    assert np.all(np.abs(v - np.array(g["v_hartree_reference_units"])) <= 2e-14)
-    vk = np.array(g["v_kcal"]) * 0.159360144e-2
+    assert np.all(np.abs(v - np.array(o2["v_hartree_reference_units"])) <= 2e-14)
+    vk = np.array(o2["v_kcal"]) * 0.159360144e-2
     assert np.all(np.abs(v - vk) <= 1e-6 * np.maximum(np.abs(vk), 1e-2))
+    n2 = g["N2"]
+    v = np.array([L.orc_diat_V(2, x) for x in r])
+    vk = np.array(n2["v_kcal"]) * 0.159360144e-2
+    assert np.all(np.abs(v - vk) <= 1e-9 * np.maximum(np.abs(vk), 1e-2))
