@@ -554,3 +554,21 @@ def test_diatomics_against_the_original_umn_modules(oracle_lib):
     v = np.array([L.orc_diat_V(2, x) for x in r])
     vk = np.array(n2["v_kcal"]) * 0.159360144e-2
     assert np.all(np.abs(v - vk) <= 1e-9 * np.maximum(np.abs(vk), 1e-2))
+
+
+def test_ring_entries_edge_cases():
+    """One ring, a zero-weight ring (no trajectories, the stream offsets unchanged), a fixed ring, and
+    the refusals (negative weights, a weight per ring)."""
+    from coarseair_gb300 import api
+    one = api.ring_entries(3, 1, 50, 7, 1e4, 15.0, [-6.0], [1])
+    assert one == [(3, 1, 50, 7, 1e4, 6.0, 15.0, 0, 0, 0.0, 0)]
+    ent = api.ring_entries(0, 0, 10, 7, 1e4, 15.0, [-2.0, -4.0, -6.0], [1, 0, 1])
+    assert [e[2] for e in ent] == [5, 0, 5] and [e[10] for e in ent] == [0, 5, 5]
+    items = api.work_items(ent)
+    assert list(items["first"]) == [0, 5, 5] and list(items["skip"]) == [0, 5, 5]
+    fixed = api.ring_entries(0, 0, 4, 7, 1e4, 15.0, [2.5], [1])
+    assert fixed[0][5] == -2.5
+    with pytest.raises(ValueError):
+        api.ring_entries(0, 0, 10, 7, 1e4, 15.0, [-2.0, -4.0], [1, -1])
+    with pytest.raises(ValueError):
+        api.ring_entries(0, 0, 10, 7, 1e4, 15.0, [-2.0, -4.0], [1])

@@ -129,3 +129,16 @@ def test_merge_follows_merge_trajectories(tmp_path):
     assert (out / "NConvTraj.dat").read_text() == "4\n"
     # a later merge appends to the existing trajectories.csv, as the script does
     assert api.merge_trajectories(dirs[:1], out) == 6
+
+
+def test_empty_inputs(tmp_path):
+    """No rows: the files hold the header alone; merging nothing writes NConvTraj.dat = 0."""
+    rows = _rows()[:0]
+    assert api.format_rows(rows) == HEADER and api.format_rows(rows, header=False) == ""
+    assert api.write_trajectories(tmp_path, rows, ham_abs_tol=1e-5, binary=tmp_path / "t.bin") == (0, 0)
+    assert (tmp_path / "trajectories.out").read_text() == HEADER
+    assert np.frombuffer((tmp_path / "t.bin").read_bytes(), "<i8").tolist() == [0]
+    out = tmp_path / "merged"
+    out.mkdir()
+    assert api.merge_trajectories([], out) == 0
+    assert (out / "NConvTraj.dat").read_text() == "0\n" and not (out / "trajectories.csv").exists()

@@ -260,3 +260,20 @@ def test_items_of_a_run_must_share_the_temperature(gpu_lib):
                                      ring_b.ctypes.data, nring.ctypes.data, C.byref(R), C.byref(nr), err, 256)
     assert rc == 1  # CAIR_EINVAL
     assert b"temperature" in err.value
+
+
+def test_no_counted_rows(gpu_lib, oracle_lib):
+    """Every row HNotCons or unfinished: no lines, no error."""
+    L = _load(gpu_lib)
+    rows = np.zeros(50, dtype=_lib.RESULT_DTYPE)
+    rows["j_i"], rows["v_i"], rows["arr_i"] = 1.5, 0.5, 16.5
+    rows["arr_f"] = 16.5
+    rows["status"] = np.where(np.arange(50) % 2 == 0, 1, 0)
+    rows["dH"] = 1.0
+    items = np.zeros(2, dtype=_lib.ITEM_DTYPE)
+    items["bmax"], items["ttra"] = 6.0, 1e4
+    rows["item"] = np.arange(50) % 2
+    P = _params(3, (0,) * 5, 1.0)
+    keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= P.ham_abs_tol)
+    assert not keep.any()
+    assert len(_host_statistics(L, P, items, rows, None, keep, 3)) == 0
