@@ -22,10 +22,7 @@ LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 10), "O3NN": ("O2", 0, 1), "O3BNN"
 # forces (Compute), so H is not conserved along their trajectories (O3_NN_PES_Class.F90:250-297 vs
 # 357-477; BNN_PES_Class.F90:395-442 vs 565-640)
 CONSERVES_H = {"O3": True, "N3": True, "O3NN": False, "O3BNN": False}
-NAMES = ["O3", "N3", "O3NN", "O3BNN"]
-# whole collisions to the end: the BNN shares the NN kernel, and its queue path is covered with an
-# attempt cap in test_gpu_bnn
-NAMES_E2E = ["O3", "N3", "O3NN"]
+NAMES = ["O3", "N3", "O3NN"]   # O3BNN runs these checks from test_gpu_strata_and_bnn
 
 
 def _setup(name, **kw):
@@ -194,7 +191,7 @@ def test_final_state_analysis_parity_on_identical_points(gpu_lib, oracle_lib, na
     assert np.allclose(fs_g["b"], [f["b"] for f in fs_o], rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.parametrize("name", NAMES_E2E)
+@pytest.mark.parametrize("name", NAMES)
 def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
     """Final (v, J, arrangement) from the GPU path against the oracle on the same initial
     conditions.  Rounding differs (FMA, exp), so chaotic trajectories can end differently; the

@@ -58,34 +58,6 @@ def test_quasibound_level_consumes_rejection_draws(gpu_lib, oracle_lib):
     assert np.allclose(ic["b"], ref["b"], rtol=1e-14, atol=0)
 
 
-@pytest.mark.parametrize("strata", ["Circles", "Rings", "Segments"])
-def test_stratified_rings_continue_one_stream(gpu_lib, oracle_lib, strata):
-    """One stream split into impact-parameter rings (ImpactParameter_Class.F90:55-221), one work item
-    per ring from api.ring_entries: every trajectory's initial condition equals the oracle's at the
-    same stream position, the third ring's positive input value is a fixed b that draws no random
-    number, and the rows are numbered along the stream with each ring's |b| as bmax."""
-    cfg, o, H, lv = _setup("N3")
-    rows = lv[[17]]
-    bring, ntring, n, seed = [-2.0, -4.5, 3.0, -7.0], [1, 2, 1, 3], 71, api.process_seed(4, 1)
-    entries = api.ring_entries(0, 0, n, seed, 10000.0, 15.0, bring, ntring, strata)
-    assert [e[2] for e in entries] == [11, 20, 10, 30] and [e[10] for e in entries] == [0, 11, 31, 41]
-    items = api.work_items(entries)
-    table = api.level_table(rows)
-    ic = api.InitialConditions(H).sample(table, items)
-    ref = o.sample_ics(n, _oracle_levels(rows), seed=seed, ttra=10000.0, dinit=15.0,
-                       rings=(bring, ntring, api.STRATA[strata]))
-    for key in ("paq", "paq0", "erra"):
-        sc = np.abs(ref[key]).max(axis=1, keepdims=True)
-        assert np.all(np.abs(ic[key] - ref[key]) <= 1e-10 * sc), key
-    assert np.allclose(ic["b"], ref["b"], rtol=1e-14, atol=0)
-    assert np.all(ic["b"][31:41] == 3.0)
-    res = api.RunTrajectories(H).run(table, items, max_attempts=2000)  # the rows' numbering and b only
-    assert list(res["idx"]) == list(range(1, n + 1))
-    assert np.array_equal(res["bmax"], np.repeat([2.0, 4.5, 3.0, 7.0], [11, 20, 10, 30]))
-    assert np.allclose(res["b"], ref["b"], rtol=1e-14, atol=0)
-    H.close()
-
-
 @pytest.mark.parametrize("name", ["N3", "O3"])
 def test_run_queue_matches_oracle_path(gpu_lib, oracle_lib, name):
     cfg, o, H, lv = _setup(name)

@@ -151,40 +151,6 @@ def test_statistics_of_an_o2_o2_queue_run(gpu_lib, oracle_lib):
     H.close()
 
 
-def test_statistics_pool_rings_and_skip_empty_ones(gpu_lib, oracle_lib):
-    """Impact-parameter rings (SetRings and the ring assignment of AddFinState): 60k synthetic rows in
-    two runs.  Run 0 has items with bmax 2, 4 and 6 bohr (Circles: each samples its whole disc, so
-    rows fall in inner rings too), and the 4-bohr item's rows are all HNotCons, so its ring is not a
-    ring of the statistics; run 1 pools two items of one bmax (two surfaces).  Cross sections sum
-    ring area x probability over the rings, against the oracle on the same rows."""
-    cfg = systems.n3_config()
-    H = api.Handle(cfg)
-    rng = np.random.default_rng(5)
-    bm = [2.0, 4.0, 6.0, 5.0, 5.0]
-    counts = [8000, 12000, 20000, 10000, 10000]
-    items = api.work_items([(0, 0, c, 1, 10000.0, b, 15.0) for c, b in zip(counts, bm)])
-    n = sum(counts)
-    rows = np.zeros(n, dtype=_lib.RESULT_DTYPE)
-    rows["item"] = np.repeat(np.arange(5), counts)
-    rows["bmax"] = np.repeat(bm, counts)
-    rows["b"] = rows["bmax"] * np.sqrt(rng.uniform(size=n))
-    rows["j_i"], rows["v_i"], rows["arr_i"] = 20.5, 0.5, 16.5
-    rows["j_f"] = rng.uniform(0.0, 45.0, n)
-    rows["v_f"] = rng.uniform(-0.5, 6.0, n)
-    rows["arr_f"] = rng.choice([16.5, 17.5, 32.5, 48.5], n)
-    rows["status"] = 0
-    rows["dH"] = np.where(rows["item"] == 1, 1.0, 1e-9)
-    runs = [0, 0, 0, 1, 1]
-    got = _compare(H, items, rows, (1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 0)), runs=runs)
-    assert set(got[got["run"] == 0]["nrings"]) == {2} and set(got[got["run"] == 1]["nrings"]) == {1}
-    # items of one run must share the temperature
-    bad = items.copy()
-    bad["ttra"][2] = 20000.0
-    with pytest.raises(api.CairError, match="temperature"):
-        api.Statistics(H).compute(bad, rows, runs=runs)
-    H.close()
-
-
 def test_rate_coefficients_within_two_sigma_of_the_oracle_path(gpu_lib, oracle_lib):
     """The same 600 initial conditions (one N2 + N run) propagated and analysed by the GPU path and
     by the oracle: every final state's rate coefficient agrees within twice the combined Monte-Carlo
