@@ -416,6 +416,7 @@ def main():
             "inflight_batches": len(streams),
             "converged_fraction": float(np.mean(res["status"] == 0)),
             "energy_not_conserved_fraction": float(np.mean(np.abs(res["dH"]) > cfg.ham_abs_tol))}
+    line.update(outcome_summary(res, cfg.ncall))
     if e2e:
         line["e2e"] = e2e
     if cpu:
@@ -435,6 +436,23 @@ def max_over_ranks(value, dist, buf):
     buf.fill_(float(value))
     dist.all_reduce(buf, op=dist.ReduceOp.MAX)
     return float(buf.item())
+
+
+def outcome_summary(res, ncall):
+    """Outcome figures of one step's result rows: the fraction of trajectories that ended at the first
+    end check, i.e. after ncall attempts (with Dinit 15 and rmax 16 bohr a pair can start beyond rmax,
+    Integrator_Class.F90:441-465), and, with more than one surface, per surface the trajectories, their
+    mean attempts and the converged fraction."""
+    per_traj = res["iste"].astype(np.int64) + res["irej"]
+    out = {"first_check_fraction": float(np.mean((per_traj <= ncall) & (res["status"] == 0)))}
+    surfaces = np.unique(res["ipes"])
+    if len(surfaces) > 1:
+        out["per_surface"] = {
+            str(int(p)): {"trajectories": int(np.sum(res["ipes"] == p)),
+                          "attempts_per_trajectory": float(per_traj[res["ipes"] == p].mean()),
+                          "converged_fraction": float(np.mean(res["status"][res["ipes"] == p] == 0))}
+            for p in surfaces}
+    return out
 
 
 def aggregate_rate(ntraj_per_rank, steps, world, ms):
