@@ -27,6 +27,7 @@ import multiprocessing as mp
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -257,6 +258,7 @@ def main():
     ap.add_argument("--cpu-wall", type=float, default=20.0, help="seconds of CPU work per core for the baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--clocks-csv", default=None, help="keep the nvidia-smi clock samples of the timed region here")
     args = ap.parse_args()
     spec = SYSTEMS[args.system]
     if args.ntraj is None:
@@ -340,8 +342,7 @@ def main():
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                    else "/tmp/bench_clocks.csv")
+    clocks = Clocks(args.clocks_csv or os.path.join(tempfile.gettempdir(), "bench_clocks_%d.csv" % os.getpid()))
     ev0 = torch.cuda.Event(enable_timing=True)
     ev_end = [torch.cuda.Event(enable_timing=True) for _ in streams]
     H.check(lib.cair_set_integrate_timing(H.h, 1), "cair_set_integrate_timing")

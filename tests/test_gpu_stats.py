@@ -204,8 +204,8 @@ def test_rate_coefficients_within_two_sigma_of_the_oracle_path(gpu_lib, oracle_l
     H.close()
 
 
-def test_config1_rates_within_two_sigma(gpu_lib, oracle_lib):
-    """BASELINE configuration 1 in full -- O2(v=0, J=1) + O on UMN_11A1, 10,000 trajectories, seed 1,
+def test_o2_o_ground_state_rates_within_two_sigma(gpu_lib, oracle_lib):
+    """O2(v=0, J=1) + O on UMN_11A1 in full -- 10,000 trajectories, seed 1,
     10,000 K, b = 6 sqrt(U) bohr, Dinit 15 bohr, rmax 16 bohr -- through the GPU queue and through the
     oracle from the same stream: every final state's rate agrees within twice the combined Monte-Carlo
     standard deviation."""
@@ -243,6 +243,6 @@ def test_config1_rates_within_two_sigma(gpu_lib, oracle_lib):
         ko, so = r.get(fs, (0.0, 0.0))
         sig = np.hypot(sg, so)
         dev.append(0.0 if sig == 0.0 else abs(kg - ko) / sig)
-    print("config 1 rates: %d final states (GPU) / %d (oracle), worst |dk|/sigma %.3f" % (len(g), len(r), max(dev)))
+    print("O2(0,1) + O rates: %d final states (GPU) / %d (oracle), worst |dk|/sigma %.3f" % (len(g), len(r), max(dev)))
     assert max(dev) <= 2.0
     H.close()
