@@ -22,7 +22,7 @@ LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 10), "O3NN": ("O2", 0, 1), "O3BNN"
 # forces (Compute), so H is not conserved along their trajectories (O3_NN_PES_Class.F90:250-297 vs
 # 357-477; BNN_PES_Class.F90:395-442 vs 565-640)
 CONSERVES_H = {"O3": True, "N3": True, "O3NN": False, "O3BNN": False}
-NAMES = ["O3", "N3", "O3NN"]   # O3BNN runs these checks from test_gpu_strata_and_bnn
+NAMES = ["O3", "N3", "O3NN"]   # O3BNN runs these checks from test_zzz_strata_and_bnn
 
 
 def _setup(name, **kw):

@@ -7,6 +7,9 @@
   pooled statistics match the oracle's.
 * Impact-parameter rings (ImpactParameter_Class.F90, Collision_Class.F90:1276-1296): one stream
   split into rings of every strata type through the queue, and statistics runs pooling rings.
+
+Collected after every other test file, so that a run that stops at the first failure has run the
+rest: these are the newest GPU paths.
 """
 import os
 
