@@ -1,24 +1,26 @@
 // C-ABI implementation (include/cair_gpu.h): handle management, host<->device staging and
 // kernel dispatch.  No CPU fallback: every numerical entry point runs on the GPU and
-// returns CAIR_ECUDA when no device is usable.
+// returns CAIR_ECUDA when no device is usable.  The cair_internal_* functions at the end are not
+// part of the ABI: they run the random-number stream and the statistics' per-row code (the same
+// source the kernels run) on the host, for tests without a GPU.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <string>
+#include <limits>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
 #include "cair_ic.cuh"
 #include "cair_launch.h"
 #include "cair_stats.cuh"
-
-#include <algorithm>
-#include <limits>
-#include <climits>
 
 using namespace cair;
 
