@@ -301,6 +301,108 @@ __global__ void cair_k_diat_v(DevSys S, const double* r, double* v, int64_t n) {
   if (k < n) v[k] = diat_v(S, r[k]);
 }
 
+// Everything cair_create derives from the system description without the GPU: the DevSys fields, Tqp and its
+// inverse Tpq (Transformation_Class.F90:53-128), the O2 UMN exponent factors, and every surface checked and packed
+// into its device layout (packed_out[p]; P.coef is left for the caller to point at the device copy).  Returns ""
+// or the error with its code.
+std::string setup_system(const cair_system_desc* d, DevSys& S, double* tqp, double* tpq,
+                         std::vector<std::vector<double>>& packed_out, int& code) {
+  auto fail_setup = [](int& c, int e, const std::string& msg) {
+    c = e;
+    return msg;
+  };
+  packed_out.assign(d->npes, {});
+  std::memset(&S, 0, sizeof(S));
+  S.natoms = d->natoms;
+  S.nv = 3 * (d->natoms - 1);
+  S.ne = 2 * S.nv;
+  S.npairs = d->natoms * (d->natoms - 1) / 2;
+  S.npes = d->npes;
+  S.nsteps = d->nsteps;
+  S.ncall = d->ncall;
+  S.incstp = d->inc_step;
+  S.diat = d->diat_model;
+  S.relax = d->relax;
+  S.eps = d->eps;
+  S.dt0 = d->dt0;
+  for (int i = 0; i < 4; ++i) S.mass[i] = d->mass[i];
+  S.rmax = d->rmax;
+  S.tmax = d->tmax;
+  S.rpimax = 1.0 / d->rmax;
+  for (int i = 0; i < d->natoms - 1; ++i) S.mMiMn[i] = -d->mass[i] / d->mass[d->natoms - 1];
+  // Tqp (Transformation_Class.F90:53-128)
+  std::memset(tqp, 0, 81 * sizeof(double));
+  double xmi = 1.0 / d->mass[d->natoms - 1];
+  int ic = 0;
+  for (int i = 0; i < d->natoms - 1; ++i) {
+    double temp1 = d->mass[i] * xmi;
+    double temp = (d->mass[d->natoms - 1] + d->mass[i]) * temp1;
+    for (int j = 0; j < 3; ++j) {
+      tqp[ic + 9 * ic] = temp;
+      for (int ip = i + 1; ip < d->natoms - 1; ++ip) {
+        double temp2 = temp1 * d->mass[ip];
+        tqp[ic + 9 * (ip * 3 + j)] = temp2;
+        tqp[(ip * 3 + j) + 9 * ic] = temp2;
+      }
+      ++ic;
+    }
+  }
+  if (d->tpq) {
+    std::memset(tpq, 0, 81 * sizeof(double));
+    for (int j = 0; j < S.nv; ++j)
+      for (int i = 0; i < S.nv; ++i) tpq[i + 9 * j] = d->tpq[i + S.nv * j];
+  } else if (invert(S.nv, tqp, tpq) != 0) {
+    return fail_setup(code, CAIR_EINVAL, "mass matrix is singular");
+  }
+  std::memcpy(S.Tpq, tpq, sizeof(S.Tpq));
+  std::memcpy(S.Tqp, tqp, sizeof(S.Tqp));
+  // O2 UMN exponent factors (O2_UMN_DiatomicPotential_Class.F90 Ev2gm2/_Grad)
+  {
+    const double a[8] = {-1.488979427684798e3, 1.881435846488955e4, -1.053475425838226e5,
+                         2.755135591229064e5,  -4.277588997761775e5, 4.404104009614092e5,
+                         -2.946204062950765e5, 1.176861219078620e5};
+    const double alpha = 9.439784362354936e-1, beta = 1.262242998506810;
+    for (int k = 0; k < 8; ++k) {
+      double bk = powi_gf(beta, k);
+      S.o2_ab[k] = alpha * bk;
+      S.o2_cd[k] = 2.0 * a[k] * alpha * bk;
+    }
+  }
+  for (int p = 0; p < d->npes; ++p) {
+    const cair_pes_desc& src = d->pes[p];
+    int expect = src.model == CAIR_PES_O3_UMN ? 56 : (src.model == CAIR_PES_N3_UMN || src.model == CAIR_PES_N4_UMN) ? 276
+                 : src.model == CAIR_PES_O4_UMN ? 430 : (src.model == CAIR_PES_O3_NN || src.model == CAIR_PES_O3_BNN) ? 0
+                 : -1;
+    if (expect < 0) return fail_setup(code, CAIR_EINVAL, "unknown surface model");
+    std::vector<double> packed;
+    if (src.model == CAIR_PES_O3_NN || src.model == CAIR_PES_O3_BNN) {
+      const bool bnn = src.model == CAIR_PES_O3_BNN;
+      if (!src.coef || src.ncoef < 12) return fail_setup(code, CAIR_EINVAL, "O3 NN: coefficient array too short");
+      if (int e = pack_o3nn(src.coef, src.ncoef, bnn, packed))
+        return fail_setup(code, e, bnn ? "O3 BNN: hidden layers must be 1..20 and 1..10 neurons and ncoef = 13 + 7 NHL1 + NHL1 NHL2 "
+                            "+ 2 NHL2"
+                          : "O3 NN: hidden layers must be 1..20 and 1..10 neurons and ncoef = 12 + 7 NHL1 + NHL1 NHL2 "
+                            "+ 2 NHL2");
+      if (d->natoms != 3) return fail_setup(code, CAIR_EINVAL, "surface/atom count mismatch");
+    } else if (src.ncoef != expect || !src.coef) {
+      return fail_setup(code, CAIR_EINVAL, "wrong coefficient count for surface");
+    } else {
+      packed.assign(src.coef, src.coef + src.ncoef);
+    }
+    if (src.model != d->pes[0].model) return fail_setup(code, CAIR_EUNSUPPORTED, "all surfaces of a handle must share a model");
+    if ((src.model == CAIR_PES_O4_UMN || src.model == CAIR_PES_N4_UMN) != (d->natoms == 4))
+      return fail_setup(code, CAIR_EINVAL, "surface/atom count mismatch");
+    DevPes& P = S.pes[p];
+    P.model = src.model;
+    P.ncoef = (int32_t)packed.size();
+    P.a = src.a; P.ab = src.ab; P.ra = src.ra; P.rb = src.rb;
+    P.inv_a = (src.a != 0.0) ? 1.0 / src.a : 0.0;
+    P.inv_ab = (src.ab != 0.0) ? 1.0 / src.ab : 0.0;
+    packed_out[p] = std::move(packed);
+  }
+  return "";
+}
+
 extern "C" {
 
 int cair_create(cair_handle** out, const cair_system_desc* d) {
@@ -328,97 +430,21 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
   if (const char* w = std::getenv("CAIR_WATCHDOG_S")) h->watchdog_s = std::atof(w);
 
   DevSys& S = h->sys;
-  std::memset(&S, 0, sizeof(S));
-  S.natoms = d->natoms;
-  S.nv = 3 * (d->natoms - 1);
-  S.ne = 2 * S.nv;
-  S.npairs = d->natoms * (d->natoms - 1) / 2;
-  S.npes = d->npes;
-  S.nsteps = d->nsteps;
-  S.ncall = d->ncall;
-  S.incstp = d->inc_step;
-  S.diat = d->diat_model;
-  S.relax = d->relax;
-  S.eps = d->eps;
-  S.dt0 = d->dt0;
-  for (int i = 0; i < 4; ++i) S.mass[i] = d->mass[i];
-  S.rmax = d->rmax;
-  S.tmax = d->tmax;
-  S.rpimax = 1.0 / d->rmax;
   for (int i = 0; i < 4; ++i) h->mass[i] = d->mass[i];
-  for (int i = 0; i < d->natoms - 1; ++i) S.mMiMn[i] = -d->mass[i] / d->mass[d->natoms - 1];
-  // Tqp (Transformation_Class.F90:53-128)
-  std::memset(h->tqp, 0, sizeof(h->tqp));
-  double xmi = 1.0 / d->mass[d->natoms - 1];
-  int ic = 0;
-  for (int i = 0; i < d->natoms - 1; ++i) {
-    double temp1 = d->mass[i] * xmi;
-    double temp = (d->mass[d->natoms - 1] + d->mass[i]) * temp1;
-    for (int j = 0; j < 3; ++j) {
-      h->tqp[ic + 9 * ic] = temp;
-      for (int ip = i + 1; ip < d->natoms - 1; ++ip) {
-        double temp2 = temp1 * d->mass[ip];
-        h->tqp[ic + 9 * (ip * 3 + j)] = temp2;
-        h->tqp[(ip * 3 + j) + 9 * ic] = temp2;
-      }
-      ++ic;
-    }
-  }
-  if (d->tpq) {
-    std::memset(h->tpq, 0, sizeof(h->tpq));
-    for (int j = 0; j < S.nv; ++j)
-      for (int i = 0; i < S.nv; ++i) h->tpq[i + 9 * j] = d->tpq[i + S.nv * j];
-  } else if (invert(S.nv, h->tqp, h->tpq) != 0) {
-    return bad(CAIR_EINVAL, "mass matrix is singular");
-  }
-  std::memcpy(S.Tpq, h->tpq, sizeof(S.Tpq));
-  std::memcpy(S.Tqp, h->tqp, sizeof(S.Tqp));
-  // O2 UMN exponent factors (O2_UMN_DiatomicPotential_Class.F90 Ev2gm2/_Grad)
   {
-    const double a[8] = {-1.488979427684798e3, 1.881435846488955e4, -1.053475425838226e5,
-                         2.755135591229064e5,  -4.277588997761775e5, 4.404104009614092e5,
-                         -2.946204062950765e5, 1.176861219078620e5};
-    const double alpha = 9.439784362354936e-1, beta = 1.262242998506810;
-    for (int k = 0; k < 8; ++k) {
-      double bk = powi_gf(beta, k);
-      S.o2_ab[k] = alpha * bk;
-      S.o2_cd[k] = 2.0 * a[k] * alpha * bk;
+    std::vector<std::vector<double>> packed;
+    int code = CAIR_OK;
+    const std::string msg = setup_system(d, S, h->tqp, h->tpq, packed, code);
+    if (!msg.empty()) return bad(code, msg);
+    for (int p = 0; p < d->npes; ++p) {
+      DevPes& P = S.pes[p];
+      if (cudaMalloc(&h->d_coef[p], sizeof(double) * packed[p].size()) != cudaSuccess)
+        return bad(CAIR_ECUDA, "cudaMalloc");
+      if (cudaMemcpy(h->d_coef[p], packed[p].data(), sizeof(double) * packed[p].size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+        return bad(CAIR_ECUDA, "cudaMemcpy coefficients");
+      P.coef = h->d_coef[p];
     }
-  }
-  for (int p = 0; p < d->npes; ++p) {
-    const cair_pes_desc& src = d->pes[p];
-    int expect = src.model == CAIR_PES_O3_UMN ? 56 : (src.model == CAIR_PES_N3_UMN || src.model == CAIR_PES_N4_UMN) ? 276
-                 : src.model == CAIR_PES_O4_UMN ? 430 : (src.model == CAIR_PES_O3_NN || src.model == CAIR_PES_O3_BNN) ? 0
-                 : -1;
-    if (expect < 0) return bad(CAIR_EINVAL, "unknown surface model");
-    std::vector<double> packed;
-    if (src.model == CAIR_PES_O3_NN || src.model == CAIR_PES_O3_BNN) {
-      const bool bnn = src.model == CAIR_PES_O3_BNN;
-      if (!src.coef || src.ncoef < 12) return bad(CAIR_EINVAL, "O3 NN: coefficient array too short");
-      if (int e = pack_o3nn(src.coef, src.ncoef, bnn, packed))
-        return bad(e, bnn ? "O3 BNN: hidden layers must be 1..20 and 1..10 neurons and ncoef = 13 + 7 NHL1 + NHL1 NHL2 "
-                            "+ 2 NHL2"
-                          : "O3 NN: hidden layers must be 1..20 and 1..10 neurons and ncoef = 12 + 7 NHL1 + NHL1 NHL2 "
-                            "+ 2 NHL2");
-      if (d->natoms != 3) return bad(CAIR_EINVAL, "surface/atom count mismatch");
-    } else if (src.ncoef != expect || !src.coef) {
-      return bad(CAIR_EINVAL, "wrong coefficient count for surface");
-    } else {
-      packed.assign(src.coef, src.coef + src.ncoef);
-    }
-    if (src.model != d->pes[0].model) return bad(CAIR_EUNSUPPORTED, "all surfaces of a handle must share a model");
-    if ((src.model == CAIR_PES_O4_UMN || src.model == CAIR_PES_N4_UMN) != (d->natoms == 4))
-      return bad(CAIR_EINVAL, "surface/atom count mismatch");
-    DevPes& P = S.pes[p];
-    P.model = src.model;
-    P.ncoef = (int32_t)packed.size();
-    P.a = src.a; P.ab = src.ab; P.ra = src.ra; P.rb = src.rb;
-    P.inv_a = (src.a != 0.0) ? 1.0 / src.a : 0.0;
-    P.inv_ab = (src.ab != 0.0) ? 1.0 / src.ab : 0.0;
-    if (cudaMalloc(&h->d_coef[p], sizeof(double) * packed.size()) != cudaSuccess) return bad(CAIR_ECUDA, "cudaMalloc");
-    if (cudaMemcpy(h->d_coef[p], packed.data(), sizeof(double) * packed.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-      return bad(CAIR_ECUDA, "cudaMemcpy coefficients");
-    P.coef = h->d_coef[p];
   }
   // final-state analysis parameters and Chebyshev-2 nodes (GAUSSQ kind 3)
   FsArgs& F = h->fs;
@@ -1281,5 +1307,40 @@ extern "C" int cair_internal_stats_rows(const cair_stats_params* P, int32_t nite
     int run;
     key[k] = cair::stats_key(A, r, fc[k], run, ring[k]);
   }
+  return 0;
+}
+
+// Internal (not in include/cair_gpu.h): what cair_create sets up, without a GPU -- the DevSys
+// (surface coefficient pointers left null) and every surface's packed device-layout coefficients,
+// concatenated, surface p at packed[offsets[p] .. offsets[p + 1]).  For tests that run the device
+// surface code on the host.
+extern "C" int64_t cair_internal_devsys_size(void) { return (int64_t)sizeof(DevSys); }
+
+extern "C" int cair_internal_setup_system(const cair_system_desc* d, void* devsys, int64_t devsys_bytes,
+                                          double* packed, int64_t packed_cap, int64_t* offsets, char* err,
+                                          int errcap) {
+  if (!d || !devsys || devsys_bytes != (int64_t)sizeof(DevSys) || !offsets || d->npes < 1 || d->npes > CAIR_MAX_PES)
+    return CAIR_EINVAL;
+  DevSys S;
+  double tqp[81], tpq[81];
+  std::vector<std::vector<double>> pk;
+  int code = CAIR_OK;
+  const std::string msg = setup_system(d, S, tqp, tpq, pk, code);
+  if (!msg.empty()) {
+    if (err && errcap > 0) {
+      std::strncpy(err, msg.c_str(), (size_t)errcap - 1);
+      err[errcap - 1] = 0;
+    }
+    return code;
+  }
+  int64_t off = 0;
+  for (int p = 0; p < d->npes; ++p) {
+    offsets[p] = off;
+    if (off + (int64_t)pk[p].size() > packed_cap) return CAIR_EINVAL;
+    if (packed) std::memcpy(packed + off, pk[p].data(), pk[p].size() * sizeof(double));
+    off += (int64_t)pk[p].size();
+  }
+  offsets[d->npes] = off;
+  std::memcpy(devsys, &S, sizeof S);
   return 0;
 }

@@ -1,0 +1,88 @@
+// Host build of the library's device surface code -- TEST INFRASTRUCTURE ONLY.
+//
+// coarseair_gb300/csrc/cair_device.cuh is included unchanged: the CUDA qualifiers are defined away and
+// the four device intrinsics it uses get host equivalents with the same bit-level meaning.  The
+// tests fill the DevSys through the library's own setup (cair_internal_setup_system) and compare
+// these evaluations with the oracle, so surface code can be checked without a GPU.  Arithmetic
+// differs from the GPU's only where nvcc contracts a * b + c into a fused multiply-add.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#define __device__
+#define __host__
+#define __forceinline__ inline
+#define __constant__
+#define __global__
+static inline int __double2loint(double d) {
+  uint64_t u;
+  std::memcpy(&u, &d, 8);
+  return (int)(uint32_t)u;
+}
+static inline int __double2hiint(double d) {
+  uint64_t u;
+  std::memcpy(&u, &d, 8);
+  return (int)(uint32_t)(u >> 32);
+}
+static inline double __hiloint2double(int hi, int lo) {
+  const uint64_t u = ((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo;
+  double d;
+  std::memcpy(&d, &u, 8);
+  return d;
+}
+template <class T>
+static inline T __ldg(const T* p) {
+  return *p;
+}
+static inline double rsqrt(double x) { return 1.0 / std::sqrt(x); }
+using std::max;
+using std::min;
+
+#include "../../coarseair_gb300/csrc/cair_device.cuh"
+
+using namespace cair;
+
+template <int MODEL>
+static void eval(const DevSys& S, int64_t n, const int32_t* ipes, const double* Rin, const double* Qin, double* V,
+                 double* dVdR, double* dVdQ, int grad) {
+  using T = Traits<MODEL>;
+  for (int64_t k = 0; k < n; ++k) {
+    const DevPes& P = S.pes[ipes ? ipes[k] : 0];
+    double R[T::NP], Ri[T::NP], Q[3 * T::NA], v, g[T::NP], m[T::NV];
+    for (int i = 0; i < T::NP; ++i) {
+      R[i] = Rin[T::NP * k + i];
+      Ri[i] = 1.0 / R[i];
+    }
+    for (int i = 0; i < 3 * T::NA; ++i) Q[i] = Qin[3 * T::NA * k + i];
+    if (grad) pes<MODEL, true>(S, P, R, Ri, Q, v, g, m);
+    else pes<MODEL, false>(S, P, R, Ri, Q, v, g, m);
+    V[k] = v;
+    if (grad) {
+      for (int i = 0; i < T::NP; ++i) dVdR[T::NP * k + i] = g[i];
+      for (int i = 0; i < T::NV; ++i) dVdQ[T::NV * k + i] = m[i];
+    }
+  }
+}
+
+extern "C" int64_t pes_host_devsys_size(void) { return (int64_t)sizeof(DevSys); }
+
+// V, dV/dR and -dV/dQ of n points as the library's k_pes_eval computes them (surface model of
+// surface 0; ipes may be null).
+extern "C" int pes_host_eval(const void* devsys, const double* packed, const int64_t* offsets, int64_t n,
+                             const int32_t* ipes, const double* R, const double* Q, double* V, double* dVdR,
+                             double* dVdQ, int grad) {
+  DevSys S;
+  std::memcpy(&S, devsys, sizeof S);
+  for (int p = 0; p < S.npes; ++p) S.pes[p].coef = packed + offsets[p];
+  switch (S.pes[0].model) {
+    case CAIR_PES_O3_UMN: eval<CAIR_PES_O3_UMN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
+    case CAIR_PES_N3_UMN: eval<CAIR_PES_N3_UMN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
+    case CAIR_PES_O4_UMN: eval<CAIR_PES_O4_UMN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
+    case CAIR_PES_O3_NN: eval<CAIR_PES_O3_NN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
+    case CAIR_PES_N4_UMN: eval<CAIR_PES_N4_UMN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
+    case CAIR_PES_O3_BNN: eval<CAIR_PES_O3_BNN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
+    default: return 1;
+  }
+  return 0;
+}
