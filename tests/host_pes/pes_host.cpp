@@ -65,6 +65,54 @@ static void eval(const DevSys& S, int64_t n, const int32_t* ipes, const double* 
   }
 }
 
+// k_bs_steps on the host: nattempts Bulirsch-Stoer attempts per trajectory with the device's Rhs and
+// bs_attempt.
+template <int MODEL, int NS>
+static void bs_steps(const DevSys& S, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                     const double* erra, int nattempts) {
+  constexpr int NE = Traits<MODEL>::NE;
+  for (int64_t k = 0; k < n; ++k) {
+    Rhs<MODEL> f(S, S.pes[ipes ? ipes[k] : 0]);
+    double y[NE];
+    for (int i = 0; i < NE; ++i) y[i] = paq[NE * k + i];
+    double x = t[k], h = dt[k], smax = 0.0, smin = 0.0;
+    int irej = 0, iste = 0;
+    for (int a = 0; a < nattempts; ++a)
+      bs_attempt<NE, NS>(f, y, x, h, erra + NE * k, S.relax, S.incstp != 0, smax, smin, irej, iste);
+    for (int i = 0; i < NE; ++i) paq[NE * k + i] = y[i];
+    t[k] = x;
+    dt[k] = h;
+  }
+}
+
+template <int MODEL>
+static int bs_steps_ns(const DevSys& S, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
+                       const double* erra, int nattempts) {
+  switch (S.nsteps) {
+    case 2: bs_steps<MODEL, 2>(S, n, ipes, paq, t, dt, erra, nattempts); return 0;
+    case 3: bs_steps<MODEL, 3>(S, n, ipes, paq, t, dt, erra, nattempts); return 0;
+    case 4: bs_steps<MODEL, 4>(S, n, ipes, paq, t, dt, erra, nattempts); return 0;
+    default: return 1;
+  }
+}
+
+extern "C" int pes_host_bs_steps(const void* devsys, const double* packed, const int64_t* offsets, int64_t n,
+                                 const int32_t* ipes, double* paq, double* t, double* dt, const double* erra,
+                                 int nattempts) {
+  DevSys S;
+  std::memcpy(&S, devsys, sizeof S);
+  for (int p = 0; p < S.npes; ++p) S.pes[p].coef = packed + offsets[p];
+  switch (S.pes[0].model) {
+    case CAIR_PES_O3_UMN: return bs_steps_ns<CAIR_PES_O3_UMN>(S, n, ipes, paq, t, dt, erra, nattempts);
+    case CAIR_PES_N3_UMN: return bs_steps_ns<CAIR_PES_N3_UMN>(S, n, ipes, paq, t, dt, erra, nattempts);
+    case CAIR_PES_O4_UMN: return bs_steps_ns<CAIR_PES_O4_UMN>(S, n, ipes, paq, t, dt, erra, nattempts);
+    case CAIR_PES_O3_NN: return bs_steps_ns<CAIR_PES_O3_NN>(S, n, ipes, paq, t, dt, erra, nattempts);
+    case CAIR_PES_N4_UMN: return bs_steps_ns<CAIR_PES_N4_UMN>(S, n, ipes, paq, t, dt, erra, nattempts);
+    case CAIR_PES_O3_BNN: return bs_steps_ns<CAIR_PES_O3_BNN>(S, n, ipes, paq, t, dt, erra, nattempts);
+    default: return 1;
+  }
+}
+
 extern "C" int64_t pes_host_devsys_size(void) { return (int64_t)sizeof(DevSys); }
 
 // V, dV/dR and -dV/dQ of n points as the library's k_pes_eval computes them (surface model of

@@ -1,11 +1,13 @@
-"""The library's device surface code on the CPU: coarseair_gb300/csrc/cair_device.cuh compiled unchanged
+"""The library's device surface and integrator code on the CPU: coarseair_gb300/csrc/cair_device.cuh compiled unchanged
 by the host compiler (tests/host_pes/pes_host.cpp, CUDA qualifiers defined away), with the DevSys and
 the packed coefficients from the library's own setup (cair_internal_setup_system, the part of
 cair_create that needs no GPU).  Every surface model -- O3, N3, O4, N4 UMN, the nine-surface O3 mix,
 O3 NN and the O3 BNN samples -- against the oracle at the same points, energies and gradients to
 1e-12 relative or the rounding-level bound of the GPU parity tests, and the energy-only path against
-the oracle's Potential.  This checks the surface arithmetic and the coefficient packing; the GPU
-tests check the same code as nvcc builds it."""
+the oracle's Potential; and the device Bulirsch-Stoer attempt (Rhs, bs_attempt) over 1000 fixed attempts
+against the oracle on the trajectories the oracle shows to be non-chaotic, to 1e-9 as on the GPU.
+This checks the surface and integrator arithmetic and the coefficient packing; the GPU tests check
+the same code as nvcc builds it."""
 import ctypes as C
 import os
 import subprocess
@@ -33,6 +35,9 @@ def _harness():
     L.pes_host_eval.restype = C.c_int
     L.pes_host_eval.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    L.pes_host_bs_steps.restype = C.c_int
+    L.pes_host_bs_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_int]
     return L
 
 
@@ -119,3 +124,27 @@ def test_layouts_agree(gpu_lib):
     lib = C.CDLL(gpu_lib)
     lib.cair_internal_devsys_size.restype = C.c_int64
     assert _harness().pes_host_devsys_size() == lib.cair_internal_devsys_size()
+
+
+@pytest.mark.parametrize("name", ["O3", "N3", "O3NN", "O3BNN"])
+def test_device_bs_attempts_on_the_host_match_the_oracle(gpu_lib, oracle_lib, name):
+    from oracle import Oracle
+    from test_gpu_parity import CFGS, LEVELS, _non_chaotic
+    cfg = CFGS[name]()
+    o = Oracle(cfg)
+    L = _harness()
+    devsys, packed, offsets, _ = _setup(gpu_lib, cfg, o.tpq)
+    mol, v0, j0 = LEVELS[name]
+    lv = systems.load_levels(mol)
+    ic = o.sample_ics(24, lv[(lv["vqn"] == v0) & (lv["jqn"] == j0)])
+    ok, a_o = _non_chaotic(o, ic, 1000)
+    assert ok.sum() >= 4
+    paq = np.ascontiguousarray(ic["paq"], np.float64).copy()
+    n = len(paq)
+    t, dt = np.zeros(n), np.full(n, cfg.dt0)
+    erra = np.ascontiguousarray(ic["erra"], np.float64)
+    ip = np.zeros(n, np.int32)
+    assert L.pes_host_bs_steps(devsys, packed.ctypes.data, offsets.ctypes.data, n, ip.ctypes.data, paq.ctypes.data,
+                               t.ctypes.data, dt.ctypes.data, erra.ctypes.data, 1000) == 0
+    rel = np.abs(paq - a_o).max(axis=1) / np.abs(a_o).max(axis=1)
+    assert np.all(rel[ok] < 1e-9), rel[ok]
