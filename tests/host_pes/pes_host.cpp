@@ -38,8 +38,22 @@ static inline T __ldg(const T* p) {
 static inline double rsqrt(double x) { return 1.0 / std::sqrt(x); }
 using std::max;
 using std::min;
+// one host "thread" that owns a 1 x 1 grid: the kernels' grid-stride loops then visit every element
+struct HostDim {
+  unsigned x, y, z;
+};
+static const HostDim threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1}, gridDim = {1, 1, 1};
+#define __launch_bounds__(...)
+template <class T>
+static inline T atomicAdd(T* p, T v) {
+  const T o = *p;
+  *p = o + v;
+  return o;
+}
+static inline void __syncwarp(unsigned = 0xffffffffu) {}
+static inline int __any_sync(unsigned, int pred) { return pred; }
 
-#include "../../coarseair_gb300/csrc/cair_device.cuh"
+#include "../../coarseair_gb300/csrc/cair_ic.cuh"
 
 using namespace cair;
 
@@ -111,6 +125,47 @@ extern "C" int pes_host_bs_steps(const void* devsys, const double* packed, const
     case CAIR_PES_O3_BNN: return bs_steps_ns<CAIR_PES_O3_BNN>(S, n, ipes, paq, t, dt, erra, nattempts);
     default: return 1;
   }
+}
+
+// Initial conditions of a batch of work items on the host: the streams drawn as k_ic_draws draws them
+// (one per stream head, rings continuing their stream), then the body of k_sample_ic3 / k_sample_ic4
+// over every trajectory.
+template <int MODEL>
+static void sample(const DevSys& S, int64_t ntot, const cair_work_item* items, const cair_level* levels,
+                   const double* draws, const int32_t* item_of, double* paq, double* paq0, double* erra, double* H0,
+                   double* b, int32_t* ipes, double* key) {
+  if (Traits<MODEL>::NA == 3)
+    k_sample_ic3<MODEL>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key);
+  else
+    k_sample_ic4<MODEL>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key);
+}
+
+extern "C" int ic_host_sample(const void* devsys, const double* packed, const int64_t* offsets,
+                              const cair_level* levels, int32_t nitems, const cair_work_item* items, int64_t ntot,
+                              double* paq, double* paq0, double* erra, double* H0, double* b, int32_t* ipes) {
+  DevSys S;
+  std::memcpy(&S, devsys, sizeof S);
+  for (int p = 0; p < S.npes; ++p) S.pes[p].coef = packed + offsets[p];
+  const int nmol = S.natoms == 4 ? 2 : 1;
+  double* draws = new double[kDraws * (ntot > 0 ? ntot : 1)];
+  int32_t* item_of = new int32_t[ntot > 0 ? ntot : 1];
+  double* key = new double[ntot > 0 ? ntot : 1];
+  for (int i = 0; i < nitems; ++i)
+    if (!continues_stream(items, i)) stream_draws(items, nitems, i, nmol, levels, draws, item_of);
+  int rc = 0;
+  switch (S.pes[0].model) {
+    case CAIR_PES_O3_UMN: sample<CAIR_PES_O3_UMN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
+    case CAIR_PES_N3_UMN: sample<CAIR_PES_N3_UMN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
+    case CAIR_PES_O4_UMN: sample<CAIR_PES_O4_UMN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
+    case CAIR_PES_O3_NN: sample<CAIR_PES_O3_NN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
+    case CAIR_PES_N4_UMN: sample<CAIR_PES_N4_UMN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
+    case CAIR_PES_O3_BNN: sample<CAIR_PES_O3_BNN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
+    default: rc = 1;
+  }
+  delete[] draws;
+  delete[] item_of;
+  delete[] key;
+  return rc;
 }
 
 extern "C" int64_t pes_host_devsys_size(void) { return (int64_t)sizeof(DevSys); }

@@ -4,8 +4,10 @@ the packed coefficients from the library's own setup (cair_internal_setup_system
 cair_create that needs no GPU).  Every surface model -- O3, N3, O4, N4 UMN, the nine-surface O3 mix,
 O3 NN and the O3 BNN samples -- against the oracle at the same points, energies and gradients to
 1e-12 relative or the rounding-level bound of the GPU parity tests, and the energy-only path against
-the oracle's Potential; and the device Bulirsch-Stoer attempt (Rhs, bs_attempt) over 1000 fixed attempts
-against the oracle on the trajectories the oracle shows to be non-chaotic, to 1e-9 as on the GPU.
+the oracle's Potential; the device Bulirsch-Stoer attempt (Rhs, bs_attempt) over 1000 fixed attempts
+against the oracle on the trajectories the oracle shows to be non-chaotic, to 1e-9 as on the GPU; and
+the initial-condition kernels (the stream code of k_ic_draws, the bodies of k_sample_ic3/4 run over a
+1 x 1 grid) for impact-parameter rings of every strata type against the oracle's stream.
 This checks the surface and integrator arithmetic and the coefficient packing; the GPU tests check
 the same code as nvcc builds it."""
 import ctypes as C
@@ -25,7 +27,7 @@ U = 1.1102230246251565e-16
 def _harness():
     src = [os.path.join(ROOT, "tests", "host_pes", "pes_host.cpp"), os.path.join(ROOT, "include", "cair_gpu.h")]
     csrc = os.path.join(ROOT, "coarseair_gb300", "csrc")
-    src += [os.path.join(csrc, "cair_device.cuh")]
+    src += [os.path.join(csrc, f) for f in ("cair_device.cuh", "cair_kernels.cuh", "cair_ic.cuh")]
     src += [os.path.join(csrc, "generated", f) for f in os.listdir(os.path.join(csrc, "generated"))]
     if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < max(os.path.getmtime(f) for f in src):
         subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
@@ -35,6 +37,9 @@ def _harness():
     L.pes_host_eval.restype = C.c_int
     L.pes_host_eval.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    L.ic_host_sample.restype = C.c_int
+    L.ic_host_sample.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64] + \
+        [C.c_void_p] * 6
     L.pes_host_bs_steps.restype = C.c_int
     L.pes_host_bs_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_int]
@@ -148,3 +153,68 @@ def test_device_bs_attempts_on_the_host_match_the_oracle(gpu_lib, oracle_lib, na
                                t.ctypes.data, dt.ctypes.data, erra.ctypes.data, 1000) == 0
     rel = np.abs(paq - a_o).max(axis=1) / np.abs(a_o).max(axis=1)
     assert np.all(rel[ok] < 1e-9), rel[ok]
+
+
+def _ic_host(L, setup, table, items):
+    devsys, packed, offsets, _ = setup
+    ntot = int(items["ntraj"].sum())
+    natoms = 3 if np.frombuffer(bytes(devsys)[:4], np.int32)[0] == 3 else 4
+    ne = 12 if natoms == 3 else 18
+    out = {k: np.zeros((ntot, ne)) for k in ("paq", "paq0", "erra")}
+    out["H0"], out["b"], out["ipes"] = np.zeros(ntot), np.zeros(ntot), np.zeros(ntot, np.int32)
+    tb = np.ascontiguousarray(table, dtype=_lib.LEVEL_DTYPE)
+    it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+    assert L.ic_host_sample(devsys, packed.ctypes.data, offsets.ctypes.data, tb.ctypes.data, len(it), it.ctypes.data,
+                            ntot, out["paq"].ctypes.data, out["paq0"].ctypes.data, out["erra"].ctypes.data,
+                            out["H0"].ctypes.data, out["b"].ctypes.data, out["ipes"].ctypes.data) == 0
+    return out
+
+
+def _levels_for_oracle(rows):
+    out = np.zeros(len(rows), dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax",
+                                                          "tau", "ri", "ro", "rlim")])
+    for c in out.dtype.names:
+        out[c] = rows[c] if c in rows.dtype.names else 0.0
+    return out
+
+
+def _close(a, b, rtol):
+    sc = np.abs(b).max(axis=1, keepdims=True)
+    return np.all(np.abs(a - b) <= rtol * sc)
+
+
+@pytest.mark.parametrize("strata", ["Circles", "Rings", "Segments"])
+def test_ic_kernels_on_the_host_for_rings(gpu_lib, oracle_lib, strata):
+    from oracle import Oracle
+    cfg = systems.n3_config(rmax=30.0)
+    o = Oracle(cfg)
+    L = _harness()
+    setup = _setup(gpu_lib, cfg, o.tpq)
+    rows = systems.load_levels("N2")[[17]]
+    bring, ntring, n, seed = [-2.0, -4.5, 3.0, -7.0], [1, 2, 1, 3], 71, api.process_seed(4, 1)
+    items = api.work_items(api.ring_entries(0, 0, n, seed, 10000.0, 15.0, bring, ntring, strata))
+    ic = _ic_host(L, setup, api.level_table(rows), items)
+    ref = o.sample_ics(n, _levels_for_oracle(rows), seed=seed, ttra=10000.0, dinit=15.0,
+                       rings=(bring, ntring, api.STRATA[strata]))
+    for key in ("paq", "paq0", "erra"):
+        assert _close(ic[key], ref[key], 1e-10), key
+    assert np.all(np.abs(ic["H0"] - ref["H0"]) <= 1e-11 * np.maximum(np.abs(ref["H0"]), 0.1))
+    assert np.allclose(ic["b"], ref["b"], rtol=1e-14, atol=0) and np.all(ic["b"][31:41] == 3.0)
+
+
+def test_ic_kernels_on_the_host_for_diatom_diatom_rings(gpu_lib, oracle_lib):
+    from oracle import Oracle
+    cfg = systems.o4_config()
+    o = Oracle(cfg)
+    L = _harness()
+    setup = _setup(gpu_lib, cfg, o.tpq)
+    rows = systems.load_levels("O2")[[0, 40]]
+    n, seed = 30, api.process_seed(2, 1)
+    items = api.work_items(api.ring_entries(0, 1, n, seed, 1e4, 18.0, [-3.0, -8.0], [1, 2], strata="Rings",
+                                            ilevel2=1))
+    ic = _ic_host(L, setup, api.level_table(rows), items)
+    lv = _levels_for_oracle(rows)
+    ref = o.sample_ics4(n, lv[0], lv[1], ttra=1e4, dinit=18.0, seed=seed, rings=([-3.0, -8.0], [1, 2], 1))
+    for key in ("paq", "paq0", "erra"):
+        assert _close(ic[key], ref[key], 1e-10), key
+    assert np.allclose(ic["b"], ref["b"], rtol=1e-14, atol=0)
