@@ -54,6 +54,8 @@ class StatsParams(C.Structure):
                 ("pres_even_odd", C.c_int32 * 5), ("ham_abs_tol", C.c_double), ("xmu", C.c_double)]
 
 
+STATS_COUNT_DTYPE = np.dtype([("run", "i4"), ("ring", "i4"), ("code", "i8"), ("count", "i8")])
+STATS_MAX_RINGS = 64
 FINAL_STATE_DTYPE = np.dtype([("run", "i4"), ("fin", "i4", 5), ("ini", "i4", 5), ("nrings", "i4"), ("count", "i8"),
                               ("nrows", "i8"), ("cross", "f8"), ("cross_sd", "f8"), ("rate", "f8"),
                               ("rate_sd", "f8")])
@@ -100,6 +102,14 @@ SIGNATURES = [
     ("cair_statistics", C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L]),
     ("cair_statistics_dev", C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, _P, C.POINTER(StatsParams), _P, C.c_int64, _L,
                                       _P]),
+    ("cair_statistics_items", C.c_int, [_P, C.c_int32, C.c_int64, _P, C.POINTER(StatsParams), _P, _P]),
+    ("cair_statistics_items_dev", C.c_int, [_P, C.c_int32, C.c_int64, _P, C.POINTER(StatsParams), _P, _P, _P]),
+    ("cair_statistics_counts", C.c_int, [_P, C.c_int32, _P, _P, _P, _P, C.c_int64, _P, C.POINTER(StatsParams), _P,
+                                         C.c_int64, _L, _P]),
+    ("cair_statistics_counts_dev", C.c_int, [_P, C.c_int32, _P, _P, _P, _P, C.c_int64, _P, C.POINTER(StatsParams),
+                                             _P, C.c_int64, _L, _P, _P]),
+    ("cair_statistics_finish", C.c_int, [C.c_int32, _P, _P, _P, _P, C.POINTER(StatsParams), C.c_int64, _P, _P, _P,
+                                         C.c_int64, _L, C.c_char_p, C.c_int32]),
     ("cair_format_rows", C.c_int, [_P, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_char_p, C.c_int64, _L]),
     ("cair_write_trajectories", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double, _L]),
     ("cair_write_trajectories_bin", C.c_int, [C.c_char_p, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double]),

@@ -455,3 +455,87 @@ class Statistics:
                                       rw.ctypes.data, C.byref(self.params), out.ctypes.data, cap, C.byref(n)),
                 "cair_statistics")
         return out[:n.value].copy()
+
+    # -- replicas: step 1 and step 2 of the host-side exchange (statistics_finish is step 3) --
+    def replica_items(self, nitems, rows):
+        """This replica's counted rows and smallest initial-state code per item."""
+        H = self.H
+        rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+        item_rows = np.zeros(int(nitems), np.uint64)
+        item_ini = np.zeros(int(nitems), np.int64)
+        H.check(H.lib.cair_statistics_items(H.h, int(nitems), len(rw), rw.ctypes.data, C.byref(self.params),
+                                            item_rows.ctypes.data, item_ini.ctypes.data), "cair_statistics_items")
+        return item_rows, item_ini
+
+    def replica_counts(self, items, rows, item_rows, item_ini, runs=None, cap=None):
+        """This replica's (run, ring, code) counts under the rings of the replicas' totals, and its rows
+        per (run, ring) as an nruns x 64 array."""
+        H = self.H
+        it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+        rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+        rn = None if runs is None else np.ascontiguousarray(runs, dtype=np.int32)
+        ir = np.ascontiguousarray(item_rows, dtype=np.uint64)
+        ii = np.ascontiguousarray(item_ini, dtype=np.int64)
+        nruns = len(it) if rn is None else int(rn.max()) + 1
+        cap = int(cap if cap is not None else max(64, len(rw)))
+        out = np.zeros(cap, dtype=_lib.STATS_COUNT_DTYPE)
+        ring_rows = np.zeros((nruns, _lib.STATS_MAX_RINGS), np.uint64)
+        n = C.c_int64(0)
+        H.check(H.lib.cair_statistics_counts(H.h, len(it), it.ctypes.data, None if rn is None else rn.ctypes.data,
+                                             ir.ctypes.data, ii.ctypes.data, len(rw), rw.ctypes.data,
+                                             C.byref(self.params), out.ctypes.data, cap, C.byref(n),
+                                             ring_rows.ctypes.data), "cair_statistics_counts")
+        return out[:n.value].copy(), ring_rows
+
+    def replica_compute(self, items, rows, runs=None, group=None, cap=None):
+        """Lines of every replica's rows together, on every rank of a torch.distributed group that ran
+        the same items from disjoint streams (see replica_statistics)."""
+        return replica_statistics(self.params, items, rows, runs, self.replica_items, self.replica_counts,
+                                  group=group, cap=cap)
+
+
+def statistics_finish(params, items, item_rows, item_ini, counts, ring_rows, runs=None, cap=None):
+    """Step 3 of the replicas' statistics (cair_statistics_finish, host code): the lines from the summed
+    totals and counts."""
+    lib = _lib.load()
+    it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+    rn = None if runs is None else np.ascontiguousarray(runs, dtype=np.int32)
+    ir = np.ascontiguousarray(item_rows, dtype=np.uint64)
+    ii = np.ascontiguousarray(item_ini, dtype=np.int64)
+    ct = np.ascontiguousarray(counts, dtype=_lib.STATS_COUNT_DTYPE)
+    rr = np.ascontiguousarray(ring_rows, dtype=np.uint64)
+    cap = int(cap if cap is not None else max(64, len(ct)))
+    out = np.zeros(cap, dtype=_lib.FINAL_STATE_DTYPE)
+    n = C.c_int64(0)
+    msg = C.create_string_buffer(256)
+    rc = lib.cair_statistics_finish(len(it), it.ctypes.data, None if rn is None else rn.ctypes.data, ir.ctypes.data,
+                                    ii.ctypes.data, C.byref(params), len(ct), ct.ctypes.data, rr.ctypes.data,
+                                    out.ctypes.data, cap, C.byref(n), msg, 256)
+    if rc != 0:
+        raise CairError("cair_statistics_finish: %s (%s)" % (_lib.STATUS.get(rc, rc), msg.value.decode()))
+    return out[:n.value].copy()
+
+
+def replica_statistics(params, items, rows, runs, items_pass, counts_pass, group=None, cap=None):
+    """The statistics of torch.distributed replicas that ran the same work items from disjoint streams,
+    with two host-side sums as the only exchange (the reference merges its processes' trajectories.out
+    files instead): items_pass(nitems, rows) -> (item_rows, item_ini); the totals summed (rows) and
+    minimised (initial codes) over ranks; counts_pass(items, rows, item_rows, item_ini, runs) -> (counts,
+    ring_rows) under the rings those totals define; the ring rows summed, the counts gathered; and
+    statistics_finish.  Every rank returns the same lines."""
+    import torch
+    import torch.distributed as dist
+    ir, ii = items_pass(len(items), rows)
+    t = torch.from_numpy(np.asarray(ir, np.int64).copy())
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    ir = t.numpy().astype(np.uint64)
+    t = torch.from_numpy(np.asarray(ii, np.int64).copy())
+    dist.all_reduce(t, op=dist.ReduceOp.MIN, group=group)
+    ii = t.numpy()
+    counts, ring_rows = counts_pass(items, rows, ir, ii, runs)
+    t = torch.from_numpy(np.asarray(ring_rows, np.int64).copy())
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    ring_rows = t.numpy().astype(np.uint64)
+    parts = [None] * dist.get_world_size(group)
+    dist.all_gather_object(parts, np.asarray(counts, dtype=_lib.STATS_COUNT_DTYPE), group=group)
+    return statistics_finish(params, items, ir, ii, np.concatenate(parts), ring_rows, runs, cap=cap)

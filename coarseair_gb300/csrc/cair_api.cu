@@ -1134,6 +1134,183 @@ int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items,
                              cap, nout, h->stream);
 }
 
+// Statistics of replicas, step 1: counted rows and the smallest initial-state code per item (pass 1).
+int cair_statistics_items_dev(cair_handle* h, int32_t nitems, int64_t ntot, const cair_traj_result* results,
+                              const cair_stats_params* params, uint64_t* item_rows, int64_t* item_ini,
+                              void* stream) {
+  if (!h || nitems < 1 || ntot < 0 || (ntot > 0 && !results) || !params || !item_rows || !item_ini)
+    return fail(h, CAIR_EINVAL, "cair_statistics_items: bad argument");
+  const cair_stats_params& P = *params;
+  const int nc = P.ncond;
+  if (nc != (h->sys.natoms == 4 ? 5 : 3))
+    return fail(h, CAIR_EINVAL, "cair_statistics_items: ncond must be 3 for diatom + atom, 5 for diatom + diatom");
+  if (P.qn_max < 2) return fail(h, CAIR_EINVAL, "cair_statistics_items: qn_max out of range");
+  const size_t need = (size_t)nitems * 16 + 4 * 256;
+  if (h->stats_bytes < need) {
+    if (h->d_stats) cudaFree(h->d_stats);
+    h->d_stats = nullptr;
+    h->stats_bytes = 0;
+    CUDA_TRY(h, cudaMalloc(&h->d_stats, need));
+    h->stats_bytes = need;
+  }
+  Carver c{(char*)h->d_stats};
+  unsigned long long* d_rows = c.take<unsigned long long>(nitems);
+  long long* d_ini = c.take<long long>(nitems);
+  int* derr = c.take<int>(2);
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(h, cudaMemsetAsync(d_rows, 0, (size_t)nitems * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(d_ini, 0x7f, (size_t)nitems * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(derr, 0, 8, st));
+  if (ntot > 0) {
+    StatsArgs A{};
+    A.ntot = ntot;
+    A.rows = results;
+    A.qnmax = P.qn_max;
+    for (int q = 0; q < 5; ++q) {
+      A.iskip[q] = P.iskip[q];
+      A.pres[q] = P.pres_even_odd[q];
+    }
+    A.ham_abs_tol = P.ham_abs_tol;
+    A.item_rows = d_rows;
+    A.item_inicode = d_ini;
+    A.error = derr;
+    if (nc == 3) k_stats_items<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
+    else k_stats_items<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
+    if (int e = check_launch(h)) return e;
+  }
+  int err = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(item_rows, d_rows, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(item_ini, d_ini, (size_t)nitems * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (err == 1) return fail(h, CAIR_EINVAL, "cair_statistics_items: a quantum number is at or above qn_max");
+  return 0;
+}
+
+// Statistics of replicas, step 2: this replica's (run, ring, code) counts under the rings of the
+// replicas' totals (pass 2).
+int cair_statistics_counts_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                               const uint64_t* item_rows, const int64_t* item_ini, int64_t ntot,
+                               const cair_traj_result* results, const cair_stats_params* params,
+                               cair_stats_count* out, int64_t cap, int64_t* nout, uint64_t* ring_rows,
+                               void* stream) {
+  if (!h || nitems < 1 || !items || !item_rows || !item_ini || ntot < 0 || (ntot > 0 && !results) || !params ||
+      cap < 0 || (cap > 0 && !out) || !nout || !ring_rows)
+    return fail(h, CAIR_EINVAL, "cair_statistics_counts: bad argument");
+  const cair_stats_params& P = *params;
+  const int nc = P.ncond;
+  if (nc != (h->sys.natoms == 4 ? 5 : 3))
+    return fail(h, CAIR_EINVAL, "cair_statistics_counts: ncond must be 3 for diatom + atom, 5 for diatom + diatom");
+  if (P.qn_max < 2) return fail(h, CAIR_EINVAL, "cair_statistics_counts: qn_max out of range");
+  StatsRuns runs;
+  if (std::string e = stats_runs(nitems, items, item_run, runs); !e.empty()) return fail(h, CAIR_EINVAL, e);
+  if (std::string e = stats_rings(P, nitems, items, (const unsigned long long*)item_rows, (const long long*)item_ini,
+                                  runs);
+      !e.empty())
+    return fail(h, CAIR_EINVAL, e);
+  const int32_t nruns = runs.nruns;
+  *nout = 0;
+  std::memset(ring_rows, 0, (size_t)nruns * kMaxRings * sizeof(uint64_t));
+  if (ntot == 0) return 0;
+  unsigned long long tsize = 1024;
+  while (tsize < 2ull * (unsigned long long)ntot) tsize <<= 1;
+  const size_t need = tsize * 32 + (size_t)nitems * 8 + (size_t)nruns * ((size_t)kMaxRings * 16 + 16) + 8 * 256;
+  if (h->stats_bytes < need) {
+    if (h->d_stats) cudaFree(h->d_stats);
+    h->d_stats = nullptr;
+    h->stats_bytes = 0;
+    CUDA_TRY(h, cudaMalloc(&h->d_stats, need));
+    h->stats_bytes = need;
+  }
+  Carver c{(char*)h->d_stats};
+  unsigned long long* keys = c.take<unsigned long long>(tsize);
+  unsigned long long* counts = c.take<unsigned long long>(tsize);
+  unsigned long long* okeys = c.take<unsigned long long>(tsize);
+  unsigned long long* ocounts = c.take<unsigned long long>(tsize);
+  double* ring_b = c.take<double>((size_t)nruns * kMaxRings);
+  unsigned long long* d_ring_rows = c.take<unsigned long long>((size_t)nruns * kMaxRings);
+  int32_t* d_run = c.take<int32_t>(nitems);
+  int32_t* d_nring = c.take<int32_t>(nruns);
+  unsigned long long* dn = c.take<unsigned long long>(2);
+  int* derr = (int*)(dn + 1);
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(h, cudaMemsetAsync(keys, 0xff, tsize * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(counts, 0, tsize * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(d_ring_rows, 0, (size_t)nruns * kMaxRings * 8, st));
+  CUDA_TRY(h, cudaMemsetAsync(dn, 0, 16, st));
+  CUDA_TRY(h, cudaMemcpyAsync(ring_b, runs.ring_b.data(), runs.ring_b.size() * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_nring, runs.nring.data(), (size_t)nruns * 4, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_run, runs.run_of.data(), (size_t)nitems * 4, cudaMemcpyHostToDevice, st));
+  StatsArgs A{};
+  A.ntot = ntot;
+  A.rows = results;
+  A.qnmax = P.qn_max;
+  for (int q = 0; q < 5; ++q) {
+    A.iskip[q] = P.iskip[q];
+    A.pres[q] = P.pres_even_odd[q];
+  }
+  A.ham_abs_tol = P.ham_abs_tol;
+  A.item_run = d_run;
+  A.ring_b = ring_b;
+  A.nring = d_nring;
+  A.nruns = nruns;
+  A.R = runs.R;
+  A.keys = keys;
+  A.counts = counts;
+  A.mask = tsize - 1;
+  A.ring_rows = d_ring_rows;
+  A.error = derr;
+  if (nc == 3) k_stats_count<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
+  else k_stats_count<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
+  k_stats_compact<<<grid_for(h, (int64_t)tsize), 256, 0, st>>>(keys, counts, tsize, okeys, ocounts, tsize, dn);
+  if (int e = check_launch(h)) return e;
+  unsigned long long n = 0;
+  int err = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(&n, dn, 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(ring_rows, d_ring_rows, (size_t)nruns * kMaxRings * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (err) return fail(h, CAIR_EINVAL, "cair_statistics_counts: a final-state key of -1 (not representable)");
+  if ((int64_t)n > cap)
+    return fail(h, CAIR_EINVAL, "cair_statistics_counts: cap too small, " + std::to_string(n) + " counts");
+  std::vector<unsigned long long> k(n), cnt(n);
+  if (n) {
+    CUDA_TRY(h, cudaMemcpyAsync(k.data(), okeys, n * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaMemcpyAsync(cnt.data(), ocounts, n * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaStreamSynchronize(st));
+  }
+  const std::vector<StatsEntry> ent = stats_decode(runs, (int64_t)n, k.data(), cnt.data());
+  for (size_t q = 0; q < ent.size(); ++q)
+    out[q] = cair_stats_count{ent[q].run, ent[q].ring, (int64_t)ent[q].code, (int64_t)ent[q].count};
+  *nout = (int64_t)n;
+  return 0;
+}
+
+int cair_statistics_items(cair_handle* h, int32_t nitems, int64_t ntot, const cair_traj_result* results,
+                          const cair_stats_params* params, uint64_t* item_rows, int64_t* item_ini) {
+  if (!h || ntot < 0 || (ntot > 0 && !results)) return fail(h, CAIR_EINVAL, "cair_statistics_items: bad argument");
+  if (int e = ensure_scratch(h, (size_t)ntot * sizeof(cair_traj_result) + 256)) return e;
+  if (ntot > 0)
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_scratch, results, (size_t)ntot * sizeof(cair_traj_result),
+                                cudaMemcpyHostToDevice, h->stream));
+  return cair_statistics_items_dev(h, nitems, ntot, (const cair_traj_result*)h->d_scratch, params, item_rows, item_ini,
+                                   h->stream);
+}
+
+int cair_statistics_counts(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                           const uint64_t* item_rows, const int64_t* item_ini, int64_t ntot,
+                           const cair_traj_result* results, const cair_stats_params* params, cair_stats_count* out,
+                           int64_t cap, int64_t* nout, uint64_t* ring_rows) {
+  if (!h || ntot < 0 || (ntot > 0 && !results)) return fail(h, CAIR_EINVAL, "cair_statistics_counts: bad argument");
+  if (int e = ensure_scratch(h, (size_t)ntot * sizeof(cair_traj_result) + 256)) return e;
+  if (ntot > 0)
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_scratch, results, (size_t)ntot * sizeof(cair_traj_result),
+                                cudaMemcpyHostToDevice, h->stream));
+  return cair_statistics_counts_dev(h, nitems, items, item_run, item_rows, item_ini, ntot,
+                                    (const cair_traj_result*)h->d_scratch, params, out, cap, nout, ring_rows,
+                                    h->stream);
+}
+
 struct cair_queue_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;

@@ -59,19 +59,12 @@ std::string stats_rings(const cair_stats_params& P, int32_t nitems, const cair_w
   return "";
 }
 
-std::string stats_finish(const cair_stats_params& P, const StatsRuns& runs, int64_t n, const unsigned long long* keys,
-                         const unsigned long long* counts, const unsigned long long* ring_rows, cair_final_state* out,
-                         int64_t cap, int64_t* nout) {
-  const int nc = P.ncond;
+std::vector<StatsEntry> stats_decode(const StatsRuns& runs, int64_t n, const unsigned long long* keys,
+                                     const unsigned long long* counts) {
   const long long R = runs.R, nruns = runs.nruns;
-  struct Entry {
-    long long code;
-    int run, ring;
-    unsigned long long count;
-  };
   // a possibly negative code: decode with floor division
   auto floordiv = [](long long a, long long b) { return a / b - ((a % b != 0) && ((a < 0) != (b < 0))); };
-  std::vector<Entry> ent((size_t)n);
+  std::vector<StatsEntry> ent((size_t)n);
   for (int64_t i = 0; i < n; ++i) {
     const long long ks = (long long)keys[i];
     const long long rest = floordiv(ks, R);
@@ -80,7 +73,20 @@ std::string stats_finish(const cair_stats_params& P, const StatsRuns& runs, int6
     ent[i].run = (int)(rest - ent[i].code * nruns);
     ent[i].count = counts[i];
   }
-  std::sort(ent.begin(), ent.end(), [](const Entry& a, const Entry& b) {
+  return ent;
+}
+
+std::string stats_finish(const cair_stats_params& P, const StatsRuns& runs, int64_t n, const unsigned long long* keys,
+                         const unsigned long long* counts, const unsigned long long* ring_rows, cair_final_state* out,
+                         int64_t cap, int64_t* nout) {
+  return stats_finish_entries(P, runs, stats_decode(runs, n, keys, counts), ring_rows, out, cap, nout);
+}
+
+std::string stats_finish_entries(const cair_stats_params& P, const StatsRuns& runs, std::vector<StatsEntry> ent,
+                                 const unsigned long long* ring_rows, cair_final_state* out, int64_t cap,
+                                 int64_t* nout) {
+  const int nc = P.ncond;
+  std::sort(ent.begin(), ent.end(), [](const StatsEntry& a, const StatsEntry& b) {
     return a.run != b.run ? a.run < b.run : (a.code != b.code ? a.code < b.code : a.ring < b.ring);
   });
   const long long qn = P.qn_max;
@@ -202,4 +208,31 @@ extern "C" int cair_internal_stats_finish(const cair_stats_params* P, int32_t ni
   if (e.empty()) e = cair::stats_rings(*P, nitems, items, item_rows, item_ini, runs);
   if (e.empty()) e = cair::stats_finish(*P, runs, n, keys, counts, ring_rows, out, cap, nout);
   return report(e, err, errcap);
+}
+
+extern "C" int cair_statistics_finish(int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                                      const uint64_t* item_rows, const int64_t* item_ini,
+                                      const cair_stats_params* params, int64_t n, const cair_stats_count* counts,
+                                      const uint64_t* ring_rows, cair_final_state* out, int64_t cap, int64_t* nout,
+                                      char* msg, int32_t msg_cap) {
+  if (nitems < 1 || !items || !item_rows || !item_ini || !params || n < 0 || (n > 0 && !counts) || !ring_rows ||
+      cap < 0 || (cap > 0 && !out) || !nout)
+    return report("cair_statistics_finish: bad argument", msg, msg_cap);
+  if (params->ncond != 3 && params->ncond != 5) return report("cair_statistics_finish: ncond must be 3 or 5", msg, msg_cap);
+  cair::StatsRuns runs;
+  std::string e = cair::stats_runs(nitems, items, item_run, runs);
+  if (e.empty())
+    e = cair::stats_rings(*params, nitems, items, (const unsigned long long*)item_rows, (const long long*)item_ini,
+                          runs);
+  if (!e.empty()) return report(e, msg, msg_cap);
+  std::vector<cair::StatsEntry> ent((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    const cair_stats_count& c = counts[i];
+    if (c.run < 0 || c.run >= runs.nruns || c.ring < 0 || c.ring >= runs.nring[c.run] || c.count < 0)
+      return report("cair_statistics_finish: a count outside the runs and rings of the totals", msg, msg_cap);
+    ent[i] = cair::StatsEntry{(long long)c.code, c.run, c.ring, (unsigned long long)c.count};
+  }
+  *nout = 0;
+  e = cair::stats_finish_entries(*params, runs, std::move(ent), (const unsigned long long*)ring_rows, out, cap, nout);
+  return report(e, msg, msg_cap);
 }

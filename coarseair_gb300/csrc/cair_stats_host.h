@@ -30,6 +30,21 @@ std::string stats_runs(int32_t nitems, const cair_work_item* items, const int32_
 // and the range check of the key.  "" or an error.
 std::string stats_rings(const cair_stats_params& P, int32_t nitems, const cair_work_item* items,
                         const unsigned long long* item_rows, const long long* item_ini, StatsRuns& runs);
+// One counted (run, final-state code, ring) entry of the table.
+struct StatsEntry {
+  long long code;
+  int run, ring;
+  unsigned long long count;
+};
+
+// The table's keys decoded: key = (code x nruns + run) x R + ring, the code possibly negative.
+std::vector<StatsEntry> stats_decode(const StatsRuns& runs, int64_t n, const unsigned long long* keys,
+                                     const unsigned long long* counts);
+// WriteFinStateProbabilities over decoded entries (any order; entries with equal run, code and ring
+// must already be summed); lines sorted by run then code.  "" or an error (cap too small).
+std::string stats_finish_entries(const cair_stats_params& P, const StatsRuns& runs, std::vector<StatsEntry> ent,
+                                 const unsigned long long* ring_rows, cair_final_state* out, int64_t cap,
+                                 int64_t* nout);
 // WriteFinStateProbabilities over the counted entries: key = (code x nruns + run) x R + ring,
 // ring_rows = TrajsPerb of each (run, ring); lines sorted by run then code.  "" or an error
 // (cap too small).

@@ -360,6 +360,48 @@ int cair_statistics(cair_handle* h, int32_t nitems, const cair_work_item* items,
                     const cair_traj_result* results, const cair_stats_params* params, cair_final_state* out,
                     int64_t cap, int64_t* nout);
 
+/* Replicas: the statistics of processes or GPUs that ran the same runs from disjoint streams (the
+ * reference's per-process outputs, merged by MergeTrajectories before TrajectoriesStats reads them),
+ * without gathering their rows.  The only exchange between replicas is two host-side sums:
+ *   1. cair_statistics_items(_dev) on every replica; sum item_rows and take the minimum of item_ini
+ *      over replicas;
+ *   2. cair_statistics_counts(_dev) on every replica with those totals, so that every replica uses the
+ *      same rings; sum ring_rows (nruns x CAIR_STATS_MAX_RINGS) and the counts of equal (run, ring, code);
+ *   3. cair_statistics_finish on the sums (host code, no handle or GPU).
+ * On one replica the three steps give the lines of cair_statistics(_dev).  Runs are numbered as
+ * item_run says (NULL: run = item); nruns = the largest run + 1. */
+#define CAIR_STATS_MAX_RINGS 64
+typedef struct cair_stats_count {
+  int32_t run;
+  int32_t ring;    /* 0-based ring of the run, rings ascending in bmax */
+  int64_t code;    /* final-state code (iquse + 2) x QuantumNumberMax^c summed over the conditions */
+  int64_t count;
+} cair_stats_count;
+/* Counted rows and the smallest initial-state code of every item (item_ini: INT64 max-like
+ * 0x7f7f7f7f7f7f7f7f for an item without counted rows). */
+int cair_statistics_items_dev(cair_handle* h, int32_t nitems, int64_t ntot, const cair_traj_result* results,
+                              const cair_stats_params* params, uint64_t* item_rows, int64_t* item_ini,
+                              void* stream);
+int cair_statistics_items(cair_handle* h, int32_t nitems, int64_t ntot, const cair_traj_result* results,
+                          const cair_stats_params* params, uint64_t* item_rows, int64_t* item_ini);
+/* (run, ring, final-state code) counts of this replica's rows with the rings given by the totals of
+ * step 1, at most `cap` entries (CAIR_EINVAL with the size needed in the message beyond), and the rows
+ * per (run, ring) in ring_rows[run * CAIR_STATS_MAX_RINGS + ring] (host array of nruns x 64). */
+int cair_statistics_counts_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                               const uint64_t* item_rows, const int64_t* item_ini, int64_t ntot,
+                               const cair_traj_result* results, const cair_stats_params* params,
+                               cair_stats_count* out, int64_t cap, int64_t* nout, uint64_t* ring_rows, void* stream);
+int cair_statistics_counts(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                           const uint64_t* item_rows, const int64_t* item_ini, int64_t ntot,
+                           const cair_traj_result* results, const cair_stats_params* params, cair_stats_count* out,
+                           int64_t cap, int64_t* nout, uint64_t* ring_rows);
+/* The statistics lines from the summed totals and counts (host code).  Returns CAIR_EINVAL, with the
+ * reason in msg when msg_cap > 0, for inconsistent input or a too-small cap. */
+int cair_statistics_finish(int32_t nitems, const cair_work_item* items, const int32_t* item_run,
+                           const uint64_t* item_rows, const int64_t* item_ini, const cair_stats_params* params,
+                           int64_t n, const cair_stats_count* counts, const uint64_t* ring_rows,
+                           cair_final_state* out, int64_t cap, int64_t* nout, char* msg, int32_t msg_cap);
+
 /* trajectories.out rows (Integrator_Class.F90:884-933): format
  * (I10, ',', I5, 2(',', ES11.5), *(',', ES14.8)) with iTraj = idx_offset + idx, iPES 1-based, bmax,
  * b_i, then for nmol = 1 (NInitMolecules, diatom + atom) j_i, v_i, arr_i, j_f, v_f, arr_f and for

@@ -57,3 +57,44 @@ def test_two_replicas_draw_disjoint_streams_and_report_the_slowest(tmp_path):
     for o in outs:
         assert o["ms_max"] == 1250.0
         assert o["rate"] == pytest.approx(3000 * 2 * world / 1.25)
+
+
+def _stats_rank(rank, world, port, out_dir):
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from coarseair_gb300 import api, build, systems
+    import test_stats_host as T
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    items, rows, runs = T._ring_rows_two_runs()
+    P = T._params(3, (1, 0, 0, 0, 0), T._xmu(systems.n3_config().masses))
+    items_pass, counts_pass = T.numpy_passes(build.LIB, P, 3)
+    sel = (rows["item"] == 1) | (np.arange(len(rows)) % 2 == 0) if rank == 0 else \
+        (rows["item"] != 1) & (np.arange(len(rows)) % 2 == 1)
+    lines = api.replica_statistics(P, items, rows[sel], runs, items_pass, counts_pass)
+    np.save(os.path.join(out_dir, "stats%d.npy" % rank), lines)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_replicas_exchange_only_statistics_sums(tmp_path, gpu_lib, oracle_lib):
+    """The multi-GPU statistics path on two gloo ranks: each rank holds half of the rows (one rank all of
+    an item's), the ranks exchange the summed totals and counts (api.replica_statistics), and both
+    end with the lines of all rows together."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as tmp
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import test_stats_host as T
+    from coarseair_gb300 import systems
+    world, port = 2, _free_port()
+    tmp.start_processes(_stats_rank, args=(world, port, str(tmp_path)), nprocs=world, join=True,
+                        start_method="spawn")
+    got = [np.load(tmp_path / ("stats%d.npy" % r)) for r in range(world)]
+    items, rows, runs = T._ring_rows_two_runs()
+    P = T._params(3, (1, 0, 0, 0, 0), T._xmu(systems.n3_config().masses))
+    keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= P.ham_abs_tol)
+    one = T._host_statistics(T._load(gpu_lib), P, items, rows, runs, keep, 3)
+    assert np.array_equal(got[0], got[1]) and np.array_equal(got[0], one)

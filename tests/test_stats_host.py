@@ -277,3 +277,100 @@ def test_no_counted_rows(gpu_lib, oracle_lib):
     keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= P.ham_abs_tol)
     assert not keep.any()
     assert len(_host_statistics(L, P, items, rows, None, keep, 3)) == 0
+
+
+def numpy_passes(gpu_lib, P, nc):
+    """The two device passes of the replicas' statistics restated in numpy (the rings from the library's
+    host half): items_pass(nitems, rows) and counts_pass(items, rows, item_rows, item_ini, runs)."""
+    L = _load(gpu_lib)
+    names = ("j", "v", "arr") if nc == 3 else ("j", "v", "j2", "v2", "arr")
+
+    def codes(rows):
+        qi = np.stack([rows[n + "_i"] for n in names], 1)
+        qf = np.stack([rows[n + "_f"] for n in names], 1)
+        keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= P.ham_abs_tol)
+        ic, fc = _codes(qi, qf, list(P.iskip)[:nc], list(P.pres_even_odd)[:nc], P.qn_max)
+        return keep, ic, fc
+
+    def items_pass(nitems, rows):
+        keep, ic, _ = codes(rows)
+        item_rows = np.bincount(rows["item"][keep], minlength=nitems).astype(np.uint64)
+        item_ini = np.full(nitems, 0x7f7f7f7f7f7f7f7f, np.int64)
+        np.minimum.at(item_ini, rows["item"][keep], ic[keep])
+        return item_rows, item_ini
+
+    def counts_pass(items, rows, item_rows, item_ini, runs):
+        nitems = len(items)
+        keep, ic, fc = codes(rows)
+        itc = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+        run_arr = None if runs is None else np.ascontiguousarray(runs, np.int32)
+        ring_b, nring = np.zeros(nitems * MAXR), np.zeros(nitems, np.int32)
+        R, nruns = C.c_int32(), C.c_int32()
+        ir, ii = np.ascontiguousarray(item_rows, np.uint64), np.ascontiguousarray(item_ini, np.int64)
+        assert L.cair_internal_stats_rings(C.byref(P), nitems, itc.ctypes.data,
+                                           None if run_arr is None else run_arr.ctypes.data, ir.ctypes.data,
+                                           ii.ctypes.data, ring_b.ctypes.data, nring.ctypes.data, C.byref(R),
+                                           C.byref(nruns), None, 0) == 0
+        run_of = np.arange(nitems) if runs is None else np.asarray(runs)
+        rr = run_of[rows["item"]]
+        ring = np.zeros(len(rows), np.int64)
+        for k in np.flatnonzero(keep):
+            e = ring_b[rr[k] * MAXR: rr[k] * MAXR + nring[rr[k]]]
+            for q in range(len(e) - 1):
+                if not (rows["b"][k] > e[q + 1] or rows["b"][k] <= e[q]):
+                    ring[k] = q + 1
+                    break
+        trip = np.stack([rr[keep], ring[keep], fc[keep]], 1)
+        u, cnt = np.unique(trip, axis=0, return_counts=True)
+        out = np.zeros(len(u), dtype=_lib.STATS_COUNT_DTYPE)
+        out["run"], out["ring"], out["code"], out["count"] = u[:, 0], u[:, 1], u[:, 2], cnt
+        ring_rows = np.zeros((nruns.value, MAXR), np.uint64)
+        np.add.at(ring_rows, (rr[keep], ring[keep]), 1)
+        return out, ring_rows
+
+    return items_pass, counts_pass
+
+
+def _ring_rows_two_runs():
+    rng = np.random.default_rng(8)
+    bm = [2.0, 4.0, 6.0, 5.0, 5.0]
+    counts = [3000, 4000, 6000, 3000, 3000]
+    n = sum(counts)
+    rows = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    rows["item"] = np.repeat(np.arange(5), counts)
+    rows["bmax"] = np.repeat(bm, counts)
+    rows["b"] = rows["bmax"] * np.sqrt(rng.uniform(size=n))
+    rows["j_i"], rows["v_i"], rows["arr_i"] = 20.5, 0.5, 16.5
+    rows["j_f"] = rng.uniform(0.0, 45.0, n)
+    rows["v_f"] = rng.uniform(-0.5, 6.0, n)
+    rows["arr_f"] = rng.choice([16.5, 17.5, 32.5, 48.5], n)
+    rows["dH"] = 1e-9
+    items = np.zeros(5, dtype=_lib.ITEM_DTYPE)
+    items["bmax"], items["ttra"] = bm, 10000.0
+    return items, rows, [0, 0, 0, 1, 1]
+
+
+def test_replicas_sum_to_the_statistics_of_all_rows(gpu_lib, oracle_lib):
+    """Two replicas with disjoint rows -- the first holds every row of the 4-bohr item, the second none,
+    so the rings only agree through the summed totals -- through the three steps of the replicas'
+    statistics: the lines equal the oracle's and the one-replica lines of all rows."""
+    from coarseair_gb300 import api
+    L = _load(gpu_lib)
+    items, rows, runs = _ring_rows_two_runs()
+    P = _params(3, (1, 0, 0, 0, 0), _xmu(systems.n3_config().masses))
+    items_pass, counts_pass = numpy_passes(gpu_lib, P, 3)
+    part = [rows[(rows["item"] == 1) | (np.arange(len(rows)) % 2 == 0)],
+            rows[(rows["item"] != 1) & (np.arange(len(rows)) % 2 == 1)]]
+    totals = [items_pass(len(items), p) for p in part]
+    ir = sum(t[0] for t in totals)
+    ii = np.minimum(totals[0][1], totals[1][1])
+    cs = [counts_pass(items, p, ir, ii, runs) for p in part]
+    got = api.statistics_finish(P, items, ir, ii, np.concatenate([c[0] for c in cs]), cs[0][1] + cs[1][1], runs)
+    keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= P.ham_abs_tol)
+    one = _host_statistics(L, P, items, rows, runs, keep, 3)
+    assert np.array_equal(got, one)
+    _check(L, items, rows, (1, 0, 0, 0, 0), 3, P.xmu, runs=runs)
+    with pytest.raises(api.CairError, match="outside the runs and rings"):
+        bad = np.concatenate([c[0] for c in cs])
+        bad["ring"][0] = 7
+        api.statistics_finish(P, items, ir, ii, bad, cs[0][1] + cs[1][1], runs)
