@@ -52,8 +52,29 @@ static inline T atomicAdd(T* p, T v) {
 }
 static inline void __syncwarp(unsigned = 0xffffffffu) {}
 static inline int __any_sync(unsigned, int pred) { return pred; }
+template <class T>
+static inline T atomicExch(T* p, T v) {
+  const T o = *p;
+  *p = v;
+  return o;
+}
+template <class T>
+static inline T atomicMin(T* p, T v) {
+  const T o = *p;
+  if (v < o) *p = v;
+  return o;
+}
+template <class T>
+static inline T atomicCAS(T* p, T cmp, T v) {
+  const T o = *p;
+  if (o == cmp) *p = v;
+  return o;
+}
 
 #include "../../coarseair_gb300/csrc/cair_ic.cuh"
+#include "../../coarseair_gb300/csrc/cair_stats.cuh"
+
+#include <vector>
 
 using namespace cair;
 
@@ -166,6 +187,61 @@ extern "C" int ic_host_sample(const void* devsys, const double* packed, const in
   delete[] item_of;
   delete[] key;
   return rc;
+}
+
+// cair_statistics_dev's steps on the host: the two counting kernels and the compaction over a 1 x 1
+// grid on host arrays, with the library's host half (stats_runs, stats_rings, stats_finish) between
+// and after them.
+extern "C" int stats_host_run(const cair_stats_params* P, int32_t nitems, const cair_work_item* items,
+                              const int32_t* item_run, int64_t ntot, const cair_traj_result* rows,
+                              cair_final_state* out, int64_t cap, int64_t* nout) {
+  StatsRuns runs;
+  if (!stats_runs(nitems, items, item_run, runs).empty()) return 1;
+  unsigned long long tsize = 1024;
+  while (tsize < 2ull * (unsigned long long)ntot) tsize <<= 1;
+  std::vector<unsigned long long> keys(tsize, kStatsEmpty), counts(tsize, 0), okeys(tsize), ocounts(tsize);
+  std::vector<unsigned long long> item_rows(nitems, 0);
+  std::vector<long long> item_ini(nitems, 0x7f7f7f7f7f7f7f7fll);
+  std::vector<double> ring_b((size_t)runs.nruns * kMaxRings, 0.0);
+  std::vector<unsigned long long> ring_rows((size_t)runs.nruns * kMaxRings, 0);
+  std::vector<int32_t> run_of(runs.run_of), nring(runs.nruns, 0);
+  int err = 0;
+  StatsArgs A{};
+  A.ntot = ntot;
+  A.rows = rows;
+  A.qnmax = P->qn_max;
+  for (int q = 0; q < 5; ++q) {
+    A.iskip[q] = P->iskip[q];
+    A.pres[q] = P->pres_even_odd[q];
+  }
+  A.ham_abs_tol = P->ham_abs_tol;
+  A.item_run = run_of.data();
+  A.ring_b = ring_b.data();
+  A.nring = nring.data();
+  A.nruns = runs.nruns;
+  A.R = 1;
+  A.keys = keys.data();
+  A.counts = counts.data();
+  A.mask = tsize - 1;
+  A.item_rows = item_rows.data();
+  A.item_inicode = item_ini.data();
+  A.ring_rows = ring_rows.data();
+  A.error = &err;
+  if (P->ncond == 3) k_stats_items<3>(A);
+  else k_stats_items<5>(A);
+  if (err) return 2;
+  if (!stats_rings(*P, nitems, items, item_rows.data(), item_ini.data(), runs).empty()) return 3;
+  std::copy(runs.ring_b.begin(), runs.ring_b.end(), ring_b.begin());
+  std::copy(runs.nring.begin(), runs.nring.end(), nring.begin());
+  A.R = runs.R;
+  if (P->ncond == 3) k_stats_count<3>(A);
+  else k_stats_count<5>(A);
+  if (err) return 4;
+  unsigned long long n = 0;
+  k_stats_compact(keys.data(), counts.data(), tsize, okeys.data(), ocounts.data(), tsize, &n);
+  return stats_finish(*P, runs, (int64_t)n, okeys.data(), ocounts.data(), ring_rows.data(), out, cap, nout).empty()
+             ? 0
+             : 5;
 }
 
 extern "C" int64_t pes_host_devsys_size(void) { return (int64_t)sizeof(DevSys); }

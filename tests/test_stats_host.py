@@ -374,3 +374,46 @@ def test_replicas_sum_to_the_statistics_of_all_rows(gpu_lib, oracle_lib):
         bad = np.concatenate([c[0] for c in cs])
         bad["ring"][0] = 7
         api.statistics_finish(P, items, ir, ii, bad, cs[0][1] + cs[1][1], runs)
+
+
+def _kernels_on_host(P, items, rows, runs):
+    from test_pes_host import _harness
+    L = _harness()
+    it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+    rw = np.ascontiguousarray(rows, dtype=_lib.RESULT_DTYPE)
+    rn = None if runs is None else np.ascontiguousarray(runs, np.int32)
+    out = np.zeros(max(64, len(rw)), dtype=_lib.FINAL_STATE_DTYPE)
+    n = C.c_int64()
+    rc = L.stats_host_run(C.addressof(P), len(it), it.ctypes.data, None if rn is None else rn.ctypes.data, len(rw),
+                          rw.ctypes.data, out.ctypes.data, len(out), C.byref(n))
+    assert rc == 0, rc
+    return out[:n.value]
+
+
+def test_statistics_kernels_run_on_the_host(gpu_lib, oracle_lib):
+    """k_stats_items, k_stats_count and k_stats_compact themselves (host build of cair_stats.cuh, a 1 x 1
+    grid, atomics emulated) in cair_statistics_dev's order with the library's host half: the same lines
+    as the restated passes, on pooled multi-ring runs (3 conditions) and on diatom + diatom rows with
+    clusters (5 conditions)."""
+    L = _load(gpu_lib)
+    items, rows, runs = _ring_rows_two_runs()
+    P = _params(3, (1, 0, 0, 0, 0), _xmu(systems.n3_config().masses))
+    keep = (rows["status"] == 0) & (np.abs(rows["dH"]) <= P.ham_abs_tol)
+    assert np.array_equal(_kernels_on_host(P, items, rows, runs), _host_statistics(L, P, items, rows, runs, keep, 3))
+    rng = np.random.default_rng(4)
+    n = 6000
+    r5 = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    r5["item"] = rng.integers(0, 2, n)
+    r5["j_i"], r5["v_i"], r5["j2_i"], r5["v2_i"], r5["arr_i"] = 1.5, 0.5, 3.5, 0.5, 26.5
+    arr = rng.choice([26.5, 42.5, 18.5, -65.5], n)
+    for c in ("j_f", "v_f", "j2_f", "v2_f"):
+        r5[c] = np.where(arr == -65.5, -0.5, rng.uniform(-1.0, 30.0 if c[0] == "j" else 6.0, n))
+    r5["arr_f"] = arr
+    r5["b"] = rng.uniform(0.0, 8.0, n)
+    r5["bmax"] = 8.0
+    r5["dH"] = 1e-9
+    it5 = np.zeros(2, dtype=_lib.ITEM_DTYPE)
+    it5["bmax"], it5["ttra"] = 8.0, 1e4
+    P5 = _params(5, (1, 0, 1, 0, 0), _xmu(systems.o4_config().masses))
+    keep5 = np.ones(n, bool)
+    assert np.array_equal(_kernels_on_host(P5, it5, r5, None), _host_statistics(L, P5, it5, r5, None, keep5, 5))
