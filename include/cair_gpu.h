@@ -11,7 +11,12 @@
  *   -> src/PESs/PES_Class.F90:43-72,252-360        (PES_Type%Compute / Potential, TransToCart)
  * and the final-state analysis of
  *   src/Collision/Trajectories/TrajectoryPoint_Class.F90:128-495 and
- *   src/Collision/MolecularState/MolecularState_Class.F90:61-429.
+ *   src/Collision/MolecularState/MolecularState_Class.F90:61-429;
+ * on either side of it, the initial conditions (Collision_Class.F90:1065-1849, with the
+ * impact-parameter rings of ImpactParameter_Class.F90), the final-state statistics and rates
+ * (app/TrajectoriesStats/Statistics_Class.F90, Process_Class.F90:122-209), and the
+ * trajectories.out / trajectories.bin writers and MergeTrajectories (Integrator_Class.F90:884-933,
+ * Statistics_Class.F90:283-314, scripts/executing/ComputeRates.sh:406-472).
  *
  * Conventions (those of the Fortran arrays, so a Fortran ISO_C_BINDING shim passes its
  * arrays unchanged):
@@ -31,8 +36,9 @@
  * status[] arrays (cair_traj_status).
  *
  * Threading: a handle is used by one host thread at a time; distinct handles may be used
- * concurrently from distinct threads.  Calls are synchronous unless named *_dev (those
- * are asynchronous on the given stream).
+ * concurrently from distinct threads.  Calls are synchronous unless named *_dev: those run
+ * on the given stream and return before it completes, except the statistics entry points,
+ * which return their results in host memory and so synchronise with it.
  */
 #ifndef CAIR_GPU_H
 #define CAIR_GPU_H
