@@ -244,6 +244,95 @@ extern "C" int stats_host_run(const cair_stats_params* P, int32_t nitems, const 
              : 5;
 }
 
+// cair_run_queue_dev's pipeline on the host, one lane: the streams and k_sample_ic3/4, the state of
+// cair_k_init_state, k_integrate over the queue in item order (the GPU's longest-first order changes
+// only the schedule), and k_results.  The final-state parameters come from the caller; the
+// Chebyshev-2 nodes and Vinf are formed as cair_create forms them.
+template <int MODEL, int NS>
+static void queue_run(const DevSys& S, const FsArgs& F, int64_t ntot, const cair_work_item* items, int32_t* item_of,
+                      double* paq, const double* paq0, const double* erra, const double* H0, const int32_t* ipes,
+                      int64_t max_attempts, cair_traj_result* out) {
+  constexpr int NE = Traits<MODEL>::NE;
+  std::vector<double> t(ntot, 0.0), dt(ntot, S.dt0), smax(ntot, -1.7976931348623157e308),
+      smin(ntot, 1.7976931348623157e308), H(ntot, 0.0);
+  std::vector<int32_t> irej(ntot, 0), iste(ntot, 0), status(ntot, 0);
+  unsigned long long ctl[6] = {0, 0, 0, 0, 0, 0};
+  IntegrateArgs A{ntot, ipes, paq, t.data(), dt.data(), erra, H.data(), smax.data(), smin.data(), irej.data(),
+                  iste.data(), status.data(), max_attempts, ctl, ctl + 1, nullptr};
+  k_integrate<MODEL, NS>(S, A);
+  (void)NE;
+  if (Traits<MODEL>::NA == 3)
+    k_results<3>(S, F, ntot, paq0, paq, H0, H.data(), t.data(), status.data(), iste.data(), irej.data(), item_of,
+                 items, out);
+  else
+    k_results<4>(S, F, ntot, paq0, paq, H0, H.data(), t.data(), status.data(), iste.data(), irej.data(), item_of,
+                 items, out);
+}
+
+template <int MODEL>
+static int queue_run_ns(const DevSys& S, const FsArgs& F, int64_t ntot, const cair_work_item* items, int32_t* item_of,
+                        double* paq, const double* paq0, const double* erra, const double* H0, const int32_t* ipes,
+                        int64_t max_attempts, cair_traj_result* out) {
+  switch (S.nsteps) {
+    case 2: queue_run<MODEL, 2>(S, F, ntot, items, item_of, paq, paq0, erra, H0, ipes, max_attempts, out); return 0;
+    case 3: queue_run<MODEL, 3>(S, F, ntot, items, item_of, paq, paq0, erra, H0, ipes, max_attempts, out); return 0;
+    case 4: queue_run<MODEL, 4>(S, F, ntot, items, item_of, paq, paq0, erra, H0, ipes, max_attempts, out); return 0;
+    default: return 1;
+  }
+}
+
+extern "C" int queue_host_run(const void* devsys, const double* packed, const int64_t* offsets,
+                              const cair_level* levels, int32_t nitems, const cair_work_item* items, int64_t ntot,
+                              int64_t max_attempts, int32_t nquad, double rsmal, double rcent, double rfact,
+                              double tthresau, cair_traj_result* out) {
+  DevSys S;
+  std::memcpy(&S, devsys, sizeof S);
+  for (int p = 0; p < S.npes; ++p) S.pes[p].coef = packed + offsets[p];
+  const int ne = S.ne, nmol = S.natoms == 4 ? 2 : 1;
+  std::vector<double> draws(kDraws * ntot), paq(ne * ntot), paq0(ne * ntot), erra(ne * ntot), H0(ntot), b(ntot),
+      key(ntot);
+  std::vector<int32_t> item_of(ntot), ipes(ntot);
+  for (int i = 0; i < nitems; ++i)
+    if (!continues_stream(items, i)) stream_draws(items, nitems, i, nmol, levels, draws.data(), item_of.data());
+  // final-state parameters (cair_create: GAUSSQ kind 3 in closed form, Vinf = the diatomic at 1e3 bohr)
+  std::vector<double> gx(nquad), gw(nquad);
+  const double pi = std::acos(-1.0);
+  for (int i = 0; i < nquad; ++i) {
+    const int k = nquad - i;
+    const double th = (double)k * pi / (double)(nquad + 1), sn = std::sin(th);
+    gx[i] = std::cos(th);
+    gw[i] = pi / (double)(nquad + 1) * (sn * sn);
+    gw[i] = gw[i] / std::sqrt(1.0 - gx[i] * gx[i]);
+  }
+  FsArgs F{};
+  F.nquad = nquad;
+  F.rsmal = rsmal;
+  F.rcent = rcent;
+  F.rfact = rfact;
+  F.tthresau = tthresau;
+  F.gx = gx.data();
+  F.gw = gw.data();
+  for (int i = 0; i < 4; ++i) F.mass[i] = S.mass[i];
+  F.vinf = diat_v(S, 1.0E+03);
+  int rc = 0;
+#define QUEUE(M)                                                                                              \
+  sample<M>(S, ntot, items, levels, draws.data(), item_of.data(), paq.data(), paq0.data(), erra.data(),        \
+            H0.data(), b.data(), ipes.data(), key.data());                                                     \
+  rc = queue_run_ns<M>(S, F, ntot, items, item_of.data(), paq.data(), paq0.data(), erra.data(), H0.data(),     \
+                       ipes.data(), max_attempts, out);
+  switch (S.pes[0].model) {
+    case CAIR_PES_O3_UMN: QUEUE(CAIR_PES_O3_UMN) break;
+    case CAIR_PES_N3_UMN: QUEUE(CAIR_PES_N3_UMN) break;
+    case CAIR_PES_O4_UMN: QUEUE(CAIR_PES_O4_UMN) break;
+    case CAIR_PES_O3_NN: QUEUE(CAIR_PES_O3_NN) break;
+    case CAIR_PES_N4_UMN: QUEUE(CAIR_PES_N4_UMN) break;
+    case CAIR_PES_O3_BNN: QUEUE(CAIR_PES_O3_BNN) break;
+    default: rc = 1;
+  }
+#undef QUEUE
+  return rc;
+}
+
 extern "C" int64_t pes_host_devsys_size(void) { return (int64_t)sizeof(DevSys); }
 
 // V, dV/dR and -dV/dQ of n points as the library's k_pes_eval computes them (surface model of

@@ -7,7 +7,8 @@ O3 NN and the O3 BNN samples -- against the oracle at the same points, energies 
 the oracle's Potential; the device Bulirsch-Stoer attempt (Rhs, bs_attempt) over 1000 fixed attempts
 against the oracle on the trajectories the oracle shows to be non-chaotic, to 1e-9 as on the GPU; and
 the initial-condition kernels (the stream code of k_ic_draws, the bodies of k_sample_ic3/4 run over a
-1 x 1 grid) for impact-parameter rings of every strata type against the oracle's stream.
+1 x 1 grid) for impact-parameter rings of every strata type against the oracle's stream; and the whole
+queue pipeline (k_integrate as one lane, k_results) for stratified rings and for the 50 BNN samples.
 This checks the surface and integrator arithmetic and the coefficient packing; the GPU tests check
 the same code as nvcc builds it."""
 import ctypes as C
@@ -44,6 +45,9 @@ def _harness():
     L.stats_host_run.restype = C.c_int
     L.stats_host_run.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                  C.c_int64, C.c_void_p]
+    L.queue_host_run.restype = C.c_int
+    L.queue_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
+                                 C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.c_void_p]
     L.pes_host_bs_steps.restype = C.c_int
     L.pes_host_bs_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_int]
@@ -222,3 +226,92 @@ def test_ic_kernels_on_the_host_for_diatom_diatom_rings(gpu_lib, oracle_lib):
     for key in ("paq", "paq0", "erra"):
         assert _close(ic[key], ref[key], 1e-10), key
     assert np.allclose(ic["b"], ref["b"], rtol=1e-14, atol=0)
+
+
+def _queue_host(L, setup, cfg, table, items, max_attempts):
+    devsys, packed, offsets, _ = setup
+    tb = np.ascontiguousarray(table, dtype=_lib.LEVEL_DTYPE)
+    it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+    ntot = int(it["ntraj"].sum())
+    out = np.zeros(ntot, dtype=_lib.RESULT_DTYPE)
+    assert L.queue_host_run(devsys, packed.ctypes.data, offsets.ctypes.data, tb.ctypes.data, len(it), it.ctypes.data,
+                            ntot, int(max_attempts), cfg.nquad, cfg.rsmal, cfg.rcent, cfg.rfact, cfg.tthresau,
+                            out.ctypes.data) == 0
+    return out
+
+
+def test_queue_pipeline_on_the_host_for_rings(gpu_lib, oracle_lib):
+    """The GPU rings test's queue half through the host pipeline: rows numbered along the stream, each
+    ring's |b| as bmax, the impact parameters of the oracle's stream, the fixed ring's b."""
+    from oracle import Oracle
+    cfg = systems.n3_config(rmax=30.0)
+    o = Oracle(cfg)
+    L = _harness()
+    setup = _setup(gpu_lib, cfg, o.tpq)
+    rows = systems.load_levels("N2")[[17]]
+    bring, ntring, n, seed = [-2.0, -4.5, 3.0, -7.0], [1, 2, 1, 3], 71, api.process_seed(4, 1)
+    for strata in ("Circles", "Rings", "Segments"):
+        items = api.work_items(api.ring_entries(0, 0, n, seed, 10000.0, 15.0, bring, ntring, strata))
+        res = _queue_host(L, setup, cfg, api.level_table(rows), items, 2000)
+        ref = o.sample_ics(n, _levels_for_oracle(rows), seed=seed, ttra=10000.0, dinit=15.0,
+                           rings=(bring, ntring, api.STRATA[strata]))
+        assert list(res["idx"]) == list(range(1, n + 1))
+        assert np.array_equal(res["bmax"], np.repeat([2.0, 4.5, 3.0, 7.0], [11, 20, 10, 30]))
+        # the row's b is the analysed impact parameter of the initial point (TrajIni%b), a magnitude;
+        # Segments strata after a sampled ring draw negative b
+        assert np.allclose(res["b"], np.abs(ref["b"]), rtol=1e-13, atol=0), strata
+        assert np.allclose(res["b"][31:41], 3.0, rtol=1e-13, atol=0)
+        if strata == "Segments":
+            assert np.any(ref["b"] < 0)
+        assert set(np.unique(res["status"])) <= {0, 1}
+
+
+def test_queue_pipeline_on_the_host_for_the_bnn_samples(gpu_lib, oracle_lib):
+    """The GPU BNN queue test through the host pipeline: 100 trajectories in 50 per-sample blocks, capped
+    at 20,000 attempts; final states against the oracle where both finished and the oracle is stable,
+    then the finished rows of all 50 samples pooled into one run by the statistics kernels."""
+    import oracle
+    from oracle import Oracle
+    from test_stats_host import _kernels_on_host
+    cfg = systems.o3bnn_config()
+    o = Oracle(cfg)
+    L = _harness()
+    setup = _setup(gpu_lib, cfg, o.tpq)
+    lv = systems.load_levels("O2")
+    row = lv[(lv["vqn"] == 0) & (lv["jqn"] == 1)]
+    counts = api.degeneracy_blocks(100, cfg.degeneracy)
+    seed, cap = api.process_seed(3, 1), 20000
+    items = api.work_items([(0, k, nn, seed, 20000.0, 6.0, 15.0) for k, nn in enumerate(counts)])
+    res = _queue_host(L, setup, cfg, api.level_table(row), items, cap)
+    ic = o.sample_ics(2, _levels_for_oracle(row), seed=seed, ttra=20000.0, bmax=6.0, dinit=15.0)
+    paq, erra = np.tile(ic["paq"], (50, 1)), np.tile(ic["erra"], (50, 1))
+    ipv = np.repeat(np.arange(50, dtype=np.int32), 2)
+    a = o.integrate(paq, erra, ipes=ipv, max_attempts=cap, procs=4)
+    b = o.integrate(paq * (1 + 1e-14), erra, ipes=ipv, max_attempts=cap, procs=4)
+
+    def qn(paqs):
+        fs = o.analyze(o.apply_transformation(paqs))
+        return api.histogram_assign(np.array([f["angmom"] for f in fs]), np.array([f["viba"] for f in fs]),
+                                    np.array([16 * f["ipair"] + f["itype"] + 0.5 for f in fs]))
+
+    fa, fb = qn(a["paq"]), qn(b["paq"])
+    fg = api.histogram_assign(res["j_f"], res["v_f"], res["arr_f"])
+    done = (res["status"] == 0) & (a["status"] == 0) & (b["status"] == 0)
+    same = (fa[0] == fg[0]) & (fa[1] == fg[1]) & (fa[2] == fg[2])
+    stable = done & (fa[0] == fb[0]) & (fa[1] == fb[1]) & (fa[2] == fb[2])
+    assert stable.sum() >= 20 and same[stable].mean() >= 0.995
+    st = api.Statistics.__new__(api.Statistics)
+    P = _lib.StatsParams()
+    P.qn_max, P.ncond = 300, 3
+    for i in range(5):
+        P.iskip[i], P.pres_even_odd[i] = (1 if i < 3 else 0), 0
+    m = cfg.masses
+    P.ham_abs_tol, P.xmu = 1.0e6, (m[0] + m[1]) * m[2] / sum(m)
+    got = _kernels_on_host(P, items, res, [0] * 50)
+    ok = res["status"] == 0
+    ref, _ = oracle.statistics(res["bmax"][ok], res["b"][ok], np.stack([res["j_i"], res["v_i"], res["arr_i"]], 1)[ok],
+                               np.stack([res["j_f"], res["v_f"], res["arr_f"]], 1)[ok], cap=200)
+    gd = {tuple(int(x) for x in r["fin"][:3]): r for r in got}
+    assert len(got) == len(ref)
+    for fs, nn, cross, sd in ref:
+        assert gd[fs]["count"] == nn and gd[fs]["cross"] == pytest.approx(cross, rel=1e-14)

@@ -150,7 +150,9 @@ def test_stratified_rings_continue_one_stream(gpu_lib, oracle_lib, strata):
     res = api.RunTrajectories(H).run(table, items, max_attempts=2000)  # the rows' numbering and b only
     assert list(res["idx"]) == list(range(1, n + 1))
     assert np.array_equal(res["bmax"], np.repeat([2.0, 4.5, 3.0, 7.0], [11, 20, 10, 30]))
-    assert np.allclose(res["b"], ref["b"], rtol=1e-14, atol=0)
+    # the row's b is the analysed impact parameter of the initial point (TrajIni%b), a magnitude; Segments
+    # strata after a sampled ring draw negative b
+    assert np.allclose(res["b"], np.abs(ref["b"]), rtol=1e-13, atol=0)
     H.close()
 
 
