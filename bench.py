@@ -22,7 +22,6 @@ same work items.
 import argparse
 import ctypes
 import json
-import math
 import multiprocessing as mp
 import os
 import subprocess

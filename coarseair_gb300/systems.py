@@ -22,7 +22,7 @@ templates (input/O3/UMN/input/CoarseAIR.inp, input/N3/UMN/input/CoarseAIR.inp).
 import gzip
 import os
 import re
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

@@ -9,7 +9,6 @@ integers, 1e-12 relative for the floating-point fields; the kernels are the same
 expected to be identical).  It also checks that a batch beyond the static capacity is rejected.
 Collected last so that a run that stops at the first failure has run every other test.
 """
-import ctypes
 
 import numpy as np
 import pytest
