@@ -304,7 +304,7 @@ def main():
         rate, n, t = cpu_baseline(table, items, cores, args.cpu_wall, args.system)
         cpu = {"value": rate, "unit": "trajectories/s", "cores": cores, "kind": "port",
                "sample": "%d trajectories of the same work items in %.1f s on %d processes "
-                         "(C restatement of the reference CPU path, -O2 no FMA)" % (n, t, cores)}
+                         "(C restatement of the reference CPU path, -O3 no FMA)" % (n, t, cores)}
 
     import torch
     from coarseair_gb300 import api, _lib

@@ -4,6 +4,7 @@ Translation units are compiled in parallel and linked into one shared library ne
 file, where coarseair_gb300._lib loads it.
 """
 import concurrent.futures as cf
+import hashlib
 import os
 import shutil
 import subprocess
@@ -38,6 +39,32 @@ def _newer(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _digest(deps, extra=()):
+    """SHA-256 over the sources, the compiler flags and the nvcc version: the library is rebuilt
+    whenever this differs from the digest stamped beside it, whatever the files' times."""
+    h = hashlib.sha256()
+    for d in sorted(deps):
+        h.update(os.path.relpath(d, HERE).encode())
+        with open(d, "rb") as f:
+            h.update(f.read())
+    h.update(repr((NVCC_FLAGS, SOURCES, list(extra))).encode())
+    try:
+        h.update(subprocess.run([nvcc(), "--version"], capture_output=True, text=True).stdout.encode())
+    except (OSError, RuntimeError):
+        pass
+    return h.hexdigest()
+
+
+STAMP = LIB + ".sha256"
+
+
+def _stale(deps, extra=()):
+    if not os.path.exists(LIB) or not os.path.exists(STAMP):
+        return True
+    with open(STAMP) as f:
+        return f.read().strip() != _digest(deps, extra)
+
+
 def _deps():
     out = []
     for root, _, files in os.walk(CSRC):
@@ -51,7 +78,7 @@ def _deps():
 def build(force=False, verbose=False, extra_flags=()):
     os.makedirs(BUILD, exist_ok=True)
     deps = _deps()
-    if not force and not _newer(LIB, deps):
+    if not force and not _stale(deps, extra_flags):
         if _newer(EXAMPLE, [os.path.join(HERE, "examples", "cair_run.c"), LIB]):
             build_example()
         return LIB
@@ -77,6 +104,8 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr[-4000:])
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(_digest(deps, extra_flags) + "\n")
     build_example()
     return LIB
 

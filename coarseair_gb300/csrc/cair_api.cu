@@ -1014,6 +1014,14 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
   return 0;
 }
 
+// The device rings a run by its items' |bmax|.  SetRings (Statistics_Class.F90:534-581) rings by the
+// rows' bMax; the queue writes each row's bmax from its item, so the two agree unless the rows were
+// edited or merged from elsewhere, and then the statistics refuse them instead of ringing them apart
+// from the reference.
+static const char* kBmaxMismatch =
+    "cair_statistics: a counted row's bmax differs from its work item's |bmax| by 1e-3 or more (the rings are "
+    "the items' bmax)";
+
 int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* items, const int32_t* item_run,
                         int64_t ntot, const cair_traj_result* results, const cair_stats_params* params,
                         cair_final_state* out, int64_t cap, int64_t* nout, void* stream) {
@@ -1035,7 +1043,7 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   unsigned long long tsize = 1024;
   while (tsize < 2ull * (unsigned long long)ntot) tsize <<= 1;
   const size_t per_run = (size_t)kMaxRings * 16 + 16;
-  const size_t need = tsize * 32 + (size_t)nitems * 24 + (size_t)nruns * per_run + 8 * 256;
+  const size_t need = tsize * 32 + (size_t)nitems * 32 + (size_t)nruns * per_run + 9 * 256;
   if (h->stats_bytes < need) {
     if (h->d_stats) cudaFree(h->d_stats);
     h->d_stats = nullptr;
@@ -1054,11 +1062,15 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   unsigned long long* ring_rows = c.take<unsigned long long>((size_t)nruns * kMaxRings);
   int32_t* d_run = c.take<int32_t>(nitems);
   int32_t* d_nring = c.take<int32_t>(nruns);
+  double* d_ibmax = c.take<double>(nitems);
   unsigned long long* dn = c.take<unsigned long long>(2);
   int* derr = (int*)(dn + 1);
   cudaStream_t st = (cudaStream_t)stream;
+  std::vector<double> ibmax(nitems);
+  for (int i = 0; i < nitems; ++i) ibmax[i] = std::fabs(items[i].bmax);
   CUDA_TRY(h, cudaMemsetAsync(keys, 0xff, tsize * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(counts, 0, tsize * 8, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_ibmax, ibmax.data(), (size_t)nitems * 8, cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemsetAsync(item_rows, 0, (size_t)nitems * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(item_ini, 0x7f, (size_t)nitems * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(ring_rows, 0, (size_t)nruns * kMaxRings * 8, st));
@@ -1080,7 +1092,8 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
               item_rows,
               item_ini,
               ring_rows,
-              derr};
+              derr,
+              d_ibmax};
   // pass 1: rows and initial-state codes of each item
   if (nc == 3) k_stats_items<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
   else k_stats_items<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
@@ -1110,6 +1123,7 @@ int cair_statistics_dev(cair_handle* h, int32_t nitems, const cair_work_item* it
   CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(perb.data(), ring_rows, perb.size() * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (err == 3) return fail(h, CAIR_EINVAL, kBmaxMismatch);
   if (err) return fail(h, CAIR_EINVAL, "cair_statistics: a final-state key of -1 (not representable)");
   std::vector<unsigned long long> k(n), cnt(n);
   if (n) {
@@ -1214,7 +1228,7 @@ int cair_statistics_counts_dev(cair_handle* h, int32_t nitems, const cair_work_i
   if (ntot == 0) return 0;
   unsigned long long tsize = 1024;
   while (tsize < 2ull * (unsigned long long)ntot) tsize <<= 1;
-  const size_t need = tsize * 32 + (size_t)nitems * 8 + (size_t)nruns * ((size_t)kMaxRings * 16 + 16) + 8 * 256;
+  const size_t need = tsize * 32 + (size_t)nitems * 16 + (size_t)nruns * ((size_t)kMaxRings * 16 + 16) + 9 * 256;
   if (h->stats_bytes < need) {
     if (h->d_stats) cudaFree(h->d_stats);
     h->d_stats = nullptr;
@@ -1231,11 +1245,15 @@ int cair_statistics_counts_dev(cair_handle* h, int32_t nitems, const cair_work_i
   unsigned long long* d_ring_rows = c.take<unsigned long long>((size_t)nruns * kMaxRings);
   int32_t* d_run = c.take<int32_t>(nitems);
   int32_t* d_nring = c.take<int32_t>(nruns);
+  double* d_ibmax = c.take<double>(nitems);
   unsigned long long* dn = c.take<unsigned long long>(2);
   int* derr = (int*)(dn + 1);
   cudaStream_t st = (cudaStream_t)stream;
+  std::vector<double> ibmax(nitems);
+  for (int i = 0; i < nitems; ++i) ibmax[i] = std::fabs(items[i].bmax);
   CUDA_TRY(h, cudaMemsetAsync(keys, 0xff, tsize * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(counts, 0, tsize * 8, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_ibmax, ibmax.data(), (size_t)nitems * 8, cudaMemcpyHostToDevice, st));
   CUDA_TRY(h, cudaMemsetAsync(d_ring_rows, 0, (size_t)nruns * kMaxRings * 8, st));
   CUDA_TRY(h, cudaMemsetAsync(dn, 0, 16, st));
   CUDA_TRY(h, cudaMemcpyAsync(ring_b, runs.ring_b.data(), runs.ring_b.size() * 8, cudaMemcpyHostToDevice, st));
@@ -1260,6 +1278,7 @@ int cair_statistics_counts_dev(cair_handle* h, int32_t nitems, const cair_work_i
   A.mask = tsize - 1;
   A.ring_rows = d_ring_rows;
   A.error = derr;
+  A.item_bmax = d_ibmax;
   if (nc == 3) k_stats_count<3><<<grid_for(h, ntot), 256, 0, st>>>(A);
   else k_stats_count<5><<<grid_for(h, ntot), 256, 0, st>>>(A);
   k_stats_compact<<<grid_for(h, (int64_t)tsize), 256, 0, st>>>(keys, counts, tsize, okeys, ocounts, tsize, dn);
@@ -1270,6 +1289,7 @@ int cair_statistics_counts_dev(cair_handle* h, int32_t nitems, const cair_work_i
   CUDA_TRY(h, cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(ring_rows, d_ring_rows, (size_t)nruns * kMaxRings * 8, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (err == 3) return fail(h, CAIR_EINVAL, kBmaxMismatch);
   if (err) return fail(h, CAIR_EINVAL, "cair_statistics_counts: a final-state key of -1 (not representable)");
   if ((int64_t)n > cap)
     return fail(h, CAIR_EINVAL, "cair_statistics_counts: cap too small, " + std::to_string(n) + " counts");

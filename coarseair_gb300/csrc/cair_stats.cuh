@@ -29,10 +29,13 @@ struct StatsArgs {
   unsigned long long* item_rows;  // counted rows of each item
   long long* item_inicode;        // smallest initial-state code of each item (IniStateCode(1))
   unsigned long long* ring_rows;  // rows of each (run, ring): TrajsPerb
-  int* error;                     // 1: a quantum number at or above qnmax; 2: an unrepresentable key
+  int* error;                     // 1: a quantum number at or above qnmax; 2: an unrepresentable key;
+                                  // 3: a counted row whose bmax is not its item's
+  const double* item_bmax;        // |bmax| of each work item (null: not checked)
 };
 
 constexpr unsigned long long kStatsEmpty = ~0ull;
+constexpr double kStatsBmaxTol = 1.0e-3;  // SetRings' tolerance for one ring (Statistics_Class.F90:534-545)
 
 // The NC conditions of a row, in trajectories.csv order: J, v, arr (3 atoms) or J1, v1, J2, v2, arr.
 template <int NC>
@@ -150,6 +153,12 @@ __global__ void __launch_bounds__(256) k_stats_count(StatsArgs A) {
     long long ic, fc;
     bool bad = false;
     stats_codes<NC>(A, r, ic, fc, bad);
+    // the rings are the items' |bmax|; SetRings takes them from the rows' bMax, which the queue
+    // copies from the items, so a row carrying another bmax cannot be ringed as the reference would
+    if (A.item_bmax && !(fabs(fabs(r.bmax) - A.item_bmax[r.item]) < kStatsBmaxTol)) {
+      atomicExch(A.error, 3);
+      continue;
+    }
     int run, ring;
     const unsigned long long key = stats_key(A, r, fc, run, ring);
     atomicAdd(A.ring_rows + (size_t)run * kMaxRings + ring, 1ull);

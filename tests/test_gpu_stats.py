@@ -90,11 +90,64 @@ def test_statistics_on_synthetic_rows(gpu_lib, oracle_lib):
     items = np.zeros(nitems, dtype=_lib.ITEM_DTYPE)
     items["bmax"] = 6.0
     items["ttra"] = [5000.0, 10000.0, 15000.0, 20000.0, 8000.0]
+    rows["bmax"] = items["bmax"][rows["item"]]      # a row carries its item's ring bound, as the queue writes it
     _compare(H, items, rows, (1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 0)))
     _compare(H, items, rows, (0, 0, 0), api.Statistics(H))
     # a table that cannot hold every final state is an error, not a truncation
     with pytest.raises(api.CairError, match="cap too small"):
         api.Statistics(H).compute(items, rows, cap=8)
+    H.close()
+
+
+def test_statistics_with_zero_bmax_are_probabilities(gpu_lib, oracle_lib):
+    """Rows whose bMax is 0 make one ring of area 0, which SetRings turns into area 1
+    (Statistics_Class.F90:578-581): the cross sections are the final states' probabilities, on the
+    device as in the oracle."""
+    cfg = systems.o3_config()
+    H = api.Handle(cfg)
+    rng = np.random.default_rng(22)
+    n, nitems = 20000, 2
+    rows = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    rows["item"] = rng.integers(0, nitems, n)
+    rows["j_i"] = 10.5
+    rows["v_i"] = 0.5 + rows["item"]
+    rows["arr_i"] = 16.5
+    rows["j_f"] = rng.uniform(0.0, 30.0, n)
+    rows["v_f"] = rng.uniform(-1.0, 6.0, n)
+    rows["arr_f"] = rng.choice([16.5, 32.5, 48.5], n)
+    rows["bmax"] = 0.0
+    rows["b"] = 0.0
+    items = np.zeros(nitems, dtype=_lib.ITEM_DTYPE)
+    items["bmax"] = 0.0
+    items["ttra"] = [10000.0, 20000.0]
+    got = _compare(H, items, rows, (0, 0, 0), api.Statistics(H))
+    assert np.all(got["nrings"] == 1)
+    for i in range(nitems):
+        g = got[got["run"] == i]
+        assert g["cross"].sum() == pytest.approx(1.0, rel=1e-12)
+        assert np.allclose(g["cross"], g["count"] / g["nrows"][0], rtol=1e-14, atol=0.0)
+    H.close()
+
+
+def test_statistics_refuse_rows_ringed_apart_from_their_item(gpu_lib):
+    """The device rings each run by its items' bmax.  A counted row whose bmax differs from its
+    item's by 1e-3 or more would be ringed differently by SetRings, which reads the rows' bMax, so
+    the statistics refuse it; a difference below SetRings' 1e-3 is one ring and is accepted."""
+    cfg = systems.o3_config()
+    H = api.Handle(cfg)
+    n = 1000
+    rows = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    rows["j_i"], rows["v_i"], rows["arr_i"] = 10.5, 0.5, 16.5
+    rows["j_f"], rows["v_f"], rows["arr_f"] = 12.5, 0.5, 16.5
+    rows["b"] = np.linspace(0.0, 6.0, n)
+    items = np.zeros(1, dtype=_lib.ITEM_DTYPE)
+    items["bmax"], items["ttra"] = 6.0, 10000.0
+    rows["bmax"] = 6.0 + 5e-4
+    got = api.Statistics(H).compute(items, rows)
+    assert got["count"].sum() == n
+    rows["bmax"][17] = 6.0 + 2e-3
+    with pytest.raises(api.CairError, match="bmax"):
+        api.Statistics(H).compute(items, rows)
     H.close()
 
 
@@ -127,6 +180,7 @@ def test_statistics_on_synthetic_diatom_diatom_rows(gpu_lib, oracle_lib):
     items = np.zeros(nitems, dtype=_lib.ITEM_DTYPE)
     items["bmax"] = 8.0
     items["ttra"] = [5000.0, 10000.0, 15000.0, 20000.0]
+    rows["bmax"] = items["bmax"][rows["item"]]
     got = _compare(H, items, rows, (1, 0, 1, 0, 0), api.Statistics(H, pres_even_odd=(1, 0, 1, 0, 0)))
     assert np.any(got["fin"][:, 4] < 0)
     _compare(H, items, rows, (0, 0, 0, 0, 0), api.Statistics(H))
