@@ -60,6 +60,16 @@ FINAL_STATE_DTYPE = np.dtype([("run", "i4"), ("fin", "i4", 5), ("ini", "i4", 5),
                               ("nrows", "i8"), ("cross", "f8"), ("cross_sd", "f8"), ("rate", "f8"),
                               ("rate_sd", "f8")])
 
+SUR_SAMPLE_DTYPE = np.dtype([("R", "f8", (3,)), ("e", "f4"), ("g", "f4", (3,))])
+SUR_NINV = 10
+
+
+class SurConsts(C.Structure):
+    _fields_ = [("mu", C.c_float * SUR_NINV), ("isd", C.c_float * SUR_NINV), ("fmin", C.c_float * SUR_NINV),
+                ("fmax", C.c_float * SUR_NINV), ("sigma_d", C.c_float), ("gate_ev", C.c_float),
+                ("gate_dmin", C.c_float)]
+
+
 LEVEL_DTYPE = np.dtype([("vqn", "i4"), ("jqn", "i4"), ("eint", "f8"), ("egam", "f8"), ("rmin", "f8"),
                         ("rmax", "f8"), ("vmin", "f8"), ("vmax", "f8"), ("tau", "f8"), ("ri", "f8"), ("ro", "f8")])
 ITEM_DTYPE = np.dtype([("ilevel", "i4"), ("ipes", "i4"), ("first", "i8"), ("ntraj", "i8"), ("seed", "i8"),
@@ -120,6 +130,24 @@ SIGNATURES = [
     ("cair_queue_graph_destroy", None, [_P]),
     ("cair_set_integrate_timing", C.c_int, [_P, C.c_int32]),
     ("cair_integrate_timings", C.c_int, [_P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_int32)]),
+    ("cair_sur_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int32]),
+    ("cair_sur_destroy", None, [_P]),
+    ("cair_sur_last_error", C.c_char_p, [_P]),
+    ("cair_sur_nparam", C.c_int, []),
+    ("cair_sur_set_consts", C.c_int, [_P, C.POINTER(SurConsts)]),
+    ("cair_sur_get_consts", C.c_int, [_P, C.POINTER(SurConsts)]),
+    ("cair_sur_set_params", C.c_int, [_P, C.c_int32, C.POINTER(C.c_float)]),
+    ("cair_sur_get_params", C.c_int, [_P, C.c_int32, C.POINTER(C.c_float)]),
+    ("cair_sur_eval_dev", C.c_int, [_P, C.c_int64, _P, _P, _P, _P, _P, _P, _P]),
+    ("cair_sur_grad_dev", C.c_int, [_P, C.c_int32, C.c_int64, _P, _P, C.c_float, C.c_float, _P]),
+    ("cair_sur_adam_dev", C.c_int, [_P, C.c_int32, C.c_float, _P]),
+    ("cair_sur_get_grad", C.c_int, [_P, C.c_int32, C.POINTER(C.c_float)]),
+    ("cair_sur_take_loss", C.c_int, [_P, _D, _P]),
+    ("cair_sur_counters", C.c_int, [_P, _L, C.c_int32]),
+    ("cair_sur_targets_dev", C.c_int, [_P, C.c_int64, _P, _P, _P]),
+    ("cair_sur_attach", C.c_int, [_P, _P]),
+    ("cair_record_samples", C.c_int, [_P, _P, C.c_int64, C.c_int32, C.c_double]),
+    ("cair_recorded_samples", C.c_int64, [_P]),
 ]
 
 _lib = None

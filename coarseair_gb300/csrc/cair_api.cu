@@ -21,6 +21,7 @@
 #include "cair_ic.cuh"
 #include "cair_launch.h"
 #include "cair_stats.cuh"
+#include "cair_sur_launch.h"
 
 using namespace cair;
 
@@ -47,6 +48,11 @@ struct cair_handle {
   bool time_integrate = false;              // bracket every integrator launch with events
   std::vector<cudaEvent_t> tev;             // pairs (start, end), reused across calls
   size_t ntev = 0;                          // pairs recorded since the last read
+  cair_surrogate* sur = nullptr;            // attached surrogate: integrator launches run on it
+  double* rec = nullptr;                    // geometry recorder of the FP64 integrator
+  unsigned long long* d_nrec = nullptr;
+  unsigned long long rec_cap = 0, rec_mod = 1;
+  double rec_rcut = 0.0;
 };
 
 namespace {
@@ -418,6 +424,8 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
   if (d->natoms != 3 && d->natoms != 4) return bad(CAIR_EINVAL, "natoms must be 3 or 4");
   if (d->npes < 1 || d->npes > CAIR_MAX_PES) return bad(CAIR_EINVAL, "npes out of range");
   if (d->nsteps < 2 || d->nsteps > 4) return bad(CAIR_EUNSUPPORTED, "Nb of extrapolation steps must be 2..4");
+  if (d->natoms == 4 && d->nsteps != 3)
+    return bad(CAIR_EUNSUPPORTED, "Nb of extrapolation steps 2 and 4 are built for diatom + atom surfaces only");
   if (d->ncall < 1) return bad(CAIR_EINVAL, "ncall must be >= 1");
   if (d->nquad < 1 || d->nquad > 256) return bad(CAIR_EINVAL, "nquad must be 1..256");
   for (int i = 0; i < d->natoms; ++i)
@@ -502,6 +510,7 @@ void cair_destroy(cair_handle* h) {
   if (h->d_work) cudaFree(h->d_work);
   if (h->d_ctl) cudaFree(h->d_ctl);
   if (h->d_stats) cudaFree(h->d_stats);
+  if (h->d_nrec) cudaFree(h->d_nrec);
   if (h->stream) cudaStreamDestroy(h->stream);
   for (cudaEvent_t e : h->tev) cudaEventDestroy(e);
   delete h;
@@ -594,7 +603,6 @@ int cair_bs_steps(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, d
   if (!h || n < 0 || !paq || !t || !dt || !erra || nattempts < 0)
     return fail(h, CAIR_EINVAL, "cair_bs_steps: bad argument");
   if (n == 0) return 0;
-  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_bs_steps: only NSteps = 3 is built");
   if (int e = check_ipes(h, n, ipes)) return e;
   const int ne = h->sys.ne;
   if (int e = ensure_scratch(h, n * (4 + (2 * ne + 2) * 8) + 2048)) return e;
@@ -616,11 +624,20 @@ int cair_bs_steps(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, d
   return wait_stream(h);
 }
 
-static int launch_integrate(cair_handle* h, const IntegrateArgs& A, cudaStream_t st) {
+static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_t st) {
+  IntegrateArgs A = A0;
+  if (h->rec && !h->sur) {
+    A.rec = h->rec;
+    A.nrec = h->d_nrec;
+    A.rec_cap = h->rec_cap;
+    A.rec_mod = h->rec_mod;
+    A.rec_rcut = h->rec_rcut;
+  }
   // 64-thread blocks: a block holding one long trajectory frees the rest of its SM for the
   // next batch on another stream
   int block = 64, per_sm = 0;
-  if (int e = with_model(h, [&](auto L) { per_sm = L.integrate_blocks_per_sm(block); })) return e;
+  if (!h->sur)
+    if (int e = with_model(h, [&](auto L) { per_sm = L.integrate_blocks_per_sm(block, h->sys.nsteps); })) return e;
   if (per_sm < 1) per_sm = 1;
   int64_t g = (int64_t)h->nsm * per_sm;
   int64_t need = (A.n + block - 1) / block;
@@ -640,7 +657,12 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A, cudaStream_t
     ++h->ntev;
     CUDA_TRY(h, cudaEventRecord(e0, st));
   }
-  if (int e = with_model(h, [&](auto L) { L.integrate((int)g, block, st, h->sys, A); })) return e;
+  if (h->sur) {
+    if (sur_integrate_launch(h->sur, h->nsm, st, h->sys, A))
+      return fail(h, CAIR_ECUDA, std::string("surrogate integrator launch: ") + cudaGetErrorString(cudaGetLastError()));
+  } else if (int e = with_model(h, [&](auto L) { L.integrate((int)g, block, st, h->sys, A); })) {
+    return e;
+  }
   if (e1) CUDA_TRY(h, cudaEventRecord(e1, st));
   return 0;
 }
@@ -652,7 +674,6 @@ int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* p
       max_attempts < 1)
     return fail(h, CAIR_EINVAL, "cair_integrate_dev: bad argument");
   if (n == 0) return 0;
-  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: only NSteps = 3 is built");
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
   IntegrateArgs A{n, ipes, paq, t, dt, erra, H, smax, smin, irej, iste, status, max_attempts, h->d_ctl,
@@ -667,7 +688,6 @@ int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, 
       max_attempts < 1)
     return fail(h, CAIR_EINVAL, "cair_integrate: bad argument");
   if (n == 0) return 0;
-  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_integrate: only NSteps = 3 is built");
   if (int e = check_ipes(h, n, ipes)) return e;
   const int ne = h->sys.ne;
   size_t bytes = n * (3 * sizeof(int32_t) + sizeof(int32_t) + sizeof(double) * (2 * ne + 5)) + 16 * 256;
@@ -706,6 +726,42 @@ int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, 
   if (int e = wait_stream(h)) return e;
   for (int i = 0; i < 5; ++i) h->last_counters[i] = (long long)ctr[i];
   return 0;
+}
+
+int cair_sur_attach(cair_handle* h, cair_surrogate* s) {
+  if (!h) return CAIR_EINVAL;
+  if (s && (h->sys.npes != 1 || h->sys.pes[0].model != CAIR_PES_N3_UMN || h->sys.nsteps != 3))
+    return fail(h, CAIR_EUNSUPPORTED, "cair_sur_attach: the surrogate is built for N3 UMN (one surface) with NSteps = 3");
+  h->sur = s;
+  return 0;
+}
+
+int cair_sur_targets_dev(cair_handle* h, int64_t n, const double* R, cair_sur_sample* out, void* stream) {
+  if (!h || n < 0 || (n > 0 && (!R || !out))) return fail(h, CAIR_EINVAL, "cair_sur_targets_dev: bad argument");
+  if (h->sys.pes[0].model != CAIR_PES_N3_UMN) return fail(h, CAIR_EUNSUPPORTED, "cair_sur_targets_dev: N3 UMN only");
+  if (n == 0) return 0;
+  if (sur_targets_launch(h->sys, h->nsm, (cudaStream_t)stream, n, R, out))
+    return fail(h, CAIR_ECUDA, std::string("cair_sur_targets_dev: ") + cudaGetErrorString(cudaGetLastError()));
+  return 0;
+}
+
+int cair_record_samples(cair_handle* h, double* rec_dev, int64_t cap, int32_t modulus, double rcut) {
+  if (!h || (rec_dev && (cap < 1 || modulus < 1))) return fail(h, CAIR_EINVAL, "cair_record_samples: bad argument");
+  if (rec_dev && h->sys.natoms != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_record_samples: three atoms only");
+  if (!h->d_nrec) CUDA_TRY(h, cudaMalloc(&h->d_nrec, sizeof(unsigned long long)));
+  CUDA_TRY(h, cudaMemset(h->d_nrec, 0, sizeof(unsigned long long)));
+  h->rec = rec_dev;
+  h->rec_cap = (unsigned long long)cap;
+  h->rec_mod = (unsigned long long)(modulus > 0 ? modulus : 1);
+  h->rec_rcut = rcut;
+  return 0;
+}
+
+int64_t cair_recorded_samples(cair_handle* h) {
+  if (!h || !h->d_nrec) return 0;
+  unsigned long long n = 0;
+  if (cudaMemcpy(&n, h->d_nrec, sizeof n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return (int64_t)n;
 }
 
 int cair_last_counters(cair_handle* h, int64_t* c5) {
@@ -864,7 +920,6 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
   if (!h || nlevels < 1 || nitems < 0 || ntot < 0 || !levels || !items || !results || max_attempts < 1)
     return fail(h, CAIR_EINVAL, "cair_run_queue_dev: bad argument");
   if (ntot == 0) return 0;
-  if (h->sys.nsteps != 3) return fail(h, CAIR_EUNSUPPORTED, "cair_run_queue: only NSteps = 3 is built");
   if (workspace && ((uintptr_t)workspace & 255)) return fail(h, CAIR_EINVAL, "workspace must be 256-byte aligned");
   BatchBufs B;
   if (workspace) carve_into((char*)workspace, ntot, h->sys.ne, B);

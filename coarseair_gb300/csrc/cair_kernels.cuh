@@ -112,7 +112,22 @@ struct IntegrateArgs {
   unsigned long long* queue;    // next queue position
   unsigned long long* counters; // attempts, accepted, rejected, grad evals, energy evals
   const int32_t* order;         // queue position -> trajectory (NULL: identity)
+  // geometry recorder (cair_record_samples; NULL: off): pair distances at end checks
+  double* rec;
+  unsigned long long* nrec;
+  unsigned long long rec_cap;
+  unsigned long long rec_mod;
+  double rec_rcut;
 };
+
+// Keep one in `mod` end checks, by a hash of trajectory and attempt count (splitmix64 finaliser).
+__device__ __forceinline__ bool rec_pick(unsigned long long k, long long att, unsigned long long mod) {
+  unsigned long long z = k * 0x9E3779B97F4A7C15ull + (unsigned long long)att;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return z % mod == 0;
+}
 
 // Minimum resident 64-thread blocks per SM the register allocation must allow (1: up to 255
 // registers per thread, 4 blocks fit; 6: at most 168 registers, more warps to hide FP64 latency).
@@ -164,6 +179,20 @@ __global__ void __launch_bounds__(64, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(Dev
       bool conv = x > S.tmax;
 #pragma unroll
       for (int p = 0; p < NP; ++p) conv = conv || (rpi[p] < S.rpimax);
+      if constexpr (NP == 3) {
+        if (A.rec) {
+          const double r0 = 1.0 / rpi[0], r1 = 1.0 / rpi[1], r2 = 1.0 / rpi[2];
+          const double mid = fmax(fmin(r0, r1), fmin(fmax(r0, r1), r2));
+          if (mid < A.rec_rcut && rec_pick(k, att, A.rec_mod)) {
+            const unsigned long long slot = atomicAdd(A.nrec, 1ull);
+            if (slot < A.rec_cap) {
+              A.rec[3 * slot] = r0;
+              A.rec[3 * slot + 1] = r1;
+              A.rec[3 * slot + 2] = r2;
+            }
+          }
+        }
+      }
       if (bad || conv || att >= A.max_attempts) {
 #pragma unroll
         for (int i = 0; i < NE; ++i) A.paq[NE * k + i] = y[i];

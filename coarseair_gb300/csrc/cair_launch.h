@@ -22,7 +22,7 @@ struct ModelLaunch {
                           const double* paq, double* H, double* Rpi);
   static void bs_steps(int grid, cudaStream_t st, const DevSys& S, int64_t n, const int32_t* ipes, double* paq,
                        double* t, double* dt, const double* erra, int32_t nattempts);
-  static int integrate_blocks_per_sm(int block);
+  static int integrate_blocks_per_sm(int block, int nsteps);
   static void integrate(int grid, int block, cudaStream_t st, const DevSys& S, const IntegrateArgs& A);
   static void sample_ic(int grid, cudaStream_t st, const DevSys& S, int64_t ntot, const cair_work_item* items,
                         const cair_level* levels, const double* draws, const int32_t* item_of, double* paq,

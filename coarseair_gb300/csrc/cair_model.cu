@@ -29,21 +29,40 @@ void ModelLaunch<MODEL>::hamiltonian(int grid, cudaStream_t st, const DevSys& S,
   k_hamiltonian<MODEL><<<grid, 128, 0, st>>>(S, n, ipes, paq, H, Rpi);
 }
 
+// NSteps ("Nb of extrapolation steps") 2..4 are built for the three-atom surfaces; the four-atom
+// surfaces, whose integrator kernels are the largest to compile, have NSteps = 3 only
+// (cair_create refuses the others for them).
+template <int MODEL>
+constexpr bool kAllNSteps = Traits<MODEL>::NA == 3;
+
 template <int MODEL>
 void ModelLaunch<MODEL>::bs_steps(int grid, cudaStream_t st, const DevSys& S, int64_t n, const int32_t* ipes,
                                   double* paq, double* t, double* dt, const double* erra, int32_t nattempts) {
+  if constexpr (kAllNSteps<MODEL>) {
+    if (S.nsteps == 2) return (void)(k_bs_steps<MODEL, 2><<<grid, 128, 0, st>>>(S, n, ipes, paq, t, dt, erra, nattempts));
+    if (S.nsteps == 4) return (void)(k_bs_steps<MODEL, 4><<<grid, 128, 0, st>>>(S, n, ipes, paq, t, dt, erra, nattempts));
+  }
   k_bs_steps<MODEL, 3><<<grid, 128, 0, st>>>(S, n, ipes, paq, t, dt, erra, nattempts);
 }
 
 template <int MODEL>
-int ModelLaunch<MODEL>::integrate_blocks_per_sm(int block) {
+int ModelLaunch<MODEL>::integrate_blocks_per_sm(int block, int nsteps) {
   int per_sm = 0;
+  if constexpr (kAllNSteps<MODEL>) {
+    if (nsteps == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate<MODEL, 2>, block, 0);
+    else if (nsteps == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate<MODEL, 4>, block, 0);
+    if (nsteps != 3) return per_sm;
+  }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate<MODEL, 3>, block, 0);
   return per_sm;
 }
 
 template <int MODEL>
 void ModelLaunch<MODEL>::integrate(int grid, int block, cudaStream_t st, const DevSys& S, const IntegrateArgs& A) {
+  if constexpr (kAllNSteps<MODEL>) {
+    if (S.nsteps == 2) return (void)(k_integrate<MODEL, 2><<<grid, block, 0, st>>>(S, A));
+    if (S.nsteps == 4) return (void)(k_integrate<MODEL, 4><<<grid, block, 0, st>>>(S, A));
+  }
   k_integrate<MODEL, 3><<<grid, block, 0, st>>>(S, A);
 }
 

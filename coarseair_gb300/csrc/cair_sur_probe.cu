@@ -1,0 +1,114 @@
+// Self-test of the tensor-core operand conventions (cair_tc.cuh): one 128 x N x 16 BF16 MMA with
+// FP32 accumulation in TMEM, its operands staged by the CTA's threads in the canonical no-swizzle
+// layouts, B either K-major or MN-major.  The descriptor's two byte offsets are arguments, so a
+// test can check which of the two assignments (K stride, M/N stride) the hardware reads.  Offsets
+// are at most 2048 B and each operand region is 40 KB: 16 core matrices at any such offset plus one
+// more stay inside the region, so no assignment reads outside the CTA's shared memory.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/cair_gpu.h"
+#include "cair_tc.cuh"
+
+namespace {
+
+using namespace cair;
+
+constexpr int kRegion = 40960;
+
+__global__ void __launch_bounds__(128) k_tc_probe(const __nv_bfloat16* __restrict__ A,
+                                                  const __nv_bfloat16* __restrict__ B, int N, int b_mn,
+                                                  uint32_t a_lbo, uint32_t a_sbo, uint32_t b_lbo, uint32_t b_sbo,
+                                                  float* __restrict__ D, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* sa = sm;
+  unsigned char* sb = sm + kRegion;
+  uint64_t* bar = (uint64_t*)(sm + 2 * kRegion);
+  uint32_t* tslot = (uint32_t*)(sm + 2 * kRegion + 16);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < 2 * kRegion / 16; i += 128) ((uint4*)sm)[i] = make_uint4(0, 0, 0, 0);
+  __syncthreads();
+  // A[128][16] K-major: core (r/8, k/8) at (k/8)*2048 + (r/8)*128
+  for (int r = tid; r < 128; r += 128)
+    for (int k = 0; k < 16; ++k) *(__nv_bfloat16*)(sa + tc::kmaj_off(r, k, 128)) = A[r * 16 + k];
+  // B[N][16]: K-major core (n/8, k/8) at (k/8)*N*16 + (n/8)*128, rows of 8 k;
+  //           MN-major core (n/8, k/8) at (n/8)*256 + (k/8)*128, rows of 8 n (one row per k)
+  for (int n = tid; n < N; n += 128)
+    for (int k = 0; k < 16; ++k) {
+      const uint32_t off = b_mn ? (uint32_t)((n >> 3) * 256 + (k >> 3) * 128 + (k & 7) * 16 + (n & 7) * 2)
+                                : tc::kmaj_off(n, k, N);
+      *(__nv_bfloat16*)(sb + off) = B[n * 16 + k];
+    }
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 128);
+    tc::tmem_relinquish();
+  }
+  tc::fence_smem_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  if (tid == 0) {
+    const uint64_t ad = tc::sdesc(tc::smem_u32(sa), a_lbo, a_sbo);
+    const uint64_t bd = tc::sdesc(tc::smem_u32(sb), b_lbo, b_sbo);
+    tc::mma_bf16(tmem, ad, bd, tc::idesc_bf16(128, N, b_mn != 0), 0u);
+    tc::mma_commit(bar);
+  }
+  const bool ok = tc::mbar_wait(bar, 0);
+  tc::fence_after_sync();
+  if (!ok) atomicExch(err, 1);
+  if (__syncthreads_or(!ok) == 0) {
+    for (int c = 0; c < N; c += 16) {
+      float v[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) D[tid * N + c + i] = v[i];
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 128);
+}
+
+}  // namespace
+
+// Internal (not in include/cair_gpu.h): D[128][N] = A[128][16] x B[N][16]^T through one tcgen05.mma,
+// with the given descriptor offsets.  N is 16 or 128.  Returns 0, CAIR_EINVAL, CAIR_ECUDA, or
+// CAIR_ETIMEOUT if the completion wait ran out.
+extern "C" int cair_internal_tc_probe(const void* A, const void* B, int N, int b_mn, uint32_t a_lbo, uint32_t a_sbo,
+                                      uint32_t b_lbo, uint32_t b_sbo, float* D) {
+  if (!A || !B || !D || (N != 16 && N != 128) || a_lbo > 2048 || a_sbo > 2048 || b_lbo > 2048 || b_sbo > 2048)
+    return CAIR_EINVAL;
+  __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+  float* dD = nullptr;
+  int* dErr = nullptr;
+  int rc = CAIR_OK;
+  const size_t smem = 2 * kRegion + 64;
+  if (cudaMalloc(&dA, 128 * 16 * 2) != cudaSuccess || cudaMalloc(&dB, (size_t)N * 16 * 2) != cudaSuccess ||
+      cudaMalloc(&dD, (size_t)128 * N * 4) != cudaSuccess || cudaMalloc(&dErr, 4) != cudaSuccess) {
+    rc = CAIR_ECUDA;
+  } else {
+    cudaMemcpy(dA, A, 128 * 16 * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(dB, B, (size_t)N * 16 * 2, cudaMemcpyHostToDevice);
+    cudaMemset(dErr, 0, 4);
+    cudaFuncSetAttribute(k_tc_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_tc_probe<<<1, 128, smem>>>(dA, dB, N, b_mn, a_lbo, a_sbo, b_lbo, b_sbo, dD, dErr);
+    int e = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = CAIR_ECUDA;
+    else {
+      cudaMemcpy(&e, dErr, 4, cudaMemcpyDeviceToHost);
+      if (e) rc = CAIR_ETIMEOUT;
+      else cudaMemcpy(D, dD, (size_t)128 * N * 4, cudaMemcpyDeviceToHost);
+    }
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dD);
+  cudaFree(dErr);
+  return rc;
+}

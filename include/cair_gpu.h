@@ -455,8 +455,81 @@ int cair_set_integrate_timing(cair_handle* h, int32_t on);
 int cair_integrate_timings(cair_handle* h, float* ms, int32_t cap, int32_t* count);
 
 /* Device counters of the last cair_integrate*: total BS attempts, accepted, rejected,
- * PES gradient evaluations, PES energy evaluations. */
+ * PES gradient evaluations, PES energy evaluations.  Calls of cair_run_queue_dev with a caller
+ * workspace (and cair_run_queue_static_dev) keep their counters in that workspace and leave these
+ * unchanged. */
 int cair_last_counters(cair_handle* h, int64_t* counters5);
+
+/* ---------------------------------------------------------------------------------------------
+ * Learned surrogate of the N3 UMN three-body term (no counterpart in the reference: the reference
+ * has no learned surface on this path; its analogue of the dense layers is
+ * O3_NN_PES_Class.F90:357-477).  The N3 UMN surface is sum_i V_N2(R_i) + (457.4 + sum C_k B_k(x))
+ * kcal/mol (N3_UMN_PES_Class.F90:332-382); its polynomial part minus 457.4, V3, vanishes in every
+ * asymptotic channel.  The surrogate keeps the FP64 diatomics and models V3 as D(x) y(f):
+ *   x_i = exp(-d_i - d_i^2/1.5) (d_i = R_i in angstrom - 1.098) the surface's own MEG variables;
+ *   f = the ten S3-orbit sums of x of degree 1..4, normalised ((raw - mu) isd), 5 zeros, 1;
+ *   y = a 16 -> 128 -> 128 -> 128 -> 1 tanh network [eV], BF16 hidden weights, FP32 output layer;
+ *   D = 1 - exp(-(x1 x2 + x1 x3 + x2 x3) / sigma_d), so V3_s = 0 exactly where V3 = 0.
+ * Hidden layers run as tcgen05 BF16 MMAs with FP32 accumulation in tensor memory, each activation
+ * split exactly into three BF16 parts (FP32-accurate products).  Two ensemble members (0 = A, the
+ * one that drives the dynamics; 1 = B) are trained from different starts; an attempt whose start
+ * has |D (yA - yB)| > gate_ev, or a feature outside [fmin, fmax] where D > gate_dmin, runs on the
+ * FP64 surface instead.  Parameters: cair_sur_nparam() floats per member, in the order W1[128][16]
+ * (column 15 is the first layer's bias), W2[128][128], W3[128][128] (row = output), b2, b3, w4
+ * [128], b4. */
+typedef struct cair_sur_sample {
+  double R[3];   /* pair distances [bohr] */
+  float e;       /* V3 [eV] */
+  float g[3];    /* dV3/dR_i [eV/bohr] */
+} cair_sur_sample;
+typedef struct cair_sur_consts {
+  float mu[10], isd[10];    /* feature normalisation */
+  float fmin[10], fmax[10]; /* normalised feature range of the training set */
+  float sigma_d;            /* damping scale */
+  float gate_ev;            /* ensemble gate [eV] (1 meV = 1e-3) */
+  float gate_dmin;          /* the range gate applies where D exceeds this */
+} cair_sur_consts;
+typedef struct cair_surrogate cair_surrogate;
+int cair_sur_create(cair_surrogate** s, int32_t device);   /* CAIR_EUNSUPPORTED off sm_103 */
+void cair_sur_destroy(cair_surrogate* s);
+const char* cair_sur_last_error(const cair_surrogate* s);
+int cair_sur_nparam(void);
+int cair_sur_set_consts(cair_surrogate* s, const cair_sur_consts* c);
+int cair_sur_get_consts(const cair_surrogate* s, cair_sur_consts* c);
+/* Host parameters of one member; set also resets its Adam state. */
+int cair_sur_set_params(cair_surrogate* s, int32_t member, const float* params);
+int cair_sur_get_params(cair_surrogate* s, int32_t member, float* params);
+/* Device pointers: at n geometries R[n][3], both members' y [eV], member A's dy/df g[n][16], and
+ * the surrogate's V3 [Eh] and dV3/dR [n][3] [Eh/bohr].  Synchronises `stream`. */
+int cair_sur_eval_dev(cair_surrogate* s, int64_t n, const double* R, float* ya, float* yb, float* g, double* v3,
+                      double* dv3, void* stream);
+/* Training, device pointers: adds to the member's gradient the parameter gradient of
+ * (w_e (D y - e)^2 + w_f |d(D y)/dR - g|^2) averaged over samples[idx[0..nbatch)]; the loss parts
+ * accumulate until cair_sur_take_loss.  cair_sur_adam_dev applies one Adam step (beta 0.9, 0.999,
+ * eps 1e-8) with learning rate lr and clears the gradient.  cair_sur_get_grad copies the gradient
+ * to the host (synchronising). */
+int cair_sur_grad_dev(cair_surrogate* s, int32_t member, int64_t nbatch, const cair_sur_sample* samples,
+                      const int64_t* idx, float w_e, float w_f, void* stream);
+int cair_sur_adam_dev(cair_surrogate* s, int32_t member, float lr, void* stream);
+int cair_sur_get_grad(cair_surrogate* s, int32_t member, float* grad);
+int cair_sur_take_loss(cair_surrogate* s, double* loss2, void* stream);
+/* Gate counters since the last reset: attempts on the FP64 surface, on the surrogate, range-gated,
+ * ensemble-gated. */
+int cair_sur_counters(cair_surrogate* s, int64_t* counters4, int32_t reset);
+/* Training targets from the handle's FP64 N3 surface at n geometries (device pointers). */
+int cair_sur_targets_dev(cair_handle* h, int64_t n, const double* R, cair_sur_sample* out, void* stream);
+/* Every integrator launch of the handle (cair_integrate*, cair_run_queue*, graphs captured after the
+ * call) runs on the surrogate s; NULL restores the FP64 surface.  The handle must be N3 UMN with
+ * NSteps = 3; s must outlive its use. */
+int cair_sur_attach(cair_handle* h, cair_surrogate* s);
+/* Geometry recorder of the FP64 integrator (the training set along the method's own trajectories):
+ * at every end check of a trajectory whose middle pair distance is below rcut [bohr], with
+ * probability 1/modulus (a hash of trajectory and attempt count), its three pair distances are
+ * appended to rec_dev[cap][3] (device).  rec_dev NULL stops recording.  cair_recorded_samples
+ * returns the number appended since the recorder was set (it may exceed cap; the excess is
+ * dropped). */
+int cair_record_samples(cair_handle* h, double* rec_dev, int64_t cap, int32_t modulus, double rcut);
+int64_t cair_recorded_samples(cair_handle* h);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,7 @@ LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 10), "O3NN": ("O2", 0, 1), "O3BNN"
 # forces (Compute), so H is not conserved along their trajectories (O3_NN_PES_Class.F90:250-297 vs
 # 357-477; BNN_PES_Class.F90:395-442 vs 565-640)
 CONSERVES_H = {"O3": True, "N3": True, "O3NN": False, "O3BNN": False}
-NAMES = ["O3", "N3", "O3NN"]   # O3BNN runs these checks from test_zzz_strata_and_bnn
+NAMES = ["O3", "N3", "O3NN"]   # O3BNN runs these checks from test_zy_strata_and_bnn
 
 
 def _setup(name, **kw):
@@ -199,7 +199,7 @@ def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
     GPU must agree on >= 99.5 % of the trajectories whose oracle outcome is stable under that
     perturbation, and overall no worse than the oracle's own reproducibility minus 1 %."""
     cfg, o, H = _setup(name)
-    n = 400
+    n = 160 if name == "O3NN" else 400  # the O3 NN oracle is the slowest surface on the CPU
     ic = _ics(o, name, n)
     ref = o.integrate(ic["paq"], ic["erra"], procs=PROCS)
     pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"], procs=PROCS)
@@ -239,3 +239,34 @@ def test_attempt_cap_and_errors(gpu_lib, oracle_lib):
     # empty batch is a no-op
     empty = api.Trajectories.start(np.zeros((0, 12)), np.zeros((0, 12)), cfg.dt0)
     api.Integrator(H).Integrate(empty)
+
+
+@pytest.mark.parametrize("nsteps", [2, 4])
+def test_other_extrapolation_step_counts(gpu_lib, oracle_lib, nsteps):
+    """"Nb of extrapolation steps" 2 and 4 (ODE_Solver.F90:225-358 is generic in NSteps) on N3:
+    1000 fixed attempts to 1e-9 on non-chaotic trajectories, whole collisions with final (v, J,
+    arrangement) equal on every oracle-stable trajectory, and 1 + sum(nseq) right-hand sides per
+    attempt in the device counters."""
+    cfg, o, H = _setup("N3", nsteps=nsteps)
+    ic = _ics(o, "N3", 24)
+    ok, a_o = _non_chaotic(o, ic, 1000)
+    assert ok.sum() >= 4
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.ODE(H).Integrate(tr, 1000)
+    rel = np.abs(tr.paq - a_o).max(axis=1) / np.abs(a_o).max(axis=1)
+    assert np.all(rel[ok] < 1e-9), rel[ok]
+    ic = _ics(o, "N3", 64, seed=4321)
+    ref = o.integrate(ic["paq"], ic["erra"], procs=PROCS)
+    pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"], procs=PROCS)
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.Integrator(H).Integrate(tr)
+    assert np.all(tr.status == 0) and np.max(np.abs(tr.H - ic["H0"])) < cfg.ham_abs_tol
+    Jo, vo, ao = _final_qn(o.analyze(o.apply_transformation(ref["paq"])))
+    Jp, vp, ap = _final_qn(o.analyze(o.apply_transformation(pert["paq"])))
+    Jg, vg, ag = _gpu_final_qn(api.MolecularState(H).FindState(api.Collision(H).ApplyTransformation(tr.paq)))
+    stable = (Jo == Jp) & (vo == vp) & (ao == ap)
+    assert stable.sum() >= 48
+    assert np.all(((Jo == Jg) & (vo == vg) & (ao == ag))[stable])
+    c = H.counters()
+    nseq = {2: 1 + 2 + 4, 4: 1 + 2 + 4 + 6 + 8}[nsteps]
+    assert c["grad_evals"] == nseq * c["attempts"]

@@ -1,0 +1,133 @@
+"""The learned surrogate end to end on the GPU (N2 + N, N3 UMN):
+
+1. geometries recorded along FP64 trajectories of the method itself (16 N2 levels, 10,000 K),
+2. FP64 three-body targets there,
+3. both ensemble members trained by the library's tensor-core training kernels and Adam,
+4. a fresh queue of trajectories run once on the FP64 surface and once on the surrogate with its
+   per-attempt gate, judged as the plain method judges it: per-trajectory energy drift |dE| against
+   the FP64 surface (median at most 1e-4 eV), and every final state's rate within twice the combined
+   Monte-Carlo standard deviation of the FP64 run's.
+
+Collected after the other GPU test files, before the allocation-free entry point's."""
+import time
+
+import numpy as np
+import pytest
+
+from coarseair_gb300 import api, surrogate, systems
+
+pytestmark = pytest.mark.gpu
+
+EV = 27.211386245988
+
+
+def _setup():
+    cfg = systems.n3_config(dinit=15.0, bmax=7.0, rmax=16.0, tmax=4.0e5)
+    lv = systems.load_levels("N2")
+    rng = np.random.default_rng(2)
+    pick = np.sort(rng.choice(len(lv), 16, replace=False))
+    return cfg, api.level_table(lv[pick])
+
+
+@pytest.fixture(scope="module")
+def trained(gpu_lib):
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    cfg, table = _setup()
+    H = api.Handle(cfg)
+    items = api.work_items([(il, 0, 600, api.process_seed(4, il + 1), 10000.0, 7.0, 15.0) for il in range(16)])
+    t0 = time.time()
+    R, _ = surrogate.record_training_set(H, table, items, cap=3_000_000, modulus=1, rcut=9.0)
+    smp = surrogate.targets(H, R)
+    torch.cuda.synchronize()
+    t_data = time.time() - t0
+    n = R.shape[0]
+    perm = torch.randperm(n, generator=torch.Generator(device="cuda").manual_seed(7), device="cuda")
+    ntr = int(0.9 * n)
+    itemsize = smp.numel() // n
+    rows = smp.view(n, itemsize)
+    train = rows[perm[:ntr]].reshape(-1).contiguous()
+    held = rows[perm[ntr:]].reshape(-1).contiguous()
+    S = surrogate.Surrogate()
+    mu, isd, lo, hi = S.fit_normalisation(R[perm[:ntr]].cpu().numpy())
+    S.set_consts(mu, isd, lo, hi)
+    t0 = time.time()
+    curves = S.train(train, epochs=12, batch=8192, lr0=2e-3, lr1=5e-5, w_e=1.0, w_f=1.0)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    print("surrogate: %d recorded geometries (%.1f s), trained %d steps x 2 members in %.1f s" %
+          (n, t_data, 12 * (ntr // 8192), t_train))
+    for ep, c in enumerate(curves):
+        print("  epoch %2d  loss A (E, F) = %.3e %.3e   B = %.3e %.3e" % (ep, c[0][0], c[0][1], c[1][0], c[1][1]))
+    yield dict(H=H, S=S, cfg=cfg, table=table, held=held, curves=curves)
+    S.detach(H)
+    S.close()
+    H.close()
+
+
+def test_training_converges_and_fits_held_out_geometries(trained):
+    S, curves = trained["S"], trained["curves"]
+    for m in (0, 1):
+        assert curves[-1][m].sum() < 0.05 * curves[0][m].sum()
+    held = surrogate.samples_numpy(trained["held"])
+    ya, yb, g, v3, dv3 = S.eval(held["R"])
+    err = np.abs(v3 * EV - held["e"])
+    ferr = np.abs(dv3 * EV - held["g"]).max(1)
+    dis = np.abs(ya - yb)
+    print("held-out: |dV3| median %.2e p90 %.2e max %.2e eV; |dV3/dR| median %.2e p90 %.2e eV/bohr; "
+          "|yA - yB| median %.2e eV; V3 range %.2f..%.2f eV" %
+          (np.median(err), np.quantile(err, 0.9), err.max(), np.median(ferr), np.quantile(ferr, 0.9), np.median(dis),
+           held["e"].min(), held["e"].max()))
+    assert np.median(err) < 0.05
+
+
+def test_surrogate_queue_conserves_energy_and_reproduces_rates(trained):
+    torch = pytest.importorskip("torch")
+    H, S, cfg, table = trained["H"], trained["S"], trained["cfg"], trained["table"]
+    items = api.work_items([(il, 0, 250, api.process_seed(8, il + 1), 10000.0, 7.0, 15.0) for il in range(16)])
+    S.detach(H)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    plain = api.RunTrajectories(H).run(table, items)
+    t_plain = time.time() - t0
+    c_plain = H.counters()
+    S.attach(H)
+    S.counters(reset=True)
+    t0 = time.time()
+    sur = api.RunTrajectories(H).run(table, items)
+    t_sur = time.time() - t0
+    c_sur = H.counters()
+    gate = S.counters()
+    S.detach(H)
+    n = len(items) * 250
+    assert np.all(plain["status"] == 0) and np.all(sur["status"] == 0)
+    de = np.abs(sur["dH"]) * EV
+    de_plain = np.abs(plain["dH"]) * EV
+    fb = gate["fp64"] / max(1, gate["fp64"] + gate["surrogate"])
+    print("surrogate queue: %d trajectories, plain %.1f s (%d attempts), surrogate %.1f s (%d attempts), "
+          "attempts on FP64 %.3f (range %d, ensemble %d)" %
+          (n, t_plain, c_plain["attempts"], t_sur, c_sur["attempts"], fb, gate["range_gated"], gate["ensemble_gated"]))
+    print("|dE| surrogate: median %.2e p90 %.2e max %.2e eV; plain median %.2e eV" %
+          (np.median(de), np.quantile(de, 0.9), de.max(), np.median(de_plain)))
+    assert np.median(de) <= 1e-4
+    # rates of every final state within 2 sigma of the FP64 run's
+    st = api.Statistics(H, pres_even_odd=(1, 0, 0))
+    runs = np.zeros(len(items), dtype=np.int32)   # one level run per item: compare per item
+    got = {}
+    for name, rows in (("plain", plain), ("sur", sur)):
+        res = st.compute(items, rows)
+        got[name] = {(int(r["run"]),) + tuple(int(x) for x in r["fin"][:3]): (r["rate"], r["rate_sd"]) for r in res}
+    worst, nbig = 0.0, 0
+    for k in set(got["plain"]) | set(got["sur"]):
+        kp, sp = got["plain"].get(k, (0.0, 0.0))
+        ks, ss = got["sur"].get(k, (0.0, 0.0))
+        sig = np.hypot(sp, ss)
+        if sig > 0:
+            z = abs(kp - ks) / sig
+            worst = max(worst, z)
+            nbig += z > 2.0
+    nstates = len(set(got["plain"]) | set(got["sur"]))
+    print("rates: %d (item, final state) pairs, worst |dk|/sigma %.2f, %d beyond 2 sigma" % (nstates, worst, nbig))
+    # with this many final states a few beyond 2 sigma are expected by chance (about 5 %)
+    assert nbig <= max(2, int(0.1 * nstates))
+    del runs
