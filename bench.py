@@ -42,7 +42,7 @@ DRAM_BYTES_PER_TRAJ = 703.0
 TEMPS = (5000.0, 10000.0, 20000.0)
 
 
-def workload(ntraj, rank=0, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=15.0):
+def workload(ntraj, rank=0, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=15.0, temps=TEMPS):
     """Level table and work items of the N2 + N configuration.  Replica `rank` draws its streams as
     processes rank * nitems + 1 ... of the run (Collision_Class.F90:295-296), so replicas never repeat
     each other's trajectories."""
@@ -51,12 +51,12 @@ def workload(ntraj, rank=0, seed_levels=2, nlevels=64, iseed=2, bmax=7.0, dinit=
     rng = np.random.default_rng(seed_levels)
     pick = np.sort(rng.choice(len(lv), nlevels, replace=False))
     table = api.level_table(lv[pick])
-    nitems = nlevels * len(TEMPS)
+    nitems = nlevels * len(temps)
     base, extra = divmod(ntraj, nitems)
     entries = []
     for il in range(nlevels):
-        for it, T in enumerate(TEMPS):
-            k = il * len(TEMPS) + it
+        for it, T in enumerate(temps):
+            k = il * len(temps) + it
             n = base + (1 if k < extra else 0)
             entries.append((il, 0, n, api.process_seed(iseed, rank * nitems + k + 1), T, bmax, dinit))
     return table, api.work_items(entries)
@@ -258,6 +258,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--clocks-csv", default=None, help="keep the nvidia-smi clock samples of the timed region here")
+    ap.add_argument("--surrogate", default="on", choices=["on", "off", "only"],
+                    help="the learned-surrogate arm (N2 + N): trained on the GPU, then timed on the same queue")
+    ap.add_argument("--sur-train-ntraj", type=int, default=200000,
+                    help="FP64 trajectories at 10,000 K whose end-check geometries form the training set")
+    ap.add_argument("--sur-cap", type=int, default=20000000, help="training geometries kept")
+    ap.add_argument("--sur-epochs", type=int, default=30)
+    ap.add_argument("--sur-steps", type=int, default=1, help="timed surrogate steps")
     args = ap.parse_args()
     spec = SYSTEMS[args.system]
     if args.ntraj is None:
@@ -336,6 +343,12 @@ def main():
                                        args.max_attempts, res_bufs[j].data_ptr(), aligned(ws[j]),
                                        streams[j].cuda_stream), "cair_run_queue_dev")
 
+    if args.surrogate == "only":
+        # the surrogate arm alone (a profiling command): no plain timing, no rate comparison
+        out = surrogate_arm(args, H, table, items, None, rank)
+        if rank == 0:
+            print(json.dumps({"surrogate": out}))
+        return
     for i in range(args.warmup):
         step(i)
     torch.cuda.synchronize()
@@ -417,6 +430,10 @@ def main():
             "converged_fraction": float(np.mean(res["status"] == 0)),
             "energy_not_conserved_fraction": float(np.mean(np.abs(res["dH"]) > cfg.ham_abs_tol))}
     line.update(outcome_summary(res, cfg.ncall))
+    if args.surrogate == "on" and args.system == "n3":
+        sur = surrogate_arm(args, H, table, items, res, rank)
+        sur["vs_plain"]["throughput_ratio"] = sur["value"] / value
+        line["surrogate"] = sur
     if e2e:
         line["e2e"] = e2e
     if cpu:
@@ -428,6 +445,95 @@ def main():
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+EV_PER_EH = 27.211386245988
+
+
+def surrogate_arm(args, H, table, items, plain_res, rank):
+    """The learned surrogate on the N2 + N queue.  Training set: the end-check geometries of
+    args.sur_train_ntraj FP64 trajectories at 10,000 K over the same 64 levels (streams of seed 4),
+    with FP64 three-body targets; both ensemble members trained on the GPU.  Then args.sur_steps
+    timed steps of the same queue as the plain arm with the surrogate attached (device-resident
+    inputs, CUDA events), judged against the plain arm's rows: per-trajectory energy drift on the FP64
+    surface, the attempts the gate sent to FP64, and every final state's rate within 2 sigma."""
+    import torch
+    from coarseair_gb300 import _lib, api, surrogate
+    lib = H.lib
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ttab, titems = workload(args.sur_train_ntraj, rank, iseed=4, temps=(10000.0,))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    R, _ = surrogate.record_training_set(H, ttab, titems, cap=args.sur_cap, modulus=1, rcut=9.0,
+                                         max_attempts=args.max_attempts)
+    smp = surrogate.targets(H, R)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    S = surrogate.Surrogate()
+    sub = R[torch.randperm(R.shape[0], device=R.device)[:min(R.shape[0], 2000000)]].cpu().numpy()
+    mu, isd, lo, hi = S.fit_normalisation(sub)
+    S.set_consts(mu, isd, lo, hi)
+    t0 = time.perf_counter()
+    curves = S.train(smp, epochs=args.sur_epochs, batch=16384, lr0=2e-3, lr1=2e-5)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del smp
+    n = int(items["ntraj"].sum())
+    d_lv = torch.from_numpy(table.view(np.uint8).copy()).to(dev)
+    d_it = torch.from_numpy(items.view(np.uint8).copy()).to(dev)
+    ws = torch.empty(int(lib.cair_queue_workspace_bytes(n)) + 256, dtype=torch.uint8, device=dev)
+    res_buf = torch.empty(n * _lib.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    st = torch.cuda.Stream(device=dev)
+    S.attach(H)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    S.counters(reset=True)
+    torch.cuda.synchronize()
+    ev0.record(st)
+    for _ in range(args.sur_steps):
+        H.check(lib.cair_run_queue_dev(H.h, len(table), d_lv.data_ptr(), len(items), d_it.data_ptr(), n,
+                                       args.max_attempts, res_buf.data_ptr(), (ws.data_ptr() + 255) & ~255,
+                                       st.cuda_stream), "cair_run_queue_dev (surrogate)")
+    ev1.record(st)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.sur_steps
+    gate = S.counters()
+    S.detach(H)
+    rows = np.frombuffer(res_buf.cpu().numpy().tobytes(), dtype=_lib.RESULT_DTYPE)
+    de = np.abs(rows["dH"]) * EV_PER_EH
+    att = rows["iste"].astype(np.int64) + rows["irej"]
+    out = {"value": n / (ms / 1e3), "unit": "trajectories/s", "steps": args.sur_steps, "ms_per_step": ms,
+           "attempts_per_trajectory": float(att.mean()),
+           "dE_eV": {"median": float(np.median(de)), "p90": float(np.quantile(de, 0.9)), "max": float(de.max())},
+           "fp64_attempt_fraction": gate["fp64"] / max(1, gate["fp64"] + gate["surrogate"]),
+           "gate": gate, "converged_fraction": float(np.mean(rows["status"] == 0)),
+           "training": {"geometries": int(R.shape[0]), "record_and_targets_s": t_data, "train_s": t_train,
+                        "epochs": args.sur_epochs, "batch": 16384,
+                        "final_loss_member_A": [float(x) for x in curves[-1][0]],
+                        "final_loss_member_B": [float(x) for x in curves[-1][1]],
+                        "loss_curve_A": [[float(x) for x in c[0]] for c in curves]},
+           "precision": "hidden layers: BF16 weights, activations split exactly into three BF16 parts, FP32 "
+                        "accumulation (tcgen05); FP32 output layer; FP64 integrator state, diatomics, gate "
+                        "fallback and energy check"}
+    if plain_res is not None:
+        sp = api.Statistics(H, pres_even_odd=(1, 0, 0))
+        a = {(int(r["run"]),) + tuple(int(x) for x in r["fin"][:3]): (r["rate"], r["rate_sd"])
+             for r in sp.compute(items, plain_res)}
+        b = {(int(r["run"]),) + tuple(int(x) for x in r["fin"][:3]): (r["rate"], r["rate_sd"])
+             for r in sp.compute(items, rows)}
+        z = []
+        for k in set(a) | set(b):
+            ka, sa = a.get(k, (0.0, 0.0))
+            kb, sb = b.get(k, (0.0, 0.0))
+            s2 = np.hypot(sa, sb)
+            if s2 > 0:
+                z.append(abs(ka - kb) / s2)
+        z = np.array(z)
+        pde = np.abs(plain_res["dH"]) * EV_PER_EH
+        out["vs_plain"] = {"rates_compared": int(len(z)), "beyond_2_sigma": int(np.sum(z > 2.0)),
+                           "fraction_beyond_2_sigma": float(np.mean(z > 2.0)) if len(z) else 0.0,
+                           "plain_dE_eV_median": float(np.median(pde))}
+    S.close()
+    return out
 
 
 def max_over_ranks(value, dist, buf):

@@ -1562,6 +1562,29 @@ extern "C" int cair_internal_stats_rows(const cair_stats_params* P, int32_t nite
   return 0;
 }
 
+// Internal (not in include/cair_gpu.h): surface 0 of the handle through the parity build
+// (cair_parity.cu: no fused multiply-adds, CUDA's exp, forward-mode PIP gradients) at n points, host
+// arrays as cair_pes_eval's.  For tests that separate this library's reordering from the surfaces'
+// own conditioning.
+extern "C" int cair_internal_pes_eval_parity(cair_handle* h, int64_t n, const double* R, const double* Q, double* V,
+                                             double* dVdR, double* dVdQ) {
+  if (!h || n < 1 || !R || !Q || !V || !dVdR || !dVdQ) return CAIR_EINVAL;
+  const int np = h->sys.npairs, nq = 3 * h->sys.natoms, nv = h->sys.nv;
+  if (int e = ensure_scratch(h, (size_t)n * 8 * (2 * np + nq + 1 + nv) + 4096)) return e;
+  Carver c{(char*)h->d_scratch};
+  double *d_R = c.take<double>(n * np), *d_Q = c.take<double>(n * nq), *d_V = c.take<double>(n),
+         *d_g = c.take<double>(n * np), *d_m = c.take<double>(n * nv);
+  cudaStream_t st = h->stream;
+  CUDA_TRY(h, cudaMemcpyAsync(d_R, R, n * np * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(h, cudaMemcpyAsync(d_Q, Q, n * nq * 8, cudaMemcpyHostToDevice, st));
+  if (int e = parity_pes_launch(h->sys, grid_for(h, n), st, n, d_R, d_Q, d_V, d_g, d_m)) return fail(h, e, "parity build");
+  CUDA_TRY(h, cudaMemcpyAsync(V, d_V, n * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(dVdR, d_g, n * np * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaMemcpyAsync(dVdQ, d_m, n * nv * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(h, cudaStreamSynchronize(st));
+  return 0;
+}
+
 // Internal (not in include/cair_gpu.h): what cair_create sets up, without a GPU -- the DevSys
 // (surface coefficient pointers left null) and every surface's packed device-layout coefficients,
 // concatenated, surface p at packed[offsets[p] .. offsets[p + 1]).  For tests that run the device

@@ -56,6 +56,9 @@ __device__ static const double kExpTab[64] = {
 };
 
 __device__ __forceinline__ double fexp(double x) {
+#ifdef CAIR_PARITY_MATH
+  return exp(x);  // the parity build (cair_parity.cu): CUDA's correctly rounded-to-within-1-ulp exp
+#endif
   if (!(fabs(x) <= 707.0)) return exp(x);
   const double shifter = 6755399441055744.0;  // 1.5 * 2^52: the sum rounds to an integer
   const double t = fma(x, CAIR_EXP_INV_L, shifter);
@@ -510,18 +513,29 @@ __device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const doub
 // Pair distances (Compute_Rp_CartCoord_3Atoms, Collision_Class.F90:2244-2275); Q has room
 // for the last atom, which is written to Q[NV..NV+2].
 // ------------------------------------------------------------------------------------------
-// Distances from one reciprocal square root each: 1/R = rsqrt(R^2), R = R^2 (1/R).
+// Distances from one reciprocal square root each: 1/R = rsqrt(R^2), R = R^2 (1/R).  The parity
+// build takes the reference's order instead: R = sqrt(R^2), then 1/R by division.
+__device__ __forceinline__ void dist_pair(double s2, double& R, double& Ri) {
+#ifdef CAIR_PARITY_MATH
+  R = sqrt(s2);
+  Ri = 1.0 / R;
+#else
+  Ri = rsqrt(s2);
+  R = s2 * Ri;
+#endif
+}
+
 __device__ __forceinline__ void rp3(const DevSys& S, double* Q, double* Rp, double* Ri) {
   const double m1 = S.mMiMn[0], m2 = S.mMiMn[1];
 #pragma unroll
   for (int c = 0; c < 3; ++c) Q[6 + c] = m1 * Q[c] + m2 * Q[3 + c];
   double a, b, c, s2;
   a = Q[0] - Q[3]; b = Q[1] - Q[4]; c = Q[2] - Q[5];
-  s2 = a * a + b * b + c * c; Ri[0] = rsqrt(s2); Rp[0] = s2 * Ri[0];
+  s2 = a * a + b * b + c * c; dist_pair(s2, Rp[0], Ri[0]);
   a = Q[0] - Q[6]; b = Q[1] - Q[7]; c = Q[2] - Q[8];
-  s2 = a * a + b * b + c * c; Ri[1] = rsqrt(s2); Rp[1] = s2 * Ri[1];
+  s2 = a * a + b * b + c * c; dist_pair(s2, Rp[1], Ri[1]);
   a = Q[3] - Q[6]; b = Q[4] - Q[7]; c = Q[5] - Q[8];
-  s2 = a * a + b * b + c * c; Ri[2] = rsqrt(s2); Rp[2] = s2 * Ri[2];
+  s2 = a * a + b * b + c * c; dist_pair(s2, Rp[2], Ri[2]);
 }
 
 // Compute_Rp_CartCoord_4Atoms (Collision_Class.F90:2279-2316): pairs 1-2, 1-3, 1-4, 2-3, 2-4, 3-4;
@@ -536,8 +550,7 @@ __device__ __forceinline__ void rp4(const DevSys& S, double* Q, double* Rp, doub
     const double a = Q[3 * pa[k]] - Q[3 * pb[k]], b = Q[3 * pa[k] + 1] - Q[3 * pb[k] + 1],
                  c = Q[3 * pa[k] + 2] - Q[3 * pb[k] + 2];
     const double s2 = a * a + b * b + c * c;
-    Ri[k] = rsqrt(s2);
-    Rp[k] = s2 * Ri[k];
+    dist_pair(s2, Rp[k], Ri[k]);
   }
 }
 

@@ -29,6 +29,11 @@ struct ModelLaunch {
                         double* paq0, double* erra, double* H0, double* b, int32_t* ipes, double* key);
 };
 
+// The parity build of the three-atom surfaces (cair_parity.cu, compiled without fused multiply-adds):
+// surface 0 of S at n points; 0, CAIR_EUNSUPPORTED for other models, or CAIR_ECUDA.
+int parity_pes_launch(const DevSys& S, int grid, cudaStream_t st, int64_t n, const double* R, const double* Q,
+                      double* V, double* dVdR, double* dVdQ);
+
 // Surface models with kernels in this library (one cair_model.cu object each)
 #define CAIR_FOR_EACH_MODEL(X) \
   X(CAIR_PES_O3_UMN) X(CAIR_PES_N3_UMN) X(CAIR_PES_O4_UMN) X(CAIR_PES_O3_NN) X(CAIR_PES_N4_UMN) X(CAIR_PES_O3_BNN)

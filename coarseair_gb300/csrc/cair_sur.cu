@@ -19,6 +19,7 @@ namespace cair {
 namespace sur {
 
 constexpr int kNtot = 13;  // right-hand-side evaluations of one NSteps = 3 attempt
+constexpr float kDSkip = 1e-9f;
 
 // ------------------------------------------------------------------------------------------
 // Parameters -> shared-memory image
@@ -75,6 +76,20 @@ struct Stage {
   static constexpr uint32_t SPLIT = 128u * KC * 2u;  // bytes of one BF16 part of the operand
 };
 
+// 16 consecutive FP32 values of a vector in shared memory (16-byte aligned), zeros for nullptr.
+__device__ __forceinline__ void ld_vec16(const float* p, float (&b)[16]) {
+  if (!p) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) b[i] = 0.0f;
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < 16; i += 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p + i);
+    b[i] = q.x; b[i + 1] = q.y; b[i + 2] = q.z; b[i + 3] = q.w;
+  }
+}
+
 // z_out = tanh(z_in + bias) x W^T over the 128 inputs.
 template <int NHALF>
 __device__ __forceinline__ void hidden(Cta& c, int* err, const unsigned char* img, int w_off, const float* bias,
@@ -85,12 +100,13 @@ __device__ __forceinline__ void hidden(Cta& c, int* err, const unsigned char* im
     if (!c.dead) {
 #pragma unroll 1
       for (int cc = 0; cc < St::KC; cc += 16) {
-        float v[16];
+        float v[16], b[16];
         ld16(c, zin + hf * St::KC + cc, v);
+        ld_vec16(bias ? bias + hf * St::KC + cc : nullptr, b);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           float t, s;
-          tanh_s(v[i] + (bias ? bias[hf * St::KC + cc + i] : 0.0f), t, s);
+          tanh_s(v[i] + b[i], t, s);
           v[i] = t;
         }
         put16<3>(buf, St::SPLIT, c.tid, cc, v);
@@ -115,15 +131,16 @@ __device__ __forceinline__ float output(Cta& c, int* err, const unsigned char* i
     if (!c.dead) {
 #pragma unroll 1
       for (int cc = 0; cc < St::KC; cc += 16) {
-        float v[16];
+        float v[16], bb[16], ww[16];
         ld16(c, z3 + hf * St::KC + cc, v);
+        ld_vec16(b3 + hf * St::KC + cc, bb);
+        ld_vec16(w4 + hf * St::KC + cc, ww);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          const int j = hf * St::KC + cc + i;
           float t, s;
-          tanh_s(v[i] + b3[j], t, s);
-          y = fmaf(w4[j], t, y);
-          v[i] = w4[j] * s;
+          tanh_s(v[i] + bb[i], t, s);
+          y = fmaf(ww[i], t, y);
+          v[i] = ww[i] * s;
         }
         if (BACK) put16<3>(buf, St::SPLIT, c.tid, cc, v);
       }
@@ -147,13 +164,14 @@ __device__ __forceinline__ void backward(Cta& c, int* err, const unsigned char* 
     if (!c.dead) {
 #pragma unroll 1
       for (int cc = 0; cc < St::KC; cc += 16) {
-        float u[16], z[16];
+        float u[16], z[16], b[16];
         ld16(c, ucol + hf * St::KC + cc, u);
         ld16(c, zcol + hf * St::KC + cc, z);
+        ld_vec16(bias ? bias + hf * St::KC + cc : nullptr, b);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           float t, s;
-          tanh_s(z[i] + (bias ? bias[hf * St::KC + cc + i] : 0.0f), t, s);
+          tanh_s(z[i] + b[i], t, s);
           u[i] *= s;
         }
         put16<3>(buf, St::SPLIT, c.tid, cc, u);
@@ -191,6 +209,21 @@ __device__ __forceinline__ float member_value(Cta& c, int* err, const unsigned c
   hidden<NHALF>(c, err, img, I_W2, nullptr, buf, 256, 384);
   hidden<NHALF>(c, err, img, I_W3, (const float*)(img + I_B2), buf, 384, 256);
   return output<NHALF, false>(c, err, img, buf, 256, 0);
+}
+
+// The integrator calls the network passes out of line: its Bulirsch-Stoer state (about 240
+// registers) is saved once around each call instead of being kept live through the epilogues, which
+// then have the register file for their 16-wide chunks.
+__device__ __noinline__ float member_eval_call(Cta& c, int* err, const unsigned char* img, unsigned char* buf,
+                                               float* g) {
+  float gg[16];
+  const float y = member_eval<2>(c, err, img, buf, gg);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) g[i] = gg[i];
+  return y;
+}
+__device__ __noinline__ float member_value_call(Cta& c, int* err, const unsigned char* img, unsigned char* buf) {
+  return member_value<2>(c, err, img, buf);
 }
 
 // V3 [Eh] and dV3/dR [Eh/bohr] from y [eV] and g, with the features recomputed at R.
@@ -692,25 +725,35 @@ struct RhsSur {
       Dv = F.D;
       put16<3>(z.buf, Stage<2>::SPLIT, z.c->tid, 0, F.f);
     }
-    float yb = 0.0f;
-    if (first) {
-      yb = member_value<2>(*z.c, z.err, z.imgB, z.buf);
-      Feat F;
-      features(*z.C, R, F);
-      put16<3>(z.buf, Stage<2>::SPLIT, z.c->tid, 0, F.f);
+    // a tile none of whose trajectories is in the three-body region (D below kDSkip, where V3_s is
+    // below 1e-9 of the network's output) skips the network: V3_s = 0 there to that accuracy
+    const bool net = __syncthreads_or(z.active && Dv > kDSkip) != 0;
+    float yb = 0.0f, ya = 0.0f, g[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) g[i] = 0.0f;
+    if (net) {
+      if (first) {
+        yb = member_value_call(*z.c, z.err, z.imgB, z.buf);
+        Feat F;
+        features(*z.C, R, F);
+        put16<3>(z.buf, Stage<2>::SPLIT, z.c->tid, 0, F.f);
+      }
+      ya = member_eval_call(*z.c, z.err, z.imgA, z.buf, g);
     }
-    float g[16];
-    const float ya = member_eval<2>(*z.c, z.err, z.imgA, z.buf, g);
     if (first) {
+      // the gate, with hysteresis: a trajectory sent to the FP64 surface stays there until it leaves
+      // the three-body region (D <= gate_dmin), so it meets the surrogate's fit error once
       const bool rng = gate_rng && Dv > z.C->gate_dmin;
       const bool ens = fabsf(Dv * (ya - yb)) > z.C->gate_ev;
-      z.fb = z.active && (rng || ens || z.c->dead);
+      z.fb = z.active && ((z.fb && Dv > z.C->gate_dmin) || rng || ens || z.c->dead);
       if (z.active) {
         if (z.fb) ++z.n_fb; else ++z.n_sur;
         if (rng) ++z.n_rng;
         if (ens) ++z.n_ens;
       }
     }
+    // the two-body part stays FP64 (in FP32 its force near the bond minimum would carry ~1e-6
+    // relative rounding, which multiplies the attempts of an eps = 1e-8 integrator)
     double dvd[3], dVdR[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -786,6 +829,7 @@ __global__ void __launch_bounds__(128, 1) k_integrate_sur(DevSys S, IntegrateArg
     irej = irej0 = A.irej[k];
     iste = iste0 = A.iste[k];
     att = 0;
+    z.fb = false;
   };
   take();
 #pragma unroll 1

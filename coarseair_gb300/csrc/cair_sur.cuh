@@ -151,11 +151,12 @@ __device__ __forceinline__ void features(const SurConst& C, const double (&R)[3]
   for (int k = 0; k < 3; ++k) F.dD[k] = e / C.sigma_d * dr[2][k] * dx[k];
 }
 
-// tanh(x) = sign(x) (1 - q), q = 2 / (exp(2|x|) + 1); returns h and s = 1 - h^2 = q (2 - q), which
-// keeps full relative accuracy where h is near +-1.
+// tanh(x) = 1 - q, q = 2 / (exp(2x) + 1), and s = 1 - tanh(x)^2 = q (2 - q): exp and the division
+// on the special-function unit, each within 2 ulp, so h and s carry FP32-level rounding (absolute
+// for s where the unit saturates); exp(2x) beyond 2^126 gives q = 0, h = 1, s = 0.
 __device__ __forceinline__ void tanh_s(float x, float& h, float& s) {
-  const float q = __fdividef(2.0f, __expf(2.0f * fabsf(x)) + 1.0f);
-  h = copysignf(1.0f - q, x);
+  const float q = __fdividef(2.0f, __expf(2.0f * x) + 1.0f);
+  h = 1.0f - q;
   s = q * (2.0f - q);
 }
 
@@ -173,23 +174,31 @@ struct Cta {
 
 // Operand rows: thread r writes 16 consecutive K values of its row r into a K-major operand of 128
 // rows (core matrices of 8 rows x 8 K), as NS exact BF16 parts stored split_bytes apart.
+// A pair of FP32 values as a packed BF16x2 (round to nearest even, low half = a) and its value back.
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&p);
+}
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
 template <int NS>
 __device__ __forceinline__ void put16(unsigned char* buf, uint32_t split_bytes, int r, int k0, const float (&v)[16]) {
   uint32_t w[NS][8];
 #pragma unroll
   for (int i = 0; i < 16; i += 2) {
-    __nv_bfloat16 h0, m0, l0, h1, m1, l1;
+    // the exact three-part split of cair_tc.cuh split3, two values per conversion
+    float a = v[i], b = v[i + 1];
+    const uint32_t p0 = pack_bf16x2(a, b);
+    w[0][i / 2] = p0;
     if (NS == 3) {
-      tc::split3(v[i], h0, m0, l0);
-      tc::split3(v[i + 1], h1, m1, l1);
-    } else {
-      h0 = __float2bfloat16_rn(v[i]);
-      h1 = __float2bfloat16_rn(v[i + 1]);
-    }
-    w[0][i / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-    if (NS == 3) {
-      w[1 % NS][i / 2] = (uint32_t)__bfloat16_as_ushort(m0) | ((uint32_t)__bfloat16_as_ushort(m1) << 16);
-      w[2 % NS][i / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+      a -= bf16_lo(p0);
+      b -= bf16_hi(p0);
+      const uint32_t p1 = pack_bf16x2(a, b);
+      a -= bf16_lo(p1);
+      b -= bf16_hi(p1);
+      w[1 % NS][i / 2] = p1;
+      w[2 % NS][i / 2] = pack_bf16x2(a, b);
     }
   }
 #pragma unroll

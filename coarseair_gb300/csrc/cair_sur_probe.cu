@@ -75,7 +75,86 @@ __global__ void __launch_bounds__(128) k_tc_probe(const __nv_bfloat16* __restric
   if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
+// Throughput of back-to-back MMAs: one CTA issues `nmma` 128 x 128 x 16 BF16 MMAs into one
+// accumulator, A and B no-swizzle K-major operands of K = 128 (K-steps cycling over the 8 steps),
+// issue and completion timed with clock64 by the issuing thread.  Operand contents do not matter.
+__global__ void __launch_bounds__(128) k_tc_rate(int nmma, int nsplit, long long* cycles, int* err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* sa = sm;                 // 3 parts x 32 KB
+  unsigned char* sb = sm + 3 * 32768;     // 32 KB
+  uint64_t* bar = (uint64_t*)(sm + 4 * 32768);
+  uint32_t* tslot = (uint32_t*)(sm + 4 * 32768 + 16);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < 4 * 32768 / 16; i += 128) ((uint4*)sm)[i] = make_uint4(0x3f803f80u, 0, 0, 0);
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 128);
+    tc::tmem_relinquish();
+  }
+  tc::fence_smem_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  long long t0 = 0, t1 = 0, t2 = 0;
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_bf16(128, 128, false);
+    t0 = clock64();
+    for (int m = 0; m < nmma; ++m) {
+      const int ks = m & 7, s = (m >> 3) % nsplit;
+      const uint64_t ad = tc::sdesc(tc::smem_u32(sa) + s * 32768 + ks * 4096, 2048, 128);
+      const uint64_t bd = tc::sdesc(tc::smem_u32(sb) + ks * 4096, 2048, 128);
+      tc::mma_bf16(tmem, ad, bd, idesc, m > 0 ? 1u : 0u);
+    }
+    tc::mma_commit(bar);
+    t1 = clock64();
+  }
+  const bool ok = tc::mbar_wait(bar, 0);
+  if (tid == 0) {
+    t2 = clock64();
+    cycles[0] = t1 - t0;
+    cycles[1] = t2 - t0;
+  }
+  if (!ok) atomicExch(err, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 128);
+}
+
 }  // namespace
+
+// Internal (not in include/cair_gpu.h): cycles to issue and to complete `nmma` back-to-back
+// 128 x 128 x 16 BF16 MMAs (k_tc_rate) on one SM.
+extern "C" int cair_internal_tc_rate(int nmma, int nsplit, long long* issue_cycles, long long* total_cycles) {
+  if (nmma < 1 || nmma > 100000 || nsplit < 1 || nsplit > 3 || !issue_cycles || !total_cycles) return CAIR_EINVAL;
+  long long* d = nullptr;
+  int* dErr = nullptr;
+  int rc = CAIR_OK;
+  const size_t smem = 4 * 32768 + 64;
+  if (cudaMalloc(&d, 16) != cudaSuccess || cudaMalloc(&dErr, 4) != cudaSuccess) {
+    rc = CAIR_ECUDA;
+  } else {
+    cudaMemset(dErr, 0, 4);
+    cudaFuncSetAttribute(k_tc_rate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_tc_rate<<<1, 128, smem>>>(nmma, nsplit, d, dErr);
+    long long h[2] = {0, 0};
+    int e = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = CAIR_ECUDA;
+    else {
+      cudaMemcpy(&e, dErr, 4, cudaMemcpyDeviceToHost);
+      cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
+      if (e) rc = CAIR_ETIMEOUT;
+      *issue_cycles = h[0];
+      *total_cycles = h[1];
+    }
+  }
+  cudaFree(d);
+  cudaFree(dErr);
+  return rc;
+}
 
 // Internal (not in include/cair_gpu.h): D[128][N] = A[128][16] x B[N][16]^T through one tcgen05.mma,
 // with the given descriptor offsets.  N is 16 or 128.  Returns 0, CAIR_EINVAL, CAIR_ECUDA, or

@@ -55,6 +55,32 @@ def _geometries(o, n, seed):
     return R, Qall
 
 
+# Fraction of points within 1e-12 relative (energy to max(|V|, 0.1 Eh), gradient row to its largest
+# component) that each surface must reach, in the production build and in the parity build
+# (cair_parity.cu: no FMA, CUDA's exp, forward-mode PIP gradient).  Measured on the GB300 over the
+# 576 points of the test below: N3 100 % / 100 % in both; O3 99.5 % / 97 % in production.
+WITHIN_1E12 = {"O3": (0.99, 0.95), "N3": (1.0, 1.0), "O3NN": (0.99, 0.99)}
+
+
+def _fraction_within(V, g, V_o, g_o):
+    vs = np.maximum(np.abs(V_o), 0.1)
+    gs = np.maximum(np.abs(g_o).max(axis=1, keepdims=True), 1e-2)
+    return float(np.mean(np.abs(V - V_o) <= 1e-12 * vs)), float(np.mean(np.all(np.abs(g - g_o) <= 1e-12 * gs, 1)))
+
+
+def _parity_build(H, R, Qall):
+    import ctypes as C
+    fn = H.lib.cair_internal_pes_eval_parity
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 5
+    n = R.shape[0]
+    R = np.ascontiguousarray(R)
+    Q = np.ascontiguousarray(Qall)
+    V, g, m = np.zeros(n), np.zeros_like(R), np.zeros((n, 6))
+    assert fn(H.h, n, R.ctypes.data, Q.ctypes.data, V.ctypes.data, g.ctypes.data, m.ctypes.data) == 0
+    return V, g
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_surface_energy_and_gradient_parity(gpu_lib, oracle_lib, name):
     cfg, o, H = _setup(name)
@@ -65,6 +91,12 @@ def test_surface_energy_and_gradient_parity(gpu_lib, oracle_lib, name):
     V_o, g_o, m_o = o.compute(R, Qall)
     V_g, g_g, m_g = api.PES(H).Compute(R, Qall)
     _check_rounding_level(o, R, V_o, g_o, [(V_g, g_g)], name)
+    fv, fg = _fraction_within(V_g, g_g, V_o, g_o)
+    V_p, g_p = _parity_build(H, R, Qall)
+    pv, pg = _fraction_within(V_p, g_p, V_o, g_o)
+    print("%s within 1e-12: production %.4f (V) %.4f (dV/dR); parity build %.4f %.4f" % (name, fv, fg, pv, pg))
+    assert fv >= WITHIN_1E12[name][0] and fg >= WITHIN_1E12[name][1]
+    _check_rounding_level(o, R, V_o, g_o, [(V_p, g_p)], name + " parity build")
     # energy-only evaluation (PES%Potential): the same function as Compute's energy on the UMN
     # surfaces, the reference's separate network on O3 NN
     Ve = api.PES(H).Potential(R, Qall)

@@ -52,11 +52,11 @@ def trained(gpu_lib):
     mu, isd, lo, hi = S.fit_normalisation(R[perm[:ntr]].cpu().numpy())
     S.set_consts(mu, isd, lo, hi)
     t0 = time.time()
-    curves = S.train(train, epochs=12, batch=8192, lr0=2e-3, lr1=5e-5, w_e=1.0, w_f=1.0)
+    curves = S.train(train, epochs=20, batch=8192, lr0=2e-3, lr1=2e-5, w_e=1.0, w_f=1.0)
     torch.cuda.synchronize()
     t_train = time.time() - t0
     print("surrogate: %d recorded geometries (%.1f s), trained %d steps x 2 members in %.1f s" %
-          (n, t_data, 12 * (ntr // 8192), t_train))
+          (n, t_data, 20 * (ntr // 8192), t_train))
     for ep, c in enumerate(curves):
         print("  epoch %2d  loss A (E, F) = %.3e %.3e   B = %.3e %.3e" % (ep, c[0][0], c[0][1], c[1][0], c[1][1]))
     yield dict(H=H, S=S, cfg=cfg, table=table, held=held, curves=curves)
