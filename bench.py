@@ -263,7 +263,7 @@ def main():
     ap.add_argument("--sur-train-ntraj", type=int, default=200000,
                     help="FP64 trajectories at 10,000 K whose end-check geometries form the training set")
     ap.add_argument("--sur-cap", type=int, default=20000000, help="training geometries kept")
-    ap.add_argument("--sur-epochs", type=int, default=30)
+    ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-steps", type=int, default=1, help="timed surrogate steps")
     args = ap.parse_args()
     spec = SYSTEMS[args.system]
@@ -337,6 +337,14 @@ def main():
         p = t.data_ptr()
         return (p + 255) & ~255
 
+    # the project's autotuner picks the integrator's launch shape on a capped sample of this job
+    tune = None
+    if args.surrogate != "only" and (args.system != "o4" or args.ntraj <= 200000):
+        shape, pts = api.autotune(H, table, items, sample=min(n, 65536), cap_attempts=200)
+        tune = {"block": shape[0], "blocks_per_sm": shape[1],
+                "points": [[int(p["block"]), int(p["per_sm"]), float(p["attempts_per_s"])] for p in pts],
+                "sample": "%d trajectories of the job's items, each capped at 200 attempts" % min(n, 65536)}
+
     def step(i):
         j = i % len(streams)
         H.check(lib.cair_run_queue_dev(H.h, len(table), d_lv.data_ptr(), len(items), d_it.data_ptr(), n,
@@ -358,6 +366,9 @@ def main():
     ev0 = torch.cuda.Event(enable_timing=True)
     ev_end = [torch.cuda.Event(enable_timing=True) for _ in streams]
     H.check(lib.cair_set_integrate_timing(H.h, 1), "cair_set_integrate_timing")
+    # the integrator's warp timeline (start and end of every warp of the launch) for the tail figures
+    wt = torch.zeros(2 * 65536, dtype=torch.int64, device=dev)
+    H.check(lib.cair_set_warp_timeline(H.h, wt.data_ptr(), 65536), "cair_set_warp_timeline")
     with clocks:
         torch.cuda.synchronize()
         ev0.record(streams[0])
@@ -375,6 +386,9 @@ def main():
     H.check(lib.cair_integrate_timings(H.h, kt, args.steps, ctypes.byref(nk)), "cair_integrate_timings")
     H.check(lib.cair_set_integrate_timing(H.h, 0), "cair_set_integrate_timing")
     integ_ms = float(np.mean(list(kt)[:nk.value]))
+    nw = int(lib.cair_warp_timeline_count(H.h))
+    H.check(lib.cair_set_warp_timeline(H.h, None, 0), "cair_set_warp_timeline")
+    tail = tail_figures(wt[:2 * nw].cpu().numpy().reshape(-1, 2)) if nw else None
     if world > 1:
         ms = max_over_ranks(ms, dist, torch.tensor([0.0], device=dev))
     value = aggregate_rate(n, args.steps, world, ms)
@@ -427,6 +441,8 @@ def main():
             "attempts_per_trajectory_quantiles": {q: int(np.quantile(per_traj, float(q))) for q in
                                                   ("0.5", "0.9", "0.99", "0.999", "1.0")},
             "inflight_batches": len(streams),
+            "autotune": tune,
+            "tail": tail,
             "converged_fraction": float(np.mean(res["status"] == 0)),
             "energy_not_conserved_fraction": float(np.mean(np.abs(res["dH"]) > cfg.ham_abs_tol))}
     line.update(outcome_summary(res, cfg.ncall))
@@ -464,7 +480,7 @@ def surrogate_arm(args, H, table, items, plain_res, rank):
     ttab, titems = workload(args.sur_train_ntraj, rank, iseed=4, temps=(10000.0,))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    R, _ = surrogate.record_training_set(H, ttab, titems, cap=args.sur_cap, modulus=1, rcut=9.0,
+    R, _ = surrogate.record_training_set(H, ttab, titems, cap=args.sur_cap, modulus=2, rcut=9.0,
                                          max_attempts=args.max_attempts)
     smp = surrogate.targets(H, R)
     torch.cuda.synchronize()
@@ -474,7 +490,7 @@ def surrogate_arm(args, H, table, items, plain_res, rank):
     mu, isd, lo, hi = S.fit_normalisation(sub)
     S.set_consts(mu, isd, lo, hi)
     t0 = time.perf_counter()
-    curves = S.train(smp, epochs=args.sur_epochs, batch=16384, lr0=2e-3, lr1=2e-5)
+    curves = S.train(smp, epochs=args.sur_epochs, batch=32768, lr0=3e-3, lr1=2e-5)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del smp
@@ -507,7 +523,7 @@ def surrogate_arm(args, H, table, items, plain_res, rank):
            "fp64_attempt_fraction": gate["fp64"] / max(1, gate["fp64"] + gate["surrogate"]),
            "gate": gate, "converged_fraction": float(np.mean(rows["status"] == 0)),
            "training": {"geometries": int(R.shape[0]), "record_and_targets_s": t_data, "train_s": t_train,
-                        "epochs": args.sur_epochs, "batch": 16384,
+                        "epochs": args.sur_epochs, "batch": 32768,
                         "final_loss_member_A": [float(x) for x in curves[-1][0]],
                         "final_loss_member_B": [float(x) for x in curves[-1][1]],
                         "loss_curve_A": [[float(x) for x in c[0]] for c in curves]},
@@ -534,6 +550,21 @@ def surrogate_arm(args, H, table, items, plain_res, rank):
                            "plain_dE_eV_median": float(np.median(pde))}
     S.close()
     return out
+
+
+def tail_figures(t):
+    """Queue-tail figures of one integrator launch from its warp timeline t[warp] = (start, end) in ns:
+    the fraction of warp-time idle after each warp ran out of work (launch length x warps - busy time),
+    and when (as fractions of the launch) 90 %, 50 % and 10 % of the warps were still busy."""
+    t = t.astype(np.float64)
+    t0, t1 = t[:, 0].min(), t[:, 1].max()
+    T = t1 - t0
+    busy = (t[:, 1] - t0) / T
+    q = np.sort(busy)[::-1]
+    at = lambda f: float(q[min(len(q) - 1, int(f * len(q)))])
+    return {"warps": int(len(t)), "launch_ms": T / 1e6, "idle_warp_time_fraction": float(1.0 - busy.mean()),
+            "time_fraction_when_busy_warps_fall_to": {"90%": at(0.1), "50%": at(0.5), "10%": at(0.9)},
+            "source": "%globaltimer at each warp's start and at its last lane's end (cair_set_warp_timeline)"}
 
 
 def max_over_ranks(value, dist, buf):

@@ -60,6 +60,7 @@ FINAL_STATE_DTYPE = np.dtype([("run", "i4"), ("fin", "i4", 5), ("ini", "i4", 5),
                               ("nrows", "i8"), ("cross", "f8"), ("cross_sd", "f8"), ("rate", "f8"),
                               ("rate_sd", "f8")])
 
+TUNE_POINT_DTYPE = np.dtype([("block", "i4"), ("per_sm", "i4"), ("ms", "f8"), ("attempts_per_s", "f8")])
 SUR_SAMPLE_DTYPE = np.dtype([("R", "f8", (3,)), ("e", "f4"), ("g", "f4", (3,))])
 SUR_NINV = 10
 
@@ -147,6 +148,11 @@ SIGNATURES = [
     ("cair_sur_targets_dev", C.c_int, [_P, C.c_int64, _P, _P, _P]),
     ("cair_sur_attach", C.c_int, [_P, _P]),
     ("cair_record_samples", C.c_int, [_P, _P, C.c_int64, C.c_int32, C.c_double]),
+    ("cair_set_warp_timeline", C.c_int, [_P, _P, C.c_int64]),
+    ("cair_warp_timeline_count", C.c_int64, [_P]),
+    ("cair_set_launch_shape", C.c_int, [_P, C.c_int32, C.c_int32]),
+    ("cair_get_launch_shape", C.c_int, [_P, _I, _I]),
+    ("cair_autotune", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, C.c_int32, _I]),
     ("cair_recorded_samples", C.c_int64, [_P]),
 ]
 

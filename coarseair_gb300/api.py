@@ -347,6 +347,22 @@ class RunTrajectories:
         return out
 
 
+def autotune(handle, levels, items, sample=65536, cap_attempts=300):
+    """The project's autotuner (cair_autotune): measures every launch shape of the persistent
+    integrator on a capped sample of these work items and keeps the fastest on the handle.  Returns
+    (chosen (block, per_sm), the measured points)."""
+    H = handle
+    lv = np.ascontiguousarray(levels, dtype=_lib.LEVEL_DTYPE)
+    it = np.ascontiguousarray(items, dtype=_lib.ITEM_DTYPE)
+    pts = np.zeros(32, dtype=_lib.TUNE_POINT_DTYPE)
+    n = C.c_int32()
+    H.check(H.lib.cair_autotune(H.h, len(lv), lv.ctypes.data, len(it), it.ctypes.data, int(sample), int(cap_attempts),
+                                pts.ctypes.data, len(pts), C.byref(n)), "cair_autotune")
+    b, p = C.c_int32(), C.c_int32()
+    H.check(H.lib.cair_get_launch_shape(H.h, C.byref(b), C.byref(p)), "cair_get_launch_shape")
+    return (b.value, p.value), pts[:n.value].copy()
+
+
 def _nint(x):
     """Fortran nint: nearest integer, halves away from zero."""
     x = np.asarray(x, dtype=np.float64)

@@ -48,6 +48,11 @@ struct cair_handle {
   bool time_integrate = false;              // bracket every integrator launch with events
   std::vector<cudaEvent_t> tev;             // pairs (start, end), reused across calls
   size_t ntev = 0;                          // pairs recorded since the last read
+  int tune_block = 64;                      // persistent integrator launch shape (cair_autotune)
+  int tune_per_sm = 0;                      // resident blocks per SM; 0 = as many as fit
+  unsigned long long* warp_times = nullptr; // warp timeline of the next integrator launches
+  int64_t warp_times_cap = 0;
+  int64_t warp_times_n = 0;                 // warps of the last launch that recorded
   cair_surrogate* sur = nullptr;            // attached surrogate: integrator launches run on it
   double* rec = nullptr;                    // geometry recorder of the FP64 integrator
   unsigned long long* d_nrec = nullptr;
@@ -633,16 +638,21 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_
     A.rec_mod = h->rec_mod;
     A.rec_rcut = h->rec_rcut;
   }
-  // 64-thread blocks: a block holding one long trajectory frees the rest of its SM for the
-  // next batch on another stream
-  int block = 64, per_sm = 0;
+  // launch shape: 64-thread blocks by default (a block holding one long trajectory frees the rest
+  // of its SM for the next batch on another stream), or what cair_autotune measured best
+  int block = h->tune_block, per_sm = 0;
   if (!h->sur)
     if (int e = with_model(h, [&](auto L) { per_sm = L.integrate_blocks_per_sm(block, h->sys.nsteps); })) return e;
+  if (h->tune_per_sm > 0 && h->tune_per_sm < per_sm) per_sm = h->tune_per_sm;
   if (per_sm < 1) per_sm = 1;
   int64_t g = (int64_t)h->nsm * per_sm;
   int64_t need = (A.n + block - 1) / block;
   if (g > need) g = need;
   if (g < 1) g = 1;
+  if (h->warp_times && !h->sur && g * block / 32 <= h->warp_times_cap) {
+    A.warp_times = h->warp_times;
+    h->warp_times_n = g * block / 32;
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (h->time_integrate) {
     if (2 * h->ntev + 2 > h->tev.size()) {
@@ -1019,6 +1029,94 @@ int cair_run_queue(cair_handle* h, int32_t nlevels, const cair_level* levels, in
   if (int e = wait_stream(h)) return e;
   for (int i = 0; i < 5; ++i) h->last_counters[i] = (long long)ctr[i];
   return 0;
+}
+
+int cair_set_warp_timeline(cair_handle* h, uint64_t* times_dev, int64_t cap_warps) {
+  if (!h || (times_dev && cap_warps < 1)) return fail(h, CAIR_EINVAL, "cair_set_warp_timeline: bad argument");
+  h->warp_times = (unsigned long long*)times_dev;
+  h->warp_times_cap = times_dev ? cap_warps : 0;
+  h->warp_times_n = 0;
+  return 0;
+}
+
+int64_t cair_warp_timeline_count(const cair_handle* h) { return h ? h->warp_times_n : 0; }
+
+int cair_set_launch_shape(cair_handle* h, int32_t block, int32_t per_sm) {
+  if (!h || (block != 32 && block != 64 && block != 128) || per_sm < 0)
+    return fail(h, CAIR_EINVAL, "cair_set_launch_shape: block must be 32, 64 or 128, per_sm >= 0");
+  h->tune_block = block;
+  h->tune_per_sm = per_sm;
+  return 0;
+}
+
+int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm) {
+  if (!h || !block || !per_sm) return CAIR_EINVAL;
+  *block = h->tune_block;
+  *per_sm = h->tune_per_sm;
+  return 0;
+}
+
+// Calibration of the persistent integrator's launch shape on the job's own work: every item keeps
+// the leading fraction of its trajectories (same streams) so that about `sample` trajectories run,
+// each capped at `cap_attempts` attempts so that every lane stays busy, once per candidate shape
+// (blocks of 32, 64 and 128 threads, 1 .. the resident maximum per SM); the shape with the most
+// Bulirsch-Stoer attempts per second of integrator time is kept on the handle.
+int cair_autotune(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                  const cair_work_item* items, int64_t sample, int64_t cap_attempts, cair_tune_point* out,
+                  int32_t cap, int32_t* nout) {
+  if (!h || nlevels < 1 || nitems < 1 || !levels || !items || sample < 1 || cap_attempts < 1 || !nout ||
+      (cap > 0 && !out))
+    return fail(h, CAIR_EINVAL, "cair_autotune: bad argument");
+  if (h->sur) return fail(h, CAIR_EUNSUPPORTED, "cair_autotune: the surrogate integrator has one launch shape");
+  int64_t ntot = 0;
+  for (int i = 0; i < nitems; ++i) ntot += items[i].ntraj;
+  if (ntot < 1) return fail(h, CAIR_EINVAL, "cair_autotune: no trajectories");
+  std::vector<cair_work_item> smp(items, items + nitems);
+  const double f = std::min(1.0, (double)sample / (double)ntot);
+  int64_t first = 0;
+  for (auto& it : smp) {
+    it.ntraj = it.ntraj > 0 ? std::max<int64_t>(1, (int64_t)std::llround(it.ntraj * f)) : 0;
+    it.first = first;
+    first += it.ntraj;
+  }
+  const int64_t n = first;
+  std::vector<cair_traj_result> rows((size_t)n);
+  const int keep_block = h->tune_block, keep_per_sm = h->tune_per_sm;
+  const bool keep_timing = h->time_integrate;
+  double best = -1.0;
+  int best_block = keep_block, best_per_sm = keep_per_sm;
+  int32_t k = 0;
+  int rc = 0;
+  for (int block : {32, 64, 128}) {
+    int occ = 0;
+    if (int e = with_model(h, [&](auto L) { occ = L.integrate_blocks_per_sm(block, h->sys.nsteps); })) return e;
+    for (int per_sm = 1; per_sm <= occ; ++per_sm) {
+      h->tune_block = block;
+      h->tune_per_sm = per_sm;
+      h->time_integrate = true;
+      h->ntev = 0;
+      rc = cair_run_queue(h, nlevels, levels, nitems, smp.data(), n, cap_attempts, rows.data());
+      float ms = 0.0f;
+      int32_t cnt = 0;
+      if (!rc) rc = cair_integrate_timings(h, &ms, 1, &cnt);
+      if (rc) break;
+      const double rate = (double)h->last_counters[0] / (ms * 1e-3);
+      if (k < cap) out[k] = cair_tune_point{block, per_sm, (double)ms, rate};
+      ++k;
+      if (rate > best) {
+        best = rate;
+        best_block = block;
+        best_per_sm = per_sm;
+      }
+    }
+    if (rc) break;
+  }
+  h->time_integrate = keep_timing;
+  h->ntev = 0;
+  h->tune_block = rc ? keep_block : best_block;
+  h->tune_per_sm = rc ? keep_per_sm : best_per_sm;
+  *nout = k;
+  return rc;
 }
 
 int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, double* fa, double* ex) {

@@ -118,7 +118,21 @@ struct IntegrateArgs {
   unsigned long long rec_cap;
   unsigned long long rec_mod;
   double rec_rcut;
+  // warp timeline (cair_set_warp_timeline; NULL: off): per warp of the launch, %globaltimer [ns] when
+  // it starts and when its last lane runs out of work, at [2 w] and [2 w + 1]
+  unsigned long long* warp_times;
 };
+
+// The GPU's nanosecond clock (0 where this source is compiled for the host by the test harness).
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+#ifdef __CUDA_ARCH__
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+#else
+  return 0;
+#endif
+}
 
 // Keep one in `mod` end checks, by a hash of trajectory and attempt count (splitmix64 finaliser).
 __device__ __forceinline__ bool rec_pick(unsigned long long k, long long att, unsigned long long mod) {
@@ -129,14 +143,15 @@ __device__ __forceinline__ bool rec_pick(unsigned long long k, long long att, un
   return z % mod == 0;
 }
 
-// Minimum resident 64-thread blocks per SM the register allocation must allow (1: up to 255
-// registers per thread, 4 blocks fit; 6: at most 168 registers, more warps to hide FP64 latency).
+// Minimum resident blocks per SM the register allocation must allow (1: up to 255 registers per
+// thread, 8 warps per SM fit).  Blocks of 32, 64 or 128 threads; cair_autotune picks the block size
+// and the blocks per SM at run time.
 #ifndef CAIR_INTEGRATE_MIN_BLOCKS
 #define CAIR_INTEGRATE_MIN_BLOCKS 1
 #endif
 
 template <int MODEL, int NS>
-__global__ void __launch_bounds__(64, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(DevSys S, IntegrateArgs A) {
+__global__ void __launch_bounds__(128, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(DevSys S, IntegrateArgs A) {
   constexpr int NE = Traits<MODEL>::NE, NP = Traits<MODEL>::NP;
   unsigned long long c_att = 0, c_acc = 0, c_rej = 0;
   const bool incstp = S.incstp != 0;
@@ -162,6 +177,10 @@ __global__ void __launch_bounds__(64, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(Dev
     iste = iste0 = A.iste[k];
     att = 0;
   };
+  const unsigned long long warp_id = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+  if (A.warp_times && (threadIdx.x & 31) == 0) {
+    A.warp_times[2 * warp_id] = globaltimer_ns();
+  }
   take();
 #pragma unroll 1
   for (;;) {
@@ -211,6 +230,9 @@ __global__ void __launch_bounds__(64, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(Dev
       }
     }
     __syncwarp();
+  }
+  if (A.warp_times && (threadIdx.x & 31) == 0) {
+    A.warp_times[2 * warp_id + 1] = globaltimer_ns();
   }
   if (c_att) {
     atomicAdd(A.counters + 0, c_att);

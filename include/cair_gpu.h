@@ -454,6 +454,32 @@ int cair_fp64_peak_probe(cair_handle* h, double* gflops);
 int cair_set_integrate_timing(cair_handle* h, int32_t on);
 int cair_integrate_timings(cair_handle* h, float* ms, int32_t cap, int32_t* count);
 
+/* Warp timeline of the persistent FP64 integrator (no counterpart in the reference; for measuring
+ * the queue's tail): while set, each launch with at most cap_warps warps writes, per warp w of the
+ * launch, %globaltimer [ns] at its start to times_dev[2 w] and when its last lane runs out of work to
+ * times_dev[2 w + 1] (device memory, cap_warps x 2 uint64).  cair_warp_timeline_count gives the warps
+ * of the last launch that recorded (0 if it had more than cap_warps).  NULL stops it. */
+int cair_set_warp_timeline(cair_handle* h, uint64_t* times_dev, int64_t cap_warps);
+int64_t cair_warp_timeline_count(const cair_handle* h);
+
+/* Launch shape of the persistent integrator (no counterpart in the reference, whose loop is
+ * serial): threads per block (32, 64 or 128) and resident blocks per SM (0 = as many as fit). */
+int cair_set_launch_shape(cair_handle* h, int32_t block, int32_t per_sm);
+int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm);
+/* Autotuner: runs a sample of about `sample` trajectories of the job's own work items (each item's
+ * leading trajectories, same streams), capped at cap_attempts attempts each, once per launch shape
+ * (block 32, 64, 128 x 1 .. the resident maximum per SM), and keeps on the handle the shape with the
+ * most attempts per second of integrator time.  out[0 .. cap) receives the measured points,
+ * *nout their number.  Host arrays; synchronous on the handle's stream. */
+typedef struct cair_tune_point {
+  int32_t block, per_sm;
+  double ms;                 /* integrator time of the sample */
+  double attempts_per_s;
+} cair_tune_point;
+int cair_autotune(cair_handle* h, int32_t nlevels, const cair_level* levels, int32_t nitems,
+                  const cair_work_item* items, int64_t sample, int64_t cap_attempts, cair_tune_point* out,
+                  int32_t cap, int32_t* nout);
+
 /* Device counters of the last cair_integrate*: total BS attempts, accepted, rejected,
  * PES gradient evaluations, PES energy evaluations.  Calls of cair_run_queue_dev with a caller
  * workspace (and cair_run_queue_static_dev) keep their counters in that workspace and leave these
