@@ -159,3 +159,21 @@ def test_surrogate_training_gradient_matches_oracle(gpu_lib):
     assert np.allclose(p1, ref, rtol=1e-5, atol=1e-7)
     assert np.all(s.grad(0) == 0.0)
     s.close()
+
+
+def test_tcgen05_mma_rate(gpu_lib):
+    """Back-to-back 128 x 128 x 16 BF16 MMAs into one TMEM accumulator (the operand layouts of the
+    surrogate's kernels) on one SM: the steady-state cycles per MMA, against the dense BF16 rate of
+    about 73 cycles per MMA (2.25 PFLOP/s over 152 SMs at 2.07 GHz)."""
+    lib = _lib.load()
+    fn = lib.cair_internal_tc_rate
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    out = {}
+    for n in (12, 1200, 12000):
+        a, b = C.c_longlong(), C.c_longlong()
+        assert fn(n, 3, C.byref(a), C.byref(b)) == 0
+        out[n] = b.value / n
+    print("tcgen05 128x128x16 BF16: %.1f cycles/MMA in a 12-MMA phase, %.1f (1200), %.1f (12000)" %
+          (out[12], out[1200], out[12000]))
+    assert out[12000] < 150
