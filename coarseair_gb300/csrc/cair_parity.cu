@@ -42,6 +42,7 @@ int parity_pes_launch(const DevSys& S, int grid, cudaStream_t st, int64_t n, con
     case CAIR_PES_O3_UMN: k_pes_parity<CAIR_PES_O3_UMN><<<grid, 128, 0, st>>>(S, n, R, Q, V, dVdR, dVdQ); break;
     case CAIR_PES_N3_UMN: k_pes_parity<CAIR_PES_N3_UMN><<<grid, 128, 0, st>>>(S, n, R, Q, V, dVdR, dVdQ); break;
     case CAIR_PES_O3_NN: k_pes_parity<CAIR_PES_O3_NN><<<grid, 128, 0, st>>>(S, n, R, Q, V, dVdR, dVdQ); break;
+    case CAIR_PES_O3_BNN: k_pes_parity<CAIR_PES_O3_BNN><<<grid, 128, 0, st>>>(S, n, R, Q, V, dVdR, dVdQ); break;
     default: return CAIR_EUNSUPPORTED;
   }
   return cudaGetLastError() == cudaSuccess ? 0 : CAIR_ECUDA;

@@ -99,7 +99,7 @@ __device__ __forceinline__ void hidden(Cta& c, int* err, const unsigned char* im
   for (int hf = 0; hf < NHALF; ++hf) {
     if (!c.dead) {
 #pragma unroll 1
-      for (int cc = 0; cc < St::KC; cc += 16) {
+      for (int cc = c.part * (St::KC / c.parts); cc < (c.part + 1) * (St::KC / c.parts); cc += 16) {
         float v[16], b[16];
         ld16(c, zin + hf * St::KC + cc, v);
         ld_vec16(bias ? bias + hf * St::KC + cc : nullptr, b);
@@ -109,7 +109,7 @@ __device__ __forceinline__ void hidden(Cta& c, int* err, const unsigned char* im
           tanh_s(v[i] + b[i], t, s);
           v[i] = t;
         }
-        put16<3>(buf, St::SPLIT, c.tid, cc, v);
+        put16<3>(buf, St::SPLIT, c.row, cc, v);
       }
     }
     phase(c, err, [&] {
@@ -130,7 +130,7 @@ __device__ __forceinline__ float output(Cta& c, int* err, const unsigned char* i
   for (int hf = 0; hf < NHALF; ++hf) {
     if (!c.dead) {
 #pragma unroll 1
-      for (int cc = 0; cc < St::KC; cc += 16) {
+      for (int cc = c.part * (St::KC / c.parts); cc < (c.part + 1) * (St::KC / c.parts); cc += 16) {
         float v[16], bb[16], ww[16];
         ld16(c, z3 + hf * St::KC + cc, v);
         ld_vec16(b3 + hf * St::KC + cc, bb);
@@ -142,13 +142,18 @@ __device__ __forceinline__ float output(Cta& c, int* err, const unsigned char* i
           y = fmaf(ww[i], t, y);
           v[i] = ww[i] * s;
         }
-        if (BACK) put16<3>(buf, St::SPLIT, c.tid, cc, v);
+        if (BACK) put16<3>(buf, St::SPLIT, c.row, cc, v);
       }
     }
     if (BACK)
       phase(c, err, [&] {
         issue_block<3>(c.tmem + u2, buf, St::SPLIT, 0, St::KC / 16, img + I_W3, hf * St::KC, 128, true, hf > 0);
       });
+  }
+  if (c.parts == 2) {  // the row's two partial sums
+    if (c.part == 1) c.yshare[c.row] = y;
+    __syncthreads();
+    if (c.part == 0) y += c.yshare[c.row];
   }
   return y + ((const float*)(img + I_B4))[0];
 }
@@ -163,7 +168,7 @@ __device__ __forceinline__ void backward(Cta& c, int* err, const unsigned char* 
   for (int hf = 0; hf < NHALF; ++hf) {
     if (!c.dead) {
 #pragma unroll 1
-      for (int cc = 0; cc < St::KC; cc += 16) {
+      for (int cc = c.part * (St::KC / c.parts); cc < (c.part + 1) * (St::KC / c.parts); cc += 16) {
         float u[16], z[16], b[16];
         ld16(c, ucol + hf * St::KC + cc, u);
         ld16(c, zcol + hf * St::KC + cc, z);
@@ -174,7 +179,7 @@ __device__ __forceinline__ void backward(Cta& c, int* err, const unsigned char* 
           tanh_s(z[i] + b[i], t, s);
           u[i] *= s;
         }
-        put16<3>(buf, St::SPLIT, c.tid, cc, u);
+        put16<3>(buf, St::SPLIT, c.row, cc, u);
       }
     }
     phase(c, err, [&] {
@@ -248,9 +253,13 @@ __device__ __forceinline__ void copy_image(unsigned char* dst, const unsigned ch
   for (int i = threadIdx.x; i < IMAGE / 16; i += blockDim.x) ((uint4*)dst)[i] = ((const uint4*)src)[i];
 }
 
-__device__ __forceinline__ void cta_open(Cta& c, uint64_t* bar, uint32_t* tslot) {
+__device__ __forceinline__ void cta_open(Cta& c, uint64_t* bar, uint32_t* tslot, float* yshare = nullptr) {
   c.tid = threadIdx.x;
-  c.lane_off = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
+  c.row = threadIdx.x & 127;
+  c.parts = blockDim.x / 128;
+  c.part = threadIdx.x >> 7;
+  c.yshare = yshare;
+  c.lane_off = (uint32_t)(((threadIdx.x >> 5) & 3) * 32) << 16;
   c.bar = bar;
   c.phase = 0;
   c.dead = false;
@@ -282,13 +291,15 @@ constexpr int SM_IMG_A = 0;
 constexpr int SM_IMG_B = ((IMAGE + 1023) / 1024) * 1024;
 constexpr int SM_BUF2 = 2 * SM_IMG_B;
 constexpr int SM_BAR2 = SM_BUF2 + 3 * (int)Stage<2>::SPLIT;
-constexpr int SMEM2 = SM_BAR2 + 64;
+constexpr int SM_Y2 = SM_BAR2 + 64;
+constexpr int SMEM2 = SM_Y2 + 128 * 4;
+constexpr int NT2 = 256;  // threads of the two-network kernels: two per tile row
 
 // ------------------------------------------------------------------------------------------
 // Batched evaluation: both members' values, member A's input gradient and the surrogate's
 // V3 and dV3/dR at n geometries (pair distances R[n][3]).  The same passes as the integrator.
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128, 1) k_sur_eval(SurConst C, const unsigned char* __restrict__ gimgA,
+__global__ void __launch_bounds__(NT2, 1) k_sur_eval(SurConst C, const unsigned char* __restrict__ gimgA,
                                                      const unsigned char* __restrict__ gimgB, int64_t n,
                                                      const double* __restrict__ Rin, float* __restrict__ ya,
                                                      float* __restrict__ yb, float* __restrict__ g,
@@ -300,22 +311,22 @@ __global__ void __launch_bounds__(128, 1) k_sur_eval(SurConst C, const unsigned 
   copy_image(imgA, gimgA);
   copy_image(imgB, gimgB);
   Cta c;
-  cta_open(c, (uint64_t*)(sm + SM_BAR2), (uint32_t*)(sm + SM_BAR2 + 16));
+  cta_open(c, (uint64_t*)(sm + SM_BAR2), (uint32_t*)(sm + SM_BAR2 + 16), (float*)(sm + SM_Y2));
   const int64_t ntile = (n + 127) / 128;
 #pragma unroll 1
   for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     if (__syncthreads_or(c.dead)) break;
-    const int64_t row = tile * 128 + threadIdx.x;
-    const bool valid = row < n;
+    const int64_t row = tile * 128 + c.row;
+    const bool valid = row < n && c.part == 0;   // the row's owner reads its input and writes its outputs
     double R[3] = {2.1, 4.0, 6.0};
     if (valid)
 #pragma unroll
       for (int k = 0; k < 3; ++k) R[k] = Rin[3 * row + k];
     Feat F;
     features(C, R, F);
-    put16<3>(buf, Stage<2>::SPLIT, c.tid, 0, F.f);
+    if (c.part == 0) put16<3>(buf, Stage<2>::SPLIT, c.row, 0, F.f);
     const float vb = member_value<2>(c, err, imgB, buf);
-    put16<3>(buf, Stage<2>::SPLIT, c.tid, 0, F.f);
+    if (c.part == 0) put16<3>(buf, Stage<2>::SPLIT, c.row, 0, F.f);
     float gg[16];
     const float va = member_eval<2>(c, err, imgA, buf, gg);
     if (valid && !c.dead) {
@@ -723,7 +734,7 @@ struct RhsSur {
       features(*z.C, R, F);
       gate_rng = !F.in_range;
       Dv = F.D;
-      put16<3>(z.buf, Stage<2>::SPLIT, z.c->tid, 0, F.f);
+      put16<3>(z.buf, Stage<2>::SPLIT, z.c->row, 0, F.f);
     }
     // a tile none of whose trajectories is in the three-body region (D below kDSkip, where V3_s is
     // below 1e-9 of the network's output) skips the network: V3_s = 0 there to that accuracy
@@ -736,7 +747,7 @@ struct RhsSur {
         yb = member_value_call(*z.c, z.err, z.imgB, z.buf);
         Feat F;
         features(*z.C, R, F);
-        put16<3>(z.buf, Stage<2>::SPLIT, z.c->tid, 0, F.f);
+        put16<3>(z.buf, Stage<2>::SPLIT, z.c->row, 0, F.f);
       }
       ya = member_eval_call(*z.c, z.err, z.imgA, z.buf, g);
     }
@@ -798,13 +809,34 @@ struct SurRunArgs {
   int* err;
 };
 
-__global__ void __launch_bounds__(128, 1) k_integrate_sur(DevSys S, IntegrateArgs A, SurRunArgs Z) {
+__global__ void __launch_bounds__(NT2, 1) k_integrate_sur(DevSys S, IntegrateArgs A, SurRunArgs Z) {
   constexpr int NE = 12, NP = 3;
   extern __shared__ __align__(1024) unsigned char sm[];
   copy_image(sm + SM_IMG_A, Z.imgA);
   copy_image(sm + SM_IMG_B, Z.imgB);
   Cta c;
-  cta_open(c, (uint64_t*)(sm + SM_BAR2), (uint32_t*)(sm + SM_BAR2 + 16));
+  cta_open(c, (uint64_t*)(sm + SM_BAR2), (uint32_t*)(sm + SM_BAR2 + 16), (float*)(sm + SM_Y2));
+  if (c.part == 1) {
+    // The second thread of each row holds no trajectory: it meets the owners' barriers one for one
+    // (the loop test, then per right-hand side the tile's network test and, when the network runs,
+    // member B at an attempt's first evaluation and member A), doing its half of each epilogue.
+    float g[16];
+    int ev = 0;
+#pragma unroll 1
+    for (;;) {
+      if (__syncthreads_or(c.dead) || !__syncthreads_or(0)) break;
+#pragma unroll 1
+      for (int e = 0; e < S.ncall * kNtot; ++e, ++ev) {
+        const bool first = (ev % kNtot) == 0;
+        if (__syncthreads_or(0)) {
+          if (first) member_value_call(c, Z.err, sm + SM_IMG_B, sm + SM_BUF2);
+          member_eval_call(c, Z.err, sm + SM_IMG_A, sm + SM_BUF2, g);
+        }
+      }
+    }
+    cta_close(c);
+    return;
+  }
   const DevPes& P = S.pes[0];
   SurLane z{&c, Z.err, sm + SM_IMG_A, sm + SM_IMG_B, sm + SM_BUF2, &Z.C, 0, false, false, 0, 0, 0, 0};
   RhsSur f(S, P, z);
@@ -946,7 +978,7 @@ int sur_integrate_launch(cair_surrogate* s, int nsm, cudaStream_t st, const DevS
   int64_t g = std::min<int64_t>(nsm, (A.n + 127) / 128);
   if (g < 1) g = 1;
   SurRunArgs Z{s->C, s->d_img[0], s->d_img[1], s->d_ctr, s->d_err};
-  k_integrate_sur<<<(int)g, 128, SMEM2, st>>>(S, A, Z);
+  k_integrate_sur<<<(int)g, NT2, SMEM2, st>>>(S, A, Z);
   return cudaGetLastError() == cudaSuccess ? 0 : CAIR_ECUDA;
 }
 
@@ -1091,7 +1123,7 @@ int cair_sur_eval_dev(cair_surrogate* s, int64_t n, const double* R, float* ya, 
   std::call_once(g_attr_once, set_attrs);
   cudaStream_t st = (cudaStream_t)stream;
   int64_t grid = std::min<int64_t>(s->nsm, (n + 127) / 128);
-  k_sur_eval<<<(int)grid, 128, SMEM2, st>>>(s->C, s->d_img[0], s->d_img[1], n, R, ya, yb, g, v3, dv3, s->d_err);
+  k_sur_eval<<<(int)grid, NT2, SMEM2, st>>>(s->C, s->d_img[0], s->d_img[1], n, R, ya, yb, g, v3, dv3, s->d_err);
   SUR_TRY(s, cudaGetLastError());
   return check_err_flag(s, st);
 }

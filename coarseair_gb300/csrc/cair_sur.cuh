@@ -163,11 +163,17 @@ __device__ __forceinline__ void tanh_s(float x, float& h, float& s) {
 // ------------------------------------------------------------------------------------------
 // CTA engine: 128 threads, one TMEM allocation of 512 columns, one mbarrier.
 // ------------------------------------------------------------------------------------------
+// A CTA of 128 or 256 threads works on one 128-row tile.  Thread t serves row t % 128 (TMEM lane
+// t % 128, which warps w and w + 4 can both read); with 256 threads the two threads of a row split
+// each epilogue's columns, part 0 (t < 128, the row's owner) taking the first half.
 struct Cta {
   uint32_t tmem;       // TMEM base address
   uint64_t* bar;       // MMA completion barrier
   uint32_t phase;      // parity of the next completion
   int tid;
+  int row;             // tile row of this thread
+  int part, parts;     // this thread's share of a row's columns, of `parts`
+  float* yshare;       // shared memory [128]: the second part's output partial sums
   uint32_t lane_off;   // this warp's TMEM lane quarter, as an address offset
   bool dead;           // a completion wait ran out: the CTA stops issuing work
 };

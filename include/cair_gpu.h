@@ -470,7 +470,9 @@ int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm)
  * leading trajectories, same streams), capped at cap_attempts attempts each, once per launch shape
  * (block 32, 64, 128 x 1 .. the resident maximum per SM), and keeps on the handle the shape with the
  * most attempts per second of integrator time.  out[0 .. cap) receives the measured points,
- * *nout their number.  Host arrays; synchronous on the handle's stream. */
+ * *nout their number.  Host arrays; synchronous on the handle's stream.  Make the sample several
+ * times the lanes a shape keeps resident (up to 32 x 8 warps per SM): a sample that ends in a
+ * partial round of lanes favours the shapes with fewer lanes. */
 typedef struct cair_tune_point {
   int32_t block, per_sm;
   double ms;                 /* integrator time of the sample */

@@ -59,7 +59,7 @@ def _geometries(o, n, seed):
 # component) that each surface must reach, in the production build and in the parity build
 # (cair_parity.cu: no FMA, CUDA's exp, forward-mode PIP gradient).  Measured on the GB300 over the
 # 576 points of the test below: N3 100 % / 100 % in both; O3 99.5 % / 97 % in production.
-WITHIN_1E12 = {"O3": (0.99, 0.95), "N3": (1.0, 1.0), "O3NN": (0.99, 0.99)}
+WITHIN_1E12 = {"O3": (0.99, 0.95), "N3": (1.0, 1.0), "O3NN": (0.99, 0.99), "O3BNN": (0.99, 0.99)}
 
 
 def _fraction_within(V, g, V_o, g_o):
@@ -231,13 +231,22 @@ def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
     GPU must agree on >= 99.5 % of the trajectories whose oracle outcome is stable under that
     perturbation, and overall no worse than the oracle's own reproducibility minus 1 %."""
     cfg, o, H = _setup(name)
-    n = 160 if name == "O3NN" else 400  # the O3 NN oracle is the slowest surface on the CPU
+    n = 400
+    # O3 NN's forces and Hamiltonian come from different networks, and a few of its trajectories
+    # run for hundreds of thousands of attempts; one GPU lane takes minutes over them.  Both sides
+    # stop those at the same attempt cap (status 1) and compare where they stopped.
+    cap = 30000 if name == "O3NN" else None
     ic = _ics(o, name, n)
-    ref = o.integrate(ic["paq"], ic["erra"], procs=PROCS)
-    pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"], procs=PROCS)
+    ref = o.integrate(ic["paq"], ic["erra"], procs=PROCS, max_attempts=cap)
+    pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"], procs=PROCS, max_attempts=cap)
     tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
-    api.Integrator(H).Integrate(tr)
-    assert np.all(tr.status == 0) and np.all(ref["status"] == 0)
+    api.Integrator(H).Integrate(tr, max_attempts=cap)
+    if cap is None:
+        assert np.all(tr.status == 0) and np.all(ref["status"] == 0)
+    else:
+        assert np.all(np.isin(tr.status, (0, 1))) and np.all(np.isin(ref["status"], (0, 1)))
+        assert np.mean(tr.status == ref["status"]) >= 0.99
+        print("%s: %d of %d trajectories reach the %d-attempt cap" % (name, int(np.sum(ref["status"] == 1)), n, cap))
     if CONSERVES_H[name]:
         assert np.max(np.abs(tr.H - ic["H0"])) < cfg.ham_abs_tol
     else:  # the returned H is the Hamiltonian of the returned point
