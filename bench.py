@@ -370,7 +370,7 @@ def main():
     ev_end = [torch.cuda.Event(enable_timing=True) for _ in streams]
     H.check(lib.cair_set_integrate_timing(H.h, 1), "cair_set_integrate_timing")
     # the integrator's warp timeline (start and end of every warp of the launch) for the tail figures
-    wt = torch.zeros(2 * 65536, dtype=torch.int64, device=dev)
+    wt = torch.zeros(4 * 65536, dtype=torch.int64, device=dev)
     H.check(lib.cair_set_warp_timeline(H.h, wt.data_ptr(), 65536), "cair_set_warp_timeline")
     with clocks:
         torch.cuda.synchronize()
@@ -391,7 +391,7 @@ def main():
     integ_ms = float(np.mean(list(kt)[:nk.value]))
     nw = int(lib.cair_warp_timeline_count(H.h))
     H.check(lib.cair_set_warp_timeline(H.h, None, 0), "cair_set_warp_timeline")
-    tail = tail_figures(wt[:2 * nw].cpu().numpy().reshape(-1, 2)) if nw else None
+    tail = tail_figures(wt[:4 * nw].cpu().numpy().reshape(-1, 4)) if nw else None
     if world > 1:
         ms = max_over_ranks(ms, dist, torch.tensor([0.0], device=dev))
     value = aggregate_rate(n, args.steps, world, ms)
@@ -560,7 +560,8 @@ def surrogate_arm(args, H, table, items, plain_res, rank):
 
 
 def tail_figures(t):
-    """Queue-tail figures of one integrator launch from its warp timeline t[warp] = (start, end) in ns:
+    """Queue-tail figures of one integrator launch from its warp timeline t[warp] = (start [ns], end [ns],
+    lane-blocks, blocks):
     the fraction of warp-time idle after each warp ran out of work (launch length x warps - busy time),
     and when (as fractions of the launch) 90 %, 50 % and 10 % of the warps were still busy."""
     t = t.astype(np.float64)
@@ -569,7 +570,11 @@ def tail_figures(t):
     busy = (t[:, 1] - t0) / T
     q = np.sort(busy)[::-1]
     at = lambda f: float(q[min(len(q) - 1, int(f * len(q)))])
+    # lanes without a trajectory inside busy warps, weighted by ncall-attempt blocks (an attempt costs
+    # the same whatever the trajectory, so blocks measure time)
+    lane_idle = float(1.0 - t[:, 2].sum() / (32.0 * t[:, 3].sum()))
     return {"warps": int(len(t)), "launch_ms": T / 1e6, "idle_warp_time_fraction": float(1.0 - busy.mean()),
+            "idle_lane_time_fraction_in_busy_warps": lane_idle,
             "time_fraction_when_busy_warps_fall_to": {"90%": at(0.1), "50%": at(0.5), "10%": at(0.9)},
             "source": "%globaltimer at each warp's start and at its last lane's end (cair_set_warp_timeline)"}
 

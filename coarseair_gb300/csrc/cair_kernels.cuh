@@ -118,8 +118,9 @@ struct IntegrateArgs {
   unsigned long long rec_cap;
   unsigned long long rec_mod;
   double rec_rcut;
-  // warp timeline (cair_set_warp_timeline; NULL: off): per warp of the launch, %globaltimer [ns] when
-  // it starts and when its last lane runs out of work, at [2 w] and [2 w + 1]
+  // warp timeline (cair_set_warp_timeline; NULL: off): per warp w of the launch, at [4 w .. 4 w + 3],
+  // %globaltimer [ns] when it starts and when its last lane runs out of work, the sum over its
+  // ncall blocks of the lanes with a trajectory, and its ncall blocks
   unsigned long long* warp_times;
 };
 
@@ -179,12 +180,16 @@ __global__ void __launch_bounds__(128, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(De
   };
   const unsigned long long warp_id = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
   if (A.warp_times && (threadIdx.x & 31) == 0) {
-    A.warp_times[2 * warp_id] = globaltimer_ns();
+    A.warp_times[4 * warp_id] = globaltimer_ns();
   }
+  unsigned long long lane_blocks = 0, blocks = 0;
   take();
 #pragma unroll 1
   for (;;) {
-    if (!__any_sync(0xffffffffu, active)) break;
+    const unsigned busy = __ballot_sync(0xffffffffu, active);
+    if (!busy) break;
+    lane_blocks += __popc(busy);
+    ++blocks;
     if (active) {
       const DevPes& P = S.pes[ip];
       Rhs<MODEL> f(S, P);
@@ -232,7 +237,9 @@ __global__ void __launch_bounds__(128, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(De
     __syncwarp();
   }
   if (A.warp_times && (threadIdx.x & 31) == 0) {
-    A.warp_times[2 * warp_id + 1] = globaltimer_ns();
+    A.warp_times[4 * warp_id + 1] = globaltimer_ns();
+    A.warp_times[4 * warp_id + 2] = lane_blocks;
+    A.warp_times[4 * warp_id + 3] = blocks;
   }
   if (c_att) {
     atomicAdd(A.counters + 0, c_att);

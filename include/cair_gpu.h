@@ -456,9 +456,11 @@ int cair_integrate_timings(cair_handle* h, float* ms, int32_t cap, int32_t* coun
 
 /* Warp timeline of the persistent FP64 integrator (no counterpart in the reference; for measuring
  * the queue's tail): while set, each launch with at most cap_warps warps writes, per warp w of the
- * launch, %globaltimer [ns] at its start to times_dev[2 w] and when its last lane runs out of work to
- * times_dev[2 w + 1] (device memory, cap_warps x 2 uint64).  cair_warp_timeline_count gives the warps
- * of the last launch that recorded (0 if it had more than cap_warps).  NULL stops it. */
+ * launch, to times_dev[4 w .. 4 w + 3] (device memory, cap_warps x 4 uint64): %globaltimer [ns] at its
+ * start, %globaltimer when its last lane runs out of work, the sum over its ncall-attempt blocks of
+ * the lanes that held a trajectory, and its number of blocks (so 1 - [2] / (32 [3]) is the warp's
+ * idle lane-time).  cair_warp_timeline_count gives the warps of the last launch that recorded (0 if
+ * it had more than cap_warps).  NULL stops it. */
 int cair_set_warp_timeline(cair_handle* h, uint64_t* times_dev, int64_t cap_warps);
 int64_t cair_warp_timeline_count(const cair_handle* h);
 

@@ -52,6 +52,9 @@ static inline T atomicAdd(T* p, T v) {
 }
 static inline void __syncwarp(unsigned = 0xffffffffu) {}
 static inline int __any_sync(unsigned, int pred) { return pred; }
+// one host lane: the ballot holds only its own bit
+static inline unsigned __ballot_sync(unsigned, int pred) { return pred ? 1u : 0u; }
+static inline int __popc(unsigned x) { return __builtin_popcount(x); }
 template <class T>
 static inline T atomicExch(T* p, T v) {
   const T o = *p;

@@ -18,13 +18,16 @@ def test_autotune_measures_every_shape_and_keeps_results(gpu_lib):
     table = api.level_table(lv[[5, 300, 2000]])
     items = api.work_items([(k, 0, 800, api.process_seed(6, k + 1), T, 7.0, 15.0)
                             for k, T in ((0, 10000.0), (1, 5000.0), (2, 20000.0))])
-    wt = torch.zeros(2 * 4096, dtype=torch.int64, device="cuda")
+    wt = torch.zeros(4 * 4096, dtype=torch.int64, device="cuda")
     H.check(H.lib.cair_set_warp_timeline(H.h, wt.data_ptr(), 4096), "cair_set_warp_timeline")
     before = api.RunTrajectories(H).run(table, items, max_attempts=4000)
     nw = int(H.lib.cair_warp_timeline_count(H.h))
     H.check(H.lib.cair_set_warp_timeline(H.h, None, 0), "cair_set_warp_timeline")
-    t = wt[:2 * nw].cpu().numpy().reshape(-1, 2)
+    t = wt[:4 * nw].cpu().numpy().reshape(-1, 4)
     assert nw == 2 * ((2400 + 63) // 64) and np.all(t[:, 1] >= t[:, 0]) and np.all(t[:, 0] > 0)
+    # lane-blocks: at most 32 per block, and every trajectory's blocks are counted once
+    att = before["iste"].astype(np.int64) + before["irej"]
+    assert np.all(t[:, 2] <= 32 * t[:, 3]) and int(t[:, 2].sum()) == int(np.sum((att + cfg.ncall - 1) // cfg.ncall))
     (block, per_sm), pts = api.autotune(H, table, items, sample=1200, cap_attempts=100)
     print("autotune: chose block %d x %d per SM; points:" % (block, per_sm),
           [(int(p["block"]), int(p["per_sm"]), round(float(p["attempts_per_s"]) / 1e6, 2)) for p in pts])
