@@ -245,7 +245,6 @@ def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
         assert np.all(tr.status == 0) and np.all(ref["status"] == 0)
     else:
         assert np.all(np.isin(tr.status, (0, 1))) and np.all(np.isin(ref["status"], (0, 1)))
-        assert np.mean(tr.status == ref["status"]) >= 0.99
         print("%s: %d of %d trajectories reach the %d-attempt cap" % (name, int(np.sum(ref["status"] == 1)), n, cap))
     if CONSERVES_H[name]:
         assert np.max(np.abs(tr.H - ic["H0"])) < cfg.ham_abs_tol
@@ -257,8 +256,9 @@ def test_end_to_end_final_states_agree(gpu_lib, oracle_lib, name):
     Jp, vp, ap = _final_qn(o.analyze(o.apply_transformation(pert["paq"])))
     fg = api.MolecularState(H).FindState(api.Collision(H).ApplyTransformation(tr.paq))
     Jg, vg, ag = _gpu_final_qn(fg)
-    same = (Jo == Jg) & (vo == vg) & (ao == ag)
-    stable = (Jo == Jp) & (vo == vp) & (ao == ap)
+    # where a cap applies, whether a trajectory reaches it is part of its outcome
+    same = (Jo == Jg) & (vo == vg) & (ao == ag) & (tr.status == ref["status"])
+    stable = (Jo == Jp) & (vo == vp) & (ao == ap) & (pert["status"] == ref["status"])
     print("%s: GPU vs oracle %.4f overall, %.4f on oracle-stable (%.4f of trajectories stable)" %
           (name, same.mean(), same[stable].mean(), stable.mean()))
     assert same[stable].mean() >= 0.995
