@@ -154,7 +154,11 @@ SIGNATURES = [
     ("cair_get_launch_shape", C.c_int, [_P, _I, _I]),
     ("cair_autotune", C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int64, C.c_int64, _P, C.c_int32, _I]),
     ("cair_recorded_samples", C.c_int64, [_P]),
+    ("cair_set_integrator_mode", C.c_int, [_P, C.c_int32]),
+    ("cair_get_integrator_mode", C.c_int32, [_P]),
+    ("cair_internal_warp_eval", C.c_int, [_P, C.c_int64, _P, _P, _P, _P, _P]),
 ]
+INTEGRATOR_THREAD, INTEGRATOR_WARP = 0, 1
 
 _lib = None
 

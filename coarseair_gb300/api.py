@@ -110,6 +110,17 @@ class Handle:
                    "cair_flop_model")
         return dict(grad=a.value, energy=b.value, attempt=c.value, exp=d.value)
 
+    @property
+    def integrator_mode(self):
+        """"thread" (a lane per trajectory, the default) or "warp" (a warp per trajectory: the latency
+        mode for small jobs, O3 and N3 UMN surfaces)."""
+        return "warp" if self.lib.cair_get_integrator_mode(self.h) == _lib.INTEGRATOR_WARP else "thread"
+
+    @integrator_mode.setter
+    def integrator_mode(self, mode):
+        m = {"thread": _lib.INTEGRATOR_THREAD, "warp": _lib.INTEGRATOR_WARP}[mode]
+        self.check(self.lib.cair_set_integrator_mode(self.h, m), "cair_set_integrator_mode")
+
     def counters(self):
         c = np.zeros(5, dtype=np.int64)
         self.check(self.lib.cair_last_counters(self.h, c.ctypes.data_as(C.POINTER(C.c_int64))), "counters")

@@ -18,7 +18,8 @@ LIB = os.path.join(HERE, "libcair_gpu.so")
 # model so the per-model kernels compile in parallel
 SOURCES = [("cair_api.cu", "cair_api.o", []), ("cair_output.cpp", "cair_output.o", []),
            ("cair_stats_host.cpp", "cair_stats_host.o", []), ("cair_sur.cu", "cair_sur.o", []),
-           ("cair_sur_probe.cu", "cair_sur_probe.o", []), ("cair_parity.cu", "cair_parity.o", ["-fmad=false"])] + [
+           ("cair_sur_probe.cu", "cair_sur_probe.o", []), ("cair_warp.cu", "cair_warp.o", []),
+           ("cair_parity.cu", "cair_parity.o", ["-fmad=false"])] + [
     ("cair_model.cu", "cair_model_%s.o" % name, ["-DCAIR_MODEL_ID=%d" % mid])
     for name, mid in (("o3_umn", 1), ("n3_umn", 2), ("o4_umn", 3), ("o3_nn", 4), ("n4_umn", 5), ("o3_bnn", 6))]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -22,6 +22,7 @@
 #include "cair_launch.h"
 #include "cair_stats.cuh"
 #include "cair_sur_launch.h"
+#include "cair_warp_launch.h"
 
 using namespace cair;
 
@@ -50,6 +51,7 @@ struct cair_handle {
   size_t ntev = 0;                          // pairs recorded since the last read
   int tune_block = 64;                      // persistent integrator launch shape (cair_autotune)
   int tune_per_sm = 0;                      // resident blocks per SM; 0 = as many as fit
+  int mode = CAIR_INTEGRATOR_THREAD;        // persistent integrator: a lane or a warp per trajectory
   unsigned long long* warp_times = nullptr; // warp timeline of the next integrator launches
   int64_t warp_times_cap = 0;
   int64_t warp_times_n = 0;                 // warps of the last launch that recorded
@@ -638,6 +640,31 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_
     A.rec_mod = h->rec_mod;
     A.rec_rcut = h->rec_rcut;
   }
+  if (!h->sur && h->mode == CAIR_INTEGRATOR_WARP) {
+    // a warp per trajectory: CTAs of warp_cta_warps() warps, as many as fit on every SM
+    cudaEvent_t w0 = nullptr, w1 = nullptr;
+    if (h->time_integrate) {
+      if (2 * h->ntev + 2 > h->tev.size()) {
+        for (int k = 0; k < 2; ++k) {
+          cudaEvent_t e;
+          CUDA_TRY(h, cudaEventCreate(&e));
+          h->tev.push_back(e);
+        }
+      }
+      w0 = h->tev[2 * h->ntev];
+      w1 = h->tev[2 * h->ntev + 1];
+      ++h->ntev;
+      CUDA_TRY(h, cudaEventRecord(w0, st));
+    }
+    int64_t nw = 0;
+    if (h->warp_times) A.warp_times = h->warp_times;
+    const int rc = warp_integrate_launch(h->nsm, 0, st, h->sys, A, h->warp_times ? h->warp_times_cap : 0, &nw);
+    if (rc == 2) return fail(h, CAIR_EUNSUPPORTED, "warp integrator: no lane-parallel programs for this system");
+    if (rc) return fail(h, CAIR_ECUDA, std::string("warp integrator launch: ") + cudaGetErrorString(cudaGetLastError()));
+    if (h->warp_times && nw > 0) h->warp_times_n = nw;
+    if (w1) CUDA_TRY(h, cudaEventRecord(w1, st));
+    return 0;
+  }
   // launch shape: 64-thread blocks by default (a block holding one long trajectory frees the rest
   // of its SM for the next batch on another stream), or what cair_autotune measured best
   int block = h->tune_block, per_sm = 0;
@@ -1055,6 +1082,19 @@ int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm)
   *per_sm = h->tune_per_sm;
   return 0;
 }
+
+int cair_set_integrator_mode(cair_handle* h, int32_t mode) {
+  if (!h || (mode != CAIR_INTEGRATOR_THREAD && mode != CAIR_INTEGRATOR_WARP))
+    return fail(h, CAIR_EINVAL, "cair_set_integrator_mode: mode must be CAIR_INTEGRATOR_THREAD or _WARP");
+  if (mode == CAIR_INTEGRATOR_WARP && !warp_integrate_supported(h->sys))
+    return fail(h, CAIR_EUNSUPPORTED,
+                "cair_set_integrator_mode: the warp integrator is built for the O3 and N3 UMN surfaces (one model "
+                "per handle) with NSteps 2..4");
+  h->mode = mode;
+  return 0;
+}
+
+int32_t cair_get_integrator_mode(const cair_handle* h) { return h ? h->mode : CAIR_INTEGRATOR_THREAD; }
 
 // Calibration of the persistent integrator's launch shape on the job's own work: every item keeps
 // the leading fraction of its trajectories (same streams) so that about `sample` trajectories run,
@@ -1687,6 +1727,18 @@ extern "C" int cair_internal_pes_eval_parity(cair_handle* h, int64_t n, const do
 // (surface coefficient pointers left null) and every surface's packed device-layout coefficients,
 // concatenated, surface p at packed[offsets[p] .. offsets[p + 1]).  For tests that run the device
 // surface code on the host.
+// Internal: dy/dt, H and 1/R_p of n points y[n][NE] through the warp integrator's lane-parallel
+// programs (device pointers; ipes may be null), synchronous on the handle's stream.
+extern "C" int cair_internal_warp_eval(cair_handle* h, int64_t n, const int32_t* ipes, const double* y, double* yp,
+                                       double* H, double* Ri) {
+  if (!h || n < 0 || !y || !yp || !H || !Ri) return CAIR_EINVAL;
+  if (n == 0) return 0;
+  const int rc = warp_eval_launch(h->nsm, h->stream, h->sys, n, ipes, y, yp, H, Ri);
+  if (rc == 2) return fail(h, CAIR_EUNSUPPORTED, "warp programs: not built for this system");
+  if (rc) return fail(h, CAIR_ECUDA, std::string("warp programs: ") + cudaGetErrorString(cudaGetLastError()));
+  return wait_stream(h);
+}
+
 extern "C" int64_t cair_internal_devsys_size(void) { return (int64_t)sizeof(DevSys); }
 
 extern "C" int cair_internal_setup_system(const cair_system_desc* d, void* devsys, int64_t devsys_bytes,

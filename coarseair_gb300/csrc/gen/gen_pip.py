@@ -640,6 +640,12 @@ def main():
     for key in ("O3", "N4", "O4"):
         s = S[key]
         print(key, len(s["mono"]), len(s["poly"]), len(s["basis"]))
+    # the same tables as data, for the lane-parallel program generator (gen_warp.py)
+    import json
+    with open(os.path.join(gen, "pip_tables.json"), "w") as f:
+        json.dump({key: {k: S[key][k] for k in ("mono", "poly", "basis", "nvar")} for key in ("O3", "N4", "O4")},
+                  f, separators=(",", ":"))
+        f.write("\n")
 
 
 if __name__ == "__main__":

@@ -468,6 +468,18 @@ int64_t cair_warp_timeline_count(const cair_handle* h);
  * serial): threads per block (32, 64 or 128) and resident blocks per SM (0 = as many as fit). */
 int cair_set_launch_shape(cair_handle* h, int32_t block, int32_t per_sm);
 int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm);
+/* Persistent integrator mode (no counterpart in the reference, whose loop is serial).
+ * CAIR_INTEGRATOR_THREAD (default): every lane of a warp integrates its own trajectory -- the
+ * throughput mode for queues of many more trajectories than the GPU has lanes.
+ * CAIR_INTEGRATOR_WARP: a warp integrates one trajectory -- its half-warps run the modified-midpoint
+ * sequences of an attempt side by side and its lanes evaluate each right-hand side together -- the
+ * latency mode for small jobs, whose time is their longest trajectory's.  Same queue, end check and
+ * outputs; built for the O3 and N3 UMN surfaces (one surface model per handle), NSteps 2..4; any
+ * other system returns CAIR_EUNSUPPORTED.  An attached surrogate takes precedence over either. */
+#define CAIR_INTEGRATOR_THREAD 0
+#define CAIR_INTEGRATOR_WARP 1
+int cair_set_integrator_mode(cair_handle* h, int32_t mode);
+int32_t cair_get_integrator_mode(const cair_handle* h);
 /* Autotuner: runs a sample of about `sample` trajectories of the job's own work items (each item's
  * leading trajectories, same streams), capped at cap_attempts attempts each, once per launch shape
  * (block 32, 64, 128 x 1 .. the resident maximum per SM), and keeps on the handle the shape with the

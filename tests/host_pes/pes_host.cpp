@@ -76,6 +76,7 @@ static inline T atomicCAS(T* p, T cmp, T v) {
 
 #include "../../coarseair_gb300/csrc/cair_ic.cuh"
 #include "../../coarseair_gb300/csrc/cair_stats.cuh"
+#include "../../coarseair_gb300/csrc/cair_warp.cuh"
 
 #include <vector>
 
@@ -356,4 +357,42 @@ extern "C" int pes_host_eval(const void* devsys, const double* packed, const int
     default: return 1;
   }
   return 0;
+}
+
+// The warp integrator's lane-parallel programs run one instruction after the other: constants of each
+// point's surface, the const program, then the grad program (y -> dy/dt) and the energy program
+// (y -> H, 1/R_p) at n phase-space points y[n][12].
+template <int MODEL>
+static void warp_eval(const DevSys& S, int64_t n, const int32_t* ipes, const double* y, double* yp, double* H,
+                      double* Ri) {
+  const WModel M = wmodel<MODEL>();
+  std::vector<double> s(M.nslot);
+  int loaded = -1;
+  for (int64_t k = 0; k < n; ++k) {
+    const int ip = ipes ? ipes[k] : 0;
+    if (ip != loaded) {
+      for (int i = 0; i < M.nconst; ++i) s[i] = wp_const(M, S, S.pes[ip], i);
+      wp_run_serial(M.cprog, s.data());
+      loaded = ip;
+    }
+    for (int i = 0; i < 12; ++i) s[M.gin[i]] = y[12 * k + i];
+    wp_run_serial(M.grad, s.data());
+    for (int i = 0; i < 12; ++i) yp[12 * k + i] = s[M.gout[i]];
+    for (int i = 0; i < 12; ++i) s[M.ein[i]] = y[12 * k + i];
+    wp_run_serial(M.energy, s.data());
+    H[k] = s[M.eout[0]];
+    for (int p = 0; p < 3; ++p) Ri[3 * k + p] = s[M.eout[1 + p]];
+  }
+}
+
+extern "C" int warp_host_eval(const void* devsys, const double* packed, const int64_t* offsets, int64_t n,
+                              const int32_t* ipes, const double* y, double* yp, double* H, double* Ri) {
+  DevSys S;
+  std::memcpy(&S, devsys, sizeof S);
+  for (int p = 0; p < S.npes; ++p) S.pes[p].coef = packed + offsets[p];
+  switch (S.pes[0].model) {
+    case CAIR_PES_O3_UMN: warp_eval<CAIR_PES_O3_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
+    case CAIR_PES_N3_UMN: warp_eval<CAIR_PES_N3_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
+    default: return 1;
+  }
 }

@@ -29,7 +29,7 @@ def _harness():
     src = [os.path.join(ROOT, "tests", "host_pes", "pes_host.cpp"), os.path.join(ROOT, "include", "cair_gpu.h")]
     csrc = os.path.join(ROOT, "coarseair_gb300", "csrc")
     src += [os.path.join(csrc, f) for f in ("cair_stats_host.cpp", "cair_device.cuh", "cair_kernels.cuh",
-                                            "cair_ic.cuh", "cair_stats.cuh", "cair_stats_host.h")]
+                                            "cair_ic.cuh", "cair_stats.cuh", "cair_stats_host.h", "cair_warp.cuh")]
     src += [os.path.join(csrc, "generated", f) for f in os.listdir(os.path.join(csrc, "generated"))]
     if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < max(os.path.getmtime(f) for f in src):
         subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
@@ -48,6 +48,9 @@ def _harness():
     L.queue_host_run.restype = C.c_int
     L.queue_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
                                  C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.c_void_p]
+    L.warp_host_eval.restype = C.c_int
+    L.warp_host_eval.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p]
     L.pes_host_bs_steps.restype = C.c_int
     L.pes_host_bs_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_int]
