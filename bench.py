@@ -38,6 +38,9 @@ import numpy as np  # noqa: E402
 # dram__bytes_write.sum = 69.13 MB for a 98,304-trajectory launch of this workload); the state is read
 # and written once per trajectory, so the full launch's traffic scales with the trajectory count
 DRAM_BYTES_PER_TRAJ = 703.0
+# --integrator auto: jobs below this many trajectories run a warp per trajectory (the latency mode);
+# the thread integrator keeps up to 152 SMs x 8 warps x 32 = 38,912 trajectories in flight
+WARP_MODE_MAX_TRAJ = 38912
 
 TEMPS = (5000.0, 10000.0, 20000.0)
 
@@ -265,6 +268,9 @@ def main():
     ap.add_argument("--sur-cap", type=int, default=20000000, help="training geometries kept")
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-steps", type=int, default=1, help="timed surrogate steps")
+    ap.add_argument("--integrator", default="auto", choices=["auto", "thread", "warp"],
+                    help="persistent integrator: a lane per trajectory (thread), a warp per trajectory (warp), "
+                         "or warp for jobs below WARP_MODE_MAX_TRAJ trajectories where the system has warp programs")
     args = ap.parse_args()
     spec = SYSTEMS[args.system]
     if args.ntraj is None:
@@ -337,9 +343,13 @@ def main():
         p = t.data_ptr()
         return (p + 255) & ~255
 
+    mode = args.integrator
+    if mode == "auto":
+        mode = "warp" if (n < WARP_MODE_MAX_TRAJ and args.system in ("n3", "o3")) else "thread"
+    H.integrator_mode = mode
     # the project's autotuner picks the integrator's launch shape on a capped sample of this job
     tune = None
-    if args.surrogate != "only" and (args.system != "o4" or args.ntraj <= 200000):
+    if mode == "thread" and args.surrogate != "only" and (args.system != "o4" or args.ntraj <= 200000):
         # eight times the most lanes any shape keeps resident (152 SMs x 8 warps x 32), so that every
         # shape's sample runs in several full rounds of its lanes
         ns = min(n, 8 * 38912)
@@ -435,7 +445,9 @@ def main():
                                            "98,304-trajectory launch (703 B per trajectory), scaled by trajectories"
                                            if args.system == "n3" else "not captured for this system",
                          "peak_source": peak_fp64["source"],
-                         "kernel": "k_integrate (persistent Bulirsch-Stoer integrator)",
+                         "kernel": "k_integrate (persistent Bulirsch-Stoer integrator, a lane per trajectory)"
+                                   if mode == "thread" else
+                                   "k_integrate_warp (persistent Bulirsch-Stoer integrator, a warp per trajectory)",
                          "kernel_ms_per_launch": integ_ms, "kernel_share_of_step": integ_ms * args.steps / ms,
                          "work": "executed FP64 operations of the pruned formulation per step "
                                  "(exp, division and sqrt counted as one operation each)"},
@@ -444,6 +456,7 @@ def main():
             "attempts_per_trajectory_quantiles": {q: int(np.quantile(per_traj, float(q))) for q in
                                                   ("0.5", "0.9", "0.99", "0.999", "1.0")},
             "inflight_batches": len(streams),
+            "integrator": mode,
             "autotune": tune,
             "tail": tail,
             "converged_fraction": float(np.mean(res["status"] == 0)),

@@ -39,7 +39,7 @@ struct DevSys {
 // Exponential on the FP64 pipe with 11 operations: Tang's table-driven method (ACM TOMS
 // 15(2), 144-157, 1989) with 64 subintervals.  x = (64 k + j) ln2/64 + r, |r| <= ln2/128;
 // exp(x) = 2^k 2^(j/64) (1 + p(r)), p the degree-6 Taylor polynomial of exp(r) - 1
-// (truncation < 1e-19).  The result is within about one ulp; |x| > 707 (not met on this
+// (truncation < 1e-19).  The result is within about one ulp; |x| >= 707 (not met on this
 // path's surfaces) goes to the CUDA library.
 // ------------------------------------------------------------------------------------------
 }  // namespace cair
@@ -59,7 +59,9 @@ __device__ __forceinline__ double fexp(double x) {
 #ifdef CAIR_PARITY_MATH
   return exp(x);  // the parity build (cair_parity.cu): CUDA's correctly rounded-to-within-1-ulp exp
 #endif
-  if (!(fabs(x) <= 707.0)) return exp(x);
+  // |x| < 707 (and not NaN) read off the high word with an integer compare: an FP64 comparison
+  // would take a slot of the FP64 pipe
+  if ((__double2hiint(x) & 0x7fffffff) >= 0x40861800) return exp(x);
   const double shifter = 6755399441055744.0;  // 1.5 * 2^52: the sum rounds to an integer
   const double t = fma(x, CAIR_EXP_INV_L, shifter);
   const double N = t - shifter;

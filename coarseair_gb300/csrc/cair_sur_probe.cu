@@ -191,3 +191,66 @@ extern "C" int cair_internal_tc_probe(const void* A, const void* B, int N, int b
   cudaFree(dErr);
   return rc;
 }
+
+// ------------------------------------------------------------------------------------------
+// FP64 timing probes for the warp integrator's design: one warp alone on the GPU runs a chain of
+// n dependent operations on `active` of its lanes and records clock64 around it.
+//   mode 0: x = fma(x, a, b)                                   (dependent DFMA latency)
+//   mode 1: four independent DFMA chains per lane              (issue rate of one warp)
+//   mode 2: a level of the programs: load from shared memory, DFMA, store, __syncwarp
+// ------------------------------------------------------------------------------------------
+__global__ void k_fp64_probe(int n, int active, int mode, long long* out, double* sink) {
+  __shared__ double s[64];
+  const int lane = threadIdx.x & 31;
+  s[lane] = 1.0 + lane * 1e-3;
+  s[lane + 32] = 1.0 - lane * 1e-3;
+  __syncwarp();
+  double x = 1.0 + lane * 1e-3, x1 = x + 0.5, x2 = x + 0.25, x3 = x + 0.125;
+  const double a = 0.9999999, b = 1e-7;
+  const long long t0 = clock64();
+  if (lane < active) {
+    if (mode == 0) {
+      for (int i = 0; i < n; ++i) x = fma(x, a, b);
+    } else if (mode == 1) {
+      for (int i = 0; i < n; ++i) {
+        x = fma(x, a, b);
+        x1 = fma(x1, a, b);
+        x2 = fma(x2, a, b);
+        x3 = fma(x3, a, b);
+      }
+      x = x + x1 + x2 + x3;
+    }
+  }
+  if (mode == 2) {
+    for (int i = 0; i < n; ++i) {
+      if (lane < active) {
+        const double v = s[(i * 7 + lane) & 63];
+        s[(i * 5 + lane + 11) & 63] = fma(v, a, b);
+      }
+      __syncwarp();
+    }
+    x = s[lane];
+  }
+  __syncwarp();
+  const long long t1 = clock64();
+  if (lane == 0) out[0] = t1 - t0;
+  sink[lane] = x;
+}
+
+// Internal (not in include/cair_gpu.h): clock64 cycles of k_fp64_probe on one warp.
+extern "C" int cair_internal_fp64_probe(int n, int active, int mode, long long* cycles) {
+  if (n < 1 || n > (1 << 20) || active < 1 || active > 32 || mode < 0 || mode > 2 || !cycles) return CAIR_EINVAL;
+  long long* d = nullptr;
+  double* sink = nullptr;
+  int rc = CAIR_OK;
+  if (cudaMalloc(&d, 8) != cudaSuccess || cudaMalloc(&sink, 32 * sizeof(double)) != cudaSuccess) {
+    rc = CAIR_ECUDA;
+  } else {
+    k_fp64_probe<<<1, 32>>>(n, active, mode, d, sink);
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = CAIR_ECUDA;
+    else cudaMemcpy(cycles, d, 8, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d);
+  cudaFree(sink);
+  return rc;
+}

@@ -55,14 +55,12 @@ template <int MODEL>
 __device__ __forceinline__ void stage_programs(unsigned* tab, WModel& M) {
   int off = 0;
   auto copy = [&](WProg& p) {
-    const int nl = 2 * p.nlev;
-    for (int i = threadIdx.x; i < nl; i += blockDim.x) tab[off + i] = p.lev[i];
-    for (int i = threadIdx.x; i < p.nnode; i += blockDim.x) tab[off + nl + i] = p.node[i];
-    for (int i = threadIdx.x; i < p.nterm; i += blockDim.x) tab[off + nl + p.nnode + i] = p.term[i];
-    p.lev = tab + off;
-    p.node = tab + off + nl;
-    p.term = tab + off + nl + p.nnode;
-    off += nl + p.nnode + p.nterm;
+    const int nw = 64 * p.nlev;
+    const uint4* src = reinterpret_cast<const uint4*>(p.rec);
+    uint4* dst = reinterpret_cast<uint4*>(tab + off);
+    for (int i = threadIdx.x; i < nw / 4; i += blockDim.x) dst[i] = src[i];
+    p.rec = tab + off;
+    off += nw;
   };
   copy(M.grad);
   copy(M.energy);
@@ -70,8 +68,8 @@ __device__ __forceinline__ void stage_programs(unsigned* tab, WModel& M) {
 
 template <int MODEL>
 __host__ __device__ constexpr int program_words() {
-  return MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_GRAD_WORDS + WP_O3_UMN_ENERGY_WORDS
-                                  : WP_N3_UMN_GRAD_WORDS + WP_N3_UMN_ENERGY_WORDS;
+  return MODEL == CAIR_PES_O3_UMN ? 64 * (WP_O3_UMN_GRAD_NLEV + WP_O3_UMN_ENERGY_NLEV)
+                                  : 64 * (WP_N3_UMN_GRAD_NLEV + WP_N3_UMN_ENERGY_NLEV);
 }
 template <int MODEL>
 __host__ __device__ constexpr int program_slots() {
@@ -79,7 +77,21 @@ __host__ __device__ constexpr int program_slots() {
 }
 template <int MODEL>
 constexpr size_t warp_smem_bytes() {
-  return (size_t)((program_words<MODEL>() + 1) & ~1) * 4 + (size_t)kWarpCta * 2 * program_slots<MODEL>() * 8;
+  return (size_t)program_words<MODEL>() * 4 + (size_t)kWarpCta * 2 * program_slots<MODEL>() * 8;
+}
+
+// The levels of a program on a half-warp: lane gl runs its record of each level (the next level's
+// record is loaded while this one computes), the half-warps meet between levels.
+__device__ __forceinline__ void run_levels(const WProg& p, double* s, int gl) {
+  const uint4* R = reinterpret_cast<const uint4*>(p.rec) + gl;
+  uint4 c = R[0];
+  for (int L = 0; L < p.nlev; ++L) {
+    uint4 nx = c;
+    if (L + 1 < p.nlev) nx = R[16 * (L + 1)];
+    if (c.x >> 31) s[c.x & 0xffffu] = wp_eval(c.x, c.y, c.z, c.w, s);
+    __syncwarp();
+    c = nx;
+  }
 }
 
 // Constants of surface P into both half-warps' slots, then the const program on each.
@@ -91,10 +103,7 @@ __device__ __forceinline__ void load_constants(const WModel& M, const DevSys& S,
     slots[M.nslot + i] = v;
   }
   __syncwarp();
-  for (int L = 0; L < M.cprog.nlev; ++L) {
-    wp_level(M.cprog, L, s, gl, 16);
-    __syncwarp();
-  }
+  run_levels(M.cprog, s, gl);
 }
 
 // One program on both half-warps: lane gl < NE puts its input, the levels run, it reads its output.
@@ -102,10 +111,7 @@ __device__ __forceinline__ double run_program(const WProg& p, double* s, int gl,
                                               double v) {
   if (io) s[in] = v;
   __syncwarp();
-  for (int L = 0; L < p.nlev; ++L) {
-    wp_level(p, L, s, gl, 16);
-    __syncwarp();
-  }
+  run_levels(p, s, gl);
   return io ? s[out] : 0.0;
 }
 
@@ -120,12 +126,14 @@ __device__ __forceinline__ void extrap_one(const double (&est)[NS], const double
 }
 
 // One Bulirsch-Stoer attempt of the warp's trajectory (Integrate_ODE_1d, ODE_Solver.F90:225-358, with
-// the same arithmetic per equation as bs_attempt).  Returns 1 when a difference of extrapolants is NaN.
+// the same arithmetic per equation as bs_attempt) from dydx = f(y).  Returns bit 0 when a difference of
+// extrapolants is NaN, bit 1 when the step was accepted (a rejected step leaves y, and so f(y), as
+// they were: the caller reuses dydx).
 template <int NS>
 __device__ __forceinline__ int warp_attempt(const WProg& G, double* s, int gl, int grp, bool io, int in, int out,
-                                            double& y, double& x, double& h, double yscal, double relax,
-                                            bool incstp, double& smax, double& smin, int& irej, int& iste) {
-  const double dydx = run_program(G, s, gl, io, in, out, y);
+                                            double dydx, double& y, double& x, double& h, double yscal,
+                                            double relax, bool incstp, double& smax, double& smin, int& irej,
+                                            int& iste) {
   double est[NS];
 #pragma unroll
   for (int j = 0; j < NS; ++j) est[j] = 0.0;
@@ -195,7 +203,8 @@ __device__ __forceinline__ int warp_attempt(const WProg& G, double* s, int gl, i
     if (!below[j - 1]) break;
     iconv = j;
   }
-  if (below[NS - 2]) {
+  const bool accept = below[NS - 2];
+  if (accept) {
     x = x + h;
     y = ylast[0];
     smin = (smin < h) ? smin : h;
@@ -213,7 +222,7 @@ __device__ __forceinline__ int warp_attempt(const WProg& G, double* s, int gl, i
     h = h / (double)nseq_of(kk - 1);
     irej += 1;
   }
-  return nan;
+  return nan | (accept ? 2 : 0);
 }
 
 template <int MODEL, int NS>
@@ -225,7 +234,7 @@ __global__ void __launch_bounds__(32 * kWarpCta, 1) k_integrate_warp(DevSys S, I
   WModel M = wmodel<MODEL>();
   stage_programs<MODEL>(tab, M);
   const int lane = threadIdx.x & 31, grp = lane >> 4, gl = lane & 15;
-  double* slots = reinterpret_cast<double*>(tab + ((program_words<MODEL>() + 1) & ~1)) +
+  double* slots = reinterpret_cast<double*>(tab + program_words<MODEL>()) +
                   (size_t)(threadIdx.x >> 5) * 2 * M.nslot;
   double* s = slots + grp * M.nslot;
   __syncthreads();
@@ -256,13 +265,19 @@ __global__ void __launch_bounds__(32 * kWarpCta, 1) k_integrate_warp(DevSys S, I
     int irej = A.irej[k], iste = A.iste[k];
     const int irej0 = irej, iste0 = iste;
     int64_t att = 0;
+    double dydx = 0.0;
+    bool fresh = false;  // dydx = f(y) of the current y
 #pragma unroll 1
     for (;;) {
       int bad = 0;
 #pragma unroll 1
-      for (int c = 0; c < ncall; ++c)
-        bad |= warp_attempt<NS>(M.grad, s, gl, grp, io, gin, gout, y, x, h, yscal, S.relax, incstp, smax, smin,
-                                irej, iste);
+      for (int c = 0; c < ncall; ++c) {
+        if (!fresh) dydx = run_program(M.grad, s, gl, io, gin, gout, y);
+        const int r = warp_attempt<NS>(M.grad, s, gl, grp, io, gin, gout, dydx, y, x, h, yscal, S.relax, incstp,
+                                       smax, smin, irej, iste);
+        bad |= r & 1;
+        fresh = !(r & 2);
+      }
       att += ncall;
       ++blocks;
       // end check (Integrator_Class.F90:457-465): H and 1/R_p of the new point
@@ -332,7 +347,7 @@ __global__ void __launch_bounds__(32 * kWarpCta, 1) k_warp_eval(DevSys S, int64_
   WModel M = wmodel<MODEL>();
   stage_programs<MODEL>(tab, M);
   const int lane = threadIdx.x & 31, grp = lane >> 4, gl = lane & 15;
-  double* s = reinterpret_cast<double*>(tab + ((program_words<MODEL>() + 1) & ~1)) +
+  double* s = reinterpret_cast<double*>(tab + program_words<MODEL>()) +
               (size_t)(threadIdx.x >> 5) * 2 * M.nslot + grp * M.nslot;
   __syncthreads();
   const bool io = gl < NE;
@@ -342,10 +357,7 @@ __global__ void __launch_bounds__(32 * kWarpCta, 1) k_warp_eval(DevSys S, int64_
     const DevPes& P = S.pes[ipes ? ipes[k] : 0];
     for (int i = gl; i < M.nconst; i += 16) s[i] = wp_const(M, S, P, i);
     __syncwarp();
-    for (int L = 0; L < M.cprog.nlev; ++L) {
-      wp_level(M.cprog, L, s, gl, 16);
-      __syncwarp();
-    }
+    run_levels(M.cprog, s, gl);
     const double v = io ? y[NE * k + gl] : 0.0;
     const double f = run_program(M.grad, s, gl, io, io ? M.gin[gl] : 0, io ? M.gout[gl] : 0, v);
     const bool mine = base + grp < n;

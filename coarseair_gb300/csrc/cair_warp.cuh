@@ -12,13 +12,11 @@ namespace cair {
 enum { WK_SOP = 0, WK_EXP = 1, WK_RSQRT = 2, WK_RECIP = 3 };
 enum { WS_LIT = 0, WS_TPQ = 1, WS_MMIMN = 2, WS_O2AB = 3, WS_COEF = 4, WS_PES = 5 };
 
-// One program: nlev levels (kind | count << 8, first node), nodes (out | nterm << 16, first term or
-// operand slot), terms (a | sign << 15 | b << 16).
+// One program: nlev levels of 16 records of 4 words (lane l of level L executes record 16 L + l):
+// w0 = active << 31 | kind << 28 | nterm << 24 | out slot; w1..w3 = terms a | sign << 15 | b << 16.
 struct WProg {
-  const unsigned* lev;
-  const unsigned* node;
-  const unsigned* term;
-  int nlev, nnode, nterm;  // nnode, nterm: array lengths in words
+  const unsigned* rec;
+  int nlev;
 };
 
 // A surface model's programs over one slot layout: constants [0, nconst) (surface / system values,
@@ -32,18 +30,13 @@ struct WModel {
   const unsigned short *gin, *gout, *ein, *eout;  // grad: y -> dy/dt; energy: y -> (H, 1/R_p)
 };
 
-#define CAIR_WPROG(key, name)                                                                                  \
-  WProg {                                                                                                      \
-    wp_##key##_##name##_lev, wp_##key##_##name##_node, wp_##key##_##name##_term,                              \
-        (int)(sizeof(wp_##key##_##name##_lev) / sizeof(unsigned) / 2),                                        \
-        (int)(sizeof(wp_##key##_##name##_node) / sizeof(unsigned)),                                           \
-        (int)(sizeof(wp_##key##_##name##_term) / sizeof(unsigned))                                            \
-  }
+#define CAIR_WPROG(key, KEY, name, NAME) \
+  WProg { wp_##key##_##name##_rec, WP_##KEY##_##NAME##_NLEV }
 #define CAIR_WMODEL(key, KEY)                                                                                  \
   WModel {                                                                                                     \
     WP_##KEY##_NSLOT, WP_##KEY##_NCONST, wp_##key##_csrc, wp_##key##_cidx, wp_##key##_clit,                   \
-        CAIR_WPROG(key, cprog), CAIR_WPROG(key, grad), CAIR_WPROG(key, energy), wp_##key##_grad_in,           \
-        wp_##key##_grad_out, wp_##key##_energy_in, wp_##key##_energy_out                                       \
+        CAIR_WPROG(key, KEY, cprog, CPROG), CAIR_WPROG(key, KEY, grad, GRAD), CAIR_WPROG(key, KEY, energy, ENERGY), \
+        wp_##key##_grad_in, wp_##key##_grad_out, wp_##key##_energy_in, wp_##key##_energy_out                   \
   }
 
 // Surface models that have programs (3-atom UMN surfaces).
@@ -72,42 +65,39 @@ __device__ __forceinline__ double wp_const(const WModel& m, const DevSys& S, con
   }
 }
 
-// One instruction: a sum of signed products (a multiply, then fused multiply-adds in term order),
-// the table-driven exponential, a reciprocal square root or a reciprocal.
-__device__ __forceinline__ double wp_eval(unsigned kind, unsigned nx, unsigned ny, const unsigned* __restrict__ term,
-                                          const double* s) {
+// One record: a sum of up to three signed products (a multiply, then fused multiply-adds in term
+// order), the table-driven exponential, a reciprocal square root or a reciprocal.  The operands of
+// every term are loaded before the arithmetic starts.
+// The term's sign goes on the first factor's sign bit with an integer XOR: a per-lane select of -a
+// would cost an FP64 instruction (a negation on the FP64 pipe) per term.
+__device__ __forceinline__ double wp_signed(double a, unsigned w) {
+  return __hiloint2double(__double2hiint(a) ^ (int)((w & 0x8000u) << 16), __double2loint(a));
+}
+
+__device__ __forceinline__ double wp_eval(unsigned w0, unsigned w1, unsigned w2, unsigned w3, const double* s) {
+  const unsigned kind = (w0 >> 28) & 3u;
   if (kind == WK_SOP) {
-    const unsigned nt = nx >> 16;
-    const unsigned* t = term + ny;
-    unsigned tm = t[0];
-    double a = s[tm & 0x7fffu];
-    double r = ((tm & 0x8000u) ? -a : a) * s[tm >> 16];
-    for (unsigned j = 1; j < nt; ++j) {
-      tm = t[j];
-      a = s[tm & 0x7fffu];
-      r = fma((tm & 0x8000u) ? -a : a, s[tm >> 16], r);
-    }
+    const unsigned nt = (w0 >> 24) & 3u;
+    const double a0 = wp_signed(s[w1 & 0x7fffu], w1), b0 = s[w1 >> 16];
+    const double a1 = wp_signed(s[w2 & 0x7fffu], w2), b1 = s[w2 >> 16];
+    const double a2 = wp_signed(s[w3 & 0x7fffu], w3), b2 = s[w3 >> 16];
+    double r = a0 * b0;
+    if (nt > 1) r = fma(a1, b1, r);
+    if (nt > 2) r = fma(a2, b2, r);
     return r;
   }
-  const double x = s[ny];
+  const double x = s[w1 & 0x7fffu];
   if (kind == WK_EXP) return fexp(x);
   if (kind == WK_RSQRT) return rsqrt(x);
   return 1.0 / x;
 }
 
-// The instructions of level L that lane gl of `width` lanes executes (gl, gl + width, ...).
-__device__ __forceinline__ void wp_level(const WProg& p, int L, double* s, int gl, int width) {
-  const unsigned lv = p.lev[2 * L], base = p.lev[2 * L + 1];
-  const unsigned kind = lv & 0xffu, cnt = lv >> 8;
-  for (unsigned i = (unsigned)gl; i < cnt; i += (unsigned)width) {
-    const unsigned nx = p.node[2 * (base + i)], ny = p.node[2 * (base + i) + 1];
-    s[nx & 0xffffu] = wp_eval(kind, nx, ny, p.term, s);
-  }
-}
-
-// A whole program by one thread (the host harness).
+// A whole program by one thread (the host harness), record after record.
 __device__ __forceinline__ void wp_run_serial(const WProg& p, double* s) {
-  for (int L = 0; L < p.nlev; ++L) wp_level(p, L, s, 0, 1);
+  for (int r = 0; r < 16 * p.nlev; ++r) {
+    const unsigned* w = p.rec + 4 * r;
+    if (w[0] >> 31) s[w[0] & 0xffffu] = wp_eval(w[0], w[1], w[2], w[3], s);
+  }
 }
 
 }  // namespace cair

@@ -36,7 +36,7 @@ import struct
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.abspath(os.path.join(HERE, ".."))
 LANES = 16          # lanes of a half-warp: instructions per level
-SPLIT = 4           # sums with more terms are split into partial sums
+SPLIT = 3           # sums with more terms are split into partial sums (a record holds 3 terms)
 COST = {"sop": None, "exp": 12, "rsqrt": 8, "recip": 10}
 KIND = {"sop": 0, "exp": 1, "rsqrt": 2, "recip": 3}
 
@@ -716,23 +716,37 @@ def compile_model(surface, tabs):
 
 
 # ----------------------------------------------------------------------------------------------
-# Emission
+# Emission: one 16-byte record per lane and level
 # ----------------------------------------------------------------------------------------------
-def encode(levels, ins, slot):
-    lev, nodes, terms = [], [], []
+def records(levels, ins, slot, width=LANES):
+    """Levels of more than `width` instructions are cut into several; lane l of level L executes
+    record L * width + l:  w0 = active << 31 | kind << 28 | nterm << 24 | out slot, w1..w3 = terms
+    a | sign << 15 | b << 16 ((+-) s[a] * s[b]; a special instruction's operand is term 0's a)."""
+    out = []
     for kind, nl in levels:
-        lev.append((KIND[kind] | (len(nl) << 8), len(nodes)))
-        for n in nl:
-            k, opd = ins[n]
-            if k == "sop":
-                nodes.append((slot[n] | (len(opd) << 16), len(terms)))
-                for s, a, b in opd:
-                    sa, sb = slot[a], slot[b]
-                    assert sa < 0x8000 and sb < 0x10000
-                    terms.append(sa | (0x8000 if s < 0 else 0) | (sb << 16))
-            else:
-                nodes.append((slot[n], slot[opd[0]]))
-    return lev, nodes, terms
+        for c in range(0, len(nl), width):
+            chunk = nl[c:c + width]
+            for lane in range(width):
+                if lane >= len(chunk):
+                    out += [0, 0, 0, 0]
+                    continue
+                n = chunk[lane]
+                k, opd = ins[n]
+                w = [0, 0, 0, 0]
+                if k == "sop":
+                    assert 1 <= len(opd) <= 3
+                    for j, (sg, x, y) in enumerate(opd):
+                        sa, sb = slot[x], slot[y]
+                        assert sa < 0x8000 and sb < 0x10000
+                        w[1 + j] = sa | (0x8000 if sg < 0 else 0) | (sb << 16)
+                    nt = len(opd)
+                else:
+                    w[1] = slot[opd[0]]
+                    nt = 1
+                assert slot[n] < 0x10000
+                w[0] = (1 << 31) | (KIND[k] << 28) | (nt << 24) | slot[n]
+                out += w
+    return out
 
 
 def stats(levels, ins):
@@ -742,16 +756,19 @@ def stats(levels, ins):
     return nins, flops, crit
 
 
-def arr(ctype, name, vals, per=12):
+def arr(ctype, name, vals, align=None):
     body = ",".join(str(v) for v in vals) if vals else "0"
-    return "__device__ static const %s %s[%d] = {%s};" % (ctype, name, max(1, len(vals)), body)
+    att = " __attribute__((aligned(%d)))" % align if align else ""
+    return "__device__ static const %s %s[%d]%s = {%s};" % (ctype, name, max(1, len(vals)), att, body)
 
 
 def emit(models, path):
     L = ["/* Lane-parallel right-hand-side programs of the warp integrator (cair_warp.cu).",
          " * Generated by csrc/gen/gen_warp.py, do not edit.",
-         " * level  = (kind | count << 8, first node); node = (out | nterm << 16, first term | operand);",
-         " * term   = a | sign << 15 | b << 16: (+-) s[a] * s[b]. */",
+         " * A program is NLEV levels of 16 records of 4 words, lane l of level L executing record 16 L + l:",
+         " * w0 = active << 31 | kind << 28 | nterm << 24 | out slot (kind 0 sum of products, 1 exp, 2 rsqrt,",
+         " * 3 reciprocal); w1..w3 = terms a | sign << 15 | b << 16, (+-) s[a] * s[b] (a special's operand is",
+         " * w1's a). */",
          "#pragma once", ""]
     for key, m in models.items():
         P = m["progs"]
@@ -765,7 +782,6 @@ def emit(models, path):
         L.append(" */")
         L.append("#define WP_%s_NSLOT %d" % (key.upper(), m["nslot"]))
         L.append("#define WP_%s_NCONST %d" % (key.upper(), m["nconst"]))
-        # constant fill table: src, idx, literal values
         cs = [c[0] if c[0] >= 0 else 255 for c in m["const_list"]]
         ci = [c[1] for c in m["const_list"]]
         lits = [repr(c[2]) if c[0] == SRC["lit"] else "0.0" for c in m["const_list"]]
@@ -773,36 +789,21 @@ def emit(models, path):
         L.append(arr("unsigned short", "wp_%s_cidx" % key, ci))
         L.append(arr("double", "wp_%s_clit" % key, lits))
         # const program: the hoisted nodes of both programs
-        L.extend(emit_prog(key, "cprog", m["cprog"]))
+        rec = []
+        for pname, lv, ins, slot, g in m["cprog"]:
+            rec += records(lv, ins, slot)
+        L.append("#define WP_%s_CPROG_NLEV %d" % (key.upper(), len(rec) // (4 * LANES)))
+        L.append(arr("unsigned int", "wp_%s_cprog_rec" % key, rec, 16))
         for name in ("grad", "energy"):
             p = P[name]
-            lev, nodes, terms = encode(p["levels"], p["ins"], p["slot"])
-            L.append("#define WP_%s_%s_NLEV %d" % (key.upper(), name.upper(), len(lev)))
-            L.append("#define WP_%s_%s_WORDS %d" % (key.upper(), name.upper(), 2 * len(lev) + 2 * len(nodes) + len(terms)))
-            L.append(arr("unsigned int", "wp_%s_%s_lev" % (key, name), [v for t in lev for v in t]))
-            L.append(arr("unsigned int", "wp_%s_%s_node" % (key, name), [v for t in nodes for v in t]))
-            L.append(arr("unsigned int", "wp_%s_%s_term" % (key, name), terms))
+            rec = records(p["levels"], p["ins"], p["slot"])
+            L.append("#define WP_%s_%s_NLEV %d" % (key.upper(), name.upper(), len(rec) // (4 * LANES)))
+            L.append(arr("unsigned int", "wp_%s_%s_rec" % (key, name), rec, 16))
             L.append(arr("unsigned short", "wp_%s_%s_in" % (key, name), p["ins_slots"]))
             L.append(arr("unsigned short", "wp_%s_%s_out" % (key, name), p["outs"]))
         L.append("")
     with open(path, "w") as f:
         f.write("\n".join(L) + "\n")
-
-
-def emit_prog(key, name, parts):
-    lev, nodes, terms = [], [], []
-    for pname, lv, ins, slot, g in parts:
-        a, b, c = encode(lv, ins, slot)
-        n0, t0 = len(nodes), len(terms)
-        lev += [(x, y + n0) for x, y in a]
-        kinds = [k for k, nl in lv for _ in nl]
-        nodes += [((x, y + t0) if k == "sop" else (x, y)) for (x, y), k in zip(b, kinds)]
-        terms += c
-    out = ["#define WP_%s_%s_NLEV %d" % (key.upper(), name.upper(), len(lev))]
-    out.append(arr("unsigned int", "wp_%s_%s_lev" % (key, name), [v for t in lev for v in t]))
-    out.append(arr("unsigned int", "wp_%s_%s_node" % (key, name), [v for t in nodes for v in t]))
-    out.append(arr("unsigned int", "wp_%s_%s_term" % (key, name), terms))
-    return out
 
 
 def main():

@@ -1,0 +1,102 @@
+"""The warp integrator (a warp per trajectory, cair_set_integrator_mode) against the oracle on the GPU.
+
+1. Its lane-parallel right-hand-side and energy programs at phase-space points, under the GPU
+   right-hand-side parity criterion (tests/test_warp_host.py runs the same programs on the host).
+2. Whole collisions through the persistent warp integrator against the oracle's: final (v, J,
+   arrangement) on the oracle-stable trajectories, energy conservation, the device counters.
+3. NSteps 2 and 4 (their half-warp schedules differ from NSteps 3's).
+4. The mode is refused where no programs are built."""
+import numpy as np
+import pytest
+
+from coarseair_gb300 import api, systems
+from test_gpu_parity import PROCS, ROUND_U, _final_qn, _gpu_final_qn, _ics, _setup
+from test_warp_host import CFGS as HOST_CFGS, _phase_points
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", list(HOST_CFGS))
+def test_warp_programs_on_the_gpu_match_the_oracle(gpu_lib, oracle_lib, name):
+    torch = pytest.importorskip("torch")
+    from oracle import Oracle
+    cfg = HOST_CFGS[name]()
+    o = Oracle(cfg)
+    H = api.Handle(cfg, tpq=o.tpq)
+    y = _phase_points(o, name, 161, 12)     # odd: the last warp has one point
+    ipes = np.arange(len(y), dtype=np.int32) % len(cfg.surfaces)
+    dev = torch.device("cuda")
+    yd = torch.from_numpy(np.ascontiguousarray(y)).to(dev)
+    ipd = torch.from_numpy(ipes).to(dev)
+    ypd = torch.zeros_like(yd)
+    Hd = torch.zeros(len(y), dtype=torch.float64, device=dev)
+    Rd = torch.zeros((len(y), 3), dtype=torch.float64, device=dev)
+    H.check(H.lib.cair_internal_warp_eval(H.h, len(y), ipd.data_ptr(), yd.data_ptr(), ypd.data_ptr(), Hd.data_ptr(),
+                                          Rd.data_ptr()), "cair_internal_warp_eval")
+    yp, h, ri = ypd.cpu().numpy(), Hd.cpu().numpy(), Rd.cpu().numpy()
+    yp_o = o.rhs(y, ipes=ipes)
+    R, _ = o.rp(y[:, 6:])
+    cs = o.condition_scale(R, ipes=ipes)
+    sc = np.maximum(1e-12 * np.abs(yp_o).max(axis=1, keepdims=True), ROUND_U * cs[:, 1:].max(axis=1, keepdims=True))
+    print("%s warp programs on the GPU: worst/bound %.2e" % (name, (np.abs(yp - yp_o) / sc).max()))
+    assert np.all(np.abs(yp - yp_o) <= sc)
+    h_o, r_o = o.hamiltonian(y, ipes=ipes)
+    hs = np.maximum(1e-12 * np.maximum(np.abs(h_o), 0.1), ROUND_U * cs[:, 0])
+    assert np.all(np.abs(h - h_o) <= hs)
+    assert np.allclose(ri, r_o, rtol=4e-16, atol=0)
+    H.close()
+
+
+def _end_to_end(name, n, seed=None, **kw):
+    cfg, o, H = _setup(name, **kw)
+    H.integrator_mode = "warp"
+    assert H.integrator_mode == "warp"
+    ic = _ics(o, name, n, seed=seed)
+    ref = o.integrate(ic["paq"], ic["erra"], procs=PROCS)
+    pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"], procs=PROCS)
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.Integrator(H).Integrate(tr)
+    assert np.all(tr.status == 0) and np.all(ref["status"] == 0)
+    assert np.max(np.abs(tr.H - ic["H0"])) < cfg.ham_abs_tol
+    Jo, vo, ao = _final_qn(o.analyze(o.apply_transformation(ref["paq"])))
+    Jp, vp, ap = _final_qn(o.analyze(o.apply_transformation(pert["paq"])))
+    Jg, vg, ag = _gpu_final_qn(api.MolecularState(H).FindState(api.Collision(H).ApplyTransformation(tr.paq)))
+    same = (Jo == Jg) & (vo == vg) & (ao == ag)
+    stable = (Jo == Jp) & (vo == vp) & (ao == ap)
+    c = H.counters()
+    return cfg, H, tr, ref, same, stable, c
+
+
+@pytest.mark.parametrize("name", ["O3", "N3"])
+def test_warp_integrator_end_to_end(gpu_lib, oracle_lib, name):
+    """Same bar as the thread integrator's end-to-end test: >= 99.5 % of the oracle-stable
+    trajectories end in the oracle's (v, J, arrangement), overall no worse than the oracle's own
+    reproducibility minus 1 %; the attempt counters add up."""
+    cfg, H, tr, ref, same, stable, c = _end_to_end(name, 400)
+    print("%s warp integrator: GPU vs oracle %.4f overall, %.4f on oracle-stable (%.4f stable); attempts %d vs %d" %
+          (name, same.mean(), same[stable].mean(), stable.mean(), int(np.sum(tr.iste + tr.irej)),
+           int(np.sum(ref["iste"] + ref["irej"])) if "iste" in ref else -1))
+    assert same[stable].mean() >= 0.995
+    assert same.mean() >= stable.mean() - 0.01
+    assert c["attempts"] == int(np.sum(tr.iste + tr.irej))
+    assert c["grad_evals"] == 13 * c["attempts"]
+    H.close()
+
+
+@pytest.mark.parametrize("nsteps", [2, 4])
+def test_warp_integrator_other_step_counts(gpu_lib, oracle_lib, nsteps):
+    cfg, H, tr, ref, same, stable, c = _end_to_end("N3", 64, seed=4321, nsteps=nsteps)
+    assert stable.sum() >= 48
+    assert np.all(same[stable])
+    nseq = {2: 1 + 2 + 4, 4: 1 + 2 + 4 + 6 + 8}[nsteps]
+    assert c["grad_evals"] == nseq * c["attempts"]
+    H.close()
+
+
+def test_warp_mode_refused_where_not_built(gpu_lib):
+    for cfg in (systems.o3nn_config(), systems.o4_config()):
+        H = api.Handle(cfg)
+        with pytest.raises(api.CairError, match="CAIR_EUNSUPPORTED"):
+            H.integrator_mode = "warp"
+        assert H.integrator_mode == "thread"
+        H.close()
