@@ -113,7 +113,7 @@ class Handle:
     @property
     def integrator_mode(self):
         """"thread" (a lane per trajectory, the default) or "warp" (a warp per trajectory: the latency
-        mode for small jobs, O3 and N3 UMN surfaces)."""
+        mode for small jobs; O3, N3, O4 and N4 UMN surfaces)."""
         return "warp" if self.lib.cair_get_integrator_mode(self.h) == _lib.INTEGRATOR_WARP else "thread"
 
     @integrator_mode.setter

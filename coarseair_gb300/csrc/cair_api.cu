@@ -641,7 +641,7 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_
     A.rec_rcut = h->rec_rcut;
   }
   if (!h->sur && h->mode == CAIR_INTEGRATOR_WARP) {
-    // a warp per trajectory: CTAs of warp_cta_warps() warps, as many as fit on every SM
+    // a warp per trajectory: CTAs of warp_cta_warps(S) warps, as many as fit on every SM
     cudaEvent_t w0 = nullptr, w1 = nullptr;
     if (h->time_integrate) {
       if (2 * h->ntev + 2 > h->tev.size()) {
@@ -1088,8 +1088,8 @@ int cair_set_integrator_mode(cair_handle* h, int32_t mode) {
     return fail(h, CAIR_EINVAL, "cair_set_integrator_mode: mode must be CAIR_INTEGRATOR_THREAD or _WARP");
   if (mode == CAIR_INTEGRATOR_WARP && !warp_integrate_supported(h->sys))
     return fail(h, CAIR_EUNSUPPORTED,
-                "cair_set_integrator_mode: the warp integrator is built for the O3 and N3 UMN surfaces (one model "
-                "per handle) with NSteps 2..4");
+                "cair_set_integrator_mode: the warp integrator is built for the O3, N3, O4 and N4 UMN surfaces with "
+                "their own diatomics (one model per handle) and NSteps 2..4");
   h->mode = mode;
   return 0;
 }

@@ -12,8 +12,10 @@ namespace cair {
 enum { WK_SOP = 0, WK_EXP = 1, WK_RSQRT = 2, WK_RECIP = 3 };
 enum { WS_LIT = 0, WS_TPQ = 1, WS_MMIMN = 2, WS_O2AB = 3, WS_COEF = 4, WS_PES = 5 };
 
-// One program: nlev levels of 16 records of 4 words (lane l of level L executes record 16 L + l):
-// w0 = active << 31 | kind << 28 | nterm << 24 | out slot; w1..w3 = terms a | sign << 15 | b << 16.
+// One program: nlev levels of W records of 8 words (lane l of level L executes record W L + l, W the
+// model's group width): w0 = active << 31 | kind << 28 | nterm << 24 | signed << 23 | term signs << 20
+// (nterm and `signed` uniform over the level), w1 = result byte offset, w2..w7 = byte offsets of the
+// factors a0, b0, a1, b1, a2, b2.
 struct WProg {
   const unsigned* rec;
   int nlev;
@@ -39,15 +41,37 @@ struct WModel {
         wp_##key##_grad_in, wp_##key##_grad_out, wp_##key##_energy_in, wp_##key##_energy_out                   \
   }
 
-// Surface models that have programs (3-atom UMN surfaces).
+// Surface models that have programs (the UMN surfaces), and the diatomic their programs evaluate.
 __host__ __device__ constexpr bool warp_model_built(int model) {
-  return model == CAIR_PES_O3_UMN || model == CAIR_PES_N3_UMN;
+  return model == CAIR_PES_O3_UMN || model == CAIR_PES_N3_UMN || model == CAIR_PES_O4_UMN ||
+         model == CAIR_PES_N4_UMN;
 }
+__host__ __device__ constexpr int warp_model_diat(int model) {
+  return (model == CAIR_PES_O3_UMN || model == CAIR_PES_O4_UMN) ? CAIR_DIAT_O2_UMN : CAIR_DIAT_N2_UMN_FORN4;
+}
+
+// Per model: lanes of the group that evaluates one right-hand side (16: a half-warp, so the two
+// halves of a warp run different midpoint sequences; 32: the whole warp, NE = 18 equations),
+// slots of a group, and the levels of the grad and energy programs.
+template <int MODEL>
+struct WCfg {
+  static constexpr int W = MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_LANES : MODEL == CAIR_PES_N3_UMN ? WP_N3_UMN_LANES
+                           : MODEL == CAIR_PES_O4_UMN ? WP_O4_UMN_LANES : WP_N4_UMN_LANES;
+  static constexpr int NSLOT = MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_NSLOT : MODEL == CAIR_PES_N3_UMN ? WP_N3_UMN_NSLOT
+                               : MODEL == CAIR_PES_O4_UMN ? WP_O4_UMN_NSLOT : WP_N4_UMN_NSLOT;
+  static constexpr int NLEV = MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_GRAD_NLEV + WP_O3_UMN_ENERGY_NLEV
+                              : MODEL == CAIR_PES_N3_UMN ? WP_N3_UMN_GRAD_NLEV + WP_N3_UMN_ENERGY_NLEV
+                              : MODEL == CAIR_PES_O4_UMN ? WP_O4_UMN_GRAD_NLEV + WP_O4_UMN_ENERGY_NLEV
+                                                         : WP_N4_UMN_GRAD_NLEV + WP_N4_UMN_ENERGY_NLEV;
+  static constexpr int NG = 32 / W;  // groups per warp
+};
 
 template <int MODEL>
 __device__ __forceinline__ WModel wmodel() {
   if (MODEL == CAIR_PES_O3_UMN) return CAIR_WMODEL(o3_umn, O3_UMN);
-  return CAIR_WMODEL(n3_umn, N3_UMN);
+  if (MODEL == CAIR_PES_N3_UMN) return CAIR_WMODEL(n3_umn, N3_UMN);
+  if (MODEL == CAIR_PES_O4_UMN) return CAIR_WMODEL(o4_umn, O4_UMN);
+  return CAIR_WMODEL(n4_umn, N4_UMN);
 }
 
 // Value of constant slot i for surface P.  Hoisted slots (source 255) are the const program's.
@@ -65,38 +89,56 @@ __device__ __forceinline__ double wp_const(const WModel& m, const DevSys& S, con
   }
 }
 
-// One record: a sum of up to three signed products (a multiply, then fused multiply-adds in term
-// order), the table-driven exponential, a reciprocal square root or a reciprocal.  The operands of
-// every term are loaded before the arithmetic starts.
-// The term's sign goes on the first factor's sign bit with an integer XOR: a per-lane select of -a
-// would cost an FP64 instruction (a negation on the FP64 pipe) per term.
-__device__ __forceinline__ double wp_signed(double a, unsigned w) {
-  return __hiloint2double(__double2hiint(a) ^ (int)((w & 0x8000u) << 16), __double2loint(a));
+// One record: a sum of up to three products (a multiply, then fused multiply-adds in term order; a
+// term's sign, where the generator could not fold it into a constant factor, goes on the first
+// factor's sign bit with an integer XOR, off the FP64 pipe), the table-driven exponential, a
+// reciprocal square root or a reciprocal.  The term count and whether signs are present are the same
+// for every lane of a level, so its branches are uniform.
+__device__ __forceinline__ double wp_ld(const char* sb, unsigned off) {
+  return *reinterpret_cast<const double*>(sb + off);
+}
+__device__ __forceinline__ double wp_flip(double a, unsigned meta, int j) {
+  return __hiloint2double(__double2hiint(a) ^ (int)((meta << (11 - j)) & 0x80000000u), __double2loint(a));
 }
 
-__device__ __forceinline__ double wp_eval(unsigned w0, unsigned w1, unsigned w2, unsigned w3, const double* s) {
-  const unsigned kind = (w0 >> 28) & 3u;
+__device__ __forceinline__ double wp_eval(uint4 c0, uint4 c1, const char* sb) {
+  const unsigned meta = c0.x, kind = (meta >> 28) & 3u;
   if (kind == WK_SOP) {
-    const unsigned nt = (w0 >> 24) & 3u;
-    const double a0 = wp_signed(s[w1 & 0x7fffu], w1), b0 = s[w1 >> 16];
-    const double a1 = wp_signed(s[w2 & 0x7fffu], w2), b1 = s[w2 >> 16];
-    const double a2 = wp_signed(s[w3 & 0x7fffu], w3), b2 = s[w3 >> 16];
+    const unsigned nt = (meta >> 24) & 3u;
+    const bool sg = (meta >> 23) & 1u;
+    double a0 = wp_ld(sb, c0.z);
+    const double b0 = wp_ld(sb, c0.w);
+    if (sg) a0 = wp_flip(a0, meta, 0);
     double r = a0 * b0;
-    if (nt > 1) r = fma(a1, b1, r);
-    if (nt > 2) r = fma(a2, b2, r);
+    if (nt > 1) {
+      double a1 = wp_ld(sb, c1.x);
+      const double b1 = wp_ld(sb, c1.y);
+      if (sg) a1 = wp_flip(a1, meta, 1);
+      r = fma(a1, b1, r);
+    }
+    if (nt > 2) {
+      double a2 = wp_ld(sb, c1.z);
+      const double b2 = wp_ld(sb, c1.w);
+      if (sg) a2 = wp_flip(a2, meta, 2);
+      r = fma(a2, b2, r);
+    }
     return r;
   }
-  const double x = s[w1 & 0x7fffu];
+  const double x = wp_ld(sb, c0.z);
   if (kind == WK_EXP) return fexp(x);
   if (kind == WK_RSQRT) return rsqrt(x);
   return 1.0 / x;
 }
 
 // A whole program by one thread (the host harness), record after record.
-__device__ __forceinline__ void wp_run_serial(const WProg& p, double* s) {
-  for (int r = 0; r < 16 * p.nlev; ++r) {
-    const unsigned* w = p.rec + 4 * r;
-    if (w[0] >> 31) s[w[0] & 0xffffu] = wp_eval(w[0], w[1], w[2], w[3], s);
+__device__ __forceinline__ void wp_run_serial(const WProg& p, int width, double* s) {
+  char* sb = reinterpret_cast<char*>(s);
+  for (int r = 0; r < width * p.nlev; ++r) {
+    const unsigned* w = p.rec + 8 * r;
+    if (w[0] >> 31) {
+      const uint4 c0 = {w[0], w[1], w[2], w[3]}, c1 = {w[4], w[5], w[6], w[7]};
+      *reinterpret_cast<double*>(sb + w[1]) = wp_eval(c0, c1, sb);
+    }
   }
 }
 

@@ -35,7 +35,6 @@ import struct
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.abspath(os.path.join(HERE, ".."))
-LANES = 16          # lanes of a half-warp: instructions per level
 SPLIT = 3           # sums with more terms are split into partial sums (a record holds 3 terms)
 COST = {"sop": None, "exp": 12, "rsqrt": 8, "recip": 10}
 KIND = {"sop": 0, "exp": 1, "rsqrt": 2, "recip": 3}
@@ -364,20 +363,65 @@ def pes_n3(g, R, tabs):
     return V, dVdR
 
 
-SURFACES = {"o3_umn": pes_o3, "n3_umn": pes_n3}
+def pes_o4(g, R, tabs):
+    """pes_o4 (O4 UMN): MEG variables of the six pairs, the O4 PIP, six O2 UMN diatomics."""
+    A = o2_coefficients()
+    x, vd, rang = [], [], []
+    for i in range(6):
+        ra = R[i] * B_TO_ANG
+        rang.append(ra)
+        d1 = ra - g.const("pes", PES_FIELD["ra"])
+        d2 = ra - g.const("pes", PES_FIELD["rb"])
+        x.append(fexp(-(d1 * g.const("pes", PES_FIELD["inv_a"])) - (d2 * d2) * g.const("pes", PES_FIELD["inv_ab"])))
+        vd.append(o2_umn(g, R[i], A))
+    vdiat = g.lit(0.0)
+    for v in vd:
+        vdiat = vdiat + v
+    vp = pip_value(g, tabs["O4"], x, lambda i: g.const("coef", i), 0.0)
+    V = vp * KCM_TO_HARTREE + vdiat
+    gp = g.grad(vp, rang)
+    dVdR = [(gp[i] * KCM_TO_HARTREE) * B_TO_ANG + g.grad(vd[i], [R[i]])[0] for i in range(6)]
+    return V, dVdR
 
 
-def system3(g, ne=12):
-    """Inputs y = [p(6), q(6)]; Tpq products, the third atom and the pair distances (rp3)."""
-    nv = ne // 2
-    y = [g.inp(i) for i in range(ne)]
+def pes_n4(g, R, tabs):
+    """pes_n4 (N4 UMN): the N4 PIP on all six MEG variables, six N2 UMN_ForN4 diatomics."""
+    x, vd, rang = [], [], []
+    for i in range(6):
+        ra = R[i] * B_TO_ANG
+        rang.append(ra)
+        d = ra - 1.098
+        x.append(fexp(-d - (d * d) * (1.0 / 1.5)))
+        vd.append(n2_umn(g, R[i]))
+    vdiat = g.lit(0.0)
+    for v in vd:
+        vdiat = vdiat + v
+    vp = pip_value(g, tabs["N4"], x, lambda i: g.const("coef", i), 457.4)
+    V = (vp * KCM_TO_HARTREE + 0.0) + vdiat
+    gp = g.grad(vp, rang)
+    dVdR = [(gp[i] * KCM_TO_HARTREE) * B_TO_ANG + g.grad(vd[i], [R[i]])[0] for i in range(6)]
+    return V, dVdR
+
+
+# surface -> (formula, atoms, lanes of the group that evaluates one right-hand side)
+MODELS = {"o3_umn": (pes_o3, 3, 16), "n3_umn": (pes_n3, 3, 16), "o4_umn": (pes_o4, 4, 32), "n4_umn": (pes_n4, 4, 32)}
+
+
+def system(g, natoms):
+    """Inputs y = [p(NV), q(NV)]; the last atom's position and the pair distances (rp3 / rp4)."""
+    nv = 3 * (natoms - 1)
+    y = [g.inp(i) for i in range(2 * nv)]
     p, q = y[:nv], y[nv:]
     Q = list(q) + [None] * 3
-    m1, m2 = g.const("mmimn", 0), g.const("mmimn", 1)
+    m = [g.const("mmimn", i) for i in range(natoms - 1)]
     for c in range(3):
-        Q[6 + c] = m1 * Q[c] + m2 * Q[3 + c]
+        acc = m[0] * Q[c]
+        for i in range(1, natoms - 1):
+            acc = acc + m[i] * Q[3 * i + c]
+        Q[nv + c] = acc
+    pairs = [(a, b) for a in range(natoms) for b in range(a + 1, natoms)]
     R, Ri = [], []
-    for a, b in ((0, 1), (0, 2), (1, 2)):
+    for a, b in pairs:
         d = [Q[3 * a + c] - Q[3 * b + c] for c in range(3)]
         s2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
         ri = rsqrt(s2)
@@ -386,10 +430,35 @@ def system3(g, ne=12):
     return y, p, q, Q, R, Ri
 
 
-def rhs3(g, surface, tabs):
-    """Rhs (Hamilton's equations): [-dV/dQ (6), Tpq p (6)]."""
-    y, p, q, Q, R, Ri = system3(g)
-    nv = 6
+def trans_to_cart(g, natoms, Ri, Q, dVdR):
+    """trans_to_cart_3 / trans_to_cart_4: dV/dQ of the NV relative coordinates."""
+    if natoms == 3:
+        d0, d1, d2 = dVdR[0] * Ri[0], dVdR[1] * Ri[1], dVdR[2] * Ri[2]
+        m1, m2 = g.const("mmimn", 0), g.const("mmimn", 1)
+        a1, b1, a2, b2 = (1.0 - m1) * d1, m1 * d2, m2 * d1, (1.0 - m2) * d2
+        m = [None] * 6
+        for c in range(3):
+            X0, X1, X2 = Q[c] - Q[3 + c], Q[c] - Q[6 + c], Q[3 + c] - Q[6 + c]
+            m[c] = d0 * X0 + a1 * X1 - b1 * X2
+            m[3 + c] = -(d0 * X0) - a2 * X1 + b2 * X2
+        return m
+    d = [dVdR[i] * Ri[i] for i in range(6)]
+    m1, m2, m3 = g.const("mmimn", 0), g.const("mmimn", 1), g.const("mmimn", 2)
+    m = [None] * 9
+    for c in range(3):
+        X0, X1, X2 = Q[c] - Q[3 + c], Q[c] - Q[6 + c], Q[c] - Q[9 + c]
+        X3, X4, X5 = Q[3 + c] - Q[6 + c], Q[3 + c] - Q[9 + c], Q[6 + c] - Q[9 + c]
+        m[c] = d[0] * X0 + d[1] * X1 + (1.0 - m1) * d[2] * X2 - m1 * d[4] * X4 - m1 * d[5] * X5
+        m[3 + c] = -(d[0] * X0) - m2 * d[2] * X2 + d[3] * X3 + (1.0 - m2) * d[4] * X4 - m2 * d[5] * X5
+        m[6 + c] = -(d[1] * X1) - m3 * d[2] * X2 - d[3] * X3 - m3 * d[4] * X4 + (1.0 - m3) * d[5] * X5
+    return m
+
+
+def rhs(g, surface, tabs):
+    """Rhs (Hamilton's equations): [-dV/dQ (NV), Tpq p (NV)]."""
+    fn, natoms, _ = MODELS[surface]
+    y, p, q, Q, R, Ri = system(g, natoms)
+    nv = len(p)
     dq = []
     for j in range(nv):
         i0 = j % 3
@@ -397,23 +466,16 @@ def rhs3(g, surface, tabs):
         for i in range(i0 + 3, nv, 3):
             acc = acc + g.const("tpq", j + 9 * i) * p[i]
         dq.append(acc)
-    V, dVdR = SURFACES[surface](g, R, tabs)
-    # trans_to_cart_3
-    d0, d1, d2 = dVdR[0] * Ri[0], dVdR[1] * Ri[1], dVdR[2] * Ri[2]
-    m1, m2 = g.const("mmimn", 0), g.const("mmimn", 1)
-    a1, b1, a2, b2 = (1.0 - m1) * d1, m1 * d2, m2 * d1, (1.0 - m2) * d2
-    m = [None] * 6
-    for c in range(3):
-        X0, X1, X2 = Q[c] - Q[3 + c], Q[c] - Q[6 + c], Q[3 + c] - Q[6 + c]
-        m[c] = d0 * X0 + a1 * X1 - b1 * X2
-        m[3 + c] = -(d0 * X0) - a2 * X1 + b2 * X2
+    V, dVdR = fn(g, R, tabs)
+    m = trans_to_cart(g, natoms, Ri, Q, dVdR)
     return [-m[i] for i in range(nv)] + dq
 
 
-def energy3(g, surface, tabs):
-    """hamiltonian: [H, 1/R_1, 1/R_2, 1/R_3]."""
-    y, p, q, Q, R, Ri = system3(g)
-    nv = 6
+def energy(g, surface, tabs):
+    """hamiltonian: [H, 1/R_p for every pair]."""
+    fn, natoms, _ = MODELS[surface]
+    y, p, q, Q, R, Ri = system(g, natoms)
+    nv = len(p)
     h = g.lit(0.0)
     for i in range(nv):
         j0 = i % 3
@@ -421,7 +483,7 @@ def energy3(g, surface, tabs):
         for j in range(j0 + 3, nv, 3):
             eki = eki + g.const("tpq", j + 9 * i) * p[j]
         h = h + p[i] * eki
-    V, _ = SURFACES[surface](g, R, tabs)
+    V, _ = fn(g, R, tabs)
     return [h * 0.5 + V] + Ri
 
 
@@ -525,8 +587,42 @@ def lower(g, outputs, ninputs):
         return r
     for n in sorted(ins):
         is_const(n)
-    # splitting of long sums (new nodes get negative ids)
+    # signs onto constant factors: a negative term takes -1 (for a sum's term x * 1), or the negated
+    # constant (a literal, or a hoisted negation of a surface / system constant), so that the only
+    # signed terms left multiply two variables
     nxt = [-1]
+    minus_one = g.lit(-1.0).n
+    negs = {}
+
+    def const_operand(x):
+        return (x >= 0 and ops[x][0] in ("lit", "const")) or const_node.get(x, False)
+
+    def negated(x):
+        if x >= 0 and ops[x][0] == "lit":
+            return g.lit(-struct.unpack("<d", ops[x][2])[0]).n
+        if x not in negs:
+            m = nxt[0]
+            nxt[0] -= 1
+            ins[m] = ("sop", [(1, x, minus_one)])
+            const_node[m] = True
+            negs[x] = m
+        return negs[x]
+    for n in sorted(list(ins)):
+        kind, opd = ins[n]
+        if kind != "sop":
+            continue
+        terms = []
+        for sg, a, b in opd:
+            if sg < 0:
+                if b == one:
+                    b, sg = minus_one, 1
+                elif const_operand(b):
+                    b, sg = negated(b), 1
+                elif const_operand(a):
+                    a, sg = negated(a), 1
+            terms.append((sg, a, b))
+        ins[n] = ("sop", terms)
+    # splitting of long sums (new nodes get negative ids)
     for n in sorted(list(ins)):
         kind, opd = ins[n]
         if kind != "sop" or len(opd) <= SPLIT:
@@ -611,18 +707,10 @@ def topo_order(nodes, deps):
     return order
 
 
-def build(surface, tabs):
-    """grad, energy and const programs of one surface over one slot layout."""
-    progs = {}
-    for name, fn in (("grad", rhs3), ("energy", energy3)):
-        g = Graph()
-        outs = fn(g, surface, tabs)
-        progs[name] = (g, outs)
-    return progs
-
-
 def compile_model(surface, tabs):
     """Lower both programs; merge their constants and hoisted nodes into one const program."""
+    _, natoms, lanes = MODELS[surface]
+    ne = 6 * (natoms - 1)
     res = {}
     const_atoms = {}   # key (src, idx) or ('lit', bits) -> slot
     const_list = []    # (src, idx, value)
@@ -632,14 +720,15 @@ def compile_model(surface, tabs):
             const_atoms[key] = len(const_list)
             const_list.append((src, idx, val))
         return const_atoms[key]
-    # the constant 1.0 first: SOP terms of sums use it as their second factor
+    # the constant 1.0 first: SOP terms of sums use it as their second factor; 0.0 pads records
     cslot(("lit", _bits(1.0)), SRC["lit"], 0, 1.0)
+    zero = cslot(("lit", _bits(0.0)), SRC["lit"], 0, 0.0)
     hoisted_all = []   # (program name, node) for the const program, program-local ids mapped later
     lowered = {}
     for name in ("grad", "energy"):
         g = Graph()
-        outs = (rhs3 if name == "grad" else energy3)(g, surface, tabs)
-        ins, cnode, one = lower(g, outs, 12)
+        outs = (rhs if name == "grad" else energy)(g, surface, tabs)
+        ins, cnode, one = lower(g, outs, ne)
         lowered[name] = (g, outs, ins, cnode, one)
     # slot map per program: atoms (lits / consts) shared, hoisted nodes in the const region
     out = {}
@@ -665,7 +754,7 @@ def compile_model(surface, tabs):
             slot[n] = cslot(("hoist", name, n), -1, 0)
     nconst = len(const_list)
     # inputs follow the constants
-    ninp = 12
+    ninp = ne
     base_in = nconst
     progs = {}
     cprog_levels = []
@@ -680,7 +769,7 @@ def compile_model(surface, tabs):
             if ops[n][0] == "in":
                 slot[n] = base_in + ops[n][2]
         body = [n for n in ins if not cnode.get(n, False)]
-        levels = schedule(ins, body, LANES)
+        levels = schedule(ins, body, lanes)
         # liveness: last level reading each value; outputs live to the end
         lvl_of = {}
         for L, (k, nodes) in enumerate(levels):
@@ -712,39 +801,44 @@ def compile_model(surface, tabs):
         progs[name] = dict(levels=levels, ins=ins, slot=slot, outs=[slot[o] for o in outset],
                            ins_slots=[base_in + i for i in range(ninp)], nslot=nslot)
     nslot = max(p["nslot"] for p in progs.values())
-    return dict(progs=progs, const_list=const_list, nconst=nconst, cprog=cprog_levels, nslot=nslot)
+    return dict(progs=progs, const_list=const_list, nconst=nconst, cprog=cprog_levels, nslot=nslot, lanes=lanes,
+                zero=zero)
 
 
 # ----------------------------------------------------------------------------------------------
 # Emission: one 16-byte record per lane and level
 # ----------------------------------------------------------------------------------------------
-def records(levels, ins, slot, width=LANES):
+def records(levels, ins, slot, width, zero):
     """Levels of more than `width` instructions are cut into several; lane l of level L executes
-    record L * width + l:  w0 = active << 31 | kind << 28 | nterm << 24 | out slot, w1..w3 = terms
-    a | sign << 15 | b << 16 ((+-) s[a] * s[b]; a special instruction's operand is term 0's a)."""
+    record L * width + l, 8 words:  w0 = active << 31 | kind << 28 | nt << 24 | signed << 23 |
+    sign of term j << (20 + j), nt and `signed` the same for every record of the level (the most
+    terms of its sums, whether any term still carries a sign); w1 = byte offset of the result;
+    w2..w7 = byte offsets of the factors a_j, b_j of the terms (+-) s[a_j] * s[b_j], missing terms
+    0 * 0 (a special instruction's operand is w2)."""
     out = []
     for kind, nl in levels:
         for c in range(0, len(nl), width):
             chunk = nl[c:c + width]
+            ntm = max((len(ins[n][1]) if ins[n][0] == "sop" else 1) for n in chunk)
+            sgn = any(t[0] < 0 for n in chunk if ins[n][0] == "sop" for t in ins[n][1])
             for lane in range(width):
                 if lane >= len(chunk):
-                    out += [0, 0, 0, 0]
+                    out += [0] * 8
                     continue
                 n = chunk[lane]
                 k, opd = ins[n]
-                w = [0, 0, 0, 0]
+                w = [0, 8 * slot[n]] + [8 * zero] * 6
+                meta = (1 << 31) | (KIND[k] << 28) | (ntm << 24) | ((1 << 23) if sgn else 0)
                 if k == "sop":
                     assert 1 <= len(opd) <= 3
                     for j, (sg, x, y) in enumerate(opd):
-                        sa, sb = slot[x], slot[y]
-                        assert sa < 0x8000 and sb < 0x10000
-                        w[1 + j] = sa | (0x8000 if sg < 0 else 0) | (sb << 16)
-                    nt = len(opd)
+                        w[2 + 2 * j], w[3 + 2 * j] = 8 * slot[x], 8 * slot[y]
+                        if sg < 0:
+                            meta |= 1 << (20 + j)
                 else:
-                    w[1] = slot[opd[0]]
-                    nt = 1
-                assert slot[n] < 0x10000
-                w[0] = (1 << 31) | (KIND[k] << 28) | (nt << 24) | slot[n]
+                    w[2] = 8 * slot[opd[0]]
+                assert max(w[1:]) < (1 << 20)
+                w[0] = meta
                 out += w
     return out
 
@@ -765,10 +859,11 @@ def arr(ctype, name, vals, align=None):
 def emit(models, path):
     L = ["/* Lane-parallel right-hand-side programs of the warp integrator (cair_warp.cu).",
          " * Generated by csrc/gen/gen_warp.py, do not edit.",
-         " * A program is NLEV levels of 16 records of 4 words, lane l of level L executing record 16 L + l:",
-         " * w0 = active << 31 | kind << 28 | nterm << 24 | out slot (kind 0 sum of products, 1 exp, 2 rsqrt,",
-         " * 3 reciprocal); w1..w3 = terms a | sign << 15 | b << 16, (+-) s[a] * s[b] (a special's operand is",
-         " * w1's a). */",
+         " * A program is NLEV levels of W records of 8 words (W the model's LANES), lane l of level L executing",
+         " * record W L + l: w0 = active << 31 | kind << 28 | nterm << 24 | signed << 23 | term signs << 20 (kind",
+         " * 0 sum of products, 1 exp, 2 rsqrt, 3 reciprocal; nterm and signed uniform over the level),",
+         " * w1 = result byte offset, w2..w7 = byte offsets of a0, b0, a1, b1, a2, b2: sum_j (+-) s[a_j] * s[b_j]",
+         " * (a special's operand is w2). */",
          "#pragma once", ""]
     for key, m in models.items():
         P = m["progs"]
@@ -780,6 +875,7 @@ def emit(models, path):
             L.append(" * %-6s: %d levels, %d instructions, %d FP64 operations, critical path %d" %
                      (name, len(P[name]["levels"]), nins, flops, crit))
         L.append(" */")
+        L.append("#define WP_%s_LANES %d" % (key.upper(), m["lanes"]))
         L.append("#define WP_%s_NSLOT %d" % (key.upper(), m["nslot"]))
         L.append("#define WP_%s_NCONST %d" % (key.upper(), m["nconst"]))
         cs = [c[0] if c[0] >= 0 else 255 for c in m["const_list"]]
@@ -791,13 +887,13 @@ def emit(models, path):
         # const program: the hoisted nodes of both programs
         rec = []
         for pname, lv, ins, slot, g in m["cprog"]:
-            rec += records(lv, ins, slot)
-        L.append("#define WP_%s_CPROG_NLEV %d" % (key.upper(), len(rec) // (4 * LANES)))
+            rec += records(lv, ins, slot, m["lanes"], m["zero"])
+        L.append("#define WP_%s_CPROG_NLEV %d" % (key.upper(), len(rec) // (8 * m["lanes"])))
         L.append(arr("unsigned int", "wp_%s_cprog_rec" % key, rec, 16))
         for name in ("grad", "energy"):
             p = P[name]
-            rec = records(p["levels"], p["ins"], p["slot"])
-            L.append("#define WP_%s_%s_NLEV %d" % (key.upper(), name.upper(), len(rec) // (4 * LANES)))
+            rec = records(p["levels"], p["ins"], p["slot"], m["lanes"], m["zero"])
+            L.append("#define WP_%s_%s_NLEV %d" % (key.upper(), name.upper(), len(rec) // (8 * m["lanes"])))
             L.append(arr("unsigned int", "wp_%s_%s_rec" % (key, name), rec, 16))
             L.append(arr("unsigned short", "wp_%s_%s_in" % (key, name), p["ins_slots"]))
             L.append(arr("unsigned short", "wp_%s_%s_out" % (key, name), p["outs"]))
@@ -809,7 +905,7 @@ def emit(models, path):
 def main():
     tabs = json.load(open(os.path.join(CSRC, "generated", "pip_tables.json")))
     models = {}
-    for key in ("o3_umn", "n3_umn"):
+    for key in MODELS:
         models[key] = compile_model(key, tabs)
         for name in ("grad", "energy"):
             p = models[key]["progs"][name]

@@ -474,8 +474,9 @@ int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm)
  * CAIR_INTEGRATOR_WARP: a warp integrates one trajectory -- its half-warps run the modified-midpoint
  * sequences of an attempt side by side and its lanes evaluate each right-hand side together -- the
  * latency mode for small jobs, whose time is their longest trajectory's.  Same queue, end check and
- * outputs; built for the O3 and N3 UMN surfaces (one surface model per handle), NSteps 2..4; any
- * other system returns CAIR_EUNSUPPORTED.  An attached surrogate takes precedence over either. */
+ * outputs; built for the O3, N3, O4 and N4 UMN surfaces with their own diatomics (one surface model
+ * per handle; diatom + diatom runs its sequences on the whole warp), NSteps 2..4; any other system
+ * returns CAIR_EUNSUPPORTED.  An attached surrogate takes precedence over either. */
 #define CAIR_INTEGRATOR_THREAD 0
 #define CAIR_INTEGRATOR_WARP 1
 int cair_set_integrator_mode(cair_handle* h, int32_t mode);

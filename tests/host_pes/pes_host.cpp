@@ -38,6 +38,9 @@ static inline T __ldg(const T* p) {
 static inline double rsqrt(double x) { return 1.0 / std::sqrt(x); }
 using std::max;
 using std::min;
+struct uint4 {
+  unsigned x, y, z, w;
+};
 // one host "thread" that owns a 1 x 1 grid: the kernels' grid-stride loops then visit every element
 struct HostDim {
   unsigned x, y, z;
@@ -361,10 +364,11 @@ extern "C" int pes_host_eval(const void* devsys, const double* packed, const int
 
 // The warp integrator's lane-parallel programs run one instruction after the other: constants of each
 // point's surface, the const program, then the grad program (y -> dy/dt) and the energy program
-// (y -> H, 1/R_p) at n phase-space points y[n][12].
+// (y -> H, 1/R_p) at n phase-space points y[n][NE].
 template <int MODEL>
 static void warp_eval(const DevSys& S, int64_t n, const int32_t* ipes, const double* y, double* yp, double* H,
                       double* Ri) {
+  constexpr int NE = Traits<MODEL>::NE, NP = Traits<MODEL>::NP, W = WCfg<MODEL>::W;
   const WModel M = wmodel<MODEL>();
   std::vector<double> s(M.nslot);
   int loaded = -1;
@@ -372,16 +376,16 @@ static void warp_eval(const DevSys& S, int64_t n, const int32_t* ipes, const dou
     const int ip = ipes ? ipes[k] : 0;
     if (ip != loaded) {
       for (int i = 0; i < M.nconst; ++i) s[i] = wp_const(M, S, S.pes[ip], i);
-      wp_run_serial(M.cprog, s.data());
+      wp_run_serial(M.cprog, W, s.data());
       loaded = ip;
     }
-    for (int i = 0; i < 12; ++i) s[M.gin[i]] = y[12 * k + i];
-    wp_run_serial(M.grad, s.data());
-    for (int i = 0; i < 12; ++i) yp[12 * k + i] = s[M.gout[i]];
-    for (int i = 0; i < 12; ++i) s[M.ein[i]] = y[12 * k + i];
-    wp_run_serial(M.energy, s.data());
+    for (int i = 0; i < NE; ++i) s[M.gin[i]] = y[NE * k + i];
+    wp_run_serial(M.grad, W, s.data());
+    for (int i = 0; i < NE; ++i) yp[NE * k + i] = s[M.gout[i]];
+    for (int i = 0; i < NE; ++i) s[M.ein[i]] = y[NE * k + i];
+    wp_run_serial(M.energy, W, s.data());
     H[k] = s[M.eout[0]];
-    for (int p = 0; p < 3; ++p) Ri[3 * k + p] = s[M.eout[1 + p]];
+    for (int p = 0; p < NP; ++p) Ri[NP * k + p] = s[M.eout[1 + p]];
   }
 }
 
@@ -393,6 +397,8 @@ extern "C" int warp_host_eval(const void* devsys, const double* packed, const in
   switch (S.pes[0].model) {
     case CAIR_PES_O3_UMN: warp_eval<CAIR_PES_O3_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
     case CAIR_PES_N3_UMN: warp_eval<CAIR_PES_N3_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
+    case CAIR_PES_O4_UMN: warp_eval<CAIR_PES_O4_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
+    case CAIR_PES_N4_UMN: warp_eval<CAIR_PES_N4_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
     default: return 1;
   }
 }

@@ -258,34 +258,48 @@ def test_rate_coefficients_within_two_sigma_of_the_oracle_path(gpu_lib, oracle_l
     H.close()
 
 
-def test_o2_o_ground_state_rates_within_two_sigma(gpu_lib, oracle_lib):
-    """O2(v=0, J=1) + O on UMN_11A1 in full -- 10,000 trajectories, seed 1,
-    10,000 K, b = 6 sqrt(U) bohr, Dinit 15 bohr, rmax 16 bohr -- through the GPU queue and through the
-    oracle from the same stream: every final state's rate agrees within twice the combined Monte-Carlo
-    standard deviation."""
+_CONFIG1_REF = {}
+
+
+def _config1_oracle_rates(o, cfg, row, nt, seed, T):
+    """The oracle's rates of config 1 (computed once for both integrator modes)."""
     import os
+    import oracle
+    if "ref" not in _CONFIG1_REF:
+        lvo = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax",
+                                                       "tau", "ri", "ro", "rlim")])
+        for c in lvo.dtype.names:
+            lvo[c] = row[c] if c in row.dtype.names else 0.0
+        ic = o.sample_ics(nt, lvo, seed=seed, ttra=T, bmax=6.0, dinit=15.0)
+        res = o.integrate(ic["paq"], ic["erra"], procs=min(16, os.cpu_count() or 1))
+        fi, ff = o.analyze(ic["paq0"]), o.analyze(o.apply_transformation(res["paq"]))
+        keep = (res["status"] == 0) & (np.abs(res["H"] - ic["H0"]) <= cfg.ham_abs_tol)
+        col = lambda fs, k: np.array([f[k] for f in fs])
+        qi = np.stack([col(fi, "angmom"), col(fi, "viba"), 16 * col(fi, "ipair") + col(fi, "itype") + 0.5], 1)
+        qf = np.stack([col(ff, "angmom"), col(ff, "viba"), 16 * col(ff, "ipair") + col(ff, "itype") + 0.5], 1)
+        _CONFIG1_REF["ref"], _ = oracle.statistics(np.full(keep.sum(), 6.0), ic["b"][keep], qi[keep], qf[keep], cap=nt)
+    return _CONFIG1_REF["ref"]
+
+
+@pytest.mark.parametrize("mode", ["thread", "warp"])
+def test_o2_o_ground_state_rates_within_two_sigma(gpu_lib, oracle_lib, mode):
+    """O2(v=0, J=1) + O on UMN_11A1 in full -- 10,000 trajectories, seed 1,
+    10,000 K, b = 6 sqrt(U) bohr, Dinit 15 bohr, rmax 16 bohr -- through the GPU queue (a lane per
+    trajectory, and a warp per trajectory, the mode a job of this size runs in) and through the oracle
+    from the same stream: every final state's rate agrees within twice the combined Monte-Carlo
+    standard deviation."""
     import oracle
     from oracle import Oracle
     cfg = systems.o3_config(dinit=15.0, bmax=6.0, rmax=16.0)
     H = api.Handle(cfg)
+    H.integrator_mode = mode
     o = Oracle(cfg)
     lv = systems.load_levels("O2")
     row = lv[(lv["vqn"] == 0) & (lv["jqn"] == 1)]
     nt, seed, T = 10000, api.process_seed(1, 1), 10000.0
     items = api.work_items([(0, 0, nt, seed, T, 6.0, 15.0)])
     rows = api.RunTrajectories(H).run(api.level_table(row), items)
-    lvo = np.zeros(1, dtype=[(c, "f8") for c in ("vqn", "jqn", "eint", "egam", "rmin", "rmax", "vmin", "vmax", "tau",
-                                                   "ri", "ro", "rlim")])
-    for c in lvo.dtype.names:
-        lvo[c] = row[c] if c in row.dtype.names else 0.0
-    ic = o.sample_ics(nt, lvo, seed=seed, ttra=T, bmax=6.0, dinit=15.0)
-    res = o.integrate(ic["paq"], ic["erra"], procs=min(16, os.cpu_count() or 1))
-    fi, ff = o.analyze(ic["paq0"]), o.analyze(o.apply_transformation(res["paq"]))
-    keep = (res["status"] == 0) & (np.abs(res["H"] - ic["H0"]) <= cfg.ham_abs_tol)
-    col = lambda fs, k: np.array([f[k] for f in fs])
-    qi = np.stack([col(fi, "angmom"), col(fi, "viba"), 16 * col(fi, "ipair") + col(fi, "itype") + 0.5], 1)
-    qf = np.stack([col(ff, "angmom"), col(ff, "viba"), 16 * col(ff, "ipair") + col(ff, "itype") + 0.5], 1)
-    ref, _ = oracle.statistics(np.full(keep.sum(), 6.0), ic["b"][keep], qi[keep], qf[keep], cap=nt)
+    ref = _config1_oracle_rates(o, cfg, row, nt, seed, T)
     m = cfg.masses
     vel = oracle.mean_velocity(T, (m[0] + m[1]) * m[2] / sum(m))
     got = api.Statistics(H).compute(items, rows)
@@ -297,6 +311,7 @@ def test_o2_o_ground_state_rates_within_two_sigma(gpu_lib, oracle_lib):
         ko, so = r.get(fs, (0.0, 0.0))
         sig = np.hypot(sg, so)
         dev.append(0.0 if sig == 0.0 else abs(kg - ko) / sig)
-    print("O2(0,1) + O rates: %d final states (GPU) / %d (oracle), worst |dk|/sigma %.3f" % (len(g), len(r), max(dev)))
+    print("O2(0,1) + O rates (%s integrator): %d final states (GPU) / %d (oracle), worst |dk|/sigma %.3f" %
+          (mode, len(g), len(r), max(dev)))
     assert max(dev) <= 2.0
     H.close()

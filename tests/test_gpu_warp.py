@@ -10,8 +10,8 @@ import numpy as np
 import pytest
 
 from coarseair_gb300 import api, systems
-from test_gpu_parity import PROCS, ROUND_U, _final_qn, _gpu_final_qn, _ics, _setup
-from test_warp_host import CFGS as HOST_CFGS, _phase_points
+from test_gpu_parity import PROCS, _final_qn, _gpu_final_qn, _ics, _setup
+from test_warp_host import CFGS as HOST_CFGS, DEPTH, U, _phase_points
 
 pytestmark = pytest.mark.gpu
 
@@ -23,20 +23,21 @@ def test_warp_programs_on_the_gpu_match_the_oracle(gpu_lib, oracle_lib, name):
     cfg = HOST_CFGS[name]()
     o = Oracle(cfg)
     H = api.Handle(cfg, tpq=o.tpq)
-    y = _phase_points(o, name, 161, 12)     # odd: the last warp has one point
+    y = _phase_points(o, name, 161, 12)     # odd: a diatom + atom warp ends with one point
     ipes = np.arange(len(y), dtype=np.int32) % len(cfg.surfaces)
     dev = torch.device("cuda")
     yd = torch.from_numpy(np.ascontiguousarray(y)).to(dev)
     ipd = torch.from_numpy(ipes).to(dev)
     ypd = torch.zeros_like(yd)
     Hd = torch.zeros(len(y), dtype=torch.float64, device=dev)
-    Rd = torch.zeros((len(y), 3), dtype=torch.float64, device=dev)
+    Rd = torch.zeros((len(y), o.npairs), dtype=torch.float64, device=dev)
     H.check(H.lib.cair_internal_warp_eval(H.h, len(y), ipd.data_ptr(), yd.data_ptr(), ypd.data_ptr(), Hd.data_ptr(),
                                           Rd.data_ptr()), "cair_internal_warp_eval")
     yp, h, ri = ypd.cpu().numpy(), Hd.cpu().numpy(), Rd.cpu().numpy()
     yp_o = o.rhs(y, ipes=ipes)
-    R, _ = o.rp(y[:, 6:])
+    R, _ = o.rp(y[:, o.nv:])
     cs = o.condition_scale(R, ipes=ipes)
+    ROUND_U = 2 * DEPTH[name] * U
     sc = np.maximum(1e-12 * np.abs(yp_o).max(axis=1, keepdims=True), ROUND_U * cs[:, 1:].max(axis=1, keepdims=True))
     print("%s warp programs on the GPU: worst/bound %.2e" % (name, (np.abs(yp - yp_o) / sc).max()))
     assert np.all(np.abs(yp - yp_o) <= sc)
@@ -44,6 +45,35 @@ def test_warp_programs_on_the_gpu_match_the_oracle(gpu_lib, oracle_lib, name):
     hs = np.maximum(1e-12 * np.maximum(np.abs(h_o), 0.1), ROUND_U * cs[:, 0])
     assert np.all(np.abs(h - h_o) <= hs)
     assert np.allclose(ri, r_o, rtol=4e-16, atol=0)
+    H.close()
+
+
+def test_warp_integrator_o4_to_the_end(gpu_lib, oracle_lib):
+    """O2 + O2 (a whole warp per trajectory, three surfaces): the thread integrator's O4 criterion,
+    final points within 1e-6 of the oracle's on its stable trajectories and H conserved."""
+    from test_gpu_o4 import _collision_points
+    from test_gpu_o4 import _setup as o4_setup
+    cfg, o, H = o4_setup()
+    H.integrator_mode = "warp"
+    y, erra = _collision_points(o, cfg, 32, 13)
+    ip = np.arange(len(y), dtype=np.int32) % 3
+    ref = o.integrate(y, erra, ipes=ip, procs=PROCS)
+    pert = o.integrate(y * (1 + 1e-14), erra, ipes=ip, procs=PROCS)
+    tr = api.Trajectories.start(y, erra, cfg.dt0, ipes=ip)
+    api.Integrator(H).Integrate(tr)
+    assert np.all(tr.status == 0) and np.all(ref["status"] == 0)
+    scale = np.abs(ref["paq"]).max(axis=1)
+    stable = np.abs(pert["paq"] - ref["paq"]).max(axis=1) / scale < 1e-9
+    rel = np.abs(tr.paq - ref["paq"]).max(axis=1) / scale
+    print("O4 warp integrator to the end: %d of %d stable, max rel on stable %.2e" % (stable.sum(), len(y),
+                                                                                     rel[stable].max()))
+    assert stable.sum() >= 4
+    assert np.all(rel[stable] < 1e-6)
+    h_o, _ = o.hamiltonian(tr.paq, ipes=ip)
+    assert np.max(np.abs(tr.H - h_o)) < 1e-9
+    assert np.max(np.abs(tr.H - o.hamiltonian(y, ipes=ip)[0])) < cfg.ham_abs_tol
+    c = H.counters()
+    assert c["attempts"] == int(np.sum(tr.iste + tr.irej))
     H.close()
 
 
@@ -94,7 +124,7 @@ def test_warp_integrator_other_step_counts(gpu_lib, oracle_lib, nsteps):
 
 
 def test_warp_mode_refused_where_not_built(gpu_lib):
-    for cfg in (systems.o3nn_config(), systems.o4_config()):
+    for cfg in (systems.o3nn_config(), systems.o3bnn_config(samples=[1])):
         H = api.Handle(cfg)
         with pytest.raises(api.CairError, match="CAIR_EUNSUPPORTED"):
             H.integrator_mode = "warp"

@@ -15,16 +15,19 @@ from coarseair_gb300 import systems
 from test_pes_host import _harness, _setup
 
 U = 1.1102230246251565e-16
-ROUND_U = 2 * 110 * U
-CFGS = {"O3": systems.o3_config, "N3": systems.n3_config, "O3_9": systems.o3_mix_config}
+CFGS = {"O3": systems.o3_config, "N3": systems.n3_config, "O3_9": systems.o3_mix_config,
+        "O4": systems.o4_config, "N4": systems.n4_config}
 LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 0), "O3_9": ("O2", 0, 1)}
+# depth of the surface graph in the rounding bound (as the surface parity tests take it)
+DEPTH = {"O3": 110, "N3": 110, "O3_9": 110, "O4": 630, "N4": 488}
 
 
 def _warp_eval(L, setup, y, ipes):
     devsys, packed, offsets, _ = setup
     n = y.shape[0]
     y = np.ascontiguousarray(y, np.float64)
-    yp, H, Ri = np.zeros_like(y), np.zeros(n), np.zeros((n, 3))
+    npairs = 3 if y.shape[1] == 12 else 6
+    yp, H, Ri = np.zeros_like(y), np.zeros(n), np.zeros((n, npairs))
     ip = np.ascontiguousarray(ipes, np.int32)
     assert L.warp_host_eval(devsys, packed.ctypes.data, offsets.ctypes.data, n, ip.ctypes.data, y.ctypes.data,
                             yp.ctypes.data, H.ctypes.data, Ri.ctypes.data) == 0
@@ -32,17 +35,24 @@ def _warp_eval(L, setup, y, ipes):
 
 
 def _phase_points(o, name, n, seed):
-    """Initial conditions of the level the tests integrate, and random geometries with random momenta."""
-    mol, v0, j0 = LEVELS[name]
-    lv = systems.load_levels(mol)
-    sel = lv[(lv["vqn"] == v0) & (lv["jqn"] == j0)]
-    ic = o.sample_ics(n // 2, sel, seed=seed)["paq"]
+    """Diatom + atom: initial conditions of the level the tests integrate, and random geometries with
+    random momenta.  Diatom + diatom: random geometries with random momenta."""
     rng = np.random.default_rng(seed)
+    nv = o.nv
+    if nv == 6:
+        mol, v0, j0 = LEVELS[name]
+        lv = systems.load_levels(mol)
+        sel = lv[(lv["vqn"] == v0) & (lv["jqn"] == j0)]
+        ic = o.sample_ics(n // 2, sel, seed=seed)["paq"]
+        lo, hi, span = 1.5, 9.0, 3.0
+    else:
+        ic = np.zeros((0, 2 * nv))
+        lo, hi, span = 1.6, 10.0, 3.5
     out = []
     while sum(len(x) for x in out) < n - len(ic):
-        Q = rng.uniform(-3.0, 3.0, size=(4 * n, 6))
+        Q = rng.uniform(-span, span, size=(4 * n, nv))
         R, _ = o.rp(Q)
-        out.append(Q[np.all((R > 1.5) & (R < 9.0), axis=1)])
+        out.append(Q[np.all((R > lo) & (R < hi), axis=1)])
     Q = np.concatenate(out)[:n - len(ic)]
     P = rng.normal(0.0, 10.0, size=Q.shape)
     return np.concatenate([ic, np.concatenate([P, Q], axis=1)])
@@ -59,7 +69,8 @@ def test_warp_programs_match_the_oracle(gpu_lib, oracle_lib, name):
     ipes = np.arange(len(y), dtype=np.int32) % len(cfg.surfaces)
     yp, H, Ri = _warp_eval(L, setup, y, ipes)
     yp_o = o.rhs(y, ipes=ipes)
-    R, _ = o.rp(y[:, 6:])
+    R, _ = o.rp(y[:, o.nv:])
+    ROUND_U = 2 * DEPTH[name] * U
     cs = o.condition_scale(R, ipes=ipes)
     sc = np.maximum(1e-12 * np.abs(yp_o).max(axis=1, keepdims=True), ROUND_U * cs[:, 1:].max(axis=1, keepdims=True))
     worst = (np.abs(yp - yp_o) / sc).max()
