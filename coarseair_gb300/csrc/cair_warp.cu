@@ -206,7 +206,7 @@ __device__ __forceinline__ int warp_attempt(const WProg& G, double* s, int gl, i
     bool ok = true;
     if (io) {
       const double dd = yt[k][0] - ylast[0];
-      if (dd != dd) nan = 1;
+      if (is_nan_bits(dd)) nan = 1;
       ok = err_below_one(dd, yscal);
     }
     below[k] = __all_sync(kFull, ok);

@@ -31,6 +31,11 @@ static inline double __hiloint2double(int hi, int lo) {
   std::memcpy(&d, &u, 8);
   return d;
 }
+static inline long long __double_as_longlong(double d) {
+  long long u;
+  std::memcpy(&u, &d, 8);
+  return u;
+}
 template <class T>
 static inline T __ldg(const T* p) {
   return *p;
@@ -401,4 +406,9 @@ extern "C" int warp_host_eval(const void* devsys, const double* packed, const in
     case CAIR_PES_N4_UMN: warp_eval<CAIR_PES_N4_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
     default: return 1;
   }
+}
+
+// The library's table-driven exponential (cair_device.cuh fexp) at n points.
+extern "C" void host_fexp(int64_t n, const double* x, double* y) {
+  for (int64_t i = 0; i < n; ++i) y[i] = fexp(x[i]);
 }

@@ -48,6 +48,8 @@ def _harness():
     L.queue_host_run.restype = C.c_int
     L.queue_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
                                  C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.c_void_p]
+    L.host_fexp.restype = None
+    L.host_fexp.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
     L.warp_host_eval.restype = C.c_int
     L.warp_host_eval.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_void_p]
@@ -357,3 +359,19 @@ def test_queue_pipeline_on_the_host_for_n2_n(gpu_lib, oracle_lib):
         stable.append((fa[0] == fb[0]) & (fa[1] == fb[1]) & (fa[2] == fb[2]))
     same, stable = np.concatenate(same), np.concatenate(stable)
     assert stable.mean() >= 0.9 and same[stable].mean() >= 0.995
+
+
+def test_table_driven_exponential_within_one_ulp():
+    """fexp (Tang's table-driven method, degree-5 polynomial) against the C library's exp: at most one
+    ulp apart over the surfaces' arguments and the whole range it serves, [-707, 707)."""
+    L = _harness()
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-60.0, 5.0, 400000), rng.uniform(-707.0, 707.0, 200000),
+                        np.linspace(-1e-3, 1e-3, 20001), rng.uniform(-0.01, 0.01, 50000)])
+    y = np.zeros_like(x)
+    L.host_fexp(len(x), x.ctypes.data, y.ctypes.data)
+    ref = np.exp(x)
+    ulp = np.spacing(ref)
+    err = np.abs(y - ref) / ulp
+    print("fexp vs libm exp: max %.3f ulp, mean %.4f ulp, %.5f exact" % (err.max(), err.mean(), np.mean(err == 0)))
+    assert err.max() <= 1.0
