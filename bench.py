@@ -38,9 +38,10 @@ import numpy as np  # noqa: E402
 # dram__bytes_write.sum = 69.13 MB for a 98,304-trajectory launch of this workload); the state is read
 # and written once per trajectory, so the full launch's traffic scales with the trajectory count
 DRAM_BYTES_PER_TRAJ = 703.0
-# --integrator auto: jobs below this many trajectories run a warp per trajectory (the latency mode);
-# the thread integrator keeps up to 152 SMs x 8 warps x 32 = 38,912 trajectories in flight
-WARP_MODE_MAX_TRAJ = 38912
+# --integrator auto: jobs below this many trajectories run a warp per trajectory (the latency mode):
+# twice the 152 SMs x 4 warps x 32 = 19,456 lanes the tuned thread integrator keeps in flight, the library's
+# CAIR_INTEGRATOR_AUTO rule for the tuned launch shape
+WARP_MODE_MAX_TRAJ = 2 * 19456
 
 TEMPS = (5000.0, 10000.0, 20000.0)
 
@@ -270,7 +271,7 @@ def main():
     ap.add_argument("--sur-steps", type=int, default=1, help="timed surrogate steps")
     ap.add_argument("--integrator", default="auto", choices=["auto", "thread", "warp"],
                     help="persistent integrator: a lane per trajectory (thread), a warp per trajectory (warp), "
-                         "or warp for jobs below WARP_MODE_MAX_TRAJ trajectories where the system has warp programs")
+                         "or warp for jobs below WARP_MODE_MAX_TRAJ trajectories (auto)")
     args = ap.parse_args()
     spec = SYSTEMS[args.system]
     if args.ntraj is None:
@@ -345,7 +346,8 @@ def main():
 
     mode = args.integrator
     if mode == "auto":
-        mode = "warp" if (n < WARP_MODE_MAX_TRAJ and args.system in ("n3", "o3")) else "thread"
+        # the library's rule (CAIR_INTEGRATOR_AUTO), resolved here so the line names the integrator that ran
+        mode = "warp" if n < WARP_MODE_MAX_TRAJ else "thread"
     H.integrator_mode = mode
     # the project's autotuner picks the integrator's launch shape on a capped sample of this job
     tune = None

@@ -110,15 +110,24 @@ class Handle:
                    "cair_flop_model")
         return dict(grad=a.value, energy=b.value, attempt=c.value, exp=d.value)
 
+    _MODES = {"thread": _lib.INTEGRATOR_THREAD, "warp": _lib.INTEGRATOR_WARP, "auto": _lib.INTEGRATOR_AUTO}
+
     @property
     def integrator_mode(self):
-        """"thread" (a lane per trajectory, the default) or "warp" (a warp per trajectory: the latency
-        mode for small jobs; O3, N3, O4 and N4 UMN surfaces)."""
-        return "warp" if self.lib.cair_get_integrator_mode(self.h) == _lib.INTEGRATOR_WARP else "thread"
+        """"thread" (a lane per trajectory, the default), "warp" (a warp per trajectory: the latency
+        mode for small jobs; O3, N3, O4 and N4 UMN surfaces) or "auto" (warp for launches of fewer
+        trajectories than twice the thread integrator's resident lanes, where it has programs)."""
+        m = self.lib.cair_get_integrator_mode(self.h)
+        return {v: k for k, v in self._MODES.items()}[m]
+
+    @property
+    def last_integrator(self):
+        """The integrator ("thread" or "warp") the handle's last launch ran."""
+        return "warp" if self.lib.cair_last_integrator(self.h) == _lib.INTEGRATOR_WARP else "thread"
 
     @integrator_mode.setter
     def integrator_mode(self, mode):
-        m = {"thread": _lib.INTEGRATOR_THREAD, "warp": _lib.INTEGRATOR_WARP}[mode]
+        m = self._MODES[mode]
         self.check(self.lib.cair_set_integrator_mode(self.h, m), "cair_set_integrator_mode")
 
     def counters(self):

@@ -52,6 +52,7 @@ struct cair_handle {
   int tune_block = 64;                      // persistent integrator launch shape (cair_autotune)
   int tune_per_sm = 0;                      // resident blocks per SM; 0 = as many as fit
   int mode = CAIR_INTEGRATOR_THREAD;        // persistent integrator: a lane or a warp per trajectory
+  int last_integrator = CAIR_INTEGRATOR_THREAD;  // the one the last launch ran
   unsigned long long* warp_times = nullptr; // warp timeline of the next integrator launches
   int64_t warp_times_cap = 0;
   int64_t warp_times_n = 0;                 // warps of the last launch that recorded
@@ -640,7 +641,16 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_
     A.rec_mod = h->rec_mod;
     A.rec_rcut = h->rec_rcut;
   }
-  if (!h->sur && h->mode == CAIR_INTEGRATOR_WARP) {
+  bool warp = h->mode == CAIR_INTEGRATOR_WARP;
+  if (!h->sur && h->mode == CAIR_INTEGRATOR_AUTO && warp_integrate_supported(h->sys)) {
+    int resident = 0;
+    if (int e = with_model(h, [&](auto L) { resident = L.integrate_blocks_per_sm(h->tune_block, h->sys.nsteps); }))
+      return e;
+    if (h->tune_per_sm > 0 && h->tune_per_sm < resident) resident = h->tune_per_sm;
+    warp = A.n < 2 * (int64_t)h->nsm * (resident > 0 ? resident : 1) * h->tune_block;
+  }
+  h->last_integrator = (!h->sur && warp) ? CAIR_INTEGRATOR_WARP : CAIR_INTEGRATOR_THREAD;
+  if (!h->sur && warp) {
     // a warp per trajectory: CTAs of warp_cta_warps(S) warps, as many as fit on every SM
     cudaEvent_t w0 = nullptr, w1 = nullptr;
     if (h->time_integrate) {
@@ -1084,8 +1094,8 @@ int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm)
 }
 
 int cair_set_integrator_mode(cair_handle* h, int32_t mode) {
-  if (!h || (mode != CAIR_INTEGRATOR_THREAD && mode != CAIR_INTEGRATOR_WARP))
-    return fail(h, CAIR_EINVAL, "cair_set_integrator_mode: mode must be CAIR_INTEGRATOR_THREAD or _WARP");
+  if (!h || (mode != CAIR_INTEGRATOR_THREAD && mode != CAIR_INTEGRATOR_WARP && mode != CAIR_INTEGRATOR_AUTO))
+    return fail(h, CAIR_EINVAL, "cair_set_integrator_mode: mode must be CAIR_INTEGRATOR_THREAD, _WARP or _AUTO");
   if (mode == CAIR_INTEGRATOR_WARP && !warp_integrate_supported(h->sys))
     return fail(h, CAIR_EUNSUPPORTED,
                 "cair_set_integrator_mode: the warp integrator is built for the O3, N3, O4 and N4 UMN surfaces with "
@@ -1095,6 +1105,8 @@ int cair_set_integrator_mode(cair_handle* h, int32_t mode) {
 }
 
 int32_t cair_get_integrator_mode(const cair_handle* h) { return h ? h->mode : CAIR_INTEGRATOR_THREAD; }
+
+int32_t cair_last_integrator(const cair_handle* h) { return h ? h->last_integrator : CAIR_INTEGRATOR_THREAD; }
 
 // Calibration of the persistent integrator's launch shape on the job's own work: every item keeps
 // the leading fraction of its trajectories (same streams) so that about `sample` trajectories run,

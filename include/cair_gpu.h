@@ -479,8 +479,15 @@ int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm)
  * returns CAIR_EUNSUPPORTED.  An attached surrogate takes precedence over either. */
 #define CAIR_INTEGRATOR_THREAD 0
 #define CAIR_INTEGRATOR_WARP 1
+/* CAIR_INTEGRATOR_AUTO: per launch, the warp integrator when the system has its programs and the launch
+ * holds fewer trajectories than twice the lanes the thread integrator keeps resident (a smaller job is as
+ * long as its longest trajectory on one lane), the thread integrator otherwise. */
+#define CAIR_INTEGRATOR_AUTO 2
 int cair_set_integrator_mode(cair_handle* h, int32_t mode);
 int32_t cair_get_integrator_mode(const cair_handle* h);
+/* The integrator the handle's last launch ran (CAIR_INTEGRATOR_THREAD or _WARP; THREAD too for a surrogate
+ * launch). */
+int32_t cair_last_integrator(const cair_handle* h);
 /* Autotuner: runs a sample of about `sample` trajectories of the job's own work items (each item's
  * leading trajectories, same streams), capped at cap_attempts attempts each, once per launch shape
  * (block 32, 64, 128 x 1 .. the resident maximum per SM), and keeps on the handle the shape with the

@@ -130,3 +130,27 @@ def test_warp_mode_refused_where_not_built(gpu_lib):
             H.integrator_mode = "warp"
         assert H.integrator_mode == "thread"
         H.close()
+
+
+def test_auto_mode_picks_by_job_size(gpu_lib, oracle_lib):
+    """CAIR_INTEGRATOR_AUTO: a launch below twice the thread integrator's resident lanes runs on the
+    warp integrator, a larger one on the thread integrator; both give the same attempt counts as the
+    explicit modes on the same trajectories."""
+    cfg, o, H = _setup("N3")
+    H.integrator_mode = "auto"
+    assert H.integrator_mode == "auto"
+    ic = _ics(o, "N3", 64, seed=99)
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.Integrator(H).Integrate(tr, max_attempts=200)
+    assert H.last_integrator == "warp"
+    big = 2 * 152 * 8 * 64 + 1     # above twice the resident lanes of any launch shape
+    paq = np.repeat(ic["paq"], big // 64 + 1, axis=0)[:big]
+    erra = np.repeat(ic["erra"], big // 64 + 1, axis=0)[:big]
+    tr2 = api.Trajectories.start(paq, erra, cfg.dt0)
+    api.Integrator(H).Integrate(tr2, max_attempts=20)
+    assert H.last_integrator == "thread"
+    assert np.all(tr2.iste + tr2.irej == 20)
+    H.integrator_mode = "thread"
+    api.Integrator(H).Integrate(api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0), max_attempts=20)
+    assert H.last_integrator == "thread"
+    H.close()
