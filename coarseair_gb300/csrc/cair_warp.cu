@@ -457,7 +457,9 @@ int with_warp_model(const DevSys& S, F f) {
     case CAIR_PES_O3_UMN: return f(std::integral_constant<int, CAIR_PES_O3_UMN>{});
     case CAIR_PES_N3_UMN: return f(std::integral_constant<int, CAIR_PES_N3_UMN>{});
     case CAIR_PES_O4_UMN: return f(std::integral_constant<int, CAIR_PES_O4_UMN>{});
-    default: return f(std::integral_constant<int, CAIR_PES_N4_UMN>{});
+    case CAIR_PES_N4_UMN: return f(std::integral_constant<int, CAIR_PES_N4_UMN>{});
+    case CAIR_PES_O3_NN: return f(std::integral_constant<int, CAIR_PES_O3_NN>{});
+    default: return f(std::integral_constant<int, CAIR_PES_O3_BNN>{});
   }
 }
 

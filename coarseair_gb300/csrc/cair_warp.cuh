@@ -9,7 +9,7 @@
 
 namespace cair {
 
-enum { WK_SOP = 0, WK_EXP = 1, WK_RSQRT = 2, WK_RECIP = 3 };
+enum { WK_SOP = 0, WK_EXP = 1, WK_RSQRT = 2, WK_RECIP = 3, WK_TANH = 4 };
 enum { WS_LIT = 0, WS_TPQ = 1, WS_MMIMN = 2, WS_O2AB = 3, WS_COEF = 4, WS_PES = 5 };
 
 // One program: nlev levels of W records of 8 words (lane l of level L executes record W L + l, W the
@@ -41,28 +41,28 @@ struct WModel {
         wp_##key##_grad_in, wp_##key##_grad_out, wp_##key##_energy_in, wp_##key##_energy_out                   \
   }
 
-// Surface models that have programs (the UMN surfaces), and the diatomic their programs evaluate.
+// Surface models that have programs (the UMN surfaces, O3 NN and the O3 BNN samples), and the diatomic
+// their programs evaluate.
 __host__ __device__ constexpr bool warp_model_built(int model) {
   return model == CAIR_PES_O3_UMN || model == CAIR_PES_N3_UMN || model == CAIR_PES_O4_UMN ||
-         model == CAIR_PES_N4_UMN;
+         model == CAIR_PES_N4_UMN || model == CAIR_PES_O3_NN || model == CAIR_PES_O3_BNN;
 }
 __host__ __device__ constexpr int warp_model_diat(int model) {
-  return (model == CAIR_PES_O3_UMN || model == CAIR_PES_O4_UMN) ? CAIR_DIAT_O2_UMN : CAIR_DIAT_N2_UMN_FORN4;
+  return (model == CAIR_PES_N3_UMN || model == CAIR_PES_N4_UMN) ? CAIR_DIAT_N2_UMN_FORN4 : CAIR_DIAT_O2_UMN;
 }
 
 // Per model: lanes of the group that evaluates one right-hand side (16: a half-warp, so the two
 // halves of a warp run different midpoint sequences; 32: the whole warp, NE = 18 equations),
 // slots of a group, and the levels of the grad and energy programs.
+#define CAIR_WPICK(MODEL, FIELD)                                                                      \
+  (MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_##FIELD : MODEL == CAIR_PES_N3_UMN ? WP_N3_UMN_##FIELD           \
+   : MODEL == CAIR_PES_O4_UMN ? WP_O4_UMN_##FIELD : MODEL == CAIR_PES_N4_UMN ? WP_N4_UMN_##FIELD         \
+   : MODEL == CAIR_PES_O3_NN ? WP_O3_NN_##FIELD : WP_O3_BNN_##FIELD)
 template <int MODEL>
 struct WCfg {
-  static constexpr int W = MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_LANES : MODEL == CAIR_PES_N3_UMN ? WP_N3_UMN_LANES
-                           : MODEL == CAIR_PES_O4_UMN ? WP_O4_UMN_LANES : WP_N4_UMN_LANES;
-  static constexpr int NSLOT = MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_NSLOT : MODEL == CAIR_PES_N3_UMN ? WP_N3_UMN_NSLOT
-                               : MODEL == CAIR_PES_O4_UMN ? WP_O4_UMN_NSLOT : WP_N4_UMN_NSLOT;
-  static constexpr int NLEV = MODEL == CAIR_PES_O3_UMN ? WP_O3_UMN_GRAD_NLEV + WP_O3_UMN_ENERGY_NLEV
-                              : MODEL == CAIR_PES_N3_UMN ? WP_N3_UMN_GRAD_NLEV + WP_N3_UMN_ENERGY_NLEV
-                              : MODEL == CAIR_PES_O4_UMN ? WP_O4_UMN_GRAD_NLEV + WP_O4_UMN_ENERGY_NLEV
-                                                         : WP_N4_UMN_GRAD_NLEV + WP_N4_UMN_ENERGY_NLEV;
+  static constexpr int W = CAIR_WPICK(MODEL, LANES);
+  static constexpr int NSLOT = CAIR_WPICK(MODEL, NSLOT);
+  static constexpr int NLEV = CAIR_WPICK(MODEL, GRAD_NLEV) + CAIR_WPICK(MODEL, ENERGY_NLEV);
   static constexpr int NG = 32 / W;  // groups per warp
 };
 
@@ -71,7 +71,9 @@ __device__ __forceinline__ WModel wmodel() {
   if (MODEL == CAIR_PES_O3_UMN) return CAIR_WMODEL(o3_umn, O3_UMN);
   if (MODEL == CAIR_PES_N3_UMN) return CAIR_WMODEL(n3_umn, N3_UMN);
   if (MODEL == CAIR_PES_O4_UMN) return CAIR_WMODEL(o4_umn, O4_UMN);
-  return CAIR_WMODEL(n4_umn, N4_UMN);
+  if (MODEL == CAIR_PES_N4_UMN) return CAIR_WMODEL(n4_umn, N4_UMN);
+  if (MODEL == CAIR_PES_O3_NN) return CAIR_WMODEL(o3_nn, O3_NN);
+  return CAIR_WMODEL(o3_bnn, O3_BNN);
 }
 
 // Value of constant slot i for surface P.  Hoisted slots (source 255) are the const program's.
@@ -92,7 +94,7 @@ __device__ __forceinline__ double wp_const(const WModel& m, const DevSys& S, con
 // One record: a sum of up to three products (a multiply, then fused multiply-adds in term order; a
 // term's sign, where the generator could not fold it into a constant factor, goes on the first
 // factor's sign bit with an integer XOR, off the FP64 pipe), the table-driven exponential, a
-// reciprocal square root or a reciprocal.  The term count and whether signs are present are the same
+// reciprocal square root, a reciprocal or tanh.  The term count and whether signs are present are the same
 // for every lane of a level, so its branches are uniform.
 __device__ __forceinline__ double wp_ld(const char* sb, unsigned off) {
   return *reinterpret_cast<const double*>(sb + off);
@@ -102,7 +104,7 @@ __device__ __forceinline__ double wp_flip(double a, unsigned meta, int j) {
 }
 
 __device__ __forceinline__ double wp_eval(uint4 c0, uint4 c1, const char* sb) {
-  const unsigned meta = c0.x, kind = (meta >> 28) & 3u;
+  const unsigned meta = c0.x, kind = (meta >> 28) & 7u;
   if (kind == WK_SOP) {
     const unsigned nt = (meta >> 24) & 3u;
     const bool sg = (meta >> 23) & 1u;
@@ -127,6 +129,7 @@ __device__ __forceinline__ double wp_eval(uint4 c0, uint4 c1, const char* sb) {
   const double x = wp_ld(sb, c0.z);
   if (kind == WK_EXP) return fexp(x);
   if (kind == WK_RSQRT) return rsqrt(x);
+  if (kind == WK_TANH) return ftanh(x);
   return 1.0 / x;
 }
 

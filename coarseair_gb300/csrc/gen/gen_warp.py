@@ -12,6 +12,7 @@ of a per-half-warp array of doubles in shared memory:
   EXP    r = exp(s[a])                           the library's table-driven exponential (fexp)
   RSQRT  r = 1 / sqrt(s[a])
   RECIP  r = 1 / s[a]
+  TANH   r = tanh(s[a])                          the library's ftanh (derivative taken as 1 - r^2)
 
 This script restates the device surfaces as expression graphs (the same formulas and constants
 as csrc/cair_device.cuh, which cites the reference routine of each), differentiates the energy
@@ -36,8 +37,8 @@ import struct
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.abspath(os.path.join(HERE, ".."))
 SPLIT = 3           # sums with more terms are split into partial sums (a record holds 3 terms)
-COST = {"sop": None, "exp": 12, "rsqrt": 8, "recip": 10}
-KIND = {"sop": 0, "exp": 1, "rsqrt": 2, "recip": 3}
+COST = {"sop": None, "exp": 12, "rsqrt": 8, "recip": 10, "tanh": 22}
+KIND = {"sop": 0, "exp": 1, "rsqrt": 2, "recip": 3, "tanh": 4}
 
 B_TO_ANG = 0.52917721092
 KCM_TO_HARTREE = 0.159360144e-2
@@ -170,6 +171,9 @@ class Graph:
             elif op == "recip":
                 r = E(self, n)
                 push(args[0], -(a * (r * r)))
+            elif op == "tanh":
+                t = E(self, n)
+                push(args[0], a * (1.0 - t * t))
             else:
                 raise ValueError("no derivative for " + op)
         res = []
@@ -226,6 +230,10 @@ def rsqrt(x):
 
 def recip(x):
     return x.g.fn("recip", x)
+
+
+def tanh(x):
+    return x.g.fn("tanh", x)
 
 
 # ----------------------------------------------------------------------------------------------
@@ -403,8 +411,81 @@ def pes_n4(g, R, tabs):
     return V, dVdR
 
 
+def nn_layout():
+    """The packed device layout of the O3 NN / BNN coefficients (the CAIR_NN_* offsets of cair_device.cuh)."""
+    text = open(os.path.join(CSRC, "cair_device.cuh")).read()
+    return {k: int(v) for k, v in re.findall(r"#define CAIR_(?:NN|BNN)_(\w+) (\d+)", text)}
+
+
+EV_TO_HARTREE = 1.0 / 27.2113839712790
+
+
+def pes_o3nn(g, R, tabs, bnn=False, grad=True):
+    """pes_o3nn: Compute (grad, six features, 6 -> 20 -> 10 -> 1 tanh network) or Potential (three scaled
+    features through W1's storage read as 3 x NHL1); the BNN takes the output through exp(v + Noise)."""
+    L = nn_layout()
+    c = lambda i: g.const("coef", i)
+    A = o2_coefficients()
+    lam, re_ = c(L["LAM"]), c(L["RE"])
+    p = [fexp(-(lam * (R[i] - re_))) for i in range(3)]
+    vd = [o2_umn(g, R[i], A) for i in range(3)]
+    vdiat = (vd[0] + vd[1]) + vd[2]
+    gvp = [p[0] * p[1], p[1] * p[2], p[2] * p[0]]
+    H1, H2 = L["H1"], L["H2"]
+    if grad:
+        gprod = gvp[0] * p[2]
+        gc = [gvp[0] * p[0], gvp[0] * p[1], gvp[1] * p[1], gvp[1] * p[2], gvp[2] * p[0], gvp[2] * p[2]]
+        G = [(gvp[0] + gvp[1]) + gvp[2], gprod,
+             ((((gc[0] + gc[1]) + gc[2]) + gc[3]) + gc[4]) + gc[5],
+             ((((gc[0] * p[0] + gc[1] * p[1]) + gc[2] * p[1]) + gc[3] * p[2]) + gc[4] * p[0]) + gc[5] * p[2],
+             (gc[0] * p[2] + gc[2] * p[0]) + gc[5] * p[1],
+             (gc[0] * p[1] + gc[2] * p[2]) + gc[4] * p[2]]
+        y1 = []
+        for j in range(H1):
+            z = g.lit(0.0)
+            for i in range(6):
+                z = z + G[i] * c(L["W1"] + i + 6 * j)
+            y1.append(tanh(z + c(L["B1"] + j)))
+        v = g.lit(0.0)
+        for k in range(H2):
+            z = g.lit(0.0)
+            for j in range(H1):
+                z = z + y1[j] * c(L["W2"] + j + H1 * k)
+            v = v + tanh(z + c(L["B2"] + k)) * c(L["W3"] + k)
+    else:
+        gvs = [p[0] + p[1], p[1] + p[2], p[2] + p[0]]
+        G = [(gvp[0] + gvp[1]) + gvp[2], gvp[0] * p[2], (gvp[0] * gvs[0] + gvp[1] * gvs[1]) + gvp[2] * gvs[2]]
+        G = [(G[i] - c(L["MEAN"] + i)) * recip(c(L["SD"] + i)) for i in range(3)]
+        y1 = []
+        for j in range(H1):
+            z = c(L["B1"] + j)
+            for l in range(3):
+                z = z + c(L["W1P"] + l + 3 * j) * G[l]
+            y1.append(tanh(z))
+        v = g.lit(0.0)
+        for k in range(H2):
+            z = c(L["B2"] + k)
+            for j in range(H1):
+                z = z + c(L["W2"] + j + H1 * k) * y1[j]
+            v = v + tanh(z) * c(L["W3"] + k)
+    v = v + c(L["B3"])
+    vout = fexp(v + c(L["NOISE"])) if bnn else v
+    V = (vout - c(L["YSC"])) * EV_TO_HARTREE + vdiat
+    dVdR = g.grad(V, R) if grad else None
+    return V, dVdR
+
+
+def pes_o3nn_pair(bnn):
+    """Compute for the right-hand side, Potential for the Hamiltonian: the two networks the surface has."""
+    def fn(g, R, tabs, grad=True):
+        return pes_o3nn(g, R, tabs, bnn=bnn, grad=grad)
+    fn.two_networks = True
+    return fn
+
+
 # surface -> (formula, atoms, lanes of the group that evaluates one right-hand side)
-MODELS = {"o3_umn": (pes_o3, 3, 16), "n3_umn": (pes_n3, 3, 16), "o4_umn": (pes_o4, 4, 32), "n4_umn": (pes_n4, 4, 32)}
+MODELS = {"o3_umn": (pes_o3, 3, 16), "n3_umn": (pes_n3, 3, 16), "o4_umn": (pes_o4, 4, 32), "n4_umn": (pes_n4, 4, 32),
+          "o3_nn": (pes_o3nn_pair(False), 3, 16), "o3_bnn": (pes_o3nn_pair(True), 3, 16)}
 
 
 def system(g, natoms):
@@ -483,7 +564,7 @@ def energy(g, surface, tabs):
         for j in range(j0 + 3, nv, 3):
             eki = eki + g.const("tpq", j + 9 * i) * p[j]
         h = h + p[i] * eki
-    V, _ = fn(g, R, tabs)
+    V, _ = fn(g, R, tabs, grad=False) if getattr(fn, "two_networks", False) else fn(g, R, tabs)
     return [h * 0.5 + V] + Ri
 
 
@@ -510,7 +591,7 @@ def lower(g, outputs, ninputs):
         for a in ops[n][1]:
             uses[a] += 1
     atom = lambda n: ops[n][0] in ("lit", "const", "in")
-    special = lambda n: ops[n][0] in ("exp", "rsqrt", "recip")
+    special = lambda n: ops[n][0] in ("exp", "rsqrt", "recip", "tanh")
     one = g.lit(1.0).n
     mat = set()
     for n in live:
@@ -810,7 +891,7 @@ def compile_model(surface, tabs):
 # ----------------------------------------------------------------------------------------------
 def records(levels, ins, slot, width, zero):
     """Levels of more than `width` instructions are cut into several; lane l of level L executes
-    record L * width + l, 8 words:  w0 = active << 31 | kind << 28 | nt << 24 | signed << 23 |
+    record L * width + l, 8 words:  w0 = active << 31 | kind << 28 (3 bits) | nt << 24 | signed << 23 |
     sign of term j << (20 + j), nt and `signed` the same for every record of the level (the most
     terms of its sums, whether any term still carries a sign); w1 = byte offset of the result;
     w2..w7 = byte offsets of the factors a_j, b_j of the terms (+-) s[a_j] * s[b_j], missing terms
@@ -861,7 +942,7 @@ def emit(models, path):
          " * Generated by csrc/gen/gen_warp.py, do not edit.",
          " * A program is NLEV levels of W records of 8 words (W the model's LANES), lane l of level L executing",
          " * record W L + l: w0 = active << 31 | kind << 28 | nterm << 24 | signed << 23 | term signs << 20 (kind",
-         " * 0 sum of products, 1 exp, 2 rsqrt, 3 reciprocal; nterm and signed uniform over the level),",
+         " * 0 sum of products, 1 exp, 2 rsqrt, 3 reciprocal, 4 tanh; nterm and signed uniform over the level),",
          " * w1 = result byte offset, w2..w7 = byte offsets of a0, b0, a1, b1, a2, b2: sum_j (+-) s[a_j] * s[b_j]",
          " * (a special's operand is w2). */",
          "#pragma once", ""]

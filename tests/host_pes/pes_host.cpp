@@ -404,6 +404,8 @@ extern "C" int warp_host_eval(const void* devsys, const double* packed, const in
     case CAIR_PES_N3_UMN: warp_eval<CAIR_PES_N3_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
     case CAIR_PES_O4_UMN: warp_eval<CAIR_PES_O4_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
     case CAIR_PES_N4_UMN: warp_eval<CAIR_PES_N4_UMN>(S, n, ipes, y, yp, H, Ri); return 0;
+    case CAIR_PES_O3_NN: warp_eval<CAIR_PES_O3_NN>(S, n, ipes, y, yp, H, Ri); return 0;
+    case CAIR_PES_O3_BNN: warp_eval<CAIR_PES_O3_BNN>(S, n, ipes, y, yp, H, Ri); return 0;
     default: return 1;
   }
 }

@@ -5,7 +5,8 @@
 2. Whole collisions through the persistent warp integrator against the oracle's: final (v, J,
    arrangement) on the oracle-stable trajectories, energy conservation, the device counters.
 3. NSteps 2 and 4 (their half-warp schedules differ from NSteps 3's).
-4. The mode is refused where no programs are built."""
+4. O3 NN (the networks as programs) end to end, the AUTO mode's choice, and the mode refused where the
+   programs do not apply."""
 import numpy as np
 import pytest
 
@@ -124,12 +125,46 @@ def test_warp_integrator_other_step_counts(gpu_lib, oracle_lib, nsteps):
 
 
 def test_warp_mode_refused_where_not_built(gpu_lib):
-    for cfg in (systems.o3nn_config(), systems.o3bnn_config(samples=[1])):
-        H = api.Handle(cfg)
-        with pytest.raises(api.CairError, match="CAIR_EUNSUPPORTED"):
-            H.integrator_mode = "warp"
-        assert H.integrator_mode == "thread"
-        H.close()
+    """An O3 UMN surface given the N2 diatomic: its programs evaluate the O2 curve, so the warp mode is
+    refused and the handle stays on the thread integrator."""
+    import dataclasses
+    cfg = dataclasses.replace(systems.o3_config(), diat_model=systems.DIAT_N2_UMN_FORN4)
+    H = api.Handle(cfg)
+    with pytest.raises(api.CairError, match="CAIR_EUNSUPPORTED"):
+        H.integrator_mode = "warp"
+    assert H.integrator_mode == "thread"
+    H.close()
+
+
+def test_warp_integrator_o3_nn_end_to_end(gpu_lib, oracle_lib):
+    """O3 NN through the warp integrator (its Compute and Potential networks as programs, tanh as an
+    instruction): both sides stop at the same attempt cap, final (v, J, arrangement) and whether the cap
+    was reached agree on >= 99.5 % of the oracle-stable trajectories; H is the Potential network's at
+    the returned point (the reference's Hamiltonian, which is not conserved for this surface)."""
+    from test_gpu_parity import ROUND_U
+    cfg, o, H = _setup("O3NN")
+    H.integrator_mode = "warp"
+    n, cap = 160, 20000
+    ic = _ics(o, "O3NN", n, seed=5)
+    ref = o.integrate(ic["paq"], ic["erra"], procs=PROCS, max_attempts=cap)
+    pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"], procs=PROCS, max_attempts=cap)
+    tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
+    api.Integrator(H).Integrate(tr, max_attempts=cap)
+    assert H.last_integrator == "warp"
+    assert np.all(np.isin(tr.status, (0, 1))) and np.all(np.isin(ref["status"], (0, 1)))
+    h_o, _ = o.hamiltonian(tr.paq)
+    hs = np.maximum(1e-12 * np.maximum(np.abs(h_o), 0.1), ROUND_U * o.condition_scale(o.rp(tr.paq[:, 6:])[0])[:, 0])
+    assert np.all(np.abs(tr.H - h_o) <= hs)
+    Jo, vo, ao = _final_qn(o.analyze(o.apply_transformation(ref["paq"])))
+    Jp, vp, ap = _final_qn(o.analyze(o.apply_transformation(pert["paq"])))
+    Jg, vg, ag = _gpu_final_qn(api.MolecularState(H).FindState(api.Collision(H).ApplyTransformation(tr.paq)))
+    same = (Jo == Jg) & (vo == vg) & (ao == ag) & (tr.status == ref["status"])
+    stable = (Jo == Jp) & (vo == vp) & (ao == ap) & (pert["status"] == ref["status"])
+    print("O3NN warp integrator: GPU vs oracle %.4f overall, %.4f on oracle-stable (%.4f stable), %d capped" %
+          (same.mean(), same[stable].mean(), stable.mean(), int(np.sum(ref["status"] == 1))))
+    assert same[stable].mean() >= 0.995
+    assert same.mean() >= stable.mean() - 0.02
+    H.close()
 
 
 def test_auto_mode_picks_by_job_size(gpu_lib, oracle_lib):

@@ -16,10 +16,11 @@ from test_pes_host import _harness, _setup
 
 U = 1.1102230246251565e-16
 CFGS = {"O3": systems.o3_config, "N3": systems.n3_config, "O3_9": systems.o3_mix_config,
-        "O4": systems.o4_config, "N4": systems.n4_config}
-LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 0), "O3_9": ("O2", 0, 1)}
+        "O4": systems.o4_config, "N4": systems.n4_config, "O3NN": systems.o3nn_config,
+        "O3BNN": lambda: systems.o3bnn_config(samples=[1, 17, 33, 50])}
+LEVELS = {"O3": ("O2", 0, 1), "N3": ("N2", 0, 0), "O3_9": ("O2", 0, 1), "O3NN": ("O2", 0, 1), "O3BNN": ("O2", 0, 1)}
 # depth of the surface graph in the rounding bound (as the surface parity tests take it)
-DEPTH = {"O3": 110, "N3": 110, "O3_9": 110, "O4": 630, "N4": 488}
+DEPTH = {"O3": 110, "N3": 110, "O3_9": 110, "O4": 630, "N4": 488, "O3NN": 110, "O3BNN": 110}
 
 
 def _warp_eval(L, setup, y, ipes):
