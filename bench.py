@@ -38,9 +38,8 @@ import numpy as np  # noqa: E402
 # dram__bytes_write.sum = 69.13 MB for a 98,304-trajectory launch of this workload); the state is read
 # and written once per trajectory, so the full launch's traffic scales with the trajectory count
 DRAM_BYTES_PER_TRAJ = 703.0
-# --integrator auto: jobs below this many trajectories run a warp per trajectory (the latency mode):
-# twice the 152 SMs x 4 warps x 32 = 19,456 lanes the tuned thread integrator keeps in flight, the library's
-# CAIR_INTEGRATOR_AUTO rule for the tuned launch shape
+# --integrator auto (CAIR_INTEGRATOR_AUTO): the library runs a warp per trajectory below twice the lanes the thread
+# integrator keeps resident; the autotuner runs for jobs at least this large (twice 152 SMs x 4 warps x 32 lanes)
 WARP_MODE_MAX_TRAJ = 2 * 19456
 
 TEMPS = (5000.0, 10000.0, 20000.0)
@@ -270,8 +269,8 @@ def main():
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-steps", type=int, default=1, help="timed surrogate steps")
     ap.add_argument("--integrator", default="auto", choices=["auto", "thread", "warp"],
-                    help="persistent integrator: a lane per trajectory (thread), a warp per trajectory (warp), "
-                         "or warp for jobs below WARP_MODE_MAX_TRAJ trajectories (auto)")
+                    help="persistent integrator: a lane per trajectory (thread), a warp per trajectory (warp), or "
+                         "the library's choice by job size, with the thread integrator's tail on warps (auto)")
     args = ap.parse_args()
     spec = SYSTEMS[args.system]
     if args.ntraj is None:
@@ -345,13 +344,12 @@ def main():
         return (p + 255) & ~255
 
     mode = args.integrator
-    if mode == "auto":
-        # the library's rule (CAIR_INTEGRATOR_AUTO), resolved here so the line names the integrator that ran
-        mode = "warp" if n < WARP_MODE_MAX_TRAJ else "thread"
-    H.integrator_mode = mode
-    # the project's autotuner picks the integrator's launch shape on a capped sample of this job
+    # the project's autotuner picks the thread integrator's launch shape on a capped sample of this job
+    # (in THREAD mode: AUTO would hand the sample's tail to the warp integrator)
+    H.integrator_mode = "thread"
     tune = None
-    if mode == "thread" and args.surrogate != "only" and (args.system != "o4" or args.ntraj <= 200000):
+    runs_thread = mode == "thread" or (mode == "auto" and n >= WARP_MODE_MAX_TRAJ)
+    if runs_thread and args.surrogate != "only" and (args.system != "o4" or args.ntraj <= 200000):
         # eight times the most lanes any shape keeps resident (152 SMs x 8 warps x 32), so that every
         # shape's sample runs in several full rounds of its lanes
         ns = min(n, 8 * 38912)
@@ -359,6 +357,10 @@ def main():
         tune = {"block": shape[0], "blocks_per_sm": shape[1],
                 "points": [[int(p["block"]), int(p["per_sm"]), float(p["attempts_per_s"])] for p in pts],
                 "sample": "%d trajectories of the job's items, each capped at 100 attempts" % ns}
+
+    # CAIR_INTEGRATOR_AUTO: a warp per trajectory below twice the thread integrator's resident lanes; above,
+    # a lane per trajectory that hands the queue's tail to the warp integrator
+    H.integrator_mode = mode
 
     def step(i):
         j = i % len(streams)
@@ -401,6 +403,8 @@ def main():
     H.check(lib.cair_integrate_timings(H.h, kt, args.steps, ctypes.byref(nk)), "cair_integrate_timings")
     H.check(lib.cair_set_integrate_timing(H.h, 0), "cair_set_integrate_timing")
     integ_ms = float(np.mean(list(kt)[:nk.value]))
+    ran = H.last_integrator
+    handoffs = H.last_handoffs() if ran == "thread" else 0
     nw = int(lib.cair_warp_timeline_count(H.h))
     H.check(lib.cair_set_warp_timeline(H.h, None, 0), "cair_set_warp_timeline")
     tail = tail_figures(wt[:4 * nw].cpu().numpy().reshape(-1, 4)) if nw else None
@@ -439,7 +443,7 @@ def main():
     line = {"metric": metric, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg_json,
-            "gpu_launches": 8 * args.steps,
+            "gpu_launches": (9 if handoffs else 8) * args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_fp64["tflops"], "unit": "TFLOP/s",
                          "frac": achieved / peak_fp64["tflops"],
                          "traffic": DRAM_BYTES_PER_TRAJ * n if args.system == "n3" else None,
@@ -447,8 +451,9 @@ def main():
                                            "98,304-trajectory launch (703 B per trajectory), scaled by trajectories"
                                            if args.system == "n3" else "not captured for this system",
                          "peak_source": peak_fp64["source"],
-                         "kernel": "k_integrate (persistent Bulirsch-Stoer integrator, a lane per trajectory)"
-                                   if mode == "thread" else
+                         "kernel": ("k_integrate (persistent Bulirsch-Stoer integrator, a lane per trajectory)" +
+                                    (", its tail on k_integrate_warp" if handoffs else ""))
+                                   if ran == "thread" else
                                    "k_integrate_warp (persistent Bulirsch-Stoer integrator, a warp per trajectory)",
                          "kernel_ms_per_launch": integ_ms, "kernel_share_of_step": integ_ms * args.steps / ms,
                          "work": "executed FP64 operations of the pruned formulation per step "
@@ -458,7 +463,7 @@ def main():
             "attempts_per_trajectory_quantiles": {q: int(np.quantile(per_traj, float(q))) for q in
                                                   ("0.5", "0.9", "0.99", "0.999", "1.0")},
             "inflight_batches": len(streams),
-            "integrator": mode,
+            "integrator": {"mode": mode, "ran": ran, "tail_handoffs": handoffs},
             "autotune": tune,
             "tail": tail,
             "converged_fraction": float(np.mean(res["status"] == 0)),

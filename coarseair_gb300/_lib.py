@@ -157,6 +157,8 @@ SIGNATURES = [
     ("cair_set_integrator_mode", C.c_int, [_P, C.c_int32]),
     ("cair_get_integrator_mode", C.c_int32, [_P]),
     ("cair_last_integrator", C.c_int32, [_P]),
+    ("cair_set_tail_handoff", C.c_int, [_P, C.c_int64]),
+    ("cair_last_handoffs", C.c_int64, [_P]),
     ("cair_internal_warp_eval", C.c_int, [_P, C.c_int64, _P, _P, _P, _P, _P]),
 ]
 INTEGRATOR_THREAD, INTEGRATOR_WARP, INTEGRATOR_AUTO = 0, 1, 2

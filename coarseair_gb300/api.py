@@ -120,6 +120,15 @@ class Handle:
         m = self.lib.cair_get_integrator_mode(self.h)
         return {v: k for k, v in self._MODES.items()}[m]
 
+    def set_tail_handoff(self, below=-1):
+        """AUTO mode's tail hand-off threshold (trajectories in flight): -1 the warp integrator's resident
+        warps, 0 off."""
+        self.check(self.lib.cair_set_tail_handoff(self.h, int(below)), "cair_set_tail_handoff")
+
+    def last_handoffs(self):
+        """Trajectories the last launch handed from the thread to the warp integrator."""
+        return int(self.lib.cair_last_handoffs(self.h))
+
     @property
     def last_integrator(self):
         """The integrator ("thread" or "warp") the handle's last launch ran."""

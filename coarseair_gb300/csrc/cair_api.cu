@@ -53,6 +53,10 @@ struct cair_handle {
   int tune_per_sm = 0;                      // resident blocks per SM; 0 = as many as fit
   int mode = CAIR_INTEGRATOR_THREAD;        // persistent integrator: a lane or a warp per trajectory
   int last_integrator = CAIR_INTEGRATOR_THREAD;  // the one the last launch ran
+  long long hand_below = -1;                // AUTO's tail hand-off: -1 the warp integrator's resident warps, 0 off
+  int64_t hand_cap = 0;                     // hand-off buffers of the cair_integrate* paths
+  void* d_hand = nullptr;
+  unsigned long long* last_hctl = nullptr;  // hand-off counters of the last launch (NULL: none)
   unsigned long long* warp_times = nullptr; // warp timeline of the next integrator launches
   int64_t warp_times_cap = 0;
   int64_t warp_times_n = 0;                 // warps of the last launch that recorded
@@ -517,6 +521,7 @@ void cair_destroy(cair_handle* h) {
   if (h->d_scratch) cudaFree(h->d_scratch);
   if (h->d_work) cudaFree(h->d_work);
   if (h->d_ctl) cudaFree(h->d_ctl);
+  if (h->d_hand) cudaFree(h->d_hand);
   if (h->d_stats) cudaFree(h->d_stats);
   if (h->d_nrec) cudaFree(h->d_nrec);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -632,8 +637,17 @@ int cair_bs_steps(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, d
   return wait_stream(h);
 }
 
-static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_t st) {
+// Device buffers of a launch's tail hand-off: the list, the attempts by trajectory, 3 control words
+// (zeroed by the caller with the rest of its control block).
+struct HandBufs {
+  int32_t* hand;
+  long long* att;
+  unsigned long long* ctl;
+};
+
+static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_t st, const HandBufs* hb = nullptr) {
   IntegrateArgs A = A0;
+  h->last_hctl = nullptr;
   if (h->rec && !h->sur) {
     A.rec = h->rec;
     A.nrec = h->d_nrec;
@@ -704,14 +718,59 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_
     ++h->ntev;
     CUDA_TRY(h, cudaEventRecord(e0, st));
   }
+  // AUTO on a large launch: the thread integrator hands its tail to the warp integrator
+  const bool handoff = !h->sur && hb && h->mode == CAIR_INTEGRATOR_AUTO && h->hand_below != 0 &&
+                       warp_integrate_supported(h->sys);
+  if (handoff) {
+    A.hand = hb->hand;
+    A.hand_att = hb->att;
+    A.hctl = hb->ctl;
+    A.hand_below = h->hand_below > 0 ? h->hand_below : warp_resident_warps(h->nsm, h->sys);
+  }
   if (h->sur) {
     if (sur_integrate_launch(h->sur, h->nsm, st, h->sys, A))
       return fail(h, CAIR_ECUDA, std::string("surrogate integrator launch: ") + cudaGetErrorString(cudaGetLastError()));
   } else if (int e = with_model(h, [&](auto L) { L.integrate((int)g, block, st, h->sys, A); })) {
     return e;
   }
+  if (handoff) {
+    // the handed-off trajectories, at most the lanes the thread launch had, each on a warp
+    IntegrateArgs W = A;
+    W.n = std::min<int64_t>(A.n, g * (int64_t)block);
+    W.order = hb->hand;
+    W.queue = hb->ctl + 2;
+    W.n_dev = hb->ctl + 1;
+    W.att0 = hb->att;
+    W.hand = nullptr;
+    W.warp_times = nullptr;
+    int64_t nw = 0;
+    if (warp_integrate_launch(h->nsm, 0, st, h->sys, W, 0, &nw))
+      return fail(h, CAIR_ECUDA, std::string("warp integrator launch: ") + cudaGetErrorString(cudaGetLastError()));
+    h->last_hctl = hb->ctl;
+  }
   if (e1) CUDA_TRY(h, cudaEventRecord(e1, st));
   return 0;
+}
+
+// Hand-off buffers for the cair_integrate* paths (the queue paths carve theirs from the batch).
+static const HandBufs* integrate_handbufs(cair_handle* h, int64_t n, HandBufs& hb, cudaStream_t st) {
+  if (h->mode != CAIR_INTEGRATOR_AUTO || h->hand_below == 0 || !warp_integrate_supported(h->sys)) return nullptr;
+  if (n > h->hand_cap) {
+    if (h->d_hand) cudaFree(h->d_hand);
+    h->d_hand = nullptr;
+    h->hand_cap = 0;
+    if (cudaMalloc(&h->d_hand, (size_t)n * 12 + 64) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    h->hand_cap = n;
+  }
+  char* base = (char*)h->d_hand;
+  hb.ctl = (unsigned long long*)base;
+  hb.att = (long long*)(base + 64);
+  hb.hand = (int32_t*)(base + 64 + 8 * (size_t)n);
+  if (cudaMemsetAsync(hb.ctl, 0, 64, st) != cudaSuccess) return nullptr;
+  return &hb;
 }
 
 int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
@@ -725,7 +784,8 @@ int cair_integrate_dev(cair_handle* h, int64_t n, const int32_t* ipes, double* p
   CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
   IntegrateArgs A{n, ipes, paq, t, dt, erra, H, smax, smin, irej, iste, status, max_attempts, h->d_ctl,
                   h->d_ctl + 1, nullptr};
-  return launch_integrate(h, A, st);
+  HandBufs hb;
+  return launch_integrate(h, A, st, integrate_handbufs(h, n, hb, st));
 }
 
 int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, double* t, double* dt,
@@ -758,7 +818,8 @@ int cair_integrate(cair_handle* h, int64_t n, const int32_t* ipes, double* paq, 
   CUDA_TRY(h, cudaMemsetAsync(h->d_ctl, 0, sizeof(unsigned long long) * 8, st));
   IntegrateArgs A{n, d_ip, d_y, d_t, d_dt, d_e, d_H, d_smax, d_smin, d_irej, d_iste, d_st, max_attempts,
                   h->d_ctl, h->d_ctl + 1, nullptr};
-  if (int e = launch_integrate(h, A, st)) return e;
+  HandBufs hb;
+  if (int e = launch_integrate(h, A, st, integrate_handbufs(h, n, hb, st))) return e;
   CUDA_TRY(h, cudaMemcpyAsync(paq, d_y, n * ne * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(t, d_t, n * sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(h, cudaMemcpyAsync(dt, d_dt, n * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -850,8 +911,11 @@ int cair_find_state(cair_handle* h, int64_t n, const double* paq_vel, cair_traj_
 }
 
 namespace {
+// control words of a batch: [0] queue head, [1..5] counters, [8..8+511] bucket counts and offsets,
+// [520..522] the tail hand-off's (in flight, hand-offs, the warp integrator's queue over them)
+constexpr int kCtl = 8 + 2 * 256 + 8, kHandCtl = 8 + 2 * 256;
 struct BatchBufs {
-  unsigned long long* ctl;  // [0] queue head, [1..5] counters, [8..8+255] bucket counts/offsets
+  unsigned long long* ctl;
   double *paq, *paq0, *erra, *t, *dt, *H, *H0, *smax, *smin, *b, *draws, *key;
   int32_t *irej, *iste, *status, *ipes, *item_of, *order;
 };
@@ -859,12 +923,12 @@ struct BatchBufs {
 // Batch state of n trajectories of ne equations (12: diatom + atom, 18: diatom + diatom)
 constexpr size_t batch_bytes(int64_t n, int ne) {
   return (size_t)n * (sizeof(double) * (ne * 3 + 9 + kDraws) + sizeof(int32_t) * 6) + 40 * 256 +
-         sizeof(unsigned long long) * (8 + 2 * 256);
+         sizeof(unsigned long long) * kCtl;
 }
 
 void carve_into(char* base, int64_t n, int ne, BatchBufs& B) {
   Carver c{base};
-  B.ctl = c.take<unsigned long long>(8 + 2 * 256);
+  B.ctl = c.take<unsigned long long>(kCtl);
   B.paq = c.take<double>(n * ne); B.paq0 = c.take<double>(n * ne); B.erra = c.take<double>(n * ne);
   B.t = c.take<double>(n); B.dt = c.take<double>(n); B.H = c.take<double>(n); B.H0 = c.take<double>(n);
   B.smax = c.take<double>(n); B.smin = c.take<double>(n); B.b = c.take<double>(n);
@@ -976,7 +1040,7 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
                               B.draws, st, B.key))
     return e;
   // queue order: longest predicted duration first (bucketed by initial relative speed)
-  CUDA_TRY(h, cudaMemsetAsync(B.ctl, 0, sizeof(unsigned long long) * (8 + 2 * 256), st));
+  CUDA_TRY(h, cudaMemsetAsync(B.ctl, 0, sizeof(unsigned long long) * kCtl, st));
   const int g = grid_for(h, ntot);
   cair_k_bucket_count<<<g, 256, 0, st>>>(ntot, B.key, B.ctl + 8);
   cair_k_bucket_scan<<<1, 256, 0, st>>>(B.ctl + 8, B.ctl + 8 + 256);
@@ -985,7 +1049,10 @@ int cair_run_queue_dev(cair_handle* h, int32_t nlevels, const cair_level* levels
   if (int e = check_launch(h)) return e;
   IntegrateArgs A{ntot, B.ipes, B.paq, B.t, B.dt, B.erra, B.H, B.smax, B.smin, B.irej, B.iste, B.status,
                   max_attempts, B.ctl, B.ctl + 1, B.order};
-  if (int e = launch_integrate(h, A, st)) return e;
+  // the initial-condition draws are spent: their space holds the tail hand-off's list and attempt counts
+  static_assert(kDraws >= 2, "hand-off list and attempts fit in the draws");
+  HandBufs hb{reinterpret_cast<int32_t*>(B.draws + ntot), reinterpret_cast<long long*>(B.draws), B.ctl + kHandCtl};
+  if (int e = launch_integrate(h, A, st, &hb)) return e;
   if (three_atoms(h))
     k_results<3><<<g, 128, 0, st>>>(h->sys, h->fs, ntot, B.paq0, B.paq, B.H0, B.H, B.t, B.status, B.iste, B.irej,
                                     B.item_of, items, results);
@@ -1107,6 +1174,21 @@ int cair_set_integrator_mode(cair_handle* h, int32_t mode) {
 int32_t cair_get_integrator_mode(const cair_handle* h) { return h ? h->mode : CAIR_INTEGRATOR_THREAD; }
 
 int32_t cair_last_integrator(const cair_handle* h) { return h ? h->last_integrator : CAIR_INTEGRATOR_THREAD; }
+
+int cair_set_tail_handoff(cair_handle* h, int64_t below) {
+  if (!h) return CAIR_EINVAL;
+  h->hand_below = below < 0 ? -1 : below;
+  return 0;
+}
+
+int64_t cair_last_handoffs(cair_handle* h) {
+  if (!h || !h->last_hctl) return 0;
+  unsigned long long n = 0;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+      cudaMemcpy(&n, h->last_hctl + 1, sizeof n, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -1;
+  return (int64_t)n;
+}
 
 // Calibration of the persistent integrator's launch shape on the job's own work: every item keeps
 // the leading fraction of its trajectories (same streams) so that about `sample` trajectories run,

@@ -122,6 +122,18 @@ struct IntegrateArgs {
   // %globaltimer [ns] when it starts and when its last lane runs out of work, the sum over its
   // ncall blocks of the lanes with a trajectory, and its ncall blocks
   unsigned long long* warp_times;
+  // tail hand-off to the warp integrator (hand NULL: off).  Once the queue is empty and at most
+  // hand_below trajectories are in flight, a lane writes its trajectory back at its next end check,
+  // records the attempts it has made (hand_att[k]) and appends k to hand[]; hctl[0] counts the
+  // trajectories in flight, hctl[1] the hand-offs.
+  int32_t* hand;
+  long long* hand_att;
+  unsigned long long* hctl;
+  long long hand_below;
+  // the warp integrator over a hand-off list: the number of entries read from *n_dev (A.n bounds it),
+  // each trajectory's earlier attempts from att0[k]
+  const unsigned long long* n_dev;
+  const long long* att0;
 };
 
 // The GPU's nanosecond clock (0 where this source is compiled for the host by the test harness).
@@ -169,6 +181,7 @@ __global__ void __launch_bounds__(128, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(De
     const unsigned long long q = atomicAdd(A.queue, 1ull);
     active = q < (unsigned long long)A.n;
     if (!active) return;
+    if (A.hand) atomicAdd(A.hctl, 1ull);
     k = A.order ? (unsigned long long)A.order[q] : q;
     ip = A.ipes ? A.ipes[k] : 0;
 #pragma unroll
@@ -231,7 +244,26 @@ __global__ void __launch_bounds__(128, CAIR_INTEGRATE_MIN_BLOCKS) k_integrate(De
         c_att += att;
         c_acc += iste - iste0;
         c_rej += irej - irej0;
+        if (A.hand) atomicAdd(A.hctl, ~0ull);  // one fewer in flight
         take();
+      } else if (A.hand && *(volatile unsigned long long*)A.queue >= (unsigned long long)A.n &&
+                 (long long)*(volatile unsigned long long*)A.hctl <= A.hand_below) {
+        // the queue's tail: the warp integrator finishes this trajectory from this end check
+#pragma unroll
+        for (int i = 0; i < NE; ++i) A.paq[NE * k + i] = y[i];
+        A.t[k] = x;
+        A.dt[k] = h;
+        A.H[k] = H;
+        A.smax[k] = smax;
+        A.smin[k] = smin;
+        A.irej[k] = irej;
+        A.iste[k] = iste;
+        A.hand_att[k] = att;
+        c_att += att;
+        c_acc += iste - iste0;
+        c_rej += irej - irej0;
+        A.hand[atomicAdd(A.hctl + 1, 1ull)] = (int32_t)k;
+        active = false;
       }
     }
     __syncwarp();

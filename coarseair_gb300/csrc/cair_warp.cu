@@ -267,12 +267,14 @@ __global__ void __launch_bounds__(32 * WLaunch<MODEL>::CTA, 1) k_integrate_warp(
   const unsigned long long warp_id = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
   if (A.warp_times && lane == 0) A.warp_times[4 * warp_id] = globaltimer_ns();
   int loaded = -1;
+  // a hand-off list's length is known only on the device
+  const unsigned long long ntraj = A.n_dev ? *A.n_dev : (unsigned long long)A.n;
 #pragma unroll 1
   for (;;) {
     unsigned long long q = 0;
     if (lane == 0) q = atomicAdd(A.queue, 1ull);
     q = __shfl_sync(kFull, q, 0);
-    if (q >= (unsigned long long)A.n) break;
+    if (q >= ntraj) break;
     const unsigned long long k = A.order ? (unsigned long long)A.order[q] : q;
     const int ip = A.ipes ? A.ipes[k] : 0;
     if (ip != loaded) {
@@ -284,7 +286,8 @@ __global__ void __launch_bounds__(32 * WLaunch<MODEL>::CTA, 1) k_integrate_warp(
     double x = A.t[k], h = A.dt[k], smax = A.smax[k], smin = A.smin[k], H = 0.0;
     int irej = A.irej[k], iste = A.iste[k];
     const int irej0 = irej, iste0 = iste;
-    int64_t att = 0;
+    int64_t att = A.att0 ? A.att0[k] : 0;
+    const int64_t att_start = att;
     double dydx = 0.0;
     bool fresh = false;  // dydx = f(y) of the current y
 #pragma unroll 1
@@ -334,7 +337,7 @@ __global__ void __launch_bounds__(32 * WLaunch<MODEL>::CTA, 1) k_integrate_warp(
           A.irej[k] = irej;
           A.iste[k] = iste;
           A.status[k] = bad ? CAIR_TRAJ_NONFINITE : (conv ? CAIR_TRAJ_DONE : CAIR_TRAJ_ATTEMPT_CAP);
-          c_att += att;
+          c_att += att - att_start;
           c_acc += iste - iste0;
           c_rej += irej - irej0;
         }
@@ -484,6 +487,19 @@ int warp_eval_launch(int nsm, cudaStream_t st, const DevSys& S, int64_t n, const
                      double* yp, double* H, double* Ri) {
   if (!warp_integrate_supported(S)) return 2;
   return with_warp_model(S, [&](auto m) { return eval_model<decltype(m)::value>(nsm, st, S, n, ipes, y, yp, H, Ri); });
+}
+
+int64_t warp_resident_warps(int nsm, const DevSys& S) {
+  if (!warp_integrate_supported(S)) return 0;
+  return with_warp_model(S, [&](auto m) {
+    using LW = WLaunch<decltype(m)::value>;
+    auto kern = k_integrate_warp<decltype(m)::value, 3>;
+    int per_sm = 0;
+    if (fit_smem(kern, LW::SMEM) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * LW::CTA, LW::SMEM) != cudaSuccess)
+      return 0;
+    return (int)((int64_t)nsm * per_sm * LW::CTA);
+  });
 }
 
 int warp_cta_warps(const DevSys& S) {

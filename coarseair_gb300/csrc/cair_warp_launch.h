@@ -21,4 +21,6 @@ int warp_integrate_launch(int nsm, int per_sm_cap, cudaStream_t st, const DevSys
 int warp_eval_launch(int nsm, cudaStream_t st, const DevSys& S, int64_t n, const int32_t* ipes, const double* y,
                      double* yp, double* H, double* Ri);
 int warp_cta_warps(const DevSys& S);
+// Warps the warp integrator keeps resident on the GPU (0 when unsupported).
+int64_t warp_resident_warps(int nsm, const DevSys& S);
 }  // namespace cair

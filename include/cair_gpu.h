@@ -486,8 +486,15 @@ int cair_get_launch_shape(const cair_handle* h, int32_t* block, int32_t* per_sm)
 int cair_set_integrator_mode(cair_handle* h, int32_t mode);
 int32_t cair_get_integrator_mode(const cair_handle* h);
 /* The integrator the handle's last launch ran (CAIR_INTEGRATOR_THREAD or _WARP; THREAD too for a surrogate
- * launch). */
+ * launch, and for a thread launch that handed its tail to the warp integrator). */
 int32_t cair_last_integrator(const cair_handle* h);
+/* Tail hand-off of CAIR_INTEGRATOR_AUTO on launches the thread integrator runs: once the queue is empty and at
+ * most `below` trajectories are still in flight, each is written back at its next end check and the warp
+ * integrator finishes it, a warp per trajectory (same attempt counts and end checks).  below < 0: the warp
+ * integrator's resident warps (the default); 0: off. */
+int cair_set_tail_handoff(cair_handle* h, int64_t below);
+/* Trajectories the handle's last launch handed to the warp integrator (synchronises the device). */
+int64_t cair_last_handoffs(cair_handle* h);
 /* Autotuner: runs a sample of about `sample` trajectories of the job's own work items (each item's
  * leading trajectories, same streams), capped at cap_attempts attempts each, once per launch shape
  * (block 32, 64, 128 x 1 .. the resident maximum per SM), and keeps on the handle the shape with the
