@@ -144,8 +144,10 @@ def test_warp_integrator_o3_nn_end_to_end(gpu_lib, oracle_lib):
     from test_gpu_parity import ROUND_U
     cfg, o, H = _setup("O3NN")
     H.integrator_mode = "warp"
-    n, cap = 160, 20000
-    ic = _ics(o, "O3NN", n, seed=5)
+    # the thread integrator's O3 NN sample and cap (test_gpu_parity): 400 trajectories, so that one chaotic
+    # trajectory the oracle's 1e-14 perturbation misses is within the 0.5 % the bar allows
+    n, cap = 400, 30000
+    ic = _ics(o, "O3NN", n)
     ref = o.integrate(ic["paq"], ic["erra"], procs=PROCS, max_attempts=cap)
     pert = o.integrate(ic["paq"] * (1 + 1e-14), ic["erra"], procs=PROCS, max_attempts=cap)
     tr = api.Trajectories.start(ic["paq"], ic["erra"], cfg.dt0)
@@ -163,7 +165,7 @@ def test_warp_integrator_o3_nn_end_to_end(gpu_lib, oracle_lib):
     print("O3NN warp integrator: GPU vs oracle %.4f overall, %.4f on oracle-stable (%.4f stable), %d capped" %
           (same.mean(), same[stable].mean(), stable.mean(), int(np.sum(ref["status"] == 1))))
     assert same[stable].mean() >= 0.995
-    assert same.mean() >= stable.mean() - 0.02
+    assert same.mean() >= stable.mean() - 0.01
     H.close()
 
 
