@@ -195,15 +195,17 @@ def test_auto_mode_picks_by_job_size(gpu_lib, oracle_lib):
 
 def test_tail_handoff_to_the_warp_integrator(gpu_lib, oracle_lib):
     """AUTO on a launch above twice the thread integrator's resident lanes (a 32 x 1 launch shape keeps 4,864
-    lanes): the thread integrator runs it and hands the queue's tail to the warp integrator.  Against the
-    thread integrator alone on the same trajectories, both capped at 300 attempts (the approach, where
-    trajectories are not chaotic): same statuses, attempt counts and points to 1e-8 on 99 % of them, the
-    counters add up; the queue path (its hand-off buffers carved from the batch) agrees the same way."""
+    lanes): the thread integrator runs it and hands the queue's tail to the warp integrator.  12,000
+    trajectories (64 initial conditions of 930 to 11,550 attempts, repeated) capped at 3,000 attempts, against
+    the thread integrator alone: a trajectory that never left the thread integrator ran the same arithmetic,
+    so at least n - (hand-offs) end bit for bit where the thread run ends; every one conserves H; statuses
+    agree; the counters add up.  The queue path (its hand-off buffers carved from the batch) the same way."""
     cfg, o, H = _setup("N3")
     H.check(H.lib.cair_set_launch_shape(H.h, 32, 1), "cair_set_launch_shape")
     ic = _ics(o, "N3", 64, seed=7)
-    n, cap = 12000, 300
+    n, cap = 12000, 3000
     paq, erra = np.resize(ic["paq"], (n, 12)), np.resize(ic["erra"], (n, 12))
+    H0 = np.resize(ic["H0"], n)
     H.integrator_mode = "thread"
     ref = api.Trajectories.start(paq, erra, cfg.dt0)
     api.Integrator(H).Integrate(ref, max_attempts=cap)
@@ -211,26 +213,30 @@ def test_tail_handoff_to_the_warp_integrator(gpu_lib, oracle_lib):
     tr = api.Trajectories.start(paq, erra, cfg.dt0)
     api.Integrator(H).Integrate(tr, max_attempts=cap)
     handed = H.last_handoffs()
-    assert H.last_integrator == "thread" and handed > 0
+    assert H.last_integrator == "thread"
     c = H.counters()
     assert c["attempts"] == int(np.sum(tr.iste + tr.irej))
-    assert np.all(tr.status == ref.status)
-    same_att = np.mean(tr.iste + tr.irej == ref.iste + ref.irej)
-    rel = np.abs(tr.paq - ref.paq).max(axis=1) / np.abs(ref.paq).max(axis=1)
-    print("tail hand-off: %d of %d trajectories finished on warps; attempts equal on %.4f, 99th percentile of "
-          "the point difference %.2e" % (handed, n, same_att, np.quantile(rel, 0.99)))
-    assert same_att >= 0.99 and np.quantile(rel, 0.99) < 1e-8
+    exact = np.all(tr.paq == ref.paq, axis=1) & (tr.iste == ref.iste) & (tr.irej == ref.irej)
+    print("tail hand-off: %d of %d trajectories finished on warps; %d end bit for bit as on the thread "
+          "integrator alone; statuses equal on %.4f" % (handed, n, int(exact.sum()), np.mean(tr.status == ref.status)))
+    assert handed > 0
+    assert exact.sum() >= n - handed
+    assert np.max(np.abs(tr.H - H0)) < cfg.ham_abs_tol
+    assert np.mean(tr.status == ref.status) >= 0.98
     # the queue path
     lv = systems.load_levels("N2")
     table = api.level_table(lv[(lv["vqn"] == 0) & (lv["jqn"] == 10)])
     items = api.work_items([(0, 0, n, api.process_seed(5, 1), 10000.0, 7.0, 15.0)])
     H.integrator_mode = "thread"
-    rows_t = api.RunTrajectories(H).run(table, items, max_attempts=400)
+    rows_t = api.RunTrajectories(H).run(table, items, max_attempts=cap)
     H.integrator_mode = "auto"
-    rows_a = api.RunTrajectories(H).run(table, items, max_attempts=400)
-    assert H.last_handoffs() > 0
-    assert np.all(rows_a["status"] == rows_t["status"])
-    for key in ("j_f", "v_f", "arr_f"):
-        d = np.abs(rows_a[key] - rows_t[key])
-        assert np.mean(d < 1e-6) >= 0.99, key
+    rows_a = api.RunTrajectories(H).run(table, items, max_attempts=cap)
+    handed = H.last_handoffs()
+    same = np.ones(n, bool)
+    for key in ("j_f", "v_f", "arr_f", "t", "dH", "iste", "irej"):
+        same &= rows_a[key] == rows_t[key]
+    print("queue path: %d handed off, %d rows bit for bit" % (handed, int(same.sum())))
+    assert handed > 0 and same.sum() >= n - handed
+    assert np.mean(rows_a["status"] == rows_t["status"]) >= 0.98
+    assert np.max(np.abs(rows_a["dH"])) < cfg.ham_abs_tol
     H.close()
