@@ -665,7 +665,7 @@ static int launch_integrate(cair_handle* h, const IntegrateArgs& A0, cudaStream_
   }
   h->last_integrator = (!h->sur && warp) ? CAIR_INTEGRATOR_WARP : CAIR_INTEGRATOR_THREAD;
   if (!h->sur && warp) {
-    // a warp per trajectory: CTAs of warp_cta_warps(S) warps, as many as fit on every SM
+    // a warp per trajectory: as many CTAs as fit on every SM
     cudaEvent_t w0 = nullptr, w1 = nullptr;
     if (h->time_integrate) {
       if (2 * h->ntev + 2 > h->tev.size()) {

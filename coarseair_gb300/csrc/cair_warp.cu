@@ -502,9 +502,4 @@ int64_t warp_resident_warps(int nsm, const DevSys& S) {
   });
 }
 
-int warp_cta_warps(const DevSys& S) {
-  if (!warp_integrate_supported(S)) return 0;
-  return with_warp_model(S, [&](auto m) { return WLaunch<decltype(m)::value>::CTA; });
-}
-
 }  // namespace cair
