@@ -9,8 +9,10 @@ device, integrates every trajectory to the end of the collision with the persist
 kernel, and analyses the initial and final points into trajectories.out rows.  The default step is
 the full 1M-trajectory configuration as one queue: trajectory lengths span 30x (slow collisions run
 to tmax), and on GB300 a lone FP64 thread barely speeds up once its SM empties, so the longest
-trajectories must start at the beginning of a job long enough to hide them (the queue is ordered
-longest-first); smaller steps (--ntraj) are dominated by their slowest trajectory.
+trajectories start at the beginning of the job (the queue is ordered longest-first) and, in the default
+AUTO integrator mode, the queue's last trajectories move to the warp integrator (a warp per trajectory)
+once fewer are left than it has resident warps.  Steps below twice the thread integrator's resident lanes
+(--ntraj, --system o3) run on the warp integrator from the start.
 
 value: device-resident inputs, CUDA events on the launch stream around K steps.
 e2e:   the public host entry point cair_run_queue from pinned host buffers (level table and work
