@@ -879,7 +879,7 @@ def compile_model(surface, tabs):
                     nslot += 1
                 slot[n] = s_
                 release.setdefault(last.get(n, L), []).append(s_)
-        progs[name] = dict(levels=levels, ins=ins, slot=slot, outs=[slot[o] for o in outset],
+        progs[name] = dict(levels=levels, ins=ins, slot=slot, outs=[slot[o] for o in outset], out_nodes=outset,
                            ins_slots=[base_in + i for i in range(ninp)], nslot=nslot)
     nslot = max(p["nslot"] for p in progs.values())
     return dict(progs=progs, const_list=const_list, nconst=nconst, cprog=cprog_levels, nslot=nslot, lanes=lanes,
