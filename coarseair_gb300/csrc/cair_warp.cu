@@ -385,8 +385,10 @@ __global__ void __launch_bounds__(32 * WLaunch<MODEL>::CTA, 1) k_warp_eval(DevSy
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t base = NG * ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5); base < n; base += NG * nwarps) {
     const int64_t k = base + grp < n ? base + grp : base;
-    const DevPes& P = S.pes[ipes ? ipes[k] : 0];
-    for (int i = gl; i < M.nconst; i += W) s[i] = wp_const(M, S, P, i);
+    const int ip = ipes ? ipes[k] : 0;
+    const bool ok = ip >= 0 && ip < S.npes;  // a surface index out of range gives NaN, not a read past S.pes
+    const DevPes& P = S.pes[ok ? ip : 0];
+    for (int i = gl; i < M.nconst; i += W) s[i] = ok ? wp_const(M, S, P, i) : __longlong_as_double(0x7ff8000000000000ll);
     __syncwarp();
     run_levels<W>(M.cprog, s, gl);
     const double v = io ? y[NE * k + gl] : 0.0;
