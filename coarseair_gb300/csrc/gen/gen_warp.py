@@ -737,7 +737,8 @@ def operands(ins, n):
 
 
 def schedule(ins, nodes, width):
-    """Levels of at most `width` instructions of one kind, by longest remaining path."""
+    """Levels of at most `width` instructions of one kind, by longest remaining path, none costlier than the
+    level's most critical instruction."""
     nodes = set(nodes)
     deps = {n: [x for x in operands(ins, n) if x in nodes] for n in nodes}
     users = {n: [] for n in nodes}
@@ -753,9 +754,12 @@ def schedule(ins, nodes, width):
     pending = {n: len(set(deps[n])) for n in nodes}
     ready = [n for n in nodes if pending[n] == 0]
     while ready:
+        # the most critical ready instruction sets the level's kind and its cost: a costlier instruction
+        # would hold the level's lanes longer than the critical path needs, so it waits for a later level
         best = max(ready, key=lambda n: (prio[n], -abs(n)))
-        kind = ins[best][0]
-        cand = sorted([n for n in ready if ins[n][0] == kind], key=lambda n: (-prio[n], abs(n)))[:width]
+        kind, budget = ins[best][0], cost[best]
+        cand = sorted([n for n in ready if ins[n][0] == kind and cost[n] <= budget],
+                      key=lambda n: (-prio[n], abs(n)))[:width]
         levels.append((kind, cand))
         cs = set(cand)
         ready = [n for n in ready if n not in cs]
