@@ -414,3 +414,48 @@ extern "C" int warp_host_eval(const void* devsys, const double* packed, const in
 extern "C" void host_fexp(int64_t n, const double* x, double* y) {
   for (int64_t i = 0; i < n; ++i) y[i] = fexp(x[i]);
 }
+
+// The thread integrator with its tail hand-off on the host (one lane): n diatom + atom trajectories from
+// paq/erra; once the queue is empty and at most hand_below are in flight, a trajectory is written back at its
+// end check and listed in hand[] (hctl: in flight, hand-offs).  status[] is left as the caller set it for a
+// handed-off trajectory.
+template <int MODEL>
+static void handoff_run(const DevSys& S, int64_t n, double* paq, const double* erra, int64_t max_attempts,
+                        long long hand_below, double* t, double* dt, double* H, int32_t* irej, int32_t* iste,
+                        int32_t* status, int32_t* hand, long long* hand_att, unsigned long long* hctl) {
+  std::vector<double> smax(n, -1.7976931348623157e308), smin(n, 1.7976931348623157e308);
+  for (int64_t k = 0; k < n; ++k) {
+    t[k] = 0.0;
+    dt[k] = S.dt0;
+    irej[k] = iste[k] = 0;
+  }
+  unsigned long long ctl[6] = {0, 0, 0, 0, 0, 0};
+  IntegrateArgs A{n, nullptr, paq, t, dt, erra, H, smax.data(), smin.data(), irej, iste, status, max_attempts,
+                  ctl, ctl + 1, nullptr};
+  A.hand = hand;
+  A.hand_att = hand_att;
+  A.hctl = hctl;
+  A.hand_below = hand_below;
+  k_integrate<MODEL, 3>(S, A);
+}
+
+extern "C" int handoff_host_run(const void* devsys, const double* packed, const int64_t* offsets, int64_t n,
+                                double* paq, const double* erra, int64_t max_attempts, long long hand_below,
+                                double* t, double* dt, double* H, int32_t* irej, int32_t* iste, int32_t* status,
+                                int32_t* hand, long long* hand_att, unsigned long long* hctl) {
+  DevSys S;
+  std::memcpy(&S, devsys, sizeof S);
+  for (int p = 0; p < S.npes; ++p) S.pes[p].coef = packed + offsets[p];
+  if (S.nsteps != 3) return 1;
+  switch (S.pes[0].model) {
+    case CAIR_PES_O3_UMN:
+      handoff_run<CAIR_PES_O3_UMN>(S, n, paq, erra, max_attempts, hand_below, t, dt, H, irej, iste, status, hand,
+                                   hand_att, hctl);
+      return 0;
+    case CAIR_PES_N3_UMN:
+      handoff_run<CAIR_PES_N3_UMN>(S, n, paq, erra, max_attempts, hand_below, t, dt, H, irej, iste, status, hand,
+                                   hand_att, hctl);
+      return 0;
+    default: return 1;
+  }
+}

@@ -48,6 +48,9 @@ def _harness():
     L.queue_host_run.restype = C.c_int
     L.queue_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
                                  C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.c_void_p]
+    L.handoff_host_run.restype = C.c_int
+    L.handoff_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64,
+                                   C.c_longlong] + [C.c_void_p] * 9
     L.host_fexp.restype = None
     L.host_fexp.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
     L.warp_host_eval.restype = C.c_int
@@ -375,3 +378,46 @@ def test_table_driven_exponential_within_one_ulp():
     err = np.abs(y - ref) / ulp
     print("fexp vs libm exp: max %.3f ulp, mean %.4f ulp, %.5f exact" % (err.max(), err.mean(), np.mean(err == 0)))
     assert err.max() <= 1.0
+
+
+@pytest.mark.parametrize("below", [0, 1])
+def test_thread_integrator_hands_its_tail_off(gpu_lib, oracle_lib, below):
+    """The thread integrator's tail hand-off, run on the host (one lane, four N2 + N trajectories).  With the
+    hand-off off every trajectory ends normally.  With it on at one trajectory in flight, the last trajectory
+    (the one in flight once the queue is empty) is written back at its first end check: listed once, its
+    attempts recorded (ncall), its status left to the warp integrator, and its state, time, step and counts
+    exactly those of ncall attempts of the same Bulirsch-Stoer code from its initial conditions."""
+    from oracle import Oracle
+    cfg = systems.n3_config()
+    o = Oracle(cfg)
+    L = _harness()
+    devsys, packed, offsets, _ = _setup(gpu_lib, cfg, o.tpq)
+    lv = systems.load_levels("N2")
+    ic = o.sample_ics(4, lv[(lv["vqn"] == 0) & (lv["jqn"] == 10)], seed=17)
+    n = 4
+    paq = np.ascontiguousarray(ic["paq"], np.float64).copy()
+    erra = np.ascontiguousarray(ic["erra"], np.float64)
+    t, dt, H = np.zeros(n), np.zeros(n), np.zeros(n)
+    irej, iste, status = np.zeros(n, np.int32), np.zeros(n, np.int32), np.full(n, -7, np.int32)
+    hand, hand_att, hctl = np.full(n, -1, np.int32), np.zeros(n, np.int64), np.zeros(3, np.uint64)
+    assert L.handoff_host_run(devsys, packed.ctypes.data, offsets.ctypes.data, n, paq.ctypes.data, erra.ctypes.data,
+                              10 ** 6, below, t.ctypes.data, dt.ctypes.data, H.ctypes.data, irej.ctypes.data,
+                              iste.ctypes.data, status.ctypes.data, hand.ctypes.data, hand_att.ctypes.data,
+                              hctl.ctypes.data) == 0
+    if below == 0:
+        assert int(hctl[1]) == 0 and np.all(status == 0)
+        return
+    assert int(hctl[1]) == 1 and hand[0] == n - 1
+    assert np.all(status[:n - 1] == 0) and status[n - 1] == -7
+    assert hand_att[n - 1] == cfg.ncall and iste[n - 1] + irej[n - 1] == cfg.ncall
+    assert int(hctl[0]) == 1                      # taken four, finished three
+    # the same ncall attempts through the fixed-attempt host code
+    y = np.ascontiguousarray(ic["paq"][n - 1:n], np.float64).copy()
+    e = np.ascontiguousarray(ic["erra"][n - 1:n], np.float64)
+    t1, dt1 = np.zeros(1), np.full(1, cfg.dt0)
+    ip = np.zeros(1, np.int32)
+    assert L.pes_host_bs_steps(devsys, packed.ctypes.data, offsets.ctypes.data, 1, ip.ctypes.data, y.ctypes.data,
+                               t1.ctypes.data, dt1.ctypes.data, e.ctypes.data, cfg.ncall) == 0
+    assert np.array_equal(paq[n - 1], y[0]) and t[n - 1] == t1[0] and dt[n - 1] == dt1[0]
+    h_o, _ = o.hamiltonian(paq[n - 1:n])
+    assert abs(H[n - 1] - h_o[0]) < 1e-12 * max(abs(h_o[0]), 0.1)
