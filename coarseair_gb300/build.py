@@ -21,7 +21,8 @@ SOURCES = [("cair_api.cu", "cair_api.o", []), ("cair_output.cpp", "cair_output.o
            ("cair_sur_probe.cu", "cair_sur_probe.o", []), ("cair_warp.cu", "cair_warp.o", []),
            ("cair_parity.cu", "cair_parity.o", ["-fmad=false"])] + [
     ("cair_model.cu", "cair_model_%s.o" % name, ["-DCAIR_MODEL_ID=%d" % mid])
-    for name, mid in (("o3_umn", 1), ("n3_umn", 2), ("o4_umn", 3), ("o3_nn", 4), ("n4_umn", 5), ("o3_bnn", 6))]
+    for name, mid in (("o3_umn", 1), ("n3_umn", 2), ("o4_umn", 3), ("o3_nn", 4), ("n4_umn", 5), ("o3_bnn", 6),
+                      ("n4_pipnn", 7))]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177",
                      "-I", os.path.join(HERE, "..", "include")]

@@ -32,6 +32,7 @@ struct cair_handle {
   DevSys sys;
   FsArgs fs;
   double* d_coef[CAIR_MAX_PES] = {nullptr};
+  double nnets[CAIR_MAX_PES] = {0.0};      // N4 PIPNN: networks selected per surface (flop model)
   double* d_gauss = nullptr;
   double tqp[81], tpq[81];
   double mass[4];
@@ -340,6 +341,10 @@ std::string setup_system(const cair_system_desc* d, DevSys& S, double* tqp, doub
   S.ncall = d->ncall;
   S.incstp = d->inc_step;
   S.diat = d->diat_model;
+  if (d->diat_model < CAIR_DIAT_O2_UMN || d->diat_model > CAIR_DIAT_N2_UMN_PIPNN_FORN4)
+    return fail_setup(code, CAIR_EINVAL, "unknown diatomic model");
+  if (d->diat_model == CAIR_DIAT_N2_UMN_PIPNN_FORN4 && d->pes[0].model != CAIR_PES_N4_PIPNN)
+    return fail_setup(code, CAIR_EUNSUPPORTED, "the UMN_PIPNN_ForN4 diatomic is built for the N4 UMN PIPNN surface");
   S.relax = d->relax;
   S.eps = d->eps;
   S.dt0 = d->dt0;
@@ -390,6 +395,7 @@ std::string setup_system(const cair_system_desc* d, DevSys& S, double* tqp, doub
     const cair_pes_desc& src = d->pes[p];
     int expect = src.model == CAIR_PES_O3_UMN ? 56 : (src.model == CAIR_PES_N3_UMN || src.model == CAIR_PES_N4_UMN) ? 276
                  : src.model == CAIR_PES_O4_UMN ? 430 : (src.model == CAIR_PES_O3_NN || src.model == CAIR_PES_O3_BNN) ? 0
+                 : src.model == CAIR_PES_N4_PIPNN ? CAIR_PIPNN_HDR + 3 * CAIR_PIPNN_NET
                  : -1;
     if (expect < 0) return fail_setup(code, CAIR_EINVAL, "unknown surface model");
     std::vector<double> packed;
@@ -404,11 +410,23 @@ std::string setup_system(const cair_system_desc* d, DevSys& S, double* tqp, doub
       if (d->natoms != 3) return fail_setup(code, CAIR_EINVAL, "surface/atom count mismatch");
     } else if (src.ncoef != expect || !src.coef) {
       return fail_setup(code, CAIR_EINVAL, "wrong coefficient count for surface");
+    } else if (src.model == CAIR_PES_N4_PIPNN) {
+      // UseSurface(3) of 0/1, at least one set; iFunc 1..3; the 276-5-90-1 networks of the shipped fit
+      const double* c = src.coef;
+      const bool use_ok = (c[0] == 0.0 || c[0] == 1.0) && (c[1] == 0.0 || c[1] == 1.0) &&
+                          (c[2] == 0.0 || c[2] == 1.0) && c[0] + c[1] + c[2] >= 1.0;
+      if (!use_ok) return fail_setup(code, CAIR_EINVAL, "N4 PIPNN: UseSurface must be 0/1 with one network selected");
+      if (!(c[3] == 1.0 || c[3] == 2.0 || c[3] == 3.0)) return fail_setup(code, CAIR_EINVAL, "N4 PIPNN: iFunc must be 1, 2 or 3");
+      if (c[4] != CAIR_PIPNN_NIN || c[5] != CAIR_PIPNN_H1 || c[6] != CAIR_PIPNN_H2 || c[7] != 1.0)
+        return fail_setup(code, CAIR_EUNSUPPORTED, "N4 PIPNN: the kernels are built for 276-5-90-1 networks");
+      for (int i = 0; i < src.ncoef; ++i)
+        if (!std::isfinite(c[i])) return fail_setup(code, CAIR_ENONFINITE, "N4 PIPNN: non-finite coefficient");
+      packed.assign(src.coef, src.coef + src.ncoef);
     } else {
       packed.assign(src.coef, src.coef + src.ncoef);
     }
     if (src.model != d->pes[0].model) return fail_setup(code, CAIR_EUNSUPPORTED, "all surfaces of a handle must share a model");
-    if ((src.model == CAIR_PES_O4_UMN || src.model == CAIR_PES_N4_UMN) != (d->natoms == 4))
+    if ((src.model == CAIR_PES_O4_UMN || src.model == CAIR_PES_N4_UMN || src.model == CAIR_PES_N4_PIPNN) != (d->natoms == 4))
       return fail_setup(code, CAIR_EINVAL, "surface/atom count mismatch");
     DevPes& P = S.pes[p];
     P.model = src.model;
@@ -464,6 +482,7 @@ int cair_create(cair_handle** out, const cair_system_desc* d) {
           cudaSuccess)
         return bad(CAIR_ECUDA, "cudaMemcpy coefficients");
       P.coef = h->d_coef[p];
+      if (P.model == CAIR_PES_N4_PIPNN) h->nnets[p] = packed[p][0] + packed[p][1] + packed[p][2];
     }
   }
   // final-state analysis parameters and Chebyshev-2 nodes (GAUSSQ kind 3)
@@ -1279,6 +1298,17 @@ int cair_flop_model(const cair_handle* h, int32_t ipes, double* fg, double* fe, 
     if (fe) *fe = 9 + 3 * diat_g + 21 + 140 + 430 + 4 + 36 + 30 + 8 + 2 * bo;
     if (fa) *fa = 811;
     if (ex) *ex = 3.0 * ((o2 ? 8 : 1) + 1) + CAIR_NN_H1 + CAIR_NN_H2 + bo;
+    return 0;
+  }
+  if (m == CAIR_PES_N4_PIPNN) {
+    // no force from the surface (dVdQ = 0): Hamilton's equations 45 and the assembly of zeros; the
+    // energy: six pair terms (~60 each), six exponentials, the 276-function basis and per selected
+    // network 276 normalisations (2) and 5 x 276 + 90 x 5 + 90 multiply-adds (2), 95 activations (~12)
+    const double nuse = h->nnets[ipes];
+    if (fg) *fg = 45 + 15;
+    if (fe) *fe = 6 * 60 + 6 + PIP_N4_BASIS_FLOPS + nuse * (2 * 276 + 2 * (5 * 276 + 90 * 5 + 90) + 95 * 12 + 2) + 72 + 45 + 8;
+    if (fa) *fa = 811.0 * 18.0 / 12.0;
+    if (ex) *ex = 6.0 + nuse * 95.0;
     return 0;
   }
   if (m == CAIR_PES_O4_UMN || m == CAIR_PES_N4_UMN) {

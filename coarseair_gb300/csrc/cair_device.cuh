@@ -154,10 +154,64 @@ __device__ __forceinline__ void n2_umn(double r, double& v, double& dv) {
   }
 }
 
+// The pair term of the N4 UMN PIPNN surface and the N2 UMN_PIPNN_ForN4 diatomic: Ev2gm2 (and
+// Ev2gm2_Grad) with the D3(BJ) dispersion of an N-N pair (iz = 7, r2r4 = 2.71175247, C6 = 19.7,
+// rs6 = 0.5299, rs8 = 2.20), N4_UMN_PIPNN_PES_Class.F90:1471-1748 and
+// N2_UMN_PIPNN_ForN4_DiatomicPotential_Class.F90:116-365.  r [Ang] -> kcal/mol, kcal/mol/Ang.
+template <bool GRAD>
+__device__ __forceinline__ void n2p_ev2gm2(double r, double& v, double& dv) {
+  const double as0 = 2.7475450369759, as1 = 0.218868498415108, as2 = 0.248885765371433,
+               as3 = -0.229295466336412, as4 = -0.653389048592838, as5 = 1.03611964035396,
+               as6 = 1.71287482791961;
+  const double de = 225.213, re = 1.098, re4 = (re * re) * (re * re);
+  const double r2 = r * r, r3 = r2 * r, r4 = r2 * r2;
+  const double y = (r4 - re4) / (r4 + re4);
+  const double y2 = y * y, y3 = y * y2, y4 = y2 * y2, y5 = y2 * y3, y6 = y3 * y3;
+  const double fy = as0 + as1 * y + as2 * y2 + as3 * y3 + as4 * y4 + as5 * y5 + as6 * y6;
+  const double u = fexp(-(fy * (r - re)));
+  // edisp on the distance in bohr
+  const double c6 = 19.7, c8 = ((3.0 * c6) * 2.71175247) * 2.71175247;
+  const double sd = 0.5299 * sqrt(c8 / c6) + 2.20;
+  const double s2 = sd * sd, s3 = s2 * sd, s4 = s2 * s2, s6 = s3 * s3, s8 = s4 * s4;
+  const double rb = r / CAIR_B_TO_ANG;
+  const double b2 = rb * rb, b3 = b2 * rb, b4 = b2 * b2, b6 = b3 * b3, b8 = b4 * b4;
+  const double d6 = b6 + s6, d8 = b8 + s8;
+  const double e6 = c6 / d6, e8 = c8 / d8;
+  const double h2k = 1.0 / CAIR_KCM_TO_HARTREE;
+  v = ((de * (1.0 - u)) * (1.0 - u) - de) + (0.0 + (-e6 - 2.0 * e8) * h2k);
+  if (GRAD) {
+    const double dfdy = as1 + 2.0 * as2 * y + 3.0 * as3 * y2 + 4.0 * as4 * y3 + 5.0 * as5 * y4 + 6.0 * as6 * y5;
+    const double rr = r4 + re4;
+    const double dfdr = dfdy * (((8.0 * r3) * re4) / (rr * rr));
+    const double e6dr = c6 * (-(6.0 * (b3 * b2))) / (d6 * d6);
+    const double e8dr = c8 * (-(8.0 * (b4 * b3))) / (d8 * d8);
+    dv = (((2.0 * de) * (1.0 - u)) * u) * (dfdr * (r - re) + fy) + ((-e6dr - 2.0 * e8dr) * h2k) / CAIR_B_TO_ANG;
+  }
+}
+
+// N2 UMN_PIPNN_ForN4 (DiatomicPotential_N2 / Compute_Vd_dVd_N2): V [Eh], dV/dR [Eh/bohr]
+template <bool GRAD>
+__device__ __forceinline__ void n2_pipnn(double r, double& v, double& dv) {
+  double vk, dk = 0.0;
+  n2p_ev2gm2<GRAD>(r * CAIR_B_TO_ANG, vk, dk);
+  v = vk * CAIR_KCM_TO_HARTREE + 0.0;
+  if (GRAD) dv = dk * CAIR_KCM_TO_HARTREE * CAIR_B_TO_ANG;
+}
+
+// The diatomic of the surfaces' own pair terms (O2 UMN, N2 UMN_ForN4)
 template <bool GRAD>
 __device__ __forceinline__ void diat(const DevSys& S, double r, double& v, double& dv) {
   if (S.diat == CAIR_DIAT_O2_UMN) o2_umn<GRAD>(S, r, v, dv);
   else n2_umn<GRAD>(r, v, dv);
+}
+
+// The system's diatomic for initial conditions and final states: any of the three.  The UMN_PIPNN_ForN4
+// one comes with the N4 UMN PIPNN surface only, whose pair term is its own, so the surfaces' kernels
+// keep the two-way choice above.
+template <bool GRAD>
+__device__ __forceinline__ void diat_any(const DevSys& S, double r, double& v, double& dv) {
+  if (S.diat == CAIR_DIAT_N2_UMN_PIPNN_FORN4) n2_pipnn<GRAD>(r, v, dv);
+  else diat<GRAD>(S, r, v, dv);
 }
 
 }  // namespace cair
@@ -166,6 +220,7 @@ __device__ __forceinline__ void diat(const DevSys& S, double r, double& v, doubl
 #include "generated/pip_o3.cuh"
 #include "generated/pip_o4.cuh"
 #include "generated/pip_n4.cuh"
+#include "generated/pip_n4nn.cuh"
 // gradient of the PIP part: reverse mode (adjoint sweep) unless CAIR_PIP_FORWARD selects the
 // forward mode, whose operation order is the reference's
 #ifdef CAIR_PIP_FORWARD
@@ -490,10 +545,126 @@ __device__ __forceinline__ void pes_n4(const DevSys& S, const DevPes& P, const d
   }
 }
 
+// N4 UMN PIPNN (N4_UMN_PIPNN_PES_Class.F90).  Coefficients as packed at cair_create:
+// UseSurface(3), iFunc, NInput = 276, NHid1 = 5, NHid2 = 90, NOutput = 1, then per network
+// pdel(277), pavg(277), W1(276, 5), b1(5), W2(5, 90), b2(90), W3(90), b3.
+#define CAIR_PIPNN_HDR 8
+#define CAIR_PIPNN_NIN 276
+#define CAIR_PIPNN_H1 5
+#define CAIR_PIPNN_H2 90
+#define CAIR_PIPNN_NET (2 * (CAIR_PIPNN_NIN + 1) + CAIR_PIPNN_NIN * CAIR_PIPNN_H1 + CAIR_PIPNN_H1 + \
+                        CAIR_PIPNN_H1 * CAIR_PIPNN_H2 + 2 * CAIR_PIPNN_H2 + 1)
+
+// tranfun (962-984): 1 tansig, 2 logsig, 3 purelin
+__device__ __forceinline__ double pipnn_tranfun(double x, int ifunc) {
+  if (ifunc == 1) return ftanh(x);
+  if (ifunc == 2) return 1.0 / (1.0 + fexp(-x));
+  return x;
+}
+
+// getpot (743-799): the inputs normalised, two hidden layers, the linear output de-normalised.  Each
+// neuron's sum runs from its bias over its inputs in ascending order, as the reference's loops do;
+// the second hidden layer feeds the output sum neuron by neuron.
+__device__ __forceinline__ double pipnn_net(const double* __restrict__ c, int ifunc, const double* b) {
+  const double* __restrict__ pdel = c;
+  const double* __restrict__ pavg = pdel + CAIR_PIPNN_NIN + 1;
+  const double* __restrict__ W1 = pavg + CAIR_PIPNN_NIN + 1;
+  const double* __restrict__ b1 = W1 + CAIR_PIPNN_NIN * CAIR_PIPNN_H1;
+  const double* __restrict__ W2 = b1 + CAIR_PIPNN_H1;
+  const double* __restrict__ b2 = W2 + CAIR_PIPNN_H1 * CAIR_PIPNN_H2;
+  const double* __restrict__ W3 = b2 + CAIR_PIPNN_H2;
+  const double* __restrict__ b3 = W3 + CAIR_PIPNN_H2;
+  double a[CAIR_PIPNN_H1];
+#pragma unroll
+  for (int j = 0; j < CAIR_PIPNN_H1; ++j) a[j] = b1[j];
+#pragma unroll 4
+  for (int i = 0; i < CAIR_PIPNN_NIN; ++i) {
+    const double y = (b[i] - pavg[i]) / pdel[i];
+#pragma unroll
+    for (int j = 0; j < CAIR_PIPNN_H1; ++j) a[j] = a[j] + y * W1[i + CAIR_PIPNN_NIN * j];
+  }
+#pragma unroll
+  for (int j = 0; j < CAIR_PIPNN_H1; ++j) a[j] = pipnn_tranfun(a[j], ifunc);
+  double o = b3[0];
+#pragma unroll 2
+  for (int k = 0; k < CAIR_PIPNN_H2; ++k) {
+    double h = b2[k];
+#pragma unroll
+    for (int j = 0; j < CAIR_PIPNN_H1; ++j) h = h + a[j] * W2[j + CAIR_PIPNN_H1 * k];
+    o = o + pipnn_tranfun(h, ifunc) * W3[k];
+  }
+  return o * pdel[CAIR_PIPNN_NIN] + pavg[CAIR_PIPNN_NIN];
+}
+
+// n4pipNN (450-657) in kcal/mol at the bond lengths rb [Ang]: the six N2 pair terms, the N4 PIP basis
+// of exp(-rb / alpha) (alpha = 1), the mean of the selected networks (eV) times 23.0605, minus VInf
+// (the mean of the selected networks' values at infinite separation, line 96).
+__device__ __forceinline__ double pipnn_kcal(const double* __restrict__ c, const double* rb) {
+  double vn2 = 0.0, x[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double v, d;
+    n2p_ev2gm2<false>(rb[i], v, d);
+    vn2 = vn2 + v;
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) x[i] = fexp(-rb[i]);
+  double b[CAIR_PIPNN_NIN];
+  pip_n4_basis(x, b);
+  const int ifunc = (int)c[3];
+  const double vinf_s[3] = {-0.021346263746904, -0.196886061330806, -0.030606048118131};
+  double vs[3] = {0.0, 0.0, 0.0}, vinf = 0.0;
+  int nuse = 0;
+#pragma unroll 1
+  for (int k = 0; k < 3; ++k)
+    if (c[k] == 1.0) {
+      vs[k] = pipnn_net(c + CAIR_PIPNN_HDR + k * CAIR_PIPNN_NET, ifunc, b);
+      vinf = vinf + vinf_s[k];
+      nuse += 1;
+    }
+  vinf = vinf / (double)nuse;
+  const double v = ((vs[0] + vs[1]) + vs[2]) / (double)nuse;
+  return (v * 23.0605 + vn2) - vinf;
+}
+
+// Compute_N4_UMN_PIPNN_PES_1d (410-439): V, dVdR by n4pipNN's central differences (dr = 1e-5 Ang; the
+// bond lengthened by dr, then shortened by 2 dr, then restored, one bond after the other) and
+// dVdQ = 0, which the reference returns, so the surface exerts no force on the trajectories (Hamilton's
+// equations for this model skip it).  One evaluation site in a loop keeps the kernels to one copy of
+// the 276-function basis.
+template <bool GRAD>
+__device__ __forceinline__ void pes_n4pipnn(const DevSys& S, const DevPes& P, const double* R, double& V,
+                                            double* dVdR, double* dVdQ) {
+  const double* __restrict__ c = P.coef;
+  const double dr = 1.0e-5;
+  double rb[6], vp = 0.0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) rb[i] = R[i] * CAIR_B_TO_ANG;
+#pragma unroll 1
+  for (int e = 0; e < (GRAD ? 13 : 1); ++e) {
+    const int i = (e - 1) >> 1;
+    if (e > 0) rb[i] = (e & 1) ? rb[i] + dr : rb[i] - 2.0 * dr;
+    const double v = pipnn_kcal(c, rb);
+    if (e == 0) {
+      V = v * CAIR_KCM_TO_HARTREE;
+    } else if (e & 1) {
+      vp = v;
+    } else {
+      dVdR[i] = ((vp - v) / (2.0 * dr)) * CAIR_KCMANG_TO_HARTB;
+      rb[i] = rb[i] + dr;
+    }
+  }
+  if (GRAD) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) dVdQ[i] = 0.0;
+  }
+}
+
 // Sizes of a surface model's system: atoms, NEqtVar, NEqtTot, pairs
 template <int MODEL>
 struct Traits {
-  static constexpr int NA = (MODEL == CAIR_PES_O4_UMN || MODEL == CAIR_PES_N4_UMN) ? 4 : 3;
+  static constexpr int NA =
+      (MODEL == CAIR_PES_O4_UMN || MODEL == CAIR_PES_N4_UMN || MODEL == CAIR_PES_N4_PIPNN) ? 4 : 3;
   static constexpr int NV = 3 * (NA - 1);
   static constexpr int NE = 2 * NV;
   static constexpr int NP = NA * (NA - 1) / 2;
@@ -507,6 +678,7 @@ __device__ __forceinline__ void pes(const DevSys& S, const DevPes& P, const doub
   else if (MODEL == CAIR_PES_O3_BNN) pes_o3nn<GRAD, true>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else if (MODEL == CAIR_PES_O4_UMN) pes_o4<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
   else if (MODEL == CAIR_PES_N4_UMN) pes_n4<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
+  else if (MODEL == CAIR_PES_N4_PIPNN) pes_n4pipnn<GRAD>(S, P, R, V, dVdR, dVdQ);
   else pes_n3<GRAD>(S, P, R, Ri, Q, V, dVdR, dVdQ);
 }
 
@@ -579,6 +751,12 @@ struct Rhs {
 #pragma unroll
       for (int i = i0 + 3; i < T::NV; i += 3) acc = acc + S.Tpq[j + 9 * i] * y[i];
       yp[T::NV + j] = acc;
+    }
+    if (MODEL == CAIR_PES_N4_PIPNN) {
+      // the surface's dVdQ is zero (Compute_N4_UMN_PIPNN_PES_1d), so dp/dt = -0
+#pragma unroll
+      for (int i = 0; i < T::NV; ++i) yp[i] = -0.0;
+      return;
     }
     double Q[3 * T::NA], R[T::NP], Ri[T::NP], V, dVdR[T::NP], dVdQ[T::NV];
 #pragma unroll

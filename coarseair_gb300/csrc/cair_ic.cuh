@@ -129,7 +129,7 @@ struct RadialRhs {
   __device__ RadialRhs(const DevSys& s, double xm, double vc) : S(s), xmui(xm), vc_r2(vc) {}
   __device__ __forceinline__ void operator()(const double (&y)[2], double (&d)[2]) const {
     double v, dv;
-    diat<true>(S, y[0], v, dv);
+    diat_any<true>(S, y[0], v, dv);
     d[0] = y[1];
     d[1] = -xmui * (dv - 2.0 * vc_r2 / ((y[0] * y[0]) * y[0]));
   }

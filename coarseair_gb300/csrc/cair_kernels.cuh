@@ -312,7 +312,7 @@ struct FsArgs {
 
 __device__ __forceinline__ double diat_v(const DevSys& S, double r) {
   double v, dv;
-  diat<false>(S, r, v, dv);
+  diat_any<false>(S, r, v, dv);
   return v;
 }
 __device__ __forceinline__ double eff_pot(const DevSys& S, double r, double vc_r2) {
@@ -336,7 +336,7 @@ static __device__ int turning_point(const DevSys& S, double ra, double rc, doubl
   }
   for (int it = 0; it < nnew; ++it) {
     double vcen = vc_r2 / (rt * rt), vb, dvb;
-    diat<true>(S, rt, vb, dvb);
+    diat_any<true>(S, rt, vb, dvb);
     double v = vb + vcen;
     double dv = dvb - 2.0 * vcen / rt;
     rt = rt + (eint - v) / dv;

@@ -36,6 +36,7 @@ int parity_pes_launch(const DevSys& S, int grid, cudaStream_t st, int64_t n, con
 
 // Surface models with kernels in this library (one cair_model.cu object each)
 #define CAIR_FOR_EACH_MODEL(X) \
-  X(CAIR_PES_O3_UMN) X(CAIR_PES_N3_UMN) X(CAIR_PES_O4_UMN) X(CAIR_PES_O3_NN) X(CAIR_PES_N4_UMN) X(CAIR_PES_O3_BNN)
+  X(CAIR_PES_O3_UMN) X(CAIR_PES_N3_UMN) X(CAIR_PES_O4_UMN) X(CAIR_PES_O3_NN) X(CAIR_PES_N4_UMN) X(CAIR_PES_O3_BNN) \
+  X(CAIR_PES_N4_PIPNN)
 
 }  // namespace cair

@@ -25,6 +25,9 @@ Sources (paths inside the CoarseAIR tree):
        ``EvPoly`` 935-1249, ``evbas`` 1254-1325, ``EvdPdr`` 1330-1976, C(276) 108-201
 * O4:  src/PESs/O4_UMN_PES_Class.F90   ``EvMono`` 571-693, ``EvdMdR`` 698-824,
        ``EvPoly`` 829-1303, ``evbas`` 1308-1388, ``EvdPdr`` 1393-1875
+* N4 PIPNN: src/PESs/N4_UMN_PIPNN_PES_Class.F90 ``evmono49`` 1023-1145, ``evpoly49`` 1150-1466,
+       ``bmx2b109`` 1753-1830: checked equal to the N4 tables; its basis values feed the networks
+       (``generated/pip_n4nn.cuh``)
 
 The derivative routines (EvdMdR / EvdPdr / UnifiedBis) are parsed only to check
 that each of their statements is the product rule applied to the matching value
@@ -261,6 +264,14 @@ def load_surfaces(ref):
     nums = re.findall(r"[-+]?\d+\.\d*D[-+]?\d+", g.group(1), re.I)
     assert len(nums) == 276, len(nums)
     out["N4_C_text"] = nums
+    # N4 UMN PIPNN: its bemsav49 (evmono49 + evpoly49) and bmx2b109 build the same 276 basis functions
+    # from exp(-r / 1 Ang) (N4_UMN_PIPNN_PES_Class.F90:1004-1466, 1753-1830)
+    t = read(os.path.join(ref, "src/PESs/N4_UMN_PIPNN_PES_Class.F90"))
+    mono = parse_monomials(subroutine_body(t, "evmono49"), "m", "x")
+    poly = parse_polynomials(subroutine_body(t, "evpoly49"), "p", "m")
+    basis = parse_basis(subroutine_body(t, "bmx2b109"), "bm2", "bm1", len(poly))
+    assert (mono, poly, basis) == (out["N4"]["mono"], out["N4"]["poly"], out["N4"]["basis"]), \
+        "N4 UMN PIPNN basis differs from the N4 PIP"
     return out
 
 
@@ -436,6 +447,43 @@ def emit_device(S, key, name, zero_vars, dirs, path, coeff_symbol, value_only=Fa
     with open(path, mode) as f:
         f.write("\n".join(out) + "\n")
     return live_v, E.nt, nflop
+
+
+def emit_device_basis(S, key, name, path):
+    """Device function writing the basis functions themselves, b[i] = B_{i+1} for i < nbasis, from
+    the variables x, in the value function's rounding order (EvMono/EvPoly, then the basis map).
+    Signature: __device__ void name(const double x[NVAR], double b[NBASIS])."""
+    s = S[key]
+    mono, poly, basis = s["mono"], s["poly"], s["basis"]
+    E = Emitter()
+    mv = []
+    for t in mono:
+        if t[0] == "one":
+            mv.append("1.0")
+        elif t[0] == "var":
+            mv.append("x[%d]" % t[1])
+        else:
+            mv.append(E.tmp("%s * %s" % (mv[t[1]], mv[t[2]])))
+    pv = []
+    for t in poly:
+        if t[0] == "sum":
+            e = E.chain([("+", mv[x]) for x in t[1]])
+            pv.append(e if len(t[1]) == 1 else E.tmp(e))
+        else:
+            a, b, subs = t[1], t[2], t[3]
+            pv.append(E.tmp(E.chain([("+", "%s * %s" % (pv[a], pv[b]))] + [("-", pv[c]) for c in subs])))
+    nflop = sum(l.count("*") + l.count(" + ") + l.count(" - ") for l in E.lines)
+    out = ["/* %s: %d basis functions, %d temporaries, %d FP64 operations. Generated, do not edit. */" %
+           (name, len(basis), E.nt, nflop),
+           "#define %s_FLOPS %d" % (name.upper(), nflop),
+           "__device__ __forceinline__ void %s(const double* __restrict__ x, double* __restrict__ b) {" % name]
+    out.extend(E.lines)
+    for i, j in enumerate(basis):
+        out.append("  b[%d] = %s;" % (i, pv[j]))
+    out.append("}")
+    with open(path, "a") as f:
+        f.write("\n".join(out) + "\n")
+    return len(basis), E.nt, nflop
 
 
 def emit_device_reverse(S, key, name, zero_vars, dirs, path, coeff_symbol):
@@ -630,6 +678,13 @@ def main():
     info = emit_device_reverse(S, "N4", "pip_n4_eval_rev", zero_vars=set(), dirs=[0, 1, 2, 3, 4, 5], path=n4,
                                coeff_symbol="C")
     print("N4 reverse:", info)
+    # N4 UMN PIPNN: the basis functions themselves, the networks' input
+    nn = os.path.join(gen, "pip_n4nn.cuh")
+    with open(nn, "w") as f:
+        f.write("/* N4 PIP basis for the N4 UMN PIPNN networks (N4_UMN_PIPNN_PES_Class.F90 bemsav49/bmx2b109, the\n"
+                " * same tables as N4_UMN_PES_Class.F90 EvMono/EvPoly/evbas). Generated by gen_pip.py, do not edit. */\n")
+    info = emit_device_basis(S, "N4", "pip_n4_basis", path=nn)
+    print("N4 basis:", info)
     # the N3 surface is this fit with three pairs pinned: one coefficient file serves both
     assert S["N4_C_text"] == S["N3_C_text"], "N4 UMN coefficients differ from the N3 UMN ones"
     with open(os.path.join(REPO, "coarseair_gb300", "data", "N3_UMN.dat"), "w") as f:

@@ -11,6 +11,8 @@ This module reads the same data the reference reads at start-up:
   stored here as ``data/N3_UMN.dat``;
 * O3 NN surfaces: ``dtb/Systems/O3/PESs/NN/<Model>/<NHL1>_<NHL2>/`` (O3_NN_PES_Class.F90:74-232):
   ``ScalingValues.csv`` and ``CalibratedParams/{Lambda,re,W1,b1,W2,b2,W3,b3}.csv``;
+* N4 UMN PIPNN: ``dtb/Systems/N4/PESs/UMN_PIPNN/{Weights,Biases}.dat``
+  (N4_UMN_PIPNN_PES_Class.F90:176-330), three networks read in list-directed format;
 * O3 BNN posterior samples: ``dtb/Systems/O3/PESs/BNN/<Folder>/`` (BNN_PES_Class.F90:95-200,
   686-770): ``ScalingValues.csv`` and ``CalibratedParams/<name>.csv.<sample>``, packed one line per
   sample into ``data/O3_BNN/<Folder>/samples.csv.gz`` by ``data/O3_BNN/pack_samples.py``;
@@ -29,8 +31,8 @@ import numpy as np
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
 AMU_TO_AU = 1822.888486209          # [amu] -> electron masses (kgm_To_au / 1000)
-PES_O3_UMN, PES_N3_UMN, PES_O4_UMN, PES_O3_NN, PES_N4_UMN, PES_O3_BNN = 1, 2, 3, 4, 5, 6
-DIAT_O2_UMN, DIAT_N2_UMN_FORN4 = 1, 2
+PES_O3_UMN, PES_N3_UMN, PES_O4_UMN, PES_O3_NN, PES_N4_UMN, PES_O3_BNN, PES_N4_PIPNN = 1, 2, 3, 4, 5, 6, 7
+DIAT_O2_UMN, DIAT_N2_UMN_FORN4, DIAT_N2_UMN_PIPNN_FORN4 = 1, 2, 3
 
 _FNUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[dDeE][-+]?\d+)?")
 
@@ -146,6 +148,72 @@ def load_o3_bnn(sample, folder="PES9_Case2_LHS50"):
     return Surface(PES_O3_BNN, coef, name="O3 BNN %s sample %d" % (folder, sample))
 
 
+class _ListDirected:
+    """Fortran list-directed reads over a file's records: every READ starts on a new record and
+    drops what is left of its last record."""
+
+    def __init__(self, path):
+        with open(path) as f:
+            self.lines = f.read().split("\n")
+        self.pos = 0
+
+    def skip(self):
+        self.pos += 1
+
+    def read(self, n):
+        vals = []
+        while len(vals) < n:
+            if self.pos >= len(self.lines):
+                raise ValueError("end of file")
+            vals += _fortran_floats(self.lines[self.pos])
+            self.pos += 1
+        return vals[:n]
+
+
+# PES_Factory_Class.F90:276-296: the PES model string selects the networks averaged
+PIPNN_VARIANTS = {"UMN_PIPNN": (1, 1, 1), "UMN_PIPNN_A": (1, 0, 0), "UMN_PIPNN_B": (0, 1, 0),
+                  "UMN_PIPNN_C": (0, 0, 1)}
+
+
+def load_n4_pipnn(model="UMN_PIPNN"):
+    """N4 UMN PIPNN as Initialize_N4_UMN_PIPNN_PES reads it (N4_UMN_PIPNN_PES_Class.F90:176-330): per
+    network a title record in each file, NInput NHid NOutput, the hidden layer sizes, iFunc NWe,
+    pdel(NScale), pavg(NScale), then for every node of every layer its weights, one per record, from
+    Weights.dat and its bias from Biases.dat.  The three networks share one set of layer sizes and one
+    iFunc (each read overwrites the last).  Packed as UseSurface(3), iFunc, NInput, NHid1, NHid2,
+    NOutput, then per network pdel, pavg, W1(NInput, NHid1), b1, W2(NHid1, NHid2), b2, W3, b3."""
+    use = PIPNN_VARIANTS[model]
+    d = os.path.join(DATA, "N4_PIPNN")
+    W, B = _ListDirected(os.path.join(d, "Weights.dat")), _ListDirected(os.path.join(d, "Biases.dat"))
+    nets, shape = [], None
+    for _ in range(3):
+        B.skip()
+        W.skip()
+        nin, nhid, nout = (int(x) for x in W.read(3))
+        nodes = [nin] + [int(x) for x in W.read(nhid)] + [nout]
+        ifunc, nwe = (int(x) for x in W.read(2))
+        pdel, pavg = W.read(nin + nout), W.read(nin + nout)
+        layers, iwe = [], 0
+        for l in range(1, len(nodes)):
+            w = np.zeros((nodes[l - 1], nodes[l]))
+            b = np.zeros(nodes[l])
+            for j in range(nodes[l]):
+                for i in range(nodes[l - 1]):
+                    w[i, j] = W.read(1)[0]
+                    iwe += 1
+                b[j] = B.read(1)[0]
+                iwe += 1
+            layers.append((w, b))
+        if iwe != nwe:
+            raise ValueError("N4 PIPNN: %d parameters read, the file gives %d" % (iwe, nwe))
+        if nhid != 2 or nout != 1:
+            raise ValueError("N4 PIPNN: two hidden layers and one output are built")
+        nets.append(np.concatenate([pdel, pavg] + [np.concatenate([w.ravel(order="F"), b]) for w, b in layers]))
+        shape = (ifunc, nin, nodes[1], nodes[2], nout)
+    coef = np.concatenate([np.array(use + shape, dtype=np.float64)] + nets)
+    return Surface(PES_N4_PIPNN, coef, name="N4 " + model)
+
+
 def load_levels(name):
     """Level list as a structured array (columns LEVEL_COLS)."""
     fn = {"N2": "N2_UMN_ForN4_FromRoss.inp.gz", "O2": "O2_UMN_FromUMN_Sorted.inp.gz"}[name]
@@ -259,6 +327,17 @@ def n4_config(mass_amu=14.0067, **kw):
     kw.setdefault("dinit", 23.0)
     kw.setdefault("rmax", 30.0)
     return SystemConfig("N2+N2 UMN", 4, (m, m, m, m), [load_n4_umn()], DIAT_N2_UMN_FORN4, **kw)
+
+
+def n4pipnn_config(model="UMN_PIPNN", diat=DIAT_N2_UMN_FORN4, mass_amu=14.0067, **kw):
+    """N2 + N2 on the N4 UMN PIPNN surface (input/N4/UMN_PIPNN/input/CoarseAIR_VS.inp: Dinit 23 bohr,
+    rmax 30 bohr).  That input pairs it with the UMN_PIPNN_ForN4 diatomic, whose level list is not
+    shipped; the level list here is the UMN_ForN4 one, so the default diatomic is UMN_ForN4."""
+    m = mass_amu * AMU_TO_AU
+    kw.setdefault("bmax", 8.0)
+    kw.setdefault("dinit", 23.0)
+    kw.setdefault("rmax", 30.0)
+    return SystemConfig("N2+N2 " + model, 4, (m, m, m, m), [load_n4_pipnn(model)], diat, **kw)
 
 
 def o4_config(mass_amu=15.9994, **kw):

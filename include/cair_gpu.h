@@ -59,14 +59,18 @@ enum cair_pes_model {
   CAIR_PES_O4_UMN = 3, /* O4_UMN_PES_Class.F90  (System O4, Model UMN_Singlet/...)  */
   CAIR_PES_O3_NN = 4,  /* O3_NN_PES_Class.F90   (System O3, Model NN_*)             */
   CAIR_PES_N4_UMN = 5, /* N4_UMN_PES_Class.F90  (System N4, Model UMN; 4 atoms)     */
-  CAIR_PES_O3_BNN = 6  /* BNN_PES_Class.F90     (System O3, Model BNN; one surface
+  CAIR_PES_O3_BNN = 6, /* BNN_PES_Class.F90     (System O3, Model BNN; one surface
                           per posterior sample, StochPESFlg)                        */
+  CAIR_PES_N4_PIPNN = 7 /* N4_UMN_PIPNN_PES_Class.F90 (System N4, Model UMN_PIPNN,
+                          UMN_PIPNN_A/_B/_C; 4 atoms)                               */
 };
 
 /* Diatomic potentials of the pairs (DiatomicPotential_Factory_Class.F90:115-229). */
 enum cair_diat_model {
-  CAIR_DIAT_O2_UMN = 1,      /* O2_UMN_DiatomicPotential_Class.F90       */
-  CAIR_DIAT_N2_UMN_FORN4 = 2 /* N2_UMN_ForN4_DiatomicPotential_Class.F90 */
+  CAIR_DIAT_O2_UMN = 1,            /* O2_UMN_DiatomicPotential_Class.F90             */
+  CAIR_DIAT_N2_UMN_FORN4 = 2,      /* N2_UMN_ForN4_DiatomicPotential_Class.F90       */
+  CAIR_DIAT_N2_UMN_PIPNN_FORN4 = 3 /* N2_UMN_PIPNN_ForN4_DiatomicPotential_Class.F90
+                                      (with CAIR_PES_N4_PIPNN only)                  */
 };
 
 enum cair_status {
@@ -94,11 +98,19 @@ enum cair_traj_status {
  * (matrices column-major as in Fortran), ncoef = 12 + 7 NHL1 + NHL1 NHL2 + 2 NHL2; the kernels
  * hold NHL1 <= 20, NHL2 <= 10.  CAIR_PES_O3_BNN packs one posterior sample the same way
  * (Initialize_BNN_PES and ReadParamPost_BNN, BNN_PES_Class.F90:95-200, 640-760: ScalingValues.csv
- * and CalibratedParams/<name>.csv.<sample>) followed by its Noise, ncoef one more.  The MEG fields
- * are unused. */
+ * and CalibratedParams/<name>.csv.<sample>) followed by its Noise, ncoef one more.
+ * CAIR_PES_N4_PIPNN packs what Initialize_N4_UMN_PIPNN_PES reads from Weights.dat and Biases.dat
+ * (N4_UMN_PIPNN_PES_Class.F90:176-330) with the PES model's UseSurface (PES_Factory_Class.F90:276-296):
+ *   UseSurface(3) (0/1), iFunc, NInput, NHid1, NHid2, NOutput, then for networks a, b, c
+ *   pdel(NInput+1), pavg(NInput+1), W1(NInput,NHid1), b1, W2(NHid1,NHid2), b2, W3(NHid2), b3
+ * (weight(inode2, inode1) column-major as in Fortran; one iFunc and one set of layer sizes for the
+ * three networks, the last ones read, as the reference keeps them), ncoef = 8 + 3 x 2570 for the
+ * shipped 276-5-90-1 networks, the only shape built.  Its Compute returns dVdQ = 0, so its
+ * trajectories feel no force from it (cair_rhs gives dp/dt = -0); cair_pes_eval returns dVdR by the
+ * reference's central differences (1e-5 Ang).  The MEG fields are unused. */
 typedef struct cair_pes_desc {
   int32_t model;       /* cair_pes_model                                      */
-  int32_t ncoef;       /* 56 (O3), 276 (N3, N4), 430 (O4), see above (NN, BNN) */
+  int32_t ncoef;       /* 56 (O3), 276 (N3, N4), 430 (O4), see above (NN, BNN, PIPNN) */
   const double* coef;  /* C(1:ncoef) [kcal/mol], copied at cair_create        */
   double a, ab, ra, rb;/* MEG parameters [Ang, Ang^2, Ang, Ang] (O3, O4)      */
   double eref;         /* O4 file value (unused by the energy, as in the reference) */

@@ -35,15 +35,18 @@ extern "C" {
 #endif
 
 enum { ORC_PES_O3_UMN = 1, ORC_PES_N3_UMN = 2, ORC_PES_O4_UMN = 3, ORC_PES_O3_NN = 4, ORC_PES_N4_UMN = 5,
-       ORC_PES_O3_BNN = 6 };
-enum { ORC_DIAT_O2_UMN = 1, ORC_DIAT_N2_UMN_FORN4 = 2 };
+       ORC_PES_O3_BNN = 6, ORC_PES_N4_PIPNN = 7 };
+enum { ORC_DIAT_O2_UMN = 1, ORC_DIAT_N2_UMN_FORN4 = 2, ORC_DIAT_N2_UMN_PIPNN_FORN4 = 3 };
 
 typedef struct orc_pes {
   int model;
   int ncoef;
   const double* coef;           /* UMN: C(1:ncoef) [kcal/mol].  O3 NN: NHL1, NHL2, Lambda, re,
                                    Scaling_MEAN(3), Scaling_SD(3), y_Scaling, W1(6,NHL1), b1, W2(NHL1,NHL2),
-                                   b2, W3, b3 (column-major, as read by O3_NN_PES_Class.F90:74-232) */
+                                   b2, W3, b3 (column-major, as read by O3_NN_PES_Class.F90:74-232).
+                                   N4 PIPNN: UseSurface(3), iFunc, NInput, NHid1, NHid2, NOutput, then per
+                                   network pdel(NInput+1), pavg(NInput+1), W1(NInput,NHid1), b1, W2(NHid1,NHid2),
+                                   b2, W3(NHid2), b3 (N4_UMN_PIPNN_PES_Class.F90:176-330) */
   double a, ab, ra, rb;         /* MEG parameters (O3, O4) */
   double eref, totdiss;         /* O4 */
 } orc_pes;
@@ -82,6 +85,11 @@ void   orc_pip_eval(int table, const double* rms, const double* dmsdr_diag, int 
                     const double* C, double V0, double* V, double* dV);
 
 void   orc_pip_scale(int table, const double* rms, const double* dmsdr_diag, const double* C, double* scale);
+/* the basis functions themselves (b[NBASIS]) and their absolute-value graph (same shape) */
+void   orc_pip_basis(int table, const double* x, double* b, double* babs);
+/* N4 UMN PIPNN: network k (0..2) at the basis values b, and the surface in kcal/mol at rb [Ang] */
+double orc_pipnn_net(const double* coef, int k, const double* b);
+double orc_pipnn_kcal(const double* coef, const double* rb);
 void   orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale);
 
 /* ---- dynamics ---- */

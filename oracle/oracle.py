@@ -112,6 +112,11 @@ def lib():
         L.orc_pes_potential.argtypes = [C.POINTER(OrcSys), C.c_int, _D]
         L.orc_pip_eval.argtypes = [C.c_int, _D, _D, C.c_int, _D, C.c_double, _D, _D]
         L.orc_pes_scale.argtypes = [C.POINTER(OrcSys), C.c_int, _D, _D]
+        L.orc_pip_basis.argtypes = [C.c_int, _D, _D, _D]
+        L.orc_pipnn_net.restype = C.c_double
+        L.orc_pipnn_net.argtypes = [_D, C.c_int, _D]
+        L.orc_pipnn_kcal.restype = C.c_double
+        L.orc_pipnn_kcal.argtypes = [_D, _D]
         L.orc_rp.argtypes = [C.POINTER(OrcSys), _D, _D, _D]
         _I64 = C.POINTER(C.c_int64)
         L.orc_sample_ic4.argtypes = [C.POINTER(OrcSys), C.POINTER(OrcRng), C.POINTER(OrcLevel), C.POINTER(OrcLevel),

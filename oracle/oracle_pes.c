@@ -108,10 +108,64 @@ static void n2_ev2gm2(double rang, double* v, double* dv) {
   }
 }
 
+/* ------------------------------------------------------------------------------------------ */
+/* N2 UMN_PIPNN_ForN4: src/DiatomicPotentials/N2_UMN_PIPNN_ForN4_DiatomicPotential_Class.F90;  */
+/* the same Ev2gm2 + D3(BJ) dispersion is the pair term of the N4 UMN PIPNN surface           */
+/* (N4_UMN_PIPNN_PES_Class.F90:1471-1748).  Powers as gfortran expands them (x^5 = x^3 x^2,   */
+/* x^6 = x^3 x^3, x^8 = x^4 x^4).                                                              */
+/* ------------------------------------------------------------------------------------------ */
+static const double N2P_AS[7] = {2.7475450369759, 0.218868498415108, 0.248885765371433, -0.229295466336412,
+                                 -0.653389048592838, 1.03611964035396, 1.71287482791961};
+static const double N2P_DE = 225.213, N2P_RE = 1.098;
+#define HARTREE_TO_KCM (1.0 / KCM_TO_HARTREE)
+
+/* edisp for one N-N pair (iz = 7: r2r4 = 2.71175247; C6 = 19.7, rs6 = 0.5299, rs8 = 2.20), r [bohr] */
+static void n2p_edisp(double r, double* e6, double* e8, double* e6dr, double* e8dr) {
+  const double c6 = 19.7, r2r4 = 2.71175247, a1 = 0.5299, a2 = 2.20;
+  const double c8 = ((3.0 * c6) * r2r4) * r2r4;
+  const double tmp = sqrt(c8 / c6), s = a1 * tmp + a2;
+  const double s2 = s * s, s3 = s2 * s, s4 = s2 * s2, s6 = s3 * s3, s8 = s4 * s4;
+  const double r2 = r * r, r3 = r2 * r, r4 = r2 * r2, r6 = r3 * r3, r8 = r4 * r4;
+  const double d6 = r6 + s6, d8 = r8 + s8;
+  *e6 = c6 / d6;
+  *e8 = c8 / d8;
+  if (e6dr) {
+    const double r5 = r3 * r2, r7 = r4 * r3;
+    *e6dr = c6 * (-(6.0 * r5)) / (d6 * d6);
+    *e8dr = c8 * (-(8.0 * r7)) / (d8 * d8);
+  }
+}
+
+/* Ev2gm2 / Ev2gm2_Grad (diatomic class 116-225; surface 1471-1551): kcal/mol, kcal/mol/Ang */
+static void n2p_ev2gm2(double rang, double* v, double* dv) {
+  const double r2 = rang * rang, r3 = r2 * rang, r4 = r2 * r2, re2 = N2P_RE * N2P_RE, re4 = re2 * re2;
+  const double y = (r4 - re4) / (r4 + re4);
+  const double y2 = y * y, y3 = y * y2, y4 = y2 * y2, y5 = y2 * y3, y6 = y3 * y3;
+  const double fy = N2P_AS[0] + N2P_AS[1] * y + N2P_AS[2] * y2 + N2P_AS[3] * y3 + N2P_AS[4] * y4 +
+                    N2P_AS[5] * y5 + N2P_AS[6] * y6;
+  const double u = exp(-(fy * (rang - N2P_RE)));
+  double e6, e8, e6dr, e8dr;
+  n2p_edisp(rang / B_TO_ANG, &e6, &e8, dv ? &e6dr : 0, dv ? &e8dr : 0);
+  *v = ((N2P_DE * (1.0 - u)) * (1.0 - u) - N2P_DE) + (0.0 + (-e6 - 2.0 * e8) * HARTREE_TO_KCM);
+  if (dv) {
+    const double dfdy = N2P_AS[1] + 2.0 * N2P_AS[2] * y + 3.0 * N2P_AS[3] * y2 + 4.0 * N2P_AS[4] * y3 +
+                        5.0 * N2P_AS[5] * y4 + 6.0 * N2P_AS[6] * y5;
+    const double rr = r4 + re4;
+    const double dydr = ((8.0 * r3) * re4) / (rr * rr);
+    const double dfdr = dfdy * dydr;
+    *dv = (((2.0 * N2P_DE) * (1.0 - u)) * u) * (dfdr * (rang - N2P_RE) + fy) +
+          ((-e6dr - 2.0 * e8dr) * HARTREE_TO_KCM) / B_TO_ANG;
+  }
+}
+
 double orc_diat_V(int model, double r) {
   double rang = r * B_TO_ANG;
   if (model == ORC_DIAT_O2_UMN) return o2_ev2gm2(rang);          /* DiatomicPotential_O2_UMN 95-106 */
   double v;
+  if (model == ORC_DIAT_N2_UMN_PIPNN_FORN4) {                     /* DiatomicPotential_N2 91-101 */
+    n2p_ev2gm2(rang, &v, 0);
+    return v * KCM_TO_HARTREE + 0.0;
+  }
   n2_ev2gm2(rang, &v, 0);
   return v * KCM_TO_HARTREE + 0.0;                                /* DiatomicPotential_N2 99-110 */
 }
@@ -122,6 +176,10 @@ void orc_diat_VdV(int model, double r, double* v, double* dv) {
     o2_ev2gm2_grad(rang, &vd, &dvd);
     *v = vd;
     *dv = dvd * B_TO_ANG;
+  } else if (model == ORC_DIAT_N2_UMN_PIPNN_FORN4) {              /* Compute_Vd_dVd_N2 105-115 */
+    n2p_ev2gm2(rang, &vd, &dvd);
+    *v = vd * KCM_TO_HARTREE + 0.0;
+    *dv = dvd * KCM_TO_HARTREE * B_TO_ANG;
   } else {                                                        /* Compute_Vd_dVd_N2 114-130 */
     n2_ev2gm2(rang, &vd, &dvd);
     *v = vd * KCM_TO_HARTREE + 0.0;
@@ -132,8 +190,30 @@ void orc_diat_VdV(int model, double r, double* v, double* dv) {
 /* Rounding-level scales of a diatomic evaluation at r [bohr]: the same sums on absolute values
  * (O2 UMN: the eight Gaussian terms cancel to ~1e-3 of their sum; N2: De (1-u)^2 - De cancels at
  * large r), for V [Eh] and dV/dr [Eh/bohr]. */
+static void n2p_scale(double rang, double* sv, double* sdv) {
+  const double r3 = (rang * rang) * rang, r4 = r3 * rang, re4 = (N2P_RE * N2P_RE) * (N2P_RE * N2P_RE), ts = r4 + re4;
+  const double y = (r4 - re4) / ts;
+  double fa = 0.0, fy = 0.0, yi = 1.0, dfa = 0.0, yj = 1.0;
+  for (int i = 0; i < 7; ++i) { fa += fabs(N2P_AS[i]) * fabs(yi); fy += N2P_AS[i] * yi; yi *= y; }
+  for (int i = 1; i < 7; ++i) { dfa += i * fabs(N2P_AS[i]) * fabs(yj); yj *= y; }
+  const double dydr = 8.0 * r3 * re4 / (ts * ts);
+  const double u = exp(-(fy * (rang - N2P_RE))), minu = 1.0 - u, dr = fabs(rang - N2P_RE);
+  const double arg = fa * dr * (1.0 + fabs(fy * (rang - N2P_RE)));
+  double e6, e8, e6dr, e8dr;
+  n2p_edisp(rang / B_TO_ANG, &e6, &e8, &e6dr, &e8dr);
+  *sv = N2P_DE * (minu * minu) + N2P_DE + 2.0 * N2P_DE * fabs(minu) * u * arg + (e6 + 2.0 * e8) * HARTREE_TO_KCM;
+  *sdv = 2.0 * N2P_DE * (fabs(minu) + u) * u * (dfa * dydr * dr + fa) * (1.0 + arg) +
+         (fabs(e6dr) + 2.0 * fabs(e8dr)) * HARTREE_TO_KCM / B_TO_ANG;
+}
+
 void orc_diat_scale(int model, double r, double* sv, double* sdv) {
   double rang = r * B_TO_ANG;
+  if (model == ORC_DIAT_N2_UMN_PIPNN_FORN4) {
+    n2p_scale(rang, sv, sdv);
+    *sv *= KCM_TO_HARTREE;
+    *sdv *= KCM_TO_HARTREE * B_TO_ANG;
+    return;
+  }
   if (model == ORC_DIAT_O2_UMN) {
     double a = 0.0, d = 0.0;
     for (int k = 0; k <= 7; ++k) {
@@ -243,6 +323,41 @@ void orc_pip_eval(int table, const double* rms, const double* dmsdr_diag, int wa
   }
 }
 
+/* Basis functions B_1..B_nbasis at the variables x (EvMono/EvPoly/evbas order; bemsav49 and
+ * bmx2b109 of N4_UMN_PIPNN_PES_Class.F90:1004-1466, 1753-1830 for table 1), and, if babs is given,
+ * the same graph on absolute values (|p_a||p_b| + sum |p_c|), the scale of each basis function's
+ * rounding error. */
+void orc_pip_basis(int table, const double* x, double* b, double* babs) {
+  pip_tab T = pip_table(table);
+  double rm[128], p[480], ra[128], pa[480];
+  for (int k = 0; k < T.nmono; ++k) {
+    if (T.mo[k] == 0) { rm[k] = 1.0; ra[k] = 1.0; }
+    else if (T.mo[k] == 1) { rm[k] = x[T.ma[k]]; ra[k] = fabs(x[T.ma[k]]); }
+    else { rm[k] = rm[T.ma[k]] * rm[T.mb[k]]; ra[k] = ra[T.ma[k]] * ra[T.mb[k]]; }
+  }
+  for (int k = 0; k < T.npoly; ++k) {
+    const short* L = T.plist + T.poff[k];
+    const int n = T.plen[k];
+    double s, sa = 0.0;
+    if (T.po[k] == 0) {
+      s = rm[L[0]];
+      for (int i = 1; i < n; ++i) s = s + rm[L[i]];
+      for (int i = 0; i < n; ++i) sa += ra[L[i]];
+    } else {
+      s = p[T.pa[k]] * p[T.pb[k]];
+      for (int i = 0; i < n; ++i) s = s - p[L[i]];
+      sa = pa[T.pa[k]] * pa[T.pb[k]];
+      for (int i = 0; i < n; ++i) sa += pa[L[i]];
+    }
+    p[k] = s;
+    pa[k] = sa;
+  }
+  for (int i = 0; i < T.nbasis; ++i) {
+    b[i] = p[T.basis[i]];
+    if (babs) babs[i] = pa[T.basis[i]];
+  }
+}
+
 /* Condition scale of the PIP sum: the same graph evaluated on absolute values (|p_a||p_b| +
  * sum |p_c| at every node, and likewise for the derivatives), i.e. the standard bound on how
  * far any other evaluation order of these sums can move the result divided by the unit
@@ -287,12 +402,17 @@ void orc_pip_scale(int table, const double* rms, const double* dmsdr_diag, const
 /* Condition scale of a 3-atom surface evaluation at distances R [bohr]: scale[0] for V [Eh],
  * scale[1..3] for dV/dR [Eh/bohr] (PIP terms plus the diatomic terms' magnitudes). */
 static void o3nn_scale(const orc_sys* s, const orc_pes* P, const double* R, double* scale);
+static void n4pipnn_scale(const orc_pes* P, const double* R, double* scale);
 
 void orc_pes_scale(const orc_sys* s, int ipes, const double* R, double* scale) {
   const orc_pes* P = &s->pes[ipes];
   double rms[6] = {0}, dms[6] = {0}, sc[7];
   if (P->model == ORC_PES_O3_NN || P->model == ORC_PES_O3_BNN) {
     o3nn_scale(s, P, R, scale);
+    return;
+  }
+  if (P->model == ORC_PES_N4_PIPNN) {
+    n4pipnn_scale(P, R, scale);
     return;
   }
   if (P->model == ORC_PES_O4_UMN || P->model == ORC_PES_N4_UMN) {   /* scale[0] for V, scale[1..6] per pair */
@@ -462,6 +582,135 @@ static void n4_compute(const orc_sys* s, const orc_pes* P, const double* R, cons
   if (!dVdR) return;
   for (int i = 0; i < 6; ++i) dVdR[i] = dvp[i] * KCM_TO_HARTREE * B_TO_ANG + dd[i];
   trans_to_cart_4(s->mMiMn, R, Qall, dVdR, dVdQ);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* N4 UMN PIPNN (N4_UMN_PIPNN_PES_Class.F90).  Packed as UseSurface(3), iFunc, NInput, NHid1, */
+/* NHid2, NOutput, then networks a, b, c.  Initialize (176-330) reads the three networks into */
+/* one set of layer sizes and one iFunc, so the last network's are the ones every network is  */
+/* evaluated with.                                                                              */
+/* ------------------------------------------------------------------------------------------ */
+#define PIPNN_HDR 8
+static const double PIPNN_VINF[3] = {-0.021346263746904, -0.196886061330806, -0.030606048118131};  /* 96 */
+
+static int pipnn_net_size(int nin, int h1, int h2) { return 2 * (nin + 1) + nin * h1 + h1 + h1 * h2 + 2 * h2 + 1; }
+
+static double pipnn_tranfun(double x, int ifunc) {          /* tranfun 962-984 */
+  if (ifunc == 1) return tanh(x);
+  if (ifunc == 2) return 1.0 / (1.0 + exp(-x));
+  return x;
+}
+
+/* getpot (743-799): normalised input, hidden layers with iFunc, linear output, de-normalised */
+double orc_pipnn_net(const double* c, int k, const double* x) {
+  const int ifunc = (int)c[3], nin = (int)c[4], h1 = (int)c[5], h2 = (int)c[6];
+  const double* pdel = c + PIPNN_HDR + k * pipnn_net_size(nin, h1, h2);
+  const double *pavg = pdel + nin + 1, *W1 = pavg + nin + 1, *b1 = W1 + nin * h1, *W2 = b1 + h1, *b2 = W2 + h1 * h2,
+               *W3 = b2 + h2, *b3 = W3 + h2;
+  double y0[512], y1[64], y2[256];
+  for (int i = 0; i < nin; ++i) y0[i] = (x[i] - pavg[i]) / pdel[i];
+  for (int j = 0; j < h1; ++j) {
+    double a = b1[j];
+    for (int i = 0; i < nin; ++i) a = a + y0[i] * W1[i + nin * j];
+    y1[j] = pipnn_tranfun(a, ifunc);
+  }
+  for (int j = 0; j < h2; ++j) {
+    double a = b2[j];
+    for (int i = 0; i < h1; ++i) a = a + y1[i] * W2[i + h1 * j];
+    y2[j] = pipnn_tranfun(a, ifunc);
+  }
+  double o = b3[0];
+  for (int i = 0; i < h2; ++i) o = o + y2[i] * W3[i];
+  return o * pdel[nin] + pavg[nin];
+}
+
+/* Magnitude of network k's output sum at x: |pdel_out| (|b3| + sum |W3_k h2_k|) + |pavg_out|, the
+ * scale of the cancellation in its de-normalised output. */
+static double pipnn_net_magnitude(const double* c, int k, const double* x) {
+  const int ifunc = (int)c[3], nin = (int)c[4], h1 = (int)c[5], h2 = (int)c[6];
+  const double* pdel = c + PIPNN_HDR + k * pipnn_net_size(nin, h1, h2);
+  const double *pavg = pdel + nin + 1, *W1 = pavg + nin + 1, *b1 = W1 + nin * h1, *W2 = b1 + h1, *b2 = W2 + h1 * h2,
+               *W3 = b2 + h2, *b3 = W3 + h2;
+  double y1[64];
+  for (int j = 0; j < h1; ++j) {
+    double a = b1[j];
+    for (int i = 0; i < nin; ++i) a = a + ((x[i] - pavg[i]) / pdel[i]) * W1[i + nin * j];
+    y1[j] = pipnn_tranfun(a, ifunc);
+  }
+  double s = fabs(b3[0]);
+  for (int j = 0; j < h2; ++j) {
+    double a = b2[j];
+    for (int i = 0; i < h1; ++i) a = a + y1[i] * W2[i + h1 * j];
+    s += fabs(W3[j] * pipnn_tranfun(a, ifunc));
+  }
+  return s * fabs(pdel[nin]) + fabs(pavg[nin]);
+}
+
+/* n4pipNN (450-657) energy in kcal/mol at the six bond lengths rb [Ang]: the N2 pair terms, the
+ * basis of exp(-rb / alpha) (alpha = 1), the mean of the selected networks in eV, minus VInf. */
+double orc_pipnn_kcal(const double* c, const double* rb) {
+  double vn2 = 0.0, x[6], b[512];
+  for (int i = 0; i < 6; ++i) {
+    double v;
+    n2p_ev2gm2(rb[i], &v, 0);
+    vn2 = vn2 + v;
+  }
+  for (int i = 0; i < 6; ++i) x[i] = exp(-(rb[i] / 1.0));
+  orc_pip_basis(1, x, b, 0);
+  double vs[3] = {0.0, 0.0, 0.0}, vinf = 0.0;
+  int nuse = 0;
+  for (int k = 0; k < 3; ++k)
+    if (c[k] == 1.0) {
+      vs[k] = orc_pipnn_net(c, k, b);
+      vinf = vinf + PIPNN_VINF[k];
+      nuse += 1;
+    }
+  vinf = vinf / nuse;
+  const double v = ((vs[0] + vs[1]) + vs[2]) / nuse;
+  return (v * 23.0605 + vn2) - vinf;
+}
+
+/* Compute_N4_UMN_PIPNN_PES_1d (410-439): V, dVdR from n4pipNN's central differences (dr = 1e-5 Ang,
+ * the bond lengthened, then shortened by 2 dr, then restored, one bond at a time), dVdQ = 0. */
+static void n4pipnn_compute(const orc_sys* s, const orc_pes* P, const double* R, double* V, double* dVdR,
+                            double* dVdQ) {
+  double rb[6];
+  for (int i = 0; i < 6; ++i) rb[i] = R[i] * B_TO_ANG;
+  *V = orc_pipnn_kcal(P->coef, rb) * KCM_TO_HARTREE;
+  if (!dVdR) return;
+  const double dr = 1.0e-5;
+  for (int i = 0; i < 6; ++i) {
+    rb[i] = rb[i] + dr;
+    const double vp = orc_pipnn_kcal(P->coef, rb);
+    rb[i] = rb[i] - 2.0 * dr;
+    const double vm = orc_pipnn_kcal(P->coef, rb);
+    dVdR[i] = ((vp - vm) / (2.0 * dr)) * KCMANG_TO_HARTB;
+    rb[i] = rb[i] + dr;
+  }
+  for (int i = 0; i < s->neqtvar; ++i) dVdQ[i] = 0.0;
+}
+
+/* Scale of the PIPNN energy [Eh]: the magnitudes of the terms summed at the top (the pair terms,
+ * 23.0605 times the selected networks' output magnitudes, VInf), each carrying the cancellation
+ * below it; and of each central difference [Eh/bohr]: that scale over 2 dr. */
+static void n4pipnn_scale(const orc_pes* P, const double* R, double* scale) {
+  const double* c = P->coef;
+  double x[6], b[512], sv = 0.0;
+  for (int i = 0; i < 6; ++i) {
+    double a, d;
+    const double rb = R[i] * B_TO_ANG;
+    n2p_scale(rb, &a, &d);
+    sv += a;
+    x[i] = exp(-rb);
+  }
+  orc_pip_basis(1, x, b, 0);
+  int nuse = 0;
+  double sn = 0.0, vinf = 0.0;
+  for (int k = 0; k < 3; ++k)
+    if (c[k] == 1.0) { sn += pipnn_net_magnitude(c, k, b); vinf += fabs(PIPNN_VINF[k]); nuse += 1; }
+  const double skcal = 23.0605 * sn / nuse + sv + vinf / nuse;
+  scale[0] = skcal * KCM_TO_HARTREE;
+  for (int i = 0; i < 6; ++i) scale[1 + i] = skcal / 2.0e-5 * KCMANG_TO_HARTB;
 }
 
 /* O4 UMN: Compute_O4_UMN_PES_1d (O4_UMN_PES_Class.F90:269-298) -> O4pes (310-370) */
@@ -693,6 +942,7 @@ void orc_pes_compute(const orc_sys* s, int ipes, const double* R, const double* 
   if (P->model == ORC_PES_O3_UMN) o3_compute(s, P, R, Qall, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_N3_UMN) n3_compute(s, P, R, Qall, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_N4_UMN) n4_compute(s, P, R, Qall, V, dVdR, dVdQ);
+  else if (P->model == ORC_PES_N4_PIPNN) n4pipnn_compute(s, P, R, V, dVdR, dVdQ);
   else if (P->model == ORC_PES_O3_NN || P->model == ORC_PES_O3_BNN) {
     if (dVdR) o3nn_compute(s, P, R, Qall, V, dVdR, dVdQ);
     else *V = o3nn_potential(s, P, R);

@@ -156,6 +156,7 @@ extern "C" int pes_host_bs_steps(const void* devsys, const double* packed, const
     case CAIR_PES_O3_NN: return bs_steps_ns<CAIR_PES_O3_NN>(S, n, ipes, paq, t, dt, erra, nattempts);
     case CAIR_PES_N4_UMN: return bs_steps_ns<CAIR_PES_N4_UMN>(S, n, ipes, paq, t, dt, erra, nattempts);
     case CAIR_PES_O3_BNN: return bs_steps_ns<CAIR_PES_O3_BNN>(S, n, ipes, paq, t, dt, erra, nattempts);
+    case CAIR_PES_N4_PIPNN: return bs_steps_ns<CAIR_PES_N4_PIPNN>(S, n, ipes, paq, t, dt, erra, nattempts);
     default: return 1;
   }
 }
@@ -193,6 +194,7 @@ extern "C" int ic_host_sample(const void* devsys, const double* packed, const in
     case CAIR_PES_O3_NN: sample<CAIR_PES_O3_NN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
     case CAIR_PES_N4_UMN: sample<CAIR_PES_N4_UMN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
     case CAIR_PES_O3_BNN: sample<CAIR_PES_O3_BNN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
+    case CAIR_PES_N4_PIPNN: sample<CAIR_PES_N4_PIPNN>(S, ntot, items, levels, draws, item_of, paq, paq0, erra, H0, b, ipes, key); break;
     default: rc = 1;
   }
   delete[] draws;
@@ -339,6 +341,7 @@ extern "C" int queue_host_run(const void* devsys, const double* packed, const in
     case CAIR_PES_O3_NN: QUEUE(CAIR_PES_O3_NN) break;
     case CAIR_PES_N4_UMN: QUEUE(CAIR_PES_N4_UMN) break;
     case CAIR_PES_O3_BNN: QUEUE(CAIR_PES_O3_BNN) break;
+    case CAIR_PES_N4_PIPNN: QUEUE(CAIR_PES_N4_PIPNN) break;
     default: rc = 1;
   }
 #undef QUEUE
@@ -362,6 +365,7 @@ extern "C" int pes_host_eval(const void* devsys, const double* packed, const int
     case CAIR_PES_O3_NN: eval<CAIR_PES_O3_NN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
     case CAIR_PES_N4_UMN: eval<CAIR_PES_N4_UMN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
     case CAIR_PES_O3_BNN: eval<CAIR_PES_O3_BNN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
+    case CAIR_PES_N4_PIPNN: eval<CAIR_PES_N4_PIPNN>(S, n, ipes, R, Q, V, dVdR, dVdQ, grad); break;
     default: return 1;
   }
   return 0;
@@ -458,4 +462,11 @@ extern "C" int handoff_host_run(const void* devsys, const double* packed, const 
       return 0;
     default: return 1;
   }
+}
+
+// The system's diatomic as the initial-condition and final-state kernels evaluate it (diat_any)
+extern "C" void diat_host_eval(const void* devsys, int64_t n, const double* r, double* v, double* dv) {
+  DevSys S;
+  std::memcpy(&S, devsys, sizeof S);
+  for (int64_t k = 0; k < n; ++k) diat_any<true>(S, r[k], v[k], dv[k]);
 }
