@@ -7,7 +7,8 @@ calls it twice in a row through the C ABI and checks both results against the re
 (cair_run_queue_dev) on the same work items, with the tolerance of the other GPU tests (exact
 integers, 1e-12 relative for the floating-point fields; the kernels are the same, so the rows are
 expected to be identical).  It also checks that a batch beyond the static capacity is rejected.
-Collected last so that a run that stops at the first failure has run every other test.
+Collected after the other tests (only the N4 PIPNN file follows it) so that a run that stops at the first
+failure has run them.
 """
 
 import numpy as np
