@@ -9,10 +9,13 @@
 // right-justified words.  The binary file is the stream that Statistics_Class.F90:283-314 writes
 // and ReadInputsUnformatted (346-506) reads: NTraj, then per row Idx, iPES, bMax, bSampled,
 // Qini(NCond), Qfin(NCond) as 8-byte integers and reals.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "../../include/cair_gpu.h"
 
@@ -88,6 +91,22 @@ bool conserved(const cair_traj_result& r, double tol) {
   return r.status == CAIR_TRAJ_DONE && std::fabs(r.dH) <= tol;
 }
 
+// Runs work(0..nt-1), work(0) on the calling thread and the others on their own threads (inline
+// when a thread cannot be started), and returns when all are done.
+template <class F>
+void run_parallel(int nt, F&& work) {
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) {
+    try {
+      th.emplace_back(work, t);
+    } catch (...) {
+      work(t);
+    }
+  }
+  work(0);
+  for (std::thread& x : th) x.join();
+}
+
 }  // namespace
 
 extern "C" {
@@ -116,22 +135,35 @@ int cair_write_trajectories(const char* dir, const cair_traj_result* rows, int64
       if (x) std::fclose(x);
     return CAIR_EINVAL;
   }
+  // Rows are formatted in batches of nt chunks, the chunks on their own threads, and written chunk
+  // by chunk in row order, so the files are the same as a sequential write's.
+  const int64_t chunk = 16384;
+  const int nt = (int)std::max<int64_t>(1, std::min<int64_t>({16, (int64_t)std::thread::hardware_concurrency(),
+                                                               (n + chunk - 1) / chunk}));
+  std::vector<std::string> part[2] = {std::vector<std::string>(nt), std::vector<std::string>(nt)};
+  std::vector<int64_t> cnt(2 * (size_t)nt, 0);
+  bool ok = std::fputs(header(nmol), f[0]) >= 0 && std::fputs(header(nmol), f[1]) >= 0;
+  for (int64_t base = 0; base < n && ok; base += chunk * nt) {
+    run_parallel(nt, [&](int t) {
+      part[0][t].clear();
+      part[1][t].clear();
+      const int64_t lo = base + chunk * t, hi = std::min(n, lo + chunk);
+      for (int64_t k = lo; k < hi; ++k) {
+        const int which = conserved(rows[k], ham_abs_tol) ? 0 : 1;
+        format_row(part[which][t], rows[k], idx_offset, nmol);
+        ++cnt[2 * (size_t)t + which];
+      }
+    });
+    for (int t = 0; t < nt; ++t)
+      for (int i = 0; i < 2; ++i)
+        ok = ok && std::fwrite(part[i][t].data(), 1, part[i][t].size(), f[i]) == part[i][t].size();
+  }
   int64_t c[2] = {0, 0};
-  std::string s[2] = {header(nmol), header(nmol)};
-  bool ok = true;
-  for (int64_t k = 0; k < n; ++k) {
-    const int which = conserved(rows[k], ham_abs_tol) ? 0 : 1;
-    format_row(s[which], rows[k], idx_offset, nmol);
-    ++c[which];
-    if (s[which].size() > (1u << 20)) {
-      ok = ok && std::fwrite(s[which].data(), 1, s[which].size(), f[which]) == s[which].size();
-      s[which].clear();
-    }
+  for (int t = 0; t < nt; ++t) {
+    c[0] += cnt[2 * (size_t)t];
+    c[1] += cnt[2 * (size_t)t + 1];
   }
-  for (int i = 0; i < 2; ++i) {
-    ok = ok && std::fwrite(s[i].data(), 1, s[i].size(), f[i]) == s[i].size();
-    ok = (std::fclose(f[i]) == 0) && ok;
-  }
+  for (int i = 0; i < 2; ++i) ok = (std::fclose(f[i]) == 0) && ok;
   if (counts) {
     counts[0] = c[0];
     counts[1] = c[1];
