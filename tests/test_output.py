@@ -142,3 +142,21 @@ def test_empty_inputs(tmp_path):
     out.mkdir()
     assert api.merge_trajectories([], out) == 0
     assert (out / "NConvTraj.dat").read_text() == "0\n" and not (out / "trajectories.csv").exists()
+
+
+def test_large_files_are_the_rows_in_order(tmp_path):
+    """Many chunks' worth of rows (the writer formats them in parallel chunks): each file is the header and
+    its rows in their original order, as cair_format_rows formats them one by one."""
+    rng = np.random.default_rng(3)
+    n = 70001
+    r = np.zeros(n, dtype=_lib.RESULT_DTYPE)
+    r["idx"] = np.arange(1, n + 1)
+    r["ipes"] = rng.integers(0, 9, n)
+    r["status"] = np.where(rng.random(n) < 0.02, 1, 0)
+    for f in ("bmax", "b", "j_i", "v_i", "arr_i", "j_f", "v_f", "arr_f"):
+        r[f] = rng.normal(size=n) * 30
+    r["dH"] = rng.normal(size=n) * 1e-5
+    ok = (r["status"] == 0) & (np.abs(r["dH"]) <= 1e-5)
+    assert api.write_trajectories(tmp_path, r, ham_abs_tol=1e-5, idx_offset=5) == (ok.sum(), n - ok.sum())
+    assert (tmp_path / "trajectories.out").read_text() == api.format_rows(r[ok], idx_offset=5)
+    assert (tmp_path / "trajectories_HNotCons.out").read_text() == api.format_rows(r[~ok], idx_offset=5)
