@@ -108,3 +108,15 @@ def test_product_fails_loudly_without_a_gpu(gpu_lib):
         pass
     with pytest.raises(api.CairError, match="CAIR_ECUDA"):
         api.Handle(systems.n3_config())
+
+
+def test_model_constants_match_the_header():
+    """The surface and diatomic model numbers the Python side passes are the header's enums."""
+    import re
+    from coarseair_gb300 import systems
+    text = open(os.path.join(ROOT, "include", "cair_gpu.h")).read()
+    enums = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(CAIR_(?:PES|DIAT)_[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+    names = {n: getattr(systems, n) for n in dir(systems) if re.match(r"^(PES|DIAT)_[A-Z0-9_]+$", n)}
+    assert len(names) == len(enums) == 10
+    for n, v in names.items():
+        assert enums["CAIR_" + n] == v, n
